@@ -1,0 +1,392 @@
+"""Benchmark: ECP pair-evaluations per second and ns/day on one GB300.
+
+Workload (default "ecp"): N = 65536 biaxial ellipsoids, semi-axes (1.5, 1, 0.5)
+(full axes sig = (3, 2, 1)), packing fraction 0.35 (number density 0.1114),
+repulsive ECP (ecpr) with the plain Newton contact solve, Nose-Hoover chains
+of length 3 on translation and rotation, T* = 1.2, dt = 0.001, Verlet list
+rc 3.0 + skin 0.3. Synthetic, seeded: an aligned lattice equilibrated on the
+device with Langevin dynamics before timing (the reference publishes no
+placement routine and no benchmark data set).
+
+A step is one full timestep (integrators, list check with conditional
+rebuild, forces) launched as one captured CUDA graph. value = listed pairs x
+steps / device time of those steps; e2e repeats the measurement through the
+C ABI with FP64 host arrays copied in and out every step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TAU_PS = 2.156  # argon LJ time unit sigma*sqrt(m/eps) in ps (sigma 3.405 A, eps/kB 119.8 K, m 39.948 u)
+
+WORKLOADS = {
+    "ecp": dict(workload="ecp_biaxial_ecpr_nhc_N65536_phi0.35", counts=(32, 32, 64), sig=(3.0, 2.0, 1.0),
+                eps=(1.0, 1.0, 1.0), density=0.1114, kind="ECPR", cutoff=3.0, list_cutoff=3.0, skin=0.3,
+                integrator="NH", T=1.2, dt=0.001, tilt=0.2),
+    "gb": dict(workload="gay_berne_3_5_2_1_langevin_N32768_rho0.30", counts=(64, 32, 16), sig=(1.0, 1.0, 3.0),
+               eps=(1.0, 1.0, 0.2), density=0.30, kind="GB", cutoff=4.0, list_cutoff=6.0, skin=0.4,
+               integrator="LANGEVIN", T=1.0, dt=0.002, tilt=0.15, mu=2, nu=1),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="ecp", choices=sorted(WORKLOADS))
+    ap.add_argument("--solver", default="newton", choices=["newton", "brent", "mlp"])
+    ap.add_argument("--equil", type=int, default=1500, help="untimed Langevin equilibration steps")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU-baseline sample")
+    ap.add_argument("--no-extras", action="store_true", help="skip the secondary measurements")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks ---
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, p[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- workload ---
+def make_system(w, seed=1003):
+    from sucrose_gb300 import GpuSystem, capi, configs
+    r, q, box = configs.aligned_lattice(w["counts"], w["sig"], w["density"], seed=seed, jitter=0.02, tilt=w["tilt"])
+    n = len(r)
+    v = configs.velocities_to_temperature(n, w["T"], seed)
+    I = configs.default_inertia(w["sig"])
+    l = configs.angular_momenta(q, I, w["T"], seed)
+    g = GpuSystem(n, box)
+    g.set_particles(sig=w["sig"], eps=w["eps"])
+    g.upload(r=r, q=q, v=v, l=l)
+    g.init_nlist(w["skin"], w["list_cutoff"], trigger_mode=1)
+    return g, box
+
+
+def pair_params(g, w, solver):
+    from sucrose_gb300 import capi
+    kind = getattr(capi, w["kind"])
+    s = {"newton": capi.SOLVER_NEWTON, "brent": capi.SOLVER_BRENT_COMPAT, "mlp": capi.SOLVER_MLP_NEWTON}[solver]
+    return g.params(kind, cutoff=w["cutoff"], mu=w.get("mu", 0), nu=w.get("nu", 0), solver=s)
+
+
+def configure(g, w, pp, langevin=False, first_step=1):
+    from sucrose_gb300 import capi
+    if langevin or w["integrator"] == "LANGEVIN":
+        g.configure_step(pp, integrator=capi.INT_LANGEVIN, dt=w["dt"], target_temp=w["T"], damping=1.0,
+                         rotations=1, first_step=first_step)
+    else:
+        g.configure_step(pp, integrator=capi.INT_NH, dt=w["dt"], target_temp=w["T"], rotations=1, rot_chain=1)
+
+
+def ecp_flops_per_pair(mean_evals):
+    """Algorithmic FP32 flops of one ECP pair (Newton), counted from the kernel
+    source: setup 60, per Newton evaluation 110, final factorisation 30, force
+    and torque terms 420 (FMA = 2 flops, rsqrt/div = 1)."""
+    return 60.0 + 110.0 * mean_evals + 30.0 + 420.0
+
+
+def timed_steps(g, torch, stream, steps, flush):
+    import ctypes
+    start = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    end = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            start[k].record(stream)
+            g.step(1)
+            end[k].record(stream)
+            flush.add_(1.0)   # write 256 MB (> L2) between timed steps
+    torch.cuda.synchronize()
+    return sum(s.elapsed_time(e) for s, e in zip(start, end)) / 1e3
+
+
+def timed_forces(g, torch, stream, pp, reps, flush):
+    start = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    end = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    with torch.cuda.stream(stream):
+        for k in range(reps):
+            g.zero_forces()
+            start[k].record(stream)
+            g.pair_forces_async(pp)
+            end[k].record(stream)
+            flush.add_(1.0)
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) / 1e3 for s, e in zip(start, end)]
+
+
+def cpu_baseline(g, w, seconds, nthreads=1):
+    """The oracle's faithful restatement of the reference pair routine (the
+    reference's Brent, per-pair setup, FP64) over a bounded sample of the
+    device's current pair list, on host cores."""
+    import oracle as O
+    r, q, v, l = g.download()
+    pi, pj = g.pairs()
+    s = O.System(g.n, g.box, fast=True)
+    s.set_defaults(sig=w["sig"], eps=w["eps"])
+    s.rx[:], s.ry[:], s.rz[:] = r.T
+    s.qw[:], s.qx[:], s.qy[:], s.qz[:] = q.T
+    kind = getattr(O, w["kind"])
+    pp = O.pair_params(kind, cutoff=w["cutoff"], solver=O.SOLVER_BRENT, mu=w.get("mu"), nu=w.get("nu"))
+    # calibrate on a small slice, then run a sample of about `seconds`
+    m0 = min(len(pi), 4000 * nthreads)
+    t = time.perf_counter()
+    s.pair_batch(pp, pi[:m0], pj[:m0], nthreads)
+    per = (time.perf_counter() - t) / max(m0, 1)
+    m = int(min(len(pi), max(m0, seconds / max(per, 1e-9))))
+    t = time.perf_counter()
+    s.pair_batch(pp, pi[:m], pj[:m], nthreads)
+    dt = time.perf_counter() - t
+    return m / dt, m
+
+
+# -------------------------------------------------------------------- ours ---
+def run_ours(a):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from sucrose_gb300 import capi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    w = WORKLOADS[a.config]
+    g, box = make_system(w, seed=1003 + rank)
+    stream = torch.cuda.ExternalStream(g.stream_ptr())
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    pp = pair_params(g, w, a.solver)
+    pp_eq = pair_params(g, w, "newton" if a.solver != "brent" else "brent")
+
+    # untimed equilibration (Langevin, rotations on) from the aligned lattice
+    configure(g, w, pp_eq, langevin=True, first_step=1)
+    g.step(a.equil)
+    g.step_check()
+    configure(g, w, pp)
+    g.step(max(a.warmup, 3))
+    g.step_check()
+    kernels_per_step = g.step_kernel_count()
+    p_before = g.npairs()
+    builds0 = g.nlist_builds()
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_dev = timed_steps(g, torch, stream, a.steps, flush)
+    g.step_check()
+    p_after = g.npairs()
+    builds = g.nlist_builds() - builds0
+    npairs = 0.5 * (p_before + p_after)
+    if dist is not None:
+        tt = torch.tensor([t_dev], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    ms_per_step = 1e3 * t_dev / a.steps
+    value = npairs * a.steps * world / t_dev
+    steps_per_s = a.steps / t_dev
+    ns_day = steps_per_s * w["dt"] * TAU_PS * 1e-3 * 86400.0
+
+    # dominant kernel: the pair-force kernel timed alone (same stream, L2 flushed)
+    _, _, st = g.pair_forces(pp, want_stats=True)
+    mean_evals = st.solver_evals / max(st.pairs, 1)
+    tf = timed_forces(g, torch, stream, pp, 20, flush)
+    t_force = statistics.median(tf)
+    peak32 = g.peak_fma(False)
+    flops = ecp_flops_per_pair(mean_evals) * npairs
+    achieved = flops / t_force / 1e12
+
+    # e2e: FP64 host arrays in and out through the C ABI every step
+    n = g.n
+    pin = lambda: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    host = [pin() for _ in range(13)]
+    r, q, v, l = g.download()
+    for k in range(3):
+        host[k][:] = r[:, k]
+        host[7 + k][:] = v[:, k]
+        host[10 + k][:] = l[:, k]
+    for k in range(4):
+        host[3 + k][:] = q[:, k]
+    import ctypes as C
+    D = C.POINTER(C.c_double)
+    ptrs = [h.ctypes.data_as(D) for h in host]
+    L = g.L
+    energies = np.zeros(4)
+    e_steps = max(10, a.steps // 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e_steps):
+        capi.check(g.ctx, L.sg_upload_state(g.ctx, *ptrs))
+        g.step(1)
+        capi.check(g.ctx, L.sg_download_state(g.ctx, *ptrs))
+        capi.check(g.ctx, L.sg_read_energies(g.ctx, energies.ctypes.data_as(D)))
+    t_e2e = time.perf_counter() - t0
+    e2e_value = npairs * e_steps / t_e2e
+    h2d = 13 * 8 * n
+    d2h = 13 * 8 * n + 32
+
+    extras = {}
+    if not a.no_extras and rank == 0:
+        extras["force_kernel_pair_evals_per_s"] = npairs / t_force
+        extras["force_kernel_ms"] = 1e3 * t_force
+        extras["newton_mean_evals_per_pair"] = mean_evals
+        extras["newton_iter_hist"] = [int(x) for x in st.iter_hist]
+        extras["newton_fp64_refined_frac"] = st.fp64_refined / max(st.pairs, 1)
+        extras["nonconverged"] = int(st.nonconverged)
+        extras["fp64_peak_tflops_measured"] = g.peak_fma(True)
+        extras["list_rebuilds_in_timed_region"] = int(builds)
+        if a.config == "ecp" and a.solver == "newton":
+            pb = pair_params(g, w, "brent")
+            _, _, stb = g.pair_forces(pb, want_stats=True)
+            tb = statistics.median(timed_forces(g, torch, stream, pb, 5, flush))
+            extras["brent_compat_force_kernel_ms"] = 1e3 * tb
+            extras["brent_compat_pair_evals_per_s"] = npairs / tb
+            extras["brent_mean_evals_per_pair"] = stb.solver_evals / max(stb.pairs, 1)
+            extras["mlp"] = "not measured: no trained weights in this run"
+
+    cpu = None
+    if rank == 0:
+        cpu_rate, m = cpu_baseline(g, w, a.cpu_seconds, nthreads=1)
+        cpu = {"value": cpu_rate, "unit": "pair-evals/s", "cores": 1, "kind": "port",
+               "sample": f"{m} listed pairs of this workload's list, reference Brent + per-pair setup, FP64, "
+                         f"oracle restatement built -O3 -ffast-math, 1 thread"}
+    if rank == 0:
+        line = {
+            "metric": "ECP pair-evals/s (plain Newton contact solve, full MD step)" if a.config == "ecp"
+            else "GB pair-evals/s (full MD step)",
+            "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (fp64 sums and residual check)", "data": "synthetic (seeded lattice, device-equilibrated)",
+            "config": {"workload": w["workload"], "n": g.n, "listed_pairs": npairs, "solver": a.solver,
+                       "dt": w["dt"], "T": w["T"], "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": "replicas only" if world > 1 else "single GPU"},
+            "ns_per_day": ns_day, "tau_per_day": steps_per_s * w["dt"] * 86400.0,
+            "e2e": {"value": e2e_value, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(kernels_per_step * a.steps),
+            "roofline": {"bound": "fp32", "kernel": "k_pair<PotECP>", "achieved": achieved, "peak": peak32,
+                         "unit": "TFLOP/s", "frac": achieved / peak32,
+                         "peak_source": "measured FMA throughput (sg_peak_fma) on this GPU",
+                         "traffic": None},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------------- reference ---
+def run_reference(a):
+    """The reference's pair routine restated on the CPU (its Fortran has no
+    compiler here), all host threads, on this workload's geometry."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle as O
+    from scipy.spatial import cKDTree
+    from sucrose_gb300 import configs
+    w = WORKLOADS[a.config]
+    r, q, box = configs.aligned_lattice(w["counts"], w["sig"], w["density"], seed=1003, jitter=0.02, tilt=w["tilt"])
+    n = len(r)
+    rw = (r + box / 2.0) % box
+    tree = cKDTree(rw, boxsize=box)
+    pairs = tree.query_pairs(w["list_cutoff"] + w["skin"], output_type="ndarray")
+    pairs.sort(axis=1)
+    pairs = pairs[np.lexsort((pairs[:, 1], pairs[:, 0]))]
+    pi, pj = pairs[:, 0].astype(np.int32), pairs[:, 1].astype(np.int32)
+    s = O.System(n, box, fast=True)
+    s.set_defaults(sig=w["sig"], eps=w["eps"])
+    s.rx[:], s.ry[:], s.rz[:] = r.T
+    s.qw[:], s.qx[:], s.qy[:], s.qz[:] = q.T
+    kind = getattr(O, w["kind"])
+    pp = O.pair_params(kind, cutoff=w["cutoff"], solver=O.SOLVER_BRENT, mu=w.get("mu"), nu=w.get("nu"))
+    nth = os.cpu_count() or 1
+    per_step = min(len(pi), 200000)
+    for _ in range(a.warmup):
+        s.pair_batch(pp, pi[:per_step // 10], pj[:per_step // 10], nth)
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        off = (k * per_step) % max(1, len(pi) - per_step + 1)
+        s.pair_batch(pp, pi[off:off + per_step], pj[off:off + per_step], nth)
+    dt = time.perf_counter() - t0
+    value = per_step * a.steps / dt
+    line = {"impl": "reference", "metric": "ECP pair-evals/s" if a.config == "ecp" else "GB pair-evals/s",
+            "value": value, "unit": "pair-evals/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * dt / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64", "data": "synthetic (seeded lattice)",
+            "config": {"workload": w["workload"], "n": n, "listed_pairs": int(len(pi)), "per_step_pairs": per_step},
+            "cpu_baseline": {"value": value, "unit": "pair-evals/s", "cores": nth, "kind": "port",
+                             "sample": f"{per_step} pairs per step of the {len(pi)}-pair list; the reference pair "
+                                       "routine (Brent, per-pair setup, FP64) restated in C++, OpenMP"},
+            "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)

@@ -1,0 +1,250 @@
+/*
+ * sucrose_gpu.h — C ABI of the GB300 (sm_103a) SUCROSE molecular-dynamics hot path.
+ *
+ * One context (sg_ctx) owns one system's device state on one GPU and one CUDA
+ * stream. State is FP32 structure-of-arrays in HBM (float4 position,
+ * quaternion, velocity, angular momentum, force, torque, shape, energy scales,
+ * inertia); energy, virial and kinetic-energy reductions are FP64.
+ *
+ * Host arrays crossing this boundary are FP64 structure-of-arrays of length N
+ * in the reference's own layout (module globals RX..RZ, QW..QZ, VX..VZ, LX..LZ,
+ * FX..FZ, TX..TY, fortran/system.f90:7-30), 0-based. The caller keeps
+ * ownership of every host array; the context copies in and out explicitly.
+ *
+ * Every entry point returns an sg_status; on error sg_last_error() holds a
+ * one-line message. Nothing here exits the process, and no kernel traps:
+ * per-pair non-convergence and list overflow are counted in device status
+ * words, then reported by the call that reads them.
+ *
+ * Threading: one context per host thread; calls on one context are serialised
+ * by the caller; contexts are independent.
+ */
+#ifndef SUCROSE_GPU_H
+#define SUCROSE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sg_ctx sg_ctx;
+
+typedef enum {
+    SG_OK = 0,
+    SG_EINVAL = 1,               /* bad argument                                   */
+    SG_ECUTOFF_GT_HALFBOX = 2,   /* init_nlist guard, fortran/system.f90:902-906   */
+    SG_ENOCONV = 3,              /* contact solve did not converge for some pairs */
+    SG_ENAN = 4,                 /* non-finite energy or force                      */
+    SG_ECAPACITY = 5,            /* neighbour list overflowed its capacity          */
+    SG_ECUDA = 6,                /* CUDA runtime error                              */
+    SG_ENOTREADY = 7             /* call order (e.g. forces before a list build)    */
+} sg_status;
+
+/* Pair-potential kinds; one entry point per family. */
+typedef enum {
+    SG_LJ = 0,     /* lj_calculate_forces     fortran/force.f90:6-49     */
+    SG_LJ12 = 1,   /* lj12_calculate_forces   fortran/force.f90:51-93    */
+    SG_LJW = 2,    /* ljw_calculate_forces    fortran/force.f90:95-146   */
+    SG_WCA = 3,    /* wca_calculate_forces    fortran/force.f90:155-190  */
+    SG_GB = 10,    /* gb_calculate_forces     fortran/force.f90:308-428  */
+    SG_GBR = 11,   /* gbr_calculate_forces    fortran/force.f90:430-533  */
+    SG_GBW = 12,   /* gbw_calculate_forces    fortran/force.f90:535-663  */
+    SG_GBC = 13,   /* gbc_calculate_forces    fortran/force.f90:665-843  */
+    SG_GBWC = 14,  /* gbwc_calculate_forces   fortran/force.f90:845-1030 */
+    SG_ECP = 20,   /* ecp_calculate_forces    fortran/force.f90:1202-1385 */
+    SG_ECPR = 21,  /* ecpr_calculate_forces   fortran/force.f90:1387-1551 */
+    SG_ECPW = 22,  /* ecpw_calculate_forces   fortran/force.f90:1553-1742 */
+    SG_ECPC = 23,  /* ecpc_calculate_forces   fortran/force.f90:1744-1984 */
+    SG_ECPWC = 24  /* ecpwc_calculate_forces  fortran/force.f90:1986-2234 */
+} sg_pair_kind;
+
+/* ECP contact-parameter solvers. */
+typedef enum {
+    SG_SOLVER_BRENT_COMPAT = 0,  /* the reference's Brent (fortran/force.f90:1046-1172), FP64, same lambda bits */
+    SG_SOLVER_NEWTON = 1,        /* Newton on dS/dlambda, FP32, FP64 residual check            */
+    SG_SOLVER_MLP_NEWTON = 2     /* MLP initial guess, <= 3 Newton steps, else the plain Newton */
+} sg_ecp_solver;
+
+/* Parameters of one pair-force call (the arguments of *_calculate_forces). */
+typedef struct {
+    int32_t kind;       /* sg_pair_kind                                            */
+    int32_t mu, nu;     /* GB / ECP exponents; 0,0 selects the reference's (1,2) for GB, (2,1) for ECP */
+    int32_t solver;     /* sg_ecp_solver (ECP only)                                 */
+    double sigma;       /* LJ/WCA sigma                                             */
+    double epsilon;     /* LJ/WCA epsilon                                           */
+    double cutoff;      /* rc (LJ), GB/ECP cutoff argument                          */
+    double wf;          /* weld width (ljw, gbw, gbwc, ecpw, ecpwc)                 */
+    double chirality;   /* gbc, gbwc, ecpc, ecpwc                                   */
+    double newton_tol;  /* bound on |S'(lambda)| / (r.K) checked in FP64; 0 selects 1e-6 */
+    int32_t newton_max_iter;  /* 0 selects 20                                       */
+    int32_t fp64_check; /* Newton: 1 = FP64 residual check (default), 0 = FP32 step-size test only */
+} sg_pair_params;
+
+/* Per-call statistics of an ECP force evaluation. */
+typedef struct {
+    int64_t pairs;          /* pairs evaluated                                      */
+    int64_t solver_evals;   /* total objective / Newton evaluations                 */
+    int64_t nonconverged;   /* pairs whose solve hit its iteration cap              */
+    int64_t fallbacks;      /* MLP path: pairs that fell back to the plain Newton   */
+    int64_t iter_hist[24];  /* Newton iterations per pair (last bin: >= 23)         */
+    int64_t fp64_refined;   /* Newton: pairs that needed the FP64-residual correction */
+} sg_ecp_stats;
+
+/* ---- context -------------------------------------------------------------- */
+int sg_create(sg_ctx** out, int32_t n, int32_t device);
+int sg_destroy(sg_ctx* ctx);
+const char* sg_last_error(const sg_ctx* ctx);
+/* Opaque: the context's CUDA stream (cudaStream_t), for callers that overlap work. */
+void* sg_stream(sg_ctx* ctx);
+int sg_synchronize(sg_ctx* ctx);
+
+/* set_box / set_periodic_boundary (fortran/system.f90:185-213) */
+int sg_set_box(sg_ctx* ctx, const double box[3], int32_t periodic);
+
+/* Per-particle constants: mass, shape (sig_*), energy scales (eps_*) and
+ * principal moments (I*). NULL arrays take initialize_system's defaults
+ * (fortran/system.f90:586-682): mass 1, shape and energy (1,1,1), inertia
+ * ((sy^2+sz^2)/20, ...). A zero mass freezes the particle. */
+int sg_set_particles(sg_ctx* ctx, const double* mass, const double* sig_x, const double* sig_y,
+                     const double* sig_z, const double* eps_x, const double* eps_y, const double* eps_z,
+                     const double* ixx, const double* iyy, const double* izz);
+
+/* Copy state in / out. Any array may be NULL to skip it. Quaternions are (w,x,y,z). */
+int sg_upload_state(sg_ctx* ctx, const double* rx, const double* ry, const double* rz, const double* qw,
+                    const double* qx, const double* qy, const double* qz, const double* vx, const double* vy,
+                    const double* vz, const double* lx, const double* ly, const double* lz);
+int sg_download_state(sg_ctx* ctx, double* rx, double* ry, double* rz, double* qw, double* qx, double* qy,
+                      double* qz, double* vx, double* vy, double* vz, double* lx, double* ly, double* lz);
+int sg_download_forces(sg_ctx* ctx, double* fx, double* fy, double* fz, double* tx, double* ty, double* tz);
+int sg_upload_forces(sg_ctx* ctx, const double* fx, const double* fy, const double* fz, const double* tx,
+                     const double* ty, const double* tz);
+
+/* initialize_forces (fortran/system.f90:423-436): zero F, T and the accumulators. */
+int sg_zero_forces(sg_ctx* ctx);
+
+/* ---- neighbour list (fortran/system.f90:885-1053) ---------------------------- */
+/* init_nlist(skin, cutoff) :895 + build_init_nlist :927. trigger_mode 0 reproduces
+ * the reference trigger (displacement^2 * 4 > (rc+skin)^2, quirk at :933,:1033);
+ * trigger_mode 1 uses skin^2. Returns SG_ECUTOFF_GT_HALFBOX like the reference stop. */
+int sg_nlist_init(sg_ctx* ctx, double skin, double cutoff, int32_t trigger_mode);
+/* needs_rebuild() :1005 — reads the device flag (synchronises). */
+int sg_nlist_needs_rebuild(sg_ctx* ctx, int32_t* flag);
+/* build_nlist() :966 — unconditional rebuild. */
+int sg_nlist_build(sg_ctx* ctx);
+/* needs_rebuild + conditional build on the device, no host synchronisation
+ * (safe inside a captured CUDA graph). */
+int sg_nlist_update(sg_ctx* ctx);
+/* Number of listed (half) pairs; synchronises. */
+int sg_nlist_count(sg_ctx* ctx, int64_t* npairs);
+/* The list in the reference's CSR (rows J>I ascending): with one_based = 1,
+ * offset[I] is the 1-based start of row I and offset[N-1] = K+1, nlist holds
+ * 1-based J, exactly as nlist/offset after build_nlist (:977-1000). With
+ * one_based = 0, offset has N+1 entries and values are 0-based. */
+int sg_nlist_export(sg_ctx* ctx, int32_t* nlist, int64_t capacity, int32_t* offset, int64_t* npairs,
+                    int32_t one_based);
+/* The listed pairs (I < J, 0-based) in the device's internal order, which is
+ * the order of per-pair outputs such as sg_ecp_lambda. */
+int sg_nlist_pairs(sg_ctx* ctx, int32_t* pi, int32_t* pj, int64_t capacity, int64_t* npairs);
+/* Number of list rebuilds performed since sg_nlist_init. */
+int sg_nlist_builds(sg_ctx* ctx, int64_t* builds);
+
+/* ---- pair forces (fortran/force.f90, README.md:86-103 accumulation) ----------- */
+/* Batched drop-in for the user's pair loop over the Verlet list calling
+ * X_calculate_forces(I, J, ...): adds F(I) += FXIJ, F(J) -= FXIJ,
+ * T(I) += TXI, T(J) += TXJ on the device and adds the summed PE to *pot_eng
+ * and the pair virial sum r_ij . F_ij to *virial (either may be NULL).
+ * stats may be NULL. */
+int sg_pair_forces(sg_ctx* ctx, const sg_pair_params* params, double* pot_eng, double* virial,
+                   sg_ecp_stats* stats);
+/* Same, without reading results back (no host synchronisation): the sums stay
+ * in the device accumulators, read by sg_read_energies. */
+int sg_pair_forces_async(sg_ctx* ctx, const sg_pair_params* params);
+/* Device accumulators: pot_eng, pair virial, kin_eng, kin_rot (FP64). */
+int sg_read_energies(sg_ctx* ctx, double out[4]);
+/* Per-pair contact parameter of the last ECP call, in the device list order
+ * that sg_nlist_pairs returns (debug / parity). */
+int sg_ecp_lambda(sg_ctx* ctx, float* lam, int64_t capacity);
+
+/* ---- integrators (fortran/integrators.f90) ----------------------------------- */
+int sg_vv_initial(sg_ctx* ctx, double dt);                       /* :7-34    */
+int sg_vv_final(sg_ctx* ctx, double dt, double* kin_eng);          /* :36-53   */
+int sg_qq_initial(sg_ctx* ctx, double dt);                       /* :123-183 */
+int sg_qq_final(sg_ctx* ctx, double dt, double* kin_rot);          /* :185-218 */
+/* Langevin :507-627 / :629-676. Noise counter (I 1-based, step, int(T*1000), stream 0|1);
+ * key NULL selects the reference's fixed key (fortran/xmath.f90:10-11). */
+int sg_lgv_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double target_temp,
+                   const uint32_t* key);
+int sg_lgv_final(sg_ctx* ctx, double dt, double damping, double* kin_eng, double* kin_rot);
+/* Nose-Hoover chain (length 3, tau 2) :303-354 / :356-392. coupling <= 0 selects
+ * the reference masses. mode 0 = the reference's per-particle chain recurrence,
+ * mode 1 = standard NHC (one chain update per half step). rot_chain = 1 adds a
+ * second chain on the rotational kinetic energy (mode 1 only). */
+int sg_nht_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode,
+                   int32_t rot_chain);
+int sg_nht_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain,
+                 double* kin_eng);
+/* Chain state (eta[3], p_eta[3], eta_rot[3], p_eta_rot[3]) in / out. */
+int sg_nht_state(sg_ctx* ctx, double* get12, const double* set12);
+/* calculate_thermo (fortran/system.f90:725-741): out = {temp, virial, pressure};
+ * dof and density as in initialize_system; kin_eng/kin_rot from the last integrator call. */
+int sg_thermo(sg_ctx* ctx, int32_t dof, double density, int32_t nrigid, double* out3);
+
+/* ---- whole timestep, captured in a CUDA graph ------------------------------- */
+/* One timestep in the reference's README order (README.md:83-115, with the
+ * Verlet list of fortran/system.f90:1005 and :966): integrator initial half
+ * step, list check with device-side conditional rebuild, initialize_forces,
+ * the pair loop, integrator final half step. */
+typedef enum {
+    SG_INT_NVE = 0,        /* vv_* (+ qq_* with rotations)                          */
+    SG_INT_LANGEVIN = 1,   /* lgv_* (rotation included when rotations = 1)          */
+    SG_INT_NH = 2,         /* nht_* standard chain (+ qq_*), optional rotational chain */
+    SG_INT_NH_REF = 3      /* nht_* with the reference's per-particle chain (+ qq_*) */
+} sg_integrator;
+
+typedef struct {
+    int32_t integrator;    /* sg_integrator                                       */
+    int32_t rotations;     /* 1: quaternion dynamics                               */
+    int32_t rot_chain;     /* SG_INT_NH: second chain on rotation                  */
+    int32_t first_step;    /* Langevin step counter of the next step               */
+    double dt, target_temp, damping, coupling;
+    uint32_t key[2];       /* Langevin Philox key (has_key = 1), else the reference key */
+    int32_t has_key;
+    int32_t reserved;
+    sg_pair_params pair;   /* the pair potential evaluated every step              */
+} sg_step_config;
+
+/* Set the step program. The first sg_step call runs one step eagerly (which
+ * allocates every buffer), then captures one step as a CUDA graph; later
+ * steps launch the graph. Reallocation (list regrowth) forces a re-capture. */
+int sg_step_configure(sg_ctx* ctx, const sg_step_config* cfg);
+/* Enqueue nsteps timesteps on the context stream; returns without waiting. */
+int sg_step(sg_ctx* ctx, int32_t nsteps);
+/* Wait, then report list overflow (SG_ECAPACITY) or a non-finite energy (SG_ENAN). */
+int sg_step_check(sg_ctx* ctx);
+/* Kernel launches in one captured step (after the first sg_step call). */
+int sg_step_kernel_count(sg_ctx* ctx, int64_t* count);
+
+/* Measured FP32 (fp64 = 0) or FP64 (fp64 = 1) FMA throughput of this GPU in
+ * TFLOP/s: the roofline denominator of the FP32-pipe pair kernels. */
+int sg_peak_fma(sg_ctx* ctx, int32_t fp64, double* tflops);
+
+/* ---- Philox4x32-10 (fortran/xmath.f90:42-113) -------------------------------- */
+/* Host-side single block, for callers that mirror philox_uniform. */
+void sg_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* n counters (4 words each) from a HOST array through a device kernel. */
+int sg_philox4x32_device(sg_ctx* ctx, int64_t n, const uint32_t* ctr, const uint32_t key[2], uint32_t* out);
+/* philox_normal_3seq on the device for n counters; out holds 3 doubles per counter. */
+int sg_philox_normal_3seq_device(sg_ctx* ctx, int64_t n, const int32_t* ctr, double* out);
+
+/* ---- learned contact-parameter guess (no counterpart in the reference) -------- */
+/* Weights of the 14(16)->64->64->64->1 MLP, FP32 master copy, packed
+ * W1[64x16] b1[64] W2[64x64] b2[64] W3[64x64] b3[64] W4[64] b4[1]. */
+int sg_mlp_set_weights(sg_ctx* ctx, const float* w, int64_t count);
+int sg_mlp_get_weights(sg_ctx* ctx, float* w, int64_t count);
+int64_t sg_mlp_weight_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,160 @@
+"""Seeded synthetic initial configurations (host-side set-up, not the hot path).
+
+fcc_lattice and velocities_to_temperature follow the reference's own
+generate_fcc_lattice (fortran/system.f90:438-523) and
+set_velocity_to_temperature (:362-421, Philox counter (I, int(T*1000), seed, 42)),
+so the Lennard-Jones README case starts from the reference's state.
+
+The reference has no placement routine for dense ellipsoid fluids. The
+ellipsoid systems here start from an aligned orthorhombic lattice whose cell
+is the particle's bounding box scaled to the target number density (no
+overlaps by construction), with a seeded jitter of positions and a seeded
+small rotation of every particle; the benchmark then equilibrates them with
+the repulsive potentials on the device before timing.
+"""
+import numpy as np
+
+M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+W0, W1 = np.uint32(0x9E3779B9), np.uint32(0xBB67AE85)
+KEY = (0x6D2B79F5, 0x1B873593)
+MASK = np.uint64(0xFFFFFFFF)
+
+
+def philox4x32(ctr, key=KEY):
+    """Vectorised Philox4x32-10 (fortran/xmath.f90:42-76); ctr: (n, 4) uint32."""
+    c = np.asarray(ctr, dtype=np.uint32).reshape(-1, 4)
+    c0, c1, c2, c3 = (c[:, k].astype(np.uint64) for k in range(4))
+    k0, k1 = np.uint32(key[0]), np.uint32(key[1])
+    with np.errstate(over="ignore"):
+        for rnd in range(10):
+            p0 = M0 * c0
+            p1 = M1 * c2
+            hi0, lo0 = p0 >> np.uint64(32), p0 & MASK
+            hi1, lo1 = p1 >> np.uint64(32), p1 & MASK
+            n0 = hi1 ^ c1 ^ np.uint64(k0)
+            n2 = hi0 ^ c3 ^ np.uint64(k1)
+            c0, c1, c2, c3 = n0, lo1, n2, lo0
+            if rnd < 9:
+                k0 = np.uint32(k0 + W0)
+                k1 = np.uint32(k1 + W1)
+    return np.stack([c0, c1, c2, c3], 1).astype(np.uint32)
+
+
+def normal_3seq(c1, c2, c3, c4, key=KEY):
+    """philox_normal_3seq (fortran/xmath.f90:78-113), vectorised; FP64."""
+    n = np.broadcast(c1, c2, c3, c4).shape[0] if np.ndim(c1) else 1
+    ctr = np.zeros((n, 4), dtype=np.uint32)
+    for k, c in enumerate((c1, c2, c3, c4)):
+        ctr[:, k] = np.broadcast_to(np.asarray(c, dtype=np.int64) & 0xFFFFFFFF, (n,)).astype(np.uint32)
+    w = philox4x32(ctr, key).astype(np.float64) * (1.0 / 4294967296.0)
+    u1 = np.maximum(w[:, 0], 1.0e-35)
+    u3 = np.maximum(w[:, 2], 1.0e-35)
+    twopi = 6.283185307179586
+    r1 = np.sqrt(-2.0 * np.log(u1))
+    r2 = np.sqrt(-2.0 * np.log(u3))
+    return np.stack([r1 * np.cos(twopi * w[:, 1]), r1 * np.sin(twopi * w[:, 1]), r2 * np.cos(twopi * w[:, 3])], 1)
+
+
+def fcc_lattice(cells, density):
+    """generate_fcc_lattice: 4 cells^3 points in a cubic box centred on 0, with
+    the reference's four basis orientations. Returns r (n,3), q (n,4), box."""
+    n = 4 * cells ** 3
+    box = (float(n) / density) ** (1.0 / 3.0)
+    cell = box / cells
+    h = cell / 2.0
+    rr3 = 1.0 / np.sqrt(3.0)
+    a, b = np.sqrt((1.0 + rr3) / 2.0), np.sqrt((1.0 - rr3) / 2.0)
+    c = rr3 / np.sqrt(1.0 - rr3 ** 2.0)
+    basis = np.array([[0.0, 0.0, 0.0], [h, h, 0.0], [0.0, h, h], [h, 0.0, h]])
+    qb = np.array([[a, b * c, -b * c, 0.0], [b, -a * c, -a * c, 0.0], [b, a * c, a * c, 0.0], [a, -b * c, b * c, 0.0]])
+    r = np.zeros((n, 3))
+    q = np.zeros((n, 4))
+    m = 0
+    for I in range(cells):
+        for J in range(cells):
+            for K in range(cells):
+                r[m:m + 4] = basis + cell * np.array([I, J, K], dtype=np.float64)
+                q[m:m + 4] = qb
+                m += 4
+    r -= box / 2.0
+    return r, q, box
+
+
+def velocities_to_temperature(n, temp, seed, nc=0, nrigid=1, remove_com=True):
+    """set_velocity_to_temperature: Philox normals with counter
+    (I, int(T*1000), seed, 42), COM removal, then sum v^2 scaled to
+    (6N - NC [-3]) * T * Nrigid (the reference's convention, mass ignored)."""
+    idx = np.arange(1, n + 1, dtype=np.int64)
+    v = normal_3seq(idx, int(temp * 1000), seed, 42)
+    n_dof = 6 * n - nc
+    if remove_com:
+        v = v - v.sum(0) / float(n)
+        n_dof -= 3
+    factor = np.sqrt(float(n_dof) * temp * nrigid / np.sum(v ** 2))
+    return v * factor
+
+
+def random_quaternions(n, seed, key=(0x2545F491, 0x4F6CDD1D)):
+    """Uniform unit quaternions from four Philox normals, seeded."""
+    idx = np.arange(1, n + 1, dtype=np.int64)
+    a = normal_3seq(idx, seed, 7, 0, key)
+    b = normal_3seq(idx, seed, 7, 1, key)
+    q = np.concatenate([a, b[:, :1]], 1)
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q[q[:, 0] < 0] *= -1
+    return q
+
+
+def _small_rotations(n, seed, angle):
+    """Rotations by a seeded random angle <= angle about seeded random axes."""
+    idx = np.arange(1, n + 1, dtype=np.int64)
+    ax = normal_3seq(idx, seed, 11, 0)
+    ax /= np.linalg.norm(ax, axis=1, keepdims=True)
+    u = philox4x32(np.stack([idx, np.full(n, seed), np.full(n, 13), np.zeros(n)], 1).astype(np.uint32))
+    th = angle * (u[:, 0].astype(np.float64) / 4294967296.0)
+    return np.concatenate([np.cos(th / 2)[:, None], np.sin(th / 2)[:, None] * ax], 1)
+
+
+def quat_mul(a, b):
+    w1, x1, y1, z1 = a.T
+    w2, x2, y2, z2 = b.T
+    return np.stack([w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2, w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
+                     w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2], 1)
+
+
+def aligned_lattice(counts, sig, density, seed, jitter=0.02, tilt=0.05):
+    """Orthorhombic lattice of nx*ny*nz particles of full axes sig = (sx, sy, sz),
+    body axes along the lab axes, cell = s * sig with s fixed by the density.
+    Returns r (n,3), q (n,4), box (3,)."""
+    nx, ny, nz = counts
+    n = nx * ny * nz
+    sx, sy, sz = sig
+    s = (1.0 / (density * sx * sy * sz)) ** (1.0 / 3.0)
+    cell = s * np.array([sx, sy, sz])
+    box = cell * np.array([nx, ny, nz], dtype=np.float64)
+    g = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    r = (g + 0.5) * cell - box / 2.0
+    idx = np.arange(1, n + 1, dtype=np.int64)
+    d = normal_3seq(idx, seed, 5, 0)
+    r = r + jitter * np.clip(d, -2.0, 2.0) * cell.min()
+    q = _small_rotations(n, seed, tilt)
+    return r, q, box
+
+
+def angular_momenta(q, inertia, temp, seed):
+    """Thermal body-frame angular momenta L_b ~ sqrt(T I) N(0,1), returned in the lab frame."""
+    n = len(q)
+    idx = np.arange(1, n + 1, dtype=np.int64)
+    lb = normal_3seq(idx, seed, 17, 3) * np.sqrt(temp * inertia)
+    w, x, y, z = q.T
+    R = np.empty((n, 3, 3))
+    R[:, 0] = np.stack([w * w + x * x - y * y - z * z, 2 * (x * y + w * z), 2 * (x * z - w * y)], 1)
+    R[:, 1] = np.stack([2 * (x * y - w * z), w * w - x * x + y * y - z * z, 2 * (y * z + w * x)], 1)
+    R[:, 2] = np.stack([2 * (x * z + w * y), 2 * (y * z - w * x), w * w - x * x - y * y + z * z], 1)
+    return np.einsum("nji,nj->ni", R, lb)
+
+
+def default_inertia(sig, mass=1.0):
+    """initialize_system default (system.f90:619-621): I_x = (s_y^2 + s_z^2)/20 ..."""
+    sx, sy, sz = sig
+    return np.array([(sy ** 2 + sz ** 2) / 20.0, (sx ** 2 + sz ** 2) / 20.0, (sx ** 2 + sy ** 2) / 20.0]) * mass

@@ -1,0 +1,552 @@
+// Integrators of the reference's verlet, quaternion, langevin and nose_hoover
+// modules (fortran/integrators.f90:1-392, :494-676) on FP32 state, one thread
+// per particle, kinetic-energy sums in FP64 (block partials finished by the
+// last block). Quaternion renormalisation is done in FP64.
+#include <cmath>
+
+#include "sg_internal.cuh"
+#include "philox.cuh"
+
+namespace {
+
+struct Geo {
+    float3 box, inv_box;
+    int periodic;
+};
+
+Geo make_geo(const sg_ctx* ctx) {
+    Geo g;
+    g.box = make_float3((float)ctx->box[0], (float)ctx->box[1], (float)ctx->box[2]);
+    g.inv_box = make_float3((float)(1.0 / ctx->box[0]), (float)(1.0 / ctx->box[1]), (float)(1.0 / ctx->box[2]));
+    g.periodic = ctx->periodic;
+    return g;
+}
+
+SG_DEV float3 wrap_pos(float3 r, const Geo& g) {
+    if (g.periodic) {
+        r.x -= roundf(r.x * g.inv_box.x) * g.box.x;
+        r.y -= roundf(r.y * g.inv_box.y) * g.box.y;
+        r.z -= roundf(r.z * g.inv_box.z) * g.box.z;
+    }
+    return r;
+}
+
+// Rotation matrix rows (body axes in the lab frame), integrators.f90:144-152.
+struct Rot { float m[3][3]; };
+SG_DEV Rot rot_of(float w, float x, float y, float z) {
+    Rot r;
+    r.m[0][0] = w * w + x * x - y * y - z * z; r.m[0][1] = 2.f * (x * y + w * z); r.m[0][2] = 2.f * (x * z - w * y);
+    r.m[1][0] = 2.f * (x * y - w * z); r.m[1][1] = w * w - x * x + y * y - z * z; r.m[1][2] = 2.f * (y * z + w * x);
+    r.m[2][0] = 2.f * (x * z + w * y); r.m[2][1] = 2.f * (y * z - w * x); r.m[2][2] = w * w - x * x - y * y + z * z;
+    return r;
+}
+SG_DEV float3 rot_apply(const Rot& r, float3 v) {   // R v (lab -> body)
+    return make_float3(r.m[0][0] * v.x + r.m[0][1] * v.y + r.m[0][2] * v.z,
+                       r.m[1][0] * v.x + r.m[1][1] * v.y + r.m[1][2] * v.z,
+                       r.m[2][0] * v.x + r.m[2][1] * v.y + r.m[2][2] * v.z);
+}
+SG_DEV float3 rot_apply_t(const Rot& r, float3 v) { // R^T v (body -> lab)
+    return make_float3(r.m[0][0] * v.x + r.m[1][0] * v.y + r.m[2][0] * v.z,
+                       r.m[0][1] * v.x + r.m[1][1] * v.y + r.m[2][1] * v.z,
+                       r.m[0][2] * v.x + r.m[1][2] * v.y + r.m[2][2] * v.z);
+}
+
+// Two fixed-point passes for the mid-step quaternion derivative
+// (integrators.f90:140-168, :572-604). Returns qdot of the last pass, the
+// rotation and body-frame angular momentum of that pass.
+SG_DEV float4 q_midpoint(float4 q, float3 L, float3 Iinv, float dt, Rot& rm, float3& Lb) {
+    float4 qn = q;
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const float4 qo = qn;
+        rm = rot_of(qo.x, qo.y, qo.z, qo.w);
+        Lb = rot_apply(rm, L);
+        const float wx = Lb.x * Iinv.x, wy = Lb.y * Iinv.y, wz = Lb.z * Iinv.z;
+        float4 qd;
+        qd.x = 0.5f * (-qo.y * wx - qo.z * wy - qo.w * wz);
+        qd.y = 0.5f * (qo.x * wx + qo.z * wz - qo.w * wy);
+        qd.z = 0.5f * (qo.x * wy - qo.y * wz + qo.w * wx);
+        qd.w = 0.5f * (qo.x * wz + qo.y * wy - qo.z * wx);
+        qn = make_float4(q.x + 0.5f * dt * qd.x, q.y + 0.5f * dt * qd.y, q.z + 0.5f * dt * qd.z, q.w + 0.5f * dt * qd.w);
+        if (it == 1) return qd;
+    }
+    return make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+SG_DEV float4 q_advance(float4 q, float4 qd, float dt) {
+    double w = (double)(q.x + dt * qd.x), x = (double)(q.y + dt * qd.y), y = (double)(q.z + dt * qd.z),
+           z = (double)(q.w + dt * qd.w);
+    double inv = 1.0 / sqrt(w * w + x * x + y * y + z * z);
+    return make_float4((float)(w * inv), (float)(x * inv), (float)(y * inv), (float)(z * inv));
+}
+
+SG_DEV double kin_rot_of(float4 q, float3 L, float3 Iinv) {
+    Rot r = rot_of(q.x, q.y, q.z, q.w);
+    float3 Lb = rot_apply(r, L);
+    return 0.5 * ((double)(Lb.x * Lb.x) * Iinv.x + (double)(Lb.y * Lb.y) * Iinv.y + (double)(Lb.z * Lb.z) * Iinv.z);
+}
+
+// ------------------------------------------------------------------- VV ----
+__global__ void k_vv_initial(int n, float dt, Geo g, float4* __restrict__ pos, float4* __restrict__ vel,
+                             const float4* __restrict__ force) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = vel[i], f = force[i], r = pos[i];
+    const float h = 0.5f * dt, im = v.w;
+    v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
+    float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g);
+    vel[i] = v;
+    pos[i] = make_float4(p.x, p.y, p.z, r.w);
+}
+
+// final half kick; KE = sum 0.5 m v^2 (mass from shape.w)
+__global__ void k_vv_final(int n, float dt, float4* __restrict__ vel, const float4* __restrict__ force,
+                           const float4* __restrict__ shape, double* partials, unsigned int* done, double* acc) {
+    double e[1] = {0.0};
+    const float h = 0.5f * dt;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 v = vel[i], f = force[i];
+        const float im = v.w;
+        v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
+        vel[i] = v;
+        e[0] += 0.5 * (double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+    }
+    block_reduce_finish<1>(e, partials, done, acc);
+}
+
+// --------------------------------------------------------------- rotation --
+__global__ void k_qq_initial(int n, float dt, float4* __restrict__ quat, float4* __restrict__ angm,
+                             const float4* __restrict__ torque, const float4* __restrict__ inert_inv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 L4 = angm[i], T = torque[i], Ii = inert_inv[i];
+    const float h = 0.5f * dt;
+    float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
+    Rot rm;
+    float3 Lb;
+    float4 qd = q_midpoint(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z), dt, rm, Lb);
+    quat[i] = q_advance(quat[i], qd, dt);
+    angm[i] = make_float4(L.x, L.y, L.z, 0.f);
+}
+
+__global__ void k_qq_final(int n, float dt, const float4* __restrict__ quat, float4* __restrict__ angm,
+                           const float4* __restrict__ torque, const float4* __restrict__ inert_inv, double* partials,
+                           unsigned int* done, double* acc) {
+    double e[1] = {0.0};
+    const float h = 0.5f * dt;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 L4 = angm[i], T = torque[i], Ii = inert_inv[i];
+        float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
+        angm[i] = make_float4(L.x, L.y, L.z, 0.f);
+        e[0] += kin_rot_of(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z));
+    }
+    block_reduce_finish<1>(e, partials, done, acc);
+}
+
+// --------------------------------------------------------------- Langevin --
+struct LgvConst {
+    const int* step_dev;   // when set, the step counter is read from the device (captured graphs)
+    float dt, ed, kk12, T;
+    double c2;          // 1 - exp(-2 gamma dt)
+    double rot_amp;     // 2 gamma T dt
+    float kk2;
+    uint32_t step, temp_int, k0, k1;
+};
+
+__global__ void k_lgv_initial(int n, LgvConst c, Geo g, float4* __restrict__ pos, float4* __restrict__ vel,
+                              const float4* __restrict__ force, float4* __restrict__ quat, float4* __restrict__ angm,
+                              const float4* __restrict__ torque, const float4* __restrict__ inert,
+                              const float4* __restrict__ inert_inv, int rotations) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float h = 0.5f * c.dt;
+    float4 v = vel[i], f = force[i], r = pos[i];
+    const float im = v.w;
+    v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
+    float3 p = make_float3(r.x + h * v.x, r.y + h * v.y, r.z + h * v.z);
+    double n1a, n1b, n1c, n2a = 0.0, n2b = 0.0, n2c = 0.0;
+    // counters (I, step, int(T*1000), stream) with I 1-based (integrators.f90:546-547)
+    const uint32_t step = c.step_dev ? (uint32_t)*c.step_dev : c.step;
+    sg_normal_3seq((uint32_t)(i + 1), step, c.temp_int, 0u, c.k0, c.k1, n1a, n1b, n1c);
+    if (rotations) sg_normal_3seq((uint32_t)(i + 1), step, c.temp_int, 1u, c.k0, c.k1, n2a, n2b, n2c);
+    const float amp = (float)sqrt((double)c.T * (double)im * c.c2);
+    v.x = c.ed * v.x + amp * (float)n1a;
+    v.y = c.ed * v.y + amp * (float)n1b;
+    v.z = c.ed * v.z + amp * (float)n1c;
+    p = wrap_pos(make_float3(p.x + h * v.x, p.y + h * v.y, p.z + h * v.z), g);
+    vel[i] = v;
+    pos[i] = make_float4(p.x, p.y, p.z, r.w);
+    if (!rotations) return;
+    float4 L4 = angm[i], T = torque[i], I4 = inert[i], Ii = inert_inv[i];
+    float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
+    Rot rm;
+    float3 Lb;
+    const float4 q = quat[i];
+    float4 qd = q_midpoint(q, L, make_float3(Ii.x, Ii.y, Ii.z), c.dt, rm, Lb);
+    Lb.x = c.kk12 * Lb.x + c.kk2 * (float)sqrt(c.rot_amp * I4.x) * (float)n2a;
+    Lb.y = c.kk12 * Lb.y + c.kk2 * (float)sqrt(c.rot_amp * I4.y) * (float)n2b;
+    Lb.z = c.kk12 * Lb.z + c.kk2 * (float)sqrt(c.rot_amp * I4.z) * (float)n2c;
+    L = rot_apply_t(rm, Lb);
+    angm[i] = make_float4(L.x, L.y, L.z, 0.f);
+    quat[i] = q_advance(q, qd, c.dt);
+}
+
+__global__ void k_lgv_final(int n, float dt, float4* __restrict__ vel, const float4* __restrict__ force,
+                            const float4* __restrict__ shape, const float4* __restrict__ quat,
+                            float4* __restrict__ angm, const float4* __restrict__ torque,
+                            const float4* __restrict__ inert_inv, int rotations, double* partials, unsigned int* done,
+                            double* acc) {
+    double e[2] = {0.0, 0.0};
+    const float h = 0.5f * dt;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 v = vel[i], f = force[i];
+        const float im = v.w;
+        v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
+        vel[i] = v;
+        e[0] += 0.5 * (double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        if (rotations) {
+            float4 L4 = angm[i], T = torque[i], Ii = inert_inv[i];
+            float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
+            angm[i] = make_float4(L.x, L.y, L.z, 0.f);
+            e[1] += kin_rot_of(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z));
+        }
+    }
+    block_reduce_finish<2>(e, partials, done, acc);
+}
+
+// ------------------------------------------------------------ Nose-Hoover --
+// integrators.f90:233-301; chain length 3. nh layout: [0..2] eta, [3..5] p_eta,
+// [6..8] eta_r, [9..11] p_eta_r, [12] translational scale, [13] rotational
+// scale, [14] sum m v^2 scratch, [15] sum L_b^2/I scratch.
+struct NhConst {
+    double dt, T, ndof, nrot;
+    double HB[3], HBr[3];
+};
+
+__device__ double exprel_d(double x) {
+    if (fabs(x) > 0.01) return (exp(x) - 1.0) / x;
+    const double g[5] = {1.0 / 1, 1.0 / 6, 1.0 / 120, 1.0 / 5040, 1.0 / 362880};
+    double y = (x / 2) * (x / 2);
+    double f = g[4];
+    for (int k = 3; k >= 0; --k) f = f * y + g[k];
+    return exp(x / 2) * f;
+}
+
+// u4_propagator: G1 from the supplied sum (m v^2 or L_b^2/I)
+__device__ void u4(double t, int j_start, int j_stop, int stride, double* p, const double* HB, double sum, double ndof,
+                   double T) {
+    for (int j = j_start; stride > 0 ? j <= j_stop : j >= j_stop; j += stride) {
+        double gj = (j == 1) ? (sum - ndof * T) : ((p[j - 2] * p[j - 2] / HB[j - 2]) - T);
+        if (j == 3) {
+            p[2] = p[2] + t * gj;
+        } else {
+            double x = t * p[j] / HB[j];
+            double c = exprel_d(-x);
+            p[j - 1] = p[j - 1] * exp(-x) + t * gj * c;
+        }
+    }
+}
+
+__global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* __restrict__ shape,
+                          const float4* __restrict__ quat, const float4* __restrict__ angm,
+                          const float4* __restrict__ inert_inv, int rot, double* partials, unsigned int* done,
+                          double* dst) {
+    double e[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 v = vel[i];
+        e[0] += (double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        if (rot) {
+            float4 L = angm[i], Ii = inert_inv[i];
+            e[1] += 2.0 * kin_rot_of(quat[i], make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z));
+        }
+    }
+    block_reduce_finish<2>(e, partials, done, dst);
+}
+
+// Standard NHC half step on the chain(s): nh[14], nh[15] hold the sums on
+// entry (zeroed by the host before the reduction). Writes the scale factors.
+__global__ void k_nhc_chain(NhConst c, double* nh, int rot) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double* eta = nh;
+    double* p = nh + 3;
+    double K = nh[14];
+    u4(c.dt / 4.0, 3, 1, -1, p, c.HB, K, c.ndof, c.T);
+    double sc = exp(-0.5 * c.dt * p[0] / c.HB[0]);
+    for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] / c.HB[k];
+    u4(c.dt / 4.0, 1, 3, 1, p, c.HB, K * sc * sc, c.ndof, c.T);
+    nh[12] = sc;
+    nh[16] = K * sc * sc;
+    if (rot) {
+        double* er = nh + 6;
+        double* pr = nh + 9;
+        double Kr = nh[15];
+        u4(c.dt / 4.0, 3, 1, -1, pr, c.HBr, Kr, c.nrot, c.T);
+        double scr = exp(-0.5 * c.dt * pr[0] / c.HBr[0]);
+        for (int k = 0; k < 3; ++k) er[k] = er[k] + 0.5 * c.dt * pr[k] / c.HBr[k];
+        u4(c.dt / 4.0, 1, 3, 1, pr, c.HBr, Kr * scr * scr, c.nrot, c.T);
+        nh[13] = scr;
+    } else {
+        nh[13] = 1.0;
+    }
+}
+
+// scale v (and L), then optionally the VV kick + drift (initial step)
+__global__ void k_nhc_apply(int n, const double* nh, int do_vv, float dt, Geo g, float4* __restrict__ pos,
+                            float4* __restrict__ vel, const float4* __restrict__ force, float4* __restrict__ angm,
+                            int rot) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float sc = (float)nh[12];
+    float4 v = vel[i];
+    v.x *= sc; v.y *= sc; v.z *= sc;
+    if (rot) {
+        const float sr = (float)nh[13];
+        float4 L = angm[i];
+        angm[i] = make_float4(L.x * sr, L.y * sr, L.z * sr, L.w);
+    }
+    if (do_vv) {
+        const float4 f = force[i], r = pos[i];
+        const float h = 0.5f * dt, im = v.w;
+        v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
+        float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g);
+        pos[i] = make_float4(p.x, p.y, p.z, r.w);
+    }
+    vel[i] = v;
+}
+
+__global__ void k_kick(int n, float dt, float4* __restrict__ vel, const float4* __restrict__ force) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = vel[i];
+    const float4 f = force[i];
+    const float h = 0.5f * dt, im = v.w;
+    v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
+    vel[i] = v;
+}
+
+// The reference's per-particle chain (integrators.f90:324-352, :372-390): a
+// serial recurrence over particles in index order. The O(N) SUM that the
+// reference repeats at every particle is carried as a running FP64 sum,
+// updated by each particle's change; per-particle terms are in FP64.
+__global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, float4* __restrict__ pos,
+                            float4* __restrict__ vel, const float4* __restrict__ force,
+                            const float4* __restrict__ shape) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double* eta = nh;
+    double* p = nh + 3;
+    double K = nh[14];
+    double ke = 0.0;
+    const double h = 0.5 * c.dt;
+    for (int i = 0; i < n; ++i) {
+        float4 v = vel[i];
+        const float4 f = force[i];
+        const double m = shape[i].w, im = v.w;
+        double vx = v.x, vy = v.y, vz = v.z;
+        if (!initial) {
+            const double ox = vx, oy = vy, oz = vz;
+            vx = vx + h * (f.x * im); vy = vy + h * (f.y * im); vz = vz + h * (f.z * im);
+            vx = (float)vx; vy = (float)vy; vz = (float)vz;
+            K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
+        }
+        u4(c.dt / 4.0, 3, 1, -1, p, c.HB, K, c.ndof, c.T);
+        const double sc = exp(-0.5 * c.dt * p[0] / c.HB[0]);
+        {
+            const double ox = vx, oy = vy, oz = vz;
+            vx = (float)(vx * sc); vy = (float)(vy * sc); vz = (float)(vz * sc);
+            K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
+        }
+        for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] / c.HB[k];
+        u4(c.dt / 4.0, 1, 3, 1, p, c.HB, K, c.ndof, c.T);
+        if (initial) {
+            const double ox = vx, oy = vy, oz = vz;
+            vx = (float)(vx + h * (f.x * im)); vy = (float)(vy + h * (f.y * im)); vz = (float)(vz + h * (f.z * im));
+            K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
+            const float4 r = pos[i];
+            float3 q = wrap_pos(make_float3(r.x + (float)c.dt * (float)vx, r.y + (float)c.dt * (float)vy,
+                                            r.z + (float)c.dt * (float)vz), g);
+            pos[i] = make_float4(q.x, q.y, q.z, r.w);
+        } else {
+            ke += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        }
+        vel[i] = make_float4((float)vx, (float)vy, (float)vz, v.w);
+    }
+    nh[14] = K;
+    nh[17] = ke;
+}
+
+__global__ void k_half_into(const double* src, double* dst) { *dst = 0.5 * *src; }
+
+int reduce_grid(const sg_ctx* ctx) { return std::max(1, std::min(2 * ctx->num_sms, (ctx->n + 255) / 256)); }
+
+NhConst nh_const(const sg_ctx* ctx, double dt, double T, double coupling) {
+    NhConst c;
+    c.dt = dt;
+    c.T = T;
+    c.ndof = 3.0 * ctx->n - 3.0;            // 3 (N / Nrigid) - 3, Nrigid = 1
+    c.nrot = 3.0 * ctx->n;
+    const double tau = 2.0;
+    for (int k = 0; k < 3; ++k) {
+        c.HB[k] = coupling > 0.0 ? coupling : T * tau * tau;
+        c.HBr[k] = coupling > 0.0 ? coupling : T * tau * tau;
+    }
+    if (!(coupling > 0.0)) {
+        c.HB[0] = c.ndof * T * tau * tau;
+        c.HBr[0] = c.nrot * T * tau * tau;
+    }
+    return c;
+}
+
+int sum_mv2(sg_ctx* ctx, int rot) {
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->nh + 14, 0, sizeof(double) * 2, ctx->stream));
+    int grid = reduce_grid(ctx);
+    if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
+    k_sum_mv2<<<grid, 256, 0, ctx->stream>>>(ctx->n, ctx->vel, ctx->shape, ctx->quat, ctx->angm, ctx->inert_inv, rot,
+                                            ctx->partials, ctx->done_counter, ctx->nh + 14);
+    SG_LAUNCH_CHECK(ctx, "k_sum_mv2");
+    return SG_OK;
+}
+
+int read_acc(sg_ctx* ctx, int idx, double* out) {
+    if (!out) return SG_OK;
+    SG_CUDA(ctx, cudaMemcpyAsync(out, ctx->acc + idx, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sg_vv_initial(sg_ctx* ctx, double dt) {
+    if (!ctx) return SG_EINVAL;
+    k_vv_initial<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, (float)dt, make_geo(ctx), ctx->pos, ctx->vel,
+                                                                ctx->force);
+    SG_LAUNCH_CHECK(ctx, "k_vv_initial");
+    return SG_OK;
+}
+
+int sg_vv_final(sg_ctx* ctx, double dt, double* kin_eng) {
+    if (!ctx) return SG_EINVAL;
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double), ctx->stream));
+    int grid = reduce_grid(ctx);
+    if (int rc = sg_ensure_partials(ctx, grid)) return rc;
+    k_vv_final<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->vel, ctx->force, ctx->shape, ctx->partials,
+                                             ctx->done_counter, ctx->acc + 2);
+    SG_LAUNCH_CHECK(ctx, "k_vv_final");
+    return read_acc(ctx, 2, kin_eng);
+}
+
+int sg_qq_initial(sg_ctx* ctx, double dt) {
+    if (!ctx) return SG_EINVAL;
+    k_qq_initial<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->quat, ctx->angm, ctx->torque,
+                                                                ctx->inert_inv);
+    SG_LAUNCH_CHECK(ctx, "k_qq_initial");
+    return SG_OK;
+}
+
+int sg_qq_final(sg_ctx* ctx, double dt, double* kin_rot) {
+    if (!ctx) return SG_EINVAL;
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 3, 0, sizeof(double), ctx->stream));
+    int grid = reduce_grid(ctx);
+    if (int rc = sg_ensure_partials(ctx, grid)) return rc;
+    k_qq_final<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->quat, ctx->angm, ctx->torque, ctx->inert_inv,
+                                             ctx->partials, ctx->done_counter, ctx->acc + 3);
+    SG_LAUNCH_CHECK(ctx, "k_qq_final");
+    return read_acc(ctx, 3, kin_rot);
+}
+
+int sg_lgv_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double target_temp, const uint32_t* key) {
+    if (!ctx) return SG_EINVAL;
+    LgvConst c;
+    c.step_dev = ctx->lgv_step_dev;
+    c.dt = (float)dt;
+    c.ed = (float)std::exp(-damping * dt);
+    c.c2 = 1.0 - std::exp(-2.0 * damping * dt);
+    const double kk1 = 1.0 - (damping * dt) / 2.0, kk2 = 1.0 / (1.0 + (damping * dt) / 2.0);
+    c.kk12 = (float)(kk2 * kk1);
+    c.kk2 = (float)kk2;
+    c.rot_amp = 2.0 * damping * target_temp * dt;
+    c.T = (float)target_temp;
+    c.step = (uint32_t)step;
+    c.temp_int = (uint32_t)(int32_t)(target_temp * 1000.0);
+    c.k0 = key ? key[0] : SG_PHILOX_KEY0;
+    c.k1 = key ? key[1] : SG_PHILOX_KEY1;
+    k_lgv_initial<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, c, make_geo(ctx), ctx->pos, ctx->vel,
+                                                                 ctx->force, ctx->quat, ctx->angm, ctx->torque,
+                                                                 ctx->inert, ctx->inert_inv, ctx->lgv_rotations);
+    SG_LAUNCH_CHECK(ctx, "k_lgv_initial");
+    return SG_OK;
+}
+
+int sg_lgv_final(sg_ctx* ctx, double dt, double damping, double* kin_eng, double* kin_rot) {
+    (void)damping;
+    if (!ctx) return SG_EINVAL;
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double) * 2, ctx->stream));
+    int grid = reduce_grid(ctx);
+    if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
+    k_lgv_final<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->vel, ctx->force, ctx->shape, ctx->quat,
+                                              ctx->angm, ctx->torque, ctx->inert_inv, ctx->lgv_rotations, ctx->partials,
+                                              ctx->done_counter, ctx->acc + 2);
+    SG_LAUNCH_CHECK(ctx, "k_lgv_final");
+    if (int rc = read_acc(ctx, 2, kin_eng)) return rc;
+    return read_acc(ctx, 3, kin_rot);
+}
+
+int sg_nht_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain) {
+    if (!ctx) return SG_EINVAL;
+    if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
+    NhConst c = nh_const(ctx, dt, target_temp, coupling);
+    const int nb = (ctx->n + 255) / 256;
+    if (mode == 0) {
+        if (rot_chain) return sg_fail(ctx, SG_EINVAL, "the reference chain (mode 0) thermostats translation only");
+        if (int rc = sum_mv2(ctx, 0)) return rc;
+        k_nh_compat<<<1, 32, 0, ctx->stream>>>(ctx->n, c, 1, make_geo(ctx), ctx->nh, ctx->pos, ctx->vel, ctx->force,
+                                               ctx->shape);
+        SG_LAUNCH_CHECK(ctx, "k_nh_compat");
+        return SG_OK;
+    }
+    if (int rc = sum_mv2(ctx, rot_chain)) return rc;
+    k_nhc_chain<<<1, 32, 0, ctx->stream>>>(c, ctx->nh, rot_chain);
+    k_nhc_apply<<<nb, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, 1, (float)dt, make_geo(ctx), ctx->pos, ctx->vel,
+                                             ctx->force, ctx->angm, rot_chain);
+    SG_LAUNCH_CHECK(ctx, "k_nhc_apply");
+    return SG_OK;
+}
+
+int sg_nht_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain,
+                 double* kin_eng) {
+    if (!ctx) return SG_EINVAL;
+    if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
+    NhConst c = nh_const(ctx, dt, target_temp, coupling);
+    const int nb = (ctx->n + 255) / 256;
+    if (mode == 0) {
+        if (rot_chain) return sg_fail(ctx, SG_EINVAL, "the reference chain (mode 0) thermostats translation only");
+        if (int rc = sum_mv2(ctx, 0)) return rc;
+        k_nh_compat<<<1, 32, 0, ctx->stream>>>(ctx->n, c, 0, make_geo(ctx), ctx->nh, ctx->pos, ctx->vel, ctx->force,
+                                               ctx->shape);
+        SG_LAUNCH_CHECK(ctx, "k_nh_compat");
+        SG_CUDA(ctx, cudaMemcpyAsync(ctx->acc + 2, ctx->nh + 17, sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        return read_acc(ctx, 2, kin_eng);
+    }
+    k_kick<<<nb, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->vel, ctx->force);
+    if (int rc = sum_mv2(ctx, rot_chain)) return rc;
+    k_nhc_chain<<<1, 32, 0, ctx->stream>>>(c, ctx->nh, rot_chain);
+    k_nhc_apply<<<nb, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, 0, (float)dt, make_geo(ctx), ctx->pos, ctx->vel,
+                                             ctx->force, ctx->angm, rot_chain);
+    SG_LAUNCH_CHECK(ctx, "k_nhc_apply");
+    // kinetic energy after scaling, summed again in FP64: acc[2] = 0.5 sum m v^2
+    if (int rc = sum_mv2(ctx, 0)) return rc;
+    k_half_into<<<1, 1, 0, ctx->stream>>>(ctx->nh + 14, ctx->acc + 2);
+    SG_LAUNCH_CHECK(ctx, "k_half_into");
+    return read_acc(ctx, 2, kin_eng);
+}
+
+int sg_nht_state(sg_ctx* ctx, double* get12, const double* set12) {
+    if (!ctx) return SG_EINVAL;
+    if (set12) SG_CUDA(ctx, cudaMemcpyAsync(ctx->nh, set12, sizeof(double) * 12, cudaMemcpyHostToDevice, ctx->stream));
+    if (get12) SG_CUDA(ctx, cudaMemcpyAsync(get12, ctx->nh, sizeof(double) * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SG_OK;
+}
+
+}  // extern "C"

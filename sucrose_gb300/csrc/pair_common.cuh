@@ -1,0 +1,165 @@
+// Pair-parallel driver shared by every pair-potential kernel.
+//
+// The half list is flattened into (pair_i, pair_j) with rows in particle
+// order, so the pairs of one particle i are contiguous. Each warp takes 32
+// consecutive pairs; each lane evaluates one pair in the reference's
+// orientation (I = pair_i < J = pair_j), then
+//   * the J-side force and torque go out as one float4 atomic each,
+//   * the I-side terms are summed across lanes with a segmented shuffle scan
+//     (segments = runs of equal i), and the last lane of each run issues one
+//     float4 atomic,
+//   * PE and the pair virial r_ij . F_ij are summed per thread in FP32, then
+//     reduced per block in FP64 and finished deterministically by the last
+//     block (block_reduce_finish).
+// The grid is persistent (a multiple of the SM count); the pair count is read
+// from device memory so the launch needs no host synchronisation.
+#pragma once
+#include "sg_internal.cuh"
+
+struct PairOut {
+    float3 f;    // force on I (FXIJ)
+    float3 ti;   // torque on I (TXI)
+    float3 tj;   // torque on J (TXJ)
+    float pe;
+    float vir;
+};
+
+struct PairLaunch {
+    const int* __restrict__ pair_i;
+    const int* __restrict__ pair_j;
+    const int* npairs;           // device
+    float4* force;
+    float4* torque;
+    double* partials;
+    unsigned int* done;
+    double* acc;                 // per-call sums: acc[0] += PE, acc[1] += virial
+    double* acc_total;           // running sums since the last zero_forces
+    unsigned long long* stats;   // solver statistics (ECP)
+};
+
+SG_DEV void atomic_add_f3(float4* p, float3 v) {
+    atomicAdd(p, make_float4(v.x, v.y, v.z, 0.f));
+}
+
+template <bool TORQUE>
+SG_DEV void segmented_scatter_i(const PairLaunch& L, int i, float3 f, float3 t) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int io = __shfl_up_sync(0xffffffffu, i, o);
+        float fx = __shfl_up_sync(0xffffffffu, f.x, o);
+        float fy = __shfl_up_sync(0xffffffffu, f.y, o);
+        float fz = __shfl_up_sync(0xffffffffu, f.z, o);
+        float tx = 0.f, ty = 0.f, tz = 0.f;
+        if (TORQUE) {
+            tx = __shfl_up_sync(0xffffffffu, t.x, o);
+            ty = __shfl_up_sync(0xffffffffu, t.y, o);
+            tz = __shfl_up_sync(0xffffffffu, t.z, o);
+        }
+        if (lane >= o && io == i) {
+            f.x += fx; f.y += fy; f.z += fz;
+            if (TORQUE) { t.x += tx; t.y += ty; t.z += tz; }
+        }
+    }
+    int inext = __shfl_down_sync(0xffffffffu, i, 1);
+    bool last = (lane == 31) || (inext != i);
+    if (last && i >= 0) {
+        atomic_add_f3(&L.force[i], f);
+        if (TORQUE) atomic_add_f3(&L.torque[i], t);
+    }
+}
+
+#define SG_NSTATS 32
+
+template <class Pot>
+__global__ void __launch_bounds__(256) k_pair(PairLaunch L, Pot pot) {
+    __shared__ unsigned long long sh_stats[SG_NSTATS];
+    if (Pot::kStats) {
+        for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x) sh_stats[k] = 0ull;
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int np = *L.npairs;
+    float pe = 0.f, vir = 0.f;
+    for (int base = gwarp * 32; base < np; base += nwarps * 32) {
+        const int t = base + lane;
+        const bool valid = t < np;
+        int i = -1, j = 0;
+        PairOut o;
+        o.f = make_float3(0.f, 0.f, 0.f);
+        o.ti = o.f;
+        o.tj = o.f;
+        o.pe = 0.f;
+        o.vir = 0.f;
+        if (valid) {
+            i = L.pair_i[t];
+            j = L.pair_j[t];
+        }
+        // called by every lane (warp-cooperative potentials need all 32)
+        pot.eval(valid, valid ? i : 0, j, t, o, sh_stats);
+        if (valid) {
+            atomic_add_f3(&L.force[j], make_float3(-o.f.x, -o.f.y, -o.f.z));
+            if (Pot::kTorque) atomic_add_f3(&L.torque[j], o.tj);
+        }
+        pe += o.pe;
+        vir += o.vir;
+        segmented_scatter_i<Pot::kTorque>(L, i, o.f, o.ti);
+    }
+    if (Pot::kStats) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x)
+            if (sh_stats[k]) atomicAdd(&L.stats[k], sh_stats[k]);
+    }
+    double e[2] = {(double)pe, (double)vir};
+    block_reduce_finish<2>(e, L.partials, L.done, L.acc, L.acc_total);
+}
+
+// Launch helper: persistent grid sized from occupancy.
+template <class Pot>
+int launch_pair(sg_ctx* ctx, const Pot& pot) {
+    if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "pair forces need sg_nlist_init first");
+    PairLaunch L;
+    L.pair_i = ctx->nl.pair_i;
+    L.pair_j = ctx->nl.pair_j;
+    L.npairs = ctx->nl.dev_flags + 2;
+    L.force = ctx->force;
+    L.torque = ctx->torque;
+    L.done = ctx->done_counter;
+    L.acc = ctx->acc + 4;
+    L.acc_total = ctx->acc;
+    L.stats = ctx->stats;
+    int grid = sg_grid_for(ctx, (const void*)k_pair<Pot>, 256, 0);
+    int64_t max_useful = (ctx->nl.pair_capacity + 255) / 256;
+    if (grid > max_useful) grid = (int)std::max<int64_t>(1, max_useful);
+    if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
+    L.partials = ctx->partials;
+    k_pair<Pot><<<grid, 256, 0, ctx->stream>>>(L, pot);
+    SG_LAUNCH_CHECK(ctx, "k_pair");
+    return SG_OK;
+}
+
+struct BoxF {
+    float3 box, inv_box;
+    int periodic;
+};
+
+inline BoxF make_boxf(const sg_ctx* ctx) {
+    BoxF b;
+    b.box = make_float3((float)ctx->box[0], (float)ctx->box[1], (float)ctx->box[2]);
+    b.inv_box = make_float3((float)(1.0 / ctx->box[0]), (float)(1.0 / ctx->box[1]), (float)(1.0 / ctx->box[2]));
+    b.periodic = ctx->periodic;
+    return b;
+}
+
+SG_DEV float3 pair_rij(const float4* __restrict__ pos, int i, int j, const BoxF& b) {
+    float4 a = pos[i], c = pos[j];
+    return min_image(make_float3(a.x - c.x, a.y - c.y, a.z - c.z), b.box, b.inv_box, b.periodic);
+}
+
+SG_DEV float ipowf(float x, int n) {
+    float r = 1.f;
+    for (int k = 0; k < n; ++k) r *= x;
+    return r;
+}

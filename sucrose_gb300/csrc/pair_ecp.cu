@@ -1,0 +1,601 @@
+// Ellipsoid Contact Potential family: ecp_, ecpr_, ecpw_, ecpc_, ecpwc_
+// (fortran/force.f90:1034-2236), with three contact-parameter solvers.
+//
+// Per particle (k_ecp_prep, once per call) the reference's per-pair setup is
+// hoisted: A_R = U^T S^2 U and A_E = U^T E U (matmul_atba, :1294-1297), the
+// body z axis and the sigma_t factor (:1299). Per pair, in FP32:
+//   EAB = A_R + B_R, eps1 = sigma_t sqrt(det EAB^-1)            (:1303-1305)
+//   lambda maximising S(l) = l(1-l) r^T [(1-l)A_R + l B_R]^-1 r    (:1307)
+//   K_E, K_R by 3x3 Cholesky, eps2, phi, sigma = phi^-1/2        (:1310-1321)
+//   envelope, forces and torques, taper                          (:1325-1376)
+// d eps1/d u is summed over the three body axes in the reference (:1346-1352);
+// sum_k m_k x (EM m_k) with m_k = s_k u_k equals the axial vector of
+// EM A_R, which is what is evaluated here (same value, 18 instead of 45 FMAs).
+//
+// Solvers:
+//   BRENT_COMPAT  the reference's Brent (:1046-1172) in FP64 with every
+//                 operation rounded once, in the reference's order: the same
+//                 lambda bits as the FP64 reference on the same input.
+//   NEWTON        Newton on S'(l) = (1-2l) r.K - l(1-l) K.D.K (D = B_R - A_R)
+//                 in FP32 with bracketing, from l = 1/2, then an FP64 check
+//                 of |S'| (one step of FP64 iterative refinement of K).
+//   MLP_NEWTON    the same Newton from the learned guess, at most three
+//                 steps, else the plain Newton (counted as a fallback).
+#include <cmath>
+
+#include "pair_common.cuh"
+#include "ecp_mlp.cuh"
+
+namespace {
+
+// ------------------------------------------------------------------ prep ---
+__global__ void k_ecp_prep(int n, const float4* __restrict__ quat, const float4* __restrict__ shape,
+                           const float4* __restrict__ eshape, float muinv, float4* __restrict__ prep,
+                           double* __restrict__ prep64) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float4 q = quat[p];
+    const float w = q.x, x = q.y, y = q.z, z = q.w;
+    // rows of the reference's U (rotation_matrix form, :1244-1252): body axes in the lab frame
+    float u[3][3];
+    u[0][0] = w * w + x * x - y * y - z * z; u[0][1] = 2.f * (x * y + w * z); u[0][2] = 2.f * (x * z - w * y);
+    u[1][0] = 2.f * (x * y - w * z); u[1][1] = w * w - x * x + y * y - z * z; u[1][2] = 2.f * (y * z + w * x);
+    u[2][0] = 2.f * (x * z + w * y); u[2][1] = 2.f * (y * z - w * x); u[2][2] = w * w - x * x - y * y + z * z;
+    const float4 s4 = shape[p], e4 = eshape[p];
+    const float sg[3] = {s4.x, s4.y, s4.z};
+    const float ep[3] = {e4.x, e4.y, e4.z};
+    const float e0 = fmaxf(fmaxf(ep[0], ep[1]), ep[2]);
+    float s2[3], E[3];
+    for (int k = 0; k < 3; ++k) {
+        float h = 0.5f * sg[k];
+        s2[k] = h * h;
+        E[k] = powf(e0 / ep[k], muinv) * 0.25f;
+    }
+    float A[6], B[6];
+    const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+    for (int m = 0; m < 6; ++m) {
+        float a = 0.f, b = 0.f;
+        for (int k = 0; k < 3; ++k) {
+            float uu = u[k][ia[m]] * u[k][ib[m]];
+            a += s2[k] * uu;
+            b += E[k] * uu;
+        }
+        A[m] = a;
+        B[m] = b;
+    }
+    const float st = (sg[0] * sg[1] + sg[2] * sg[2]) * sqrtf(2.f * sg[0] * sg[1]) * 0.125f;
+    prep[4 * p + 0] = make_float4(A[0], A[1], A[2], A[3]);
+    prep[4 * p + 1] = make_float4(A[4], A[5], B[0], B[1]);
+    prep[4 * p + 2] = make_float4(B[2], B[3], B[4], B[5]);
+    prep[4 * p + 3] = make_float4(u[2][0], u[2][1], u[2][2], st);
+    if (prep64) {
+        // A_R in FP64 with the reference's operation order (xmath.f90:194-208, :262-279)
+        const double W = w, X = x, Y = y, Z = z;
+        double r[3][3];
+        r[0][0] = __dsub_rn(__dsub_rn(__dadd_rn(__dmul_rn(W, W), __dmul_rn(X, X)), __dmul_rn(Y, Y)), __dmul_rn(Z, Z));
+        r[0][1] = __dmul_rn(2.0, __dadd_rn(__dmul_rn(X, Y), __dmul_rn(W, Z)));
+        r[0][2] = __dmul_rn(2.0, __dsub_rn(__dmul_rn(X, Z), __dmul_rn(W, Y)));
+        r[1][0] = __dmul_rn(2.0, __dsub_rn(__dmul_rn(X, Y), __dmul_rn(W, Z)));
+        r[1][1] = __dsub_rn(__dadd_rn(__dsub_rn(__dmul_rn(W, W), __dmul_rn(X, X)), __dmul_rn(Y, Y)), __dmul_rn(Z, Z));
+        r[1][2] = __dmul_rn(2.0, __dadd_rn(__dmul_rn(Y, Z), __dmul_rn(W, X)));
+        r[2][0] = __dmul_rn(2.0, __dadd_rn(__dmul_rn(X, Z), __dmul_rn(W, Y)));
+        r[2][1] = __dmul_rn(2.0, __dsub_rn(__dmul_rn(Y, Z), __dmul_rn(W, X)));
+        r[2][2] = __dadd_rn(__dsub_rn(__dsub_rn(__dmul_rn(W, W), __dmul_rn(X, X)), __dmul_rn(Y, Y)), __dmul_rn(Z, Z));
+        double b[3];
+        for (int k = 0; k < 3; ++k) {
+            double h = __ddiv_rn((double)sg[k], 2.0);
+            b[k] = __dmul_rn(h, h);
+        }
+        for (int m = 0; m < 6; ++m) {
+            const int c1 = ia[m], c2 = ib[m];
+            double t0 = __dmul_rn(__dmul_rn(r[0][c1], b[0]), r[0][c2]);
+            double t1 = __dmul_rn(__dmul_rn(r[1][c1], b[1]), r[1][c2]);
+            double t2 = __dmul_rn(__dmul_rn(r[2][c1], b[2]), r[2][c2]);
+            prep64[6 * (size_t)p + m] = __dadd_rn(__dadd_rn(t0, t1), t2);
+        }
+    }
+}
+
+// ------------------------------------------------------------- 3x3 SPD ----
+// symmetric storage: 0 xx, 1 xy, 2 xz, 3 yy, 4 yz, 5 zz
+struct Chol { float i11, l21, l31, i22, l32, i33; };
+
+SG_DEV Chol chol(const float* g) {
+    Chol c;
+    c.i11 = rsqrtf(g[0]);
+    c.l21 = g[1] * c.i11;
+    c.l31 = g[2] * c.i11;
+    c.i22 = rsqrtf(g[3] - c.l21 * c.l21);
+    c.l32 = (g[4] - c.l31 * c.l21) * c.i22;
+    c.i33 = rsqrtf(g[5] - c.l31 * c.l31 - c.l32 * c.l32);
+    return c;
+}
+
+SG_DEV float3 chol_solve(const Chol& c, float3 b) {
+    float y1 = b.x * c.i11;
+    float y2 = (b.y - c.l21 * y1) * c.i22;
+    float y3 = (b.z - c.l31 * y1 - c.l32 * y2) * c.i33;
+    float x3 = y3 * c.i33;
+    float x2 = (y2 - c.l32 * x3) * c.i22;
+    float x1 = (y1 - c.l21 * x2 - c.l31 * x3) * c.i11;
+    return make_float3(x1, x2, x3);
+}
+
+SG_DEV float3 symv(const float* m, float3 v) {
+    return make_float3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[1] * v.x + m[3] * v.y + m[4] * v.z,
+                       m[2] * v.x + m[4] * v.y + m[5] * v.z);
+}
+
+// Axial vector of M = S1 * S2 (both symmetric): v_a = eps_abc M_cb.
+SG_DEV float3 axial_prod(const float* s1, const float* s2) {
+    // M_cb = sum_k s1[c][k] s2[k][b]
+    auto e = [](const float* s, int r, int c) {
+        const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+        return s[idx[r][c]];
+    };
+    auto M = [&](int c, int b) { return e(s1, c, 0) * e(s2, 0, b) + e(s1, c, 1) * e(s2, 1, b) + e(s1, c, 2) * e(s2, 2, b); };
+    return make_float3(M(2, 1) - M(1, 2), M(0, 2) - M(2, 0), M(1, 0) - M(0, 1));
+}
+
+// --------------------------------------------------- FP64 reference Brent --
+struct DPair { double ar[6], br[6]; double r[3]; };
+
+__device__ __forceinline__ double ref_optim_dist(double L, const DPair& p) {
+    // G = (1-L)*AR + L*BR elementwise (force.f90:1195)
+    const double oml = __dsub_rn(1.0, L);
+    double g[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) g[m] = __dadd_rn(__dmul_rn(oml, p.ar[m]), __dmul_rn(L, p.br[m]));
+    // cholesky_solve (xmath.f90:281-304)
+    const double inv_l11 = __ddiv_rn(1.0, __dsqrt_rn(g[0]));
+    const double l21 = __dmul_rn(g[1], inv_l11);
+    const double l31 = __dmul_rn(g[2], inv_l11);
+    const double inv_l22 = __ddiv_rn(1.0, __dsqrt_rn(__dsub_rn(g[3], __dmul_rn(l21, l21))));
+    const double l32 = __dmul_rn(__dsub_rn(g[4], __dmul_rn(l31, l21)), inv_l22);
+    const double inv_l33 = __ddiv_rn(1.0, __dsqrt_rn(__dsub_rn(__dsub_rn(g[5], __dmul_rn(l31, l31)), __dmul_rn(l32, l32))));
+    const double y1 = __dmul_rn(p.r[0], inv_l11);
+    const double y2 = __dmul_rn(__dsub_rn(p.r[1], __dmul_rn(l21, y1)), inv_l22);
+    const double y3 = __dmul_rn(__dsub_rn(__dsub_rn(p.r[2], __dmul_rn(l31, y1)), __dmul_rn(l32, y2)), inv_l33);
+    const double k3 = __dmul_rn(y3, inv_l33);
+    const double k2 = __dmul_rn(__dsub_rn(y2, __dmul_rn(l32, k3)), inv_l22);
+    const double k1 = __dmul_rn(__dsub_rn(__dsub_rn(y1, __dmul_rn(l21, k2)), __dmul_rn(l31, k3)), inv_l11);
+    const double dot = __dadd_rn(__dadd_rn(__dmul_rn(p.r[0], k1), __dmul_rn(p.r[1], k2)), __dmul_rn(p.r[2], k3));
+    return -__dmul_rn(__dmul_rn(L, oml), dot);
+}
+
+// brent (force.f90:1046-1172): atol 1e-3, rtol 1e-2, <= 10000 iterations,
+// including the two evaluations at a and b that the reference discards.
+__device__ double ref_brent(const DPair& pair, int& nevals) {
+    const int max_iter = 10000;
+    const double psi = __dmul_rn(0.5, __dsub_rn(3.0, __dsqrt_rn(5.0)));
+    const double atol = 1e-3, rtol = 1e-2;
+    double a = 0.0, b = 1.0;
+    double c = __dadd_rn(__dmul_rn(__dsub_rn(1.0, psi), a), __dmul_rn(psi, b));
+    volatile double fa = ref_optim_dist(a, pair);
+    volatile double fb = ref_optim_dist(b, pair);
+    (void)fa; (void)fb;
+    double fc = ref_optim_dist(c, pair);
+    nevals = 3;
+    double v = c, w = v, x = w;
+    double fv = fc, fw = fv, ft = fw;
+    double deltax = 0.0, rat = 0.0;
+    for (int iter = 0; iter < max_iter; ++iter) {
+        const double tol1 = __dadd_rn(__dmul_rn(rtol, fabs(x)), atol);
+        const double tol2 = __dmul_rn(2.0, tol1);
+        const double xmid = __dmul_rn(0.5, __dadd_rn(a, b));
+        if (fabs(__dsub_rn(x, xmid)) < __dsub_rn(tol2, __dmul_rn(0.5, __dsub_rn(b, a)))) break;
+        if (fabs(deltax) <= tol1) {
+            deltax = (x >= xmid) ? __dsub_rn(a, x) : __dsub_rn(b, x);
+            rat = __dmul_rn(psi, deltax);
+        } else {
+            double tmp1 = __dmul_rn(__dsub_rn(x, w), __dsub_rn(ft, fv));
+            double tmp2 = __dmul_rn(__dsub_rn(x, v), __dsub_rn(ft, fw));
+            double pp = __dsub_rn(__dmul_rn(__dsub_rn(x, v), tmp2), __dmul_rn(__dsub_rn(x, w), tmp1));
+            tmp2 = __dmul_rn(2.0, __dsub_rn(tmp2, tmp1));
+            if (tmp2 > 0.0) pp = -pp;
+            tmp2 = fabs(tmp2);
+            const double dx_temp = deltax;
+            deltax = rat;
+            if ((pp > __dmul_rn(tmp2, __dsub_rn(a, x))) && (pp < __dmul_rn(tmp2, __dsub_rn(b, x))) &&
+                (fabs(pp) < fabs(__dmul_rn(__dmul_rn(0.5, tmp2), dx_temp)))) {
+                rat = __ddiv_rn(__dmul_rn(pp, 1.0), tmp2);
+                const double u = __dadd_rn(x, rat);
+                if (__dsub_rn(u, a) < tol2 || __dsub_rn(b, u) < tol2) rat = (__dsub_rn(xmid, x) >= 0) ? tol1 : -tol1;
+            } else {
+                deltax = (x >= xmid) ? __dsub_rn(a, x) : __dsub_rn(b, x);
+                rat = __dmul_rn(psi, deltax);
+            }
+        }
+        double u;
+        if (fabs(rat) < tol1) u = (rat >= 0) ? __dadd_rn(x, tol1) : __dsub_rn(x, tol1);
+        else u = __dadd_rn(x, rat);
+        const double fu = ref_optim_dist(u, pair);
+        ++nevals;
+        if (fu > ft) {
+            if (u < x) a = u; else b = u;
+            if ((fu <= fw) || (w == x)) { v = w; w = u; fv = fw; fw = fu; }
+            else if ((fu <= fv) || (v == x) || (v == w)) { v = u; fv = fu; }
+        } else {
+            if (u >= x) a = x; else b = x;
+            v = w; w = x; x = u;
+            fv = fw; fw = ft; ft = fu;
+        }
+    }
+    return x;
+}
+
+// -------------------------------------------------------- Newton (FP32) ----
+// Bracketed Newton on S'(l) in FP32. Quadratic convergence makes the step
+// after one of size < step_tol land at the FP32 noise floor, so that step is
+// taken, K is recomputed at the new lambda, and the loop ends.
+struct NewtonResult { float lam; int iters; bool converged; Chol c; float3 K; };
+
+SG_DEV NewtonResult newton_solve(const float* A, const float* D, float3 r, float lam0, int max_iter, float step_tol) {
+    NewtonResult res;
+    float lam = lam0, lo = 0.f, hi = 1.f;
+    res.converged = false;
+    res.iters = 0;
+    float g[6];
+    for (int it = 0; it < max_iter; ++it) {
+#pragma unroll
+        for (int m = 0; m < 6; ++m) g[m] = fmaf(lam, D[m], A[m]);
+        res.c = chol(g);
+        res.K = chol_solve(res.c, r);
+        res.lam = lam;
+        res.iters = it + 1;
+        const float3 DK = symv(D, res.K);
+        const float3 Z = chol_solve(res.c, DK);
+        const float rK = dot3(r, res.K), KDK = dot3(res.K, DK), DKZ = dot3(DK, Z);
+        const float l1 = lam * (1.f - lam);
+        const float s1 = (1.f - 2.f * lam) * rK - l1 * KDK;
+        const float s2 = -2.f * rK - 2.f * (1.f - 2.f * lam) * KDK + 2.f * l1 * DKZ;
+        if (s1 == 0.f) { res.converged = true; break; }
+        if (s1 > 0.f) lo = lam; else hi = lam;
+        float ln = (s2 < 0.f) ? lam - s1 / s2 : 0.5f * (lo + hi);
+        if (!(ln > lo && ln < hi)) ln = 0.5f * (lo + hi);
+        const bool last = fabsf(ln - lam) < step_tol;
+        lam = ln;
+        if (last) {
+#pragma unroll
+            for (int m = 0; m < 6; ++m) g[m] = fmaf(lam, D[m], A[m]);
+            res.c = chol(g);
+            res.K = chol_solve(res.c, r);
+            res.lam = lam;
+            res.converged = true;
+            break;
+        }
+    }
+    return res;
+}
+
+// Normalised FP64 residual S'(lambda) / (r.K), with one step of FP64
+// iterative refinement of K = G^-1 r (G and the residual r - G K in FP64,
+// the correction solved with the FP32 factor). Also returns S'' from FP32.
+SG_DEV double residual64(const float* A, const float* D, float3 r, float lam, const Chol& c, float3 K, float& s2) {
+    const double L = lam;
+    double g[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) g[m] = (double)A[m] + L * (double)D[m];
+    const double kx = K.x, ky = K.y, kz = K.z;
+    const double ex = (double)r.x - (g[0] * kx + g[1] * ky + g[2] * kz);
+    const double ey = (double)r.y - (g[1] * kx + g[3] * ky + g[4] * kz);
+    const double ez = (double)r.z - (g[2] * kx + g[4] * ky + g[5] * kz);
+    const float3 dk = chol_solve(c, make_float3((float)ex, (float)ey, (float)ez));
+    const double Kx = kx + dk.x, Ky = ky + dk.y, Kz = kz + dk.z;
+    const double dkx = D[0] * Kx + D[1] * Ky + D[2] * Kz;
+    const double dky = D[1] * Kx + D[3] * Ky + D[4] * Kz;
+    const double dkz = D[2] * Kx + D[4] * Ky + D[5] * Kz;
+    const double rK = r.x * Kx + r.y * Ky + r.z * Kz;
+    const double KDK = Kx * dkx + Ky * dky + Kz * dkz;
+    const float3 DK = symv(D, K);
+    const float3 Z = chol_solve(c, DK);
+    const float l1 = lam * (1.f - lam);
+    s2 = -2.f * dot3(r, K) - 2.f * (1.f - 2.f * lam) * dot3(K, DK) + 2.f * l1 * dot3(DK, Z);
+    const double s1 = (1.0 - 2.0 * L) * rK - L * (1.0 - L) * KDK;
+    return s1 / fmax(rK, 1e-30);
+}
+
+template <int SOLVER>
+struct PotECP {
+    static constexpr bool kTorque = true;
+    static constexpr bool kStats = true;
+    const float4* __restrict__ pos;
+    const float4* __restrict__ quat;
+    const float4* __restrict__ shape;
+    const float4* __restrict__ prep;
+    const double* __restrict__ prep64;
+    float* __restrict__ lam_out;
+    MlpDev mlp;
+    BoxF b;
+    double bx, by, bz;
+    int kind, mu, nu, max_iter, fp64_check;
+    float cutoff, wf, chirality, tol, step_tol;
+    bool weld, chiral, rep;
+
+    SG_DEV void eval(bool valid, int i, int j, int t, PairOut& o, unsigned long long* sh) const;
+    SG_DEV float solve_lambda(int i, int j, float3 r, const float* A, const float* Bm, float lam0, Chol& cR,
+                              float3& KR, unsigned& evals, unsigned& iters, bool& nonconv, bool& fallback,
+                              bool& refined) const;
+};
+
+template <int SOLVER>
+SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A, const float* Bm, float lam0,
+                                          Chol& cR, float3& KR, unsigned& evals, unsigned& iters, bool& nonconv,
+                                          bool& fallback, bool& refined) const {
+    float D[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) D[m] = Bm[m] - A[m];
+    float lam;
+    if (SOLVER == SG_SOLVER_BRENT_COMPAT) {
+        DPair dp;
+        const float4 a = pos[i], c = pos[j];
+        double dx = __dsub_rn((double)a.x, (double)c.x), dy = __dsub_rn((double)a.y, (double)c.y),
+               dz = __dsub_rn((double)a.z, (double)c.z);
+        if (b.periodic) {
+            dx = __dsub_rn(dx, __dmul_rn(round(__ddiv_rn(dx, bx)), bx));
+            dy = __dsub_rn(dy, __dmul_rn(round(__ddiv_rn(dy, by)), by));
+            dz = __dsub_rn(dz, __dmul_rn(round(__ddiv_rn(dz, bz)), bz));
+        }
+        dp.r[0] = dx; dp.r[1] = dy; dp.r[2] = dz;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) { dp.ar[m] = prep64[6 * (size_t)i + m]; dp.br[m] = prep64[6 * (size_t)j + m]; }
+        int nev = 0;
+        lam = (float)ref_brent(dp, nev);
+        evals = nev;
+        iters = nev;
+        float g[6];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) g[m] = fmaf(lam, D[m], A[m]);
+        cR = chol(g);
+        KR = chol_solve(cR, r);
+        return lam;
+    }
+    const int budget = (SOLVER == SG_SOLVER_MLP_NEWTON) ? 3 : max_iter;
+    NewtonResult nr = newton_solve(A, D, r, lam0, budget, step_tol);
+    evals = nr.iters;
+    if (SOLVER == SG_SOLVER_MLP_NEWTON && !nr.converged) {
+        fallback = true;
+        nr = newton_solve(A, D, r, 0.5f, max_iter, step_tol);
+        evals += nr.iters;
+    }
+    iters = nr.iters;
+    lam = nr.lam;
+    nonconv = !nr.converged;
+    if (fp64_check) {
+        float s2;
+        const double rho = residual64(A, D, r, lam, nr.c, nr.K, s2);
+        if (fabs(rho) > (double)tol) {
+            // one Newton step driven by the FP64 residual
+            refined = true;
+            evals += 1;
+            if (s2 < 0.f) {
+                const double rK = dot3(r, nr.K);
+                const float ln = lam - (float)(rho * rK / (double)s2);
+                if (ln > 0.f && ln < 1.f) {
+                    lam = ln;
+                    float g[6];
+#pragma unroll
+                    for (int m = 0; m < 6; ++m) g[m] = fmaf(lam, D[m], A[m]);
+                    nr.c = chol(g);
+                    nr.K = chol_solve(nr.c, r);
+                }
+            }
+            if (fabs(residual64(A, D, r, lam, nr.c, nr.K, s2)) > (double)tol) nonconv = true;
+        }
+    }
+    cR = nr.c;
+    KR = nr.K;
+    return lam;
+}
+
+template <int SOLVER>
+SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, unsigned long long* sh) const {
+    const float3 r = pair_rij(pos, i, j, b);     // invalid lanes evaluate (0,0): never used
+    float lam0 = 0.5f;
+    if (SOLVER == SG_SOLVER_MLP_NEWTON) {
+        float f[16];
+        mlp_features(valid ? r : make_float3(1.f, 0.f, 0.f), quat[i], quat[j], shape[i], shape[j], f);
+        lam0 = mlp_warp_guess(mlp, f);   // all 32 lanes
+    }
+    const float rsq = dot3(r, r);
+    const float rinv = rsqrtf(rsq);
+    const float rmag = rsq * rinv;
+    const float3 rhat = rinv * r;
+    const float4 pi0 = prep[4 * i], pi1 = prep[4 * i + 1], pi2 = prep[4 * i + 2], pi3 = prep[4 * i + 3];
+    const float4 pj0 = prep[4 * j], pj1 = prep[4 * j + 1], pj2 = prep[4 * j + 2], pj3 = prep[4 * j + 3];
+    const float A[6] = {pi0.x, pi0.y, pi0.z, pi0.w, pi1.x, pi1.y};
+    const float Bm[6] = {pj0.x, pj0.y, pj0.z, pj0.w, pj1.x, pj1.y};
+    const float AE[6] = {pi1.z, pi1.w, pi2.x, pi2.y, pi2.z, pi2.w};
+    const float BE[6] = {pj1.z, pj1.w, pj2.x, pj2.y, pj2.z, pj2.w};
+
+    unsigned evals = 0, iters = 0;
+    bool nonconv = false, fallback = false, refined = false;
+    Chol cR;
+    float3 KR = make_float3(0.f, 0.f, 0.f);
+    float lam = 0.5f;
+    if (valid) {
+        lam = solve_lambda(i, j, r, A, Bm, lam0, cR, KR, evals, iters, nonconv, fallback, refined);
+        if (lam_out) lam_out[t] = lam;
+    }
+    {
+        // warp-aggregated solver statistics into the block's shared counters
+        const unsigned full = 0xffffffffu;
+        const int lane = threadIdx.x & 31;
+        const unsigned ev = __reduce_add_sync(full, valid ? evals : 0u);
+        const unsigned np = __popc(__ballot_sync(full, valid));
+        const unsigned nc = __popc(__ballot_sync(full, valid && nonconv));
+        const unsigned fb = __popc(__ballot_sync(full, valid && fallback));
+        const unsigned rf = __popc(__ballot_sync(full, valid && refined));
+        const unsigned key = valid ? min(iters, 23u) : 255u;
+        const unsigned peers = __match_any_sync(full, key);
+        if (key != 255u && lane == __ffs(peers) - 1) atomicAdd(&sh[4 + key], (unsigned long long)__popc(peers));
+        if (lane == 0) {
+            atomicAdd(&sh[0], (unsigned long long)np);
+            atomicAdd(&sh[1], (unsigned long long)ev);
+            if (nc) atomicAdd(&sh[2], (unsigned long long)nc);
+            if (fb) atomicAdd(&sh[3], (unsigned long long)fb);
+            if (rf) atomicAdd(&sh[28], (unsigned long long)rf);
+        }
+    }
+    if (!valid) return;
+    // eps1 = sigma_t sqrt(det (A+B)^-1); EM = (A+B)^-1 (symmetric)
+    float S[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) S[m] = A[m] + Bm[m];
+    const float c00 = S[3] * S[5] - S[4] * S[4], c01 = S[2] * S[4] - S[1] * S[5], c02 = S[1] * S[4] - S[2] * S[3];
+    const float c11 = S[0] * S[5] - S[2] * S[2], c12 = S[1] * S[2] - S[0] * S[4], c22 = S[0] * S[3] - S[1] * S[1];
+    const float det = S[0] * c00 + S[1] * c01 + S[2] * c02;
+    const float idet = 1.f / det;
+    const float EM[6] = {c00 * idet, c01 * idet, c02 * idet, c11 * idet, c12 * idet, c22 * idet};
+    const float eps1 = sqrtf(pi3.w * pj3.w * idet);
+    const float oml = 1.f - lam;
+    float GE[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) GE[m] = oml * AE[m] + lam * BE[m];
+    const Chol cE = chol(GE);
+    const float3 KE = chol_solve(cE, r);
+    const float l1 = lam * oml;
+    const float rKE = dot3(r, KE), rKR = dot3(r, KR);
+    const float inv_rsq = rinv * rinv;
+    const float eps2 = l1 * rKE * inv_rsq;
+    const float phi = l1 * rKR * inv_rsq;
+    const float sigma = rsqrtf(phi);
+    const float fac = 2.f * l1 * inv_rsq;   // efac = rfac (lambda_E = lambda_R, force.f90:1308)
+    const float pi32 = sigma * sigma * sigma;
+    const float reach = weld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
+    const bool active = rep ? (rmag <= sigma) : (rmag < reach);
+    if (!active) return;
+    float sr;
+    if (weld) {
+        if (rmag < sigma) sr = 1.f / (rmag - sigma + 1.f);
+        else if (rmag <= sigma + wf) sr = 1.f;
+        else sr = 1.f / (rmag - sigma + 1.f - wf);
+    } else {
+        sr = 1.f / (rmag - sigma + 1.f);
+    }
+    const float sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+    float srx = sr12 - 2.f * sr6;
+    if (rep) srx += 1.f;
+    float srd = 12.f * (sr6 - sr12) * sr;
+    const float e1n = ipowf(eps1, nu), e2m = ipowf(eps2, mu);
+    const float ee = e1n * e2m;
+    const float e2fac = e1n * ((float)mu * ipowf(eps2, mu - 1));
+    const float e1fac = e2m * ((float)nu * ipowf(eps1, nu));
+    const float rhKR = rKR * rinv, rhKE = rKE * rinv;
+    const float3 dR_dr = rhat + (0.5f * fac * pi32) * (KR - rhKR * rhat);
+    const float3 de2_dr = (e2fac * fac) * (KE - rhKE * rhat);
+    const float3 ax1 = axial_prod(EM, A), ax2 = axial_prod(EM, Bm);
+    const float3 xa = cross3(symv(AE, KE), KE), xb = cross3(symv(A, KR), KR);
+    const float3 xc = cross3(symv(BE, KE), KE), xd = cross3(symv(Bm, KR), KR);
+    // terms without the envelope factors srx / srd
+    const float3 de1_du1 = e1fac * ax1, de1_du2 = e1fac * ax2;
+    const float3 de2_du1 = (e2fac * oml * fac) * xa, de2_du2 = (e2fac * lam * fac) * xc;
+    const float3 dR_du1 = (ee * 0.5f * oml * fac * pi32) * xb, dR_du2 = (ee * 0.5f * lam * fac * pi32) * xd;
+    float pot = ee * srx;
+    float3 F = -1.f * ((ee * srd) * dR_dr + srx * de2_dr);
+    float3 TQ1 = srx * (de1_du1 + de2_du1) + srd * dR_du1;
+    float3 TQ2 = srx * (de1_du2 + de2_du2) + srd * dR_du2;
+    if (chiral) {
+        // ecpc_ (force.f90:1774-1826) / ecpwc_ (:2021-2073)
+        if (kind == SG_ECPC) { srx = sr6 * sr; srd = -7.f * sr6 * sr2; }
+        else { srx = sr12 - (12.f / 7.f) * sr6 * sr; srd = 12.f * (sr6 * sr2 - sr12 * sr); }
+        const float3 u1z = make_float3(pi3.x, pi3.y, pi3.z), u2z = make_float3(pj3.x, pj3.y, pj3.z);
+        const float3 u1xu2 = cross3(u1z, u2z), u2xr = cross3(u2z, rhat), rxu1 = cross3(rhat, u1z);
+        const float uur = dot3(u1xu2, rhat), uu = dot3(u1z, u2z);
+        const float su = srx * uur * uu, du = srd * uur * uu;
+        const float3 Fc = -1.f * (su * de2_dr + (du * ee) * dR_dr + ((ee * srx * uu) * rinv) * (u1xu2 - uur * rhat));
+        const float3 t1 = (ee * srx * uu) * u2xr + (ee * srx * uur) * u2z;
+        const float3 t2 = (ee * srx * uu) * rxu1 + (ee * srx * uur) * u1z;
+        const float3 T1c = su * (de1_du1 + de2_du1) + du * dR_du1 - cross3(u1z, t1);
+        const float3 T2c = su * (de1_du2 + de2_du2) + du * dR_du2 - cross3(u2z, t2);
+        pot += chirality * (ee * srx * uur * uu);
+        F = F + chirality * Fc;
+        TQ1 = TQ1 + chirality * T1c;
+        TQ2 = TQ2 + chirality * T2c;
+    }
+    if (!rep) {
+        const float sw = 0.9f * reach;
+        if (rmag >= sw && rmag <= reach) {
+            const float factor = 1.f / (reach - sw);
+            const float xx = (rmag - sw) * factor;
+            const float x2 = xx * xx, x3 = x2 * xx;
+            const float sx = 1.f - 6.f * x3 * x2 + 15.f * x2 * x2 - 10.f * x3;
+            const float sdx = -30.f * x2 * x2 + 60.f * x3 - 30.f * x2;
+            const float sub = sdx * pot * factor;   // scalar subtracted from each component (reference quirk)
+            F = make_float3(sx * F.x - sub, sx * F.y - sub, sx * F.z - sub);
+            TQ1 = make_float3(sx * TQ1.x - sub, sx * TQ1.y - sub, sx * TQ1.z - sub);
+            TQ2 = make_float3(sx * TQ2.x - sub, sx * TQ2.y - sub, sx * TQ2.z - sub);
+            pot = sx * pot;
+        }
+    }
+    o.pe = pot;
+    o.f = F;
+    o.ti = TQ1;
+    o.tj = TQ2;
+    o.vir = dot3(r, F);
+}
+
+template <int SOLVER>
+int launch_ecp(sg_ctx* ctx, const sg_pair_params* p, int mu, int nu) {
+    PotECP<SOLVER> pot;
+    pot.pos = ctx->pos;
+    pot.quat = ctx->quat;
+    pot.shape = ctx->shape;
+    pot.prep = ctx->ecp_prep;
+    pot.prep64 = ctx->ecp_prep64;
+    pot.lam_out = ctx->ecp_lambda;
+    if (ctx->mlp_ready) pot.mlp = *(const MlpDev*)ctx->mlp_host_desc;
+    else pot.mlp = MlpDev{};
+    pot.b = make_boxf(ctx);
+    pot.bx = ctx->box[0]; pot.by = ctx->box[1]; pot.bz = ctx->box[2];
+    pot.kind = p->kind;
+    pot.mu = mu;
+    pot.nu = nu;
+    pot.max_iter = p->newton_max_iter > 0 ? p->newton_max_iter : 20;
+    pot.fp64_check = p->fp64_check;
+    pot.cutoff = (float)p->cutoff;
+    pot.wf = (float)p->wf;
+    pot.chirality = (float)p->chirality;
+    pot.tol = (float)(p->newton_tol > 0.0 ? p->newton_tol : 1e-6);
+    pot.step_tol = 1e-4f;
+    pot.weld = (p->kind == SG_ECPW || p->kind == SG_ECPWC);
+    pot.chiral = (p->kind == SG_ECPC || p->kind == SG_ECPWC);
+    pot.rep = (p->kind == SG_ECPR);
+    return launch_pair(ctx, pot);
+}
+
+}  // namespace
+
+int sg_ecp_prepare(sg_ctx* ctx, const sg_pair_params* p, int need64) {
+    int mu = p->mu > 0 ? p->mu : 2;
+    if (!ctx->ecp_prep) SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep, sizeof(float4) * 4 * (size_t)ctx->n));
+    if (need64 && !ctx->ecp_prep64) SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep64, sizeof(double) * 6 * (size_t)ctx->n));
+    k_ecp_prep<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->quat, ctx->shape, ctx->eshape,
+                                                             1.f / (float)mu, ctx->ecp_prep,
+                                                             need64 ? ctx->ecp_prep64 : nullptr);
+    SG_LAUNCH_CHECK(ctx, "k_ecp_prep");
+    return SG_OK;
+}
+
+int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p) {
+    int mu = p->mu, nu = p->nu;
+    if (mu == 0 && nu == 0) { mu = 2; nu = 1; }
+    if (mu < 1 || nu < 1 || mu > 8 || nu > 8) return sg_fail(ctx, SG_EINVAL, "ECP exponents must be in 1..8");
+    const int brent = p->solver == SG_SOLVER_BRENT_COMPAT;
+    if (p->solver == SG_SOLVER_MLP_NEWTON && !ctx->mlp_ready)
+        return sg_fail(ctx, SG_ENOTREADY, "MLP solver selected but no weights were set (sg_mlp_set_weights)");
+    if (int rc = sg_ecp_prepare(ctx, p, brent)) return rc;
+    if (ctx->ecp_lambda_cap < ctx->nl.pair_capacity) {
+        ctx->graph_epoch++;
+        if (ctx->ecp_lambda) cudaFree(ctx->ecp_lambda);
+        ctx->ecp_lambda = nullptr;
+        SG_CUDA(ctx, cudaMalloc(&ctx->ecp_lambda, sizeof(float) * (size_t)ctx->nl.pair_capacity));
+        ctx->ecp_lambda_cap = ctx->nl.pair_capacity;
+    }
+    switch (p->solver) {
+        case SG_SOLVER_BRENT_COMPAT: return launch_ecp<SG_SOLVER_BRENT_COMPAT>(ctx, p, mu, nu);
+        case SG_SOLVER_NEWTON: return launch_ecp<SG_SOLVER_NEWTON>(ctx, p, mu, nu);
+        case SG_SOLVER_MLP_NEWTON: return launch_ecp<SG_SOLVER_MLP_NEWTON>(ctx, p, mu, nu);
+        default: return sg_fail(ctx, SG_EINVAL, "unknown ECP solver %d", p->solver);
+    }
+}

@@ -1,0 +1,188 @@
+// Internal declarations shared by the CUDA translation units of libsucrose_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sucrose_gpu.h"
+
+#define SG_DEV __device__ __forceinline__
+
+// ------------------------------------------------------------------ context --
+struct sg_nlist_state {
+    int initialized = 0;
+    int trigger_mode = 0;
+    double cutoff = 0.0, skin = 0.0;
+    double rl2 = 0.0;                // (rc+skin)^2 in FP64, the reference's r_skin_sq after a build
+    double trigger_sq = 0.0;         // compared with 4 * max displacement^2
+    int use_cells = 0;
+    int ncell[3] = {0, 0, 0};
+    int ncells = 0;
+    int max_nb = 0;                  // capacity per particle (half list)
+    int64_t pair_capacity = 0;       // capacity of the flattened list
+    int* cell_count = nullptr;       // [ncells]
+    int* cell_start = nullptr;       // [ncells + 1]
+    int* cell_fill = nullptr;        // [ncells]
+    int* cell_particles = nullptr;   // [n]
+    int* particle_cell = nullptr;    // [n]
+    int* nb_count = nullptr;         // [n]
+    int* nb_pad = nullptr;           // [max_nb * n], column-major (k * n + i)
+    int* row_off = nullptr;          // [n + 1]
+    int* scan_tmp = nullptr;         // block sums of the scan
+    int* pair_i = nullptr;           // [pair_capacity]
+    int* pair_j = nullptr;           // [pair_capacity]
+    int* dev_flags = nullptr;        // [0] rebuild requested, [1] overflow (max row seen), [2] npairs, [3] builds
+    float4* pos_last = nullptr;      // positions at the last build
+};
+
+struct sg_ctx {
+    int n = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    double box[3] = {0, 0, 0};
+    int periodic = 1;
+    char err[512] = {0};
+
+    // FP32 SoA state, float4 each
+    float4* pos = nullptr;       // x y z 0
+    float4* quat = nullptr;      // w x y z
+    float4* vel = nullptr;       // vx vy vz inv_mass
+    float4* angm = nullptr;      // lx ly lz 0
+    float4* force = nullptr;     // fx fy fz 0
+    float4* torque = nullptr;    // tx ty tz 0
+    float4* shape = nullptr;     // sig_x sig_y sig_z mass
+    float4* eshape = nullptr;    // eps_x eps_y eps_z 0
+    float4* inert = nullptr;     // Ixx Iyy Izz 0
+    float4* inert_inv = nullptr; // 1/Ixx 1/Iyy 1/Izz 0
+
+    // FP64 accumulators: [0] pot_eng [1] pair virial [2] kin_eng [3] kin_rot
+    double* acc = nullptr;
+    // FP64 scratch for reductions: per-block partials and completion counter
+    double* partials = nullptr;
+    unsigned int* done_counter = nullptr;
+    int partial_slots = 0;
+    // ECP / solver statistics (unsigned long long): [0] pairs [1] evals [2] nonconv [3] fallbacks [4..27] hist
+    unsigned long long* stats = nullptr;
+    // Nose-Hoover chain state, FP64: eta[3] p_eta[3] eta_r[3] p_eta_r[3] + scratch
+    double* nh = nullptr;
+
+    // ECP per-particle prep (FP32) and FP64 copies for the bit-exact Brent
+    float4* ecp_prep = nullptr;      // 6 float4 per particle
+    double* ecp_prep64 = nullptr;    // 12 doubles per particle (A_R 6, A_E 6)
+    float* ecp_lambda = nullptr;     // per pair
+    int64_t ecp_lambda_cap = 0;
+
+    // MLP weights (FP32 master) and BF16 packed copy
+    float* mlp_w = nullptr;
+    void* mlp_wbf16 = nullptr;       // device: bf16 W1 W2 W3 then f32 b1 b2 b3 w4
+    unsigned char mlp_host_desc[128];  // host copy of the MlpDev descriptor (device pointers)
+    int mlp_ready = 0;
+
+    // staging (pinned host) for uploads / downloads
+    float4* h_stage = nullptr;
+    size_t h_stage_bytes = 0;
+    double* d_stage = nullptr;       // device FP64 staging for packing (16 n doubles)
+    int sync_transfers = 1;          // uploads wait for completion (the host may free its arrays)
+
+    // captured whole-step graph (sg_step)
+    cudaGraphExec_t graph_exec = nullptr;
+    int* step_dev = nullptr;         // device step counter used by the captured Langevin kernel
+    const int* lgv_step_dev = nullptr;  // set while enqueuing a step: Langevin reads the counter here
+    int lgv_rotations = 1;           // Langevin also thermostats rotation
+    unsigned graph_epoch = 0;        // bumped whenever a buffer a captured graph uses is reallocated
+    unsigned graph_epoch_captured = 0;
+    int graph_kernels = 0;
+    unsigned char step_cfg[256];     // copy of the sg_step_config the graph was captured with
+    int step_ready = 0;
+
+    sg_nlist_state nl;
+};
+
+// --------------------------------------------------------------- errors ----
+int sg_fail(sg_ctx* ctx, int code, const char* fmt, ...);
+int sg_cuda_check(sg_ctx* ctx, cudaError_t e, const char* what);
+#define SG_CUDA(ctx, call)                                              \
+    do {                                                                \
+        cudaError_t _e = (call);                                        \
+        if (_e != cudaSuccess) return sg_cuda_check((ctx), _e, #call);  \
+    } while (0)
+#define SG_LAUNCH_CHECK(ctx, what) SG_CUDA(ctx, cudaGetLastError())
+
+int sg_ensure_partials(sg_ctx* ctx, int slots);
+int sg_ensure_stage(sg_ctx* ctx, size_t bytes);
+extern "C" int sg_ensure_dstage(sg_ctx* ctx);
+int sg_grid_for(sg_ctx* ctx, const void* kernel, int block, size_t smem);
+
+// ------------------------------------------------------- device helpers ----
+SG_DEV float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+SG_DEV float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+SG_DEV float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+SG_DEV float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+SG_DEV float3 operator*(float3 a, float s) { return make_float3(s * a.x, s * a.y, s * a.z); }
+SG_DEV float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SG_DEV float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// Minimum image with the reference's ANINT (round half away from zero).
+SG_DEV float3 min_image(float3 d, float3 box, float3 inv_box, int periodic) {
+    if (periodic) {
+        d.x -= roundf(d.x * inv_box.x) * box.x;
+        d.y -= roundf(d.y * inv_box.y) * box.y;
+        d.z -= roundf(d.z * inv_box.z) * box.z;
+    }
+    return d;
+}
+
+// Shared block reduction of K doubles; the last block to finish adds the
+// per-block partials, in block order, into acc[k] (deterministic). Must be
+// called by every thread of the block. partials holds gridDim.x * K slots.
+template <int K>
+__device__ void block_reduce_finish(double (&v)[K], double* partials, unsigned int* done, double* acc,
+                                    double* acc_also = nullptr) {
+    __shared__ double sh[32][K];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[warp][k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double s = 0.0;
+        for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
+        partials[(size_t)blockIdx.x * K + threadIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int t = atomicAdd(done, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        if (threadIdx.x < K) {
+            double s = 0.0;
+            for (unsigned int b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[(size_t)b * K + threadIdx.x];
+            acc[threadIdx.x] += s;
+            if (acc_also) acc_also[threadIdx.x] += s;
+        }
+        if (threadIdx.x == 0) *done = 0u;
+    }
+}
+
+// --------------------------------------------------- internal entry points --
+int sg_ecp_prepare(sg_ctx* ctx, const sg_pair_params* p, int need64);
+int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p);
+int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p);
+int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p);
+int sg_nlist_free(sg_ctx* ctx);

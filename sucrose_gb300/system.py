@@ -1,0 +1,308 @@
+"""Host-side mirror of the reference's system / neighbour_list / force /
+integrator modules (fortran/system.f90, fortran/force.f90,
+fortran/integrators.f90), backed by the CUDA library through its C ABI.
+
+A GpuSystem owns one device context. Arrays handed in and out are FP64
+structure-of-arrays in the reference's layout (RX..RZ, QW..QZ, VX..VZ,
+LX..LZ, FX..FZ, TX..TZ), 0-based; the device state is FP32. Errors come back
+as SgError carrying the C status (the reference stops the program instead).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import PairParams, EcpStats, check
+
+_D = C.POINTER(C.c_double)
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _f64(a, n):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (n,)))
+    return a
+
+
+class GpuSystem:
+    def __init__(self, n, box, periodic=True, device=0):
+        self.L = capi.load()
+        self.n = int(n)
+        ctx = C.c_void_p()
+        rc = self.L.sg_create(C.byref(ctx), self.n, int(device))
+        self.ctx = ctx
+        check(ctx, rc)
+        self.set_box(box, periodic)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.sg_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, rc):
+        return check(self.ctx, rc)
+
+    # ---- configuration ----------------------------------------------------
+    def set_box(self, box, periodic=True):
+        b = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+        self.box = b.copy()
+        self.periodic = bool(periodic)
+        self._c(self.L.sg_set_box(self.ctx, _dp(b), 1 if periodic else 0))
+
+    def set_particles(self, mass=None, sig=None, eps=None, inertia=None):
+        """Per-particle constants; each of sig, eps, inertia is None, a 3-tuple
+        applied to every particle, or an (n, 3) array."""
+        n = self.n
+
+        def cols(a):
+            if a is None:
+                return [None] * 3
+            a = np.asarray(a, dtype=np.float64)
+            if a.ndim == 1:
+                return [_f64(a[k], n) for k in range(3)]
+            return [np.ascontiguousarray(a[:, k]) for k in range(3)]
+
+        m = _f64(mass, n)
+        s, e, I = cols(sig), cols(eps), cols(inertia)
+        self._keep = (m, s, e, I)
+        self._c(self.L.sg_set_particles(self.ctx, _dp(m), *[_dp(a) for a in s], *[_dp(a) for a in e],
+                                        *[_dp(a) for a in I]))
+
+    # ---- state transfer -------------------------------------------------------
+    def upload(self, r=None, q=None, v=None, l=None):
+        """r, v, l: (n,3) FP64; q: (n,4) (w,x,y,z)."""
+        cols = []
+        for a, k in ((r, 3), (q, 4), (v, 3), (l, 3)):
+            if a is None:
+                cols += [None] * k
+            else:
+                a = np.asarray(a, dtype=np.float64)
+                cols += [np.ascontiguousarray(a[:, d]) for d in range(k)]
+        self._c(self.L.sg_upload_state(self.ctx, *[_dp(c) for c in cols]))
+
+    def download(self):
+        n = self.n
+        arrs = [np.empty(n) for _ in range(13)]
+        self._c(self.L.sg_download_state(self.ctx, *[_dp(a) for a in arrs]))
+        r = np.stack(arrs[0:3], 1)
+        q = np.stack(arrs[3:7], 1)
+        v = np.stack(arrs[7:10], 1)
+        l = np.stack(arrs[10:13], 1)
+        return r, q, v, l
+
+    def forces(self):
+        n = self.n
+        arrs = [np.empty(n) for _ in range(6)]
+        self._c(self.L.sg_download_forces(self.ctx, *[_dp(a) for a in arrs]))
+        return np.stack(arrs[0:3], 1), np.stack(arrs[3:6], 1)
+
+    def set_forces(self, f, t=None):
+        f = np.asarray(f, dtype=np.float64)
+        cols = [np.ascontiguousarray(f[:, d]) for d in range(3)]
+        tc = [None] * 3 if t is None else [np.ascontiguousarray(np.asarray(t, dtype=np.float64)[:, d]) for d in range(3)]
+        self._c(self.L.sg_upload_forces(self.ctx, *[_dp(c) for c in cols], *[_dp(c) for c in tc]))
+
+    def zero_forces(self):
+        """initialize_forces (system.f90:423)."""
+        self._c(self.L.sg_zero_forces(self.ctx))
+
+    # ---- neighbour list -----------------------------------------------------
+    def init_nlist(self, skin, cutoff, trigger_mode=0):
+        self._c(self.L.sg_nlist_init(self.ctx, float(skin), float(cutoff), int(trigger_mode)))
+
+    def needs_rebuild(self):
+        f = C.c_int32(0)
+        self._c(self.L.sg_nlist_needs_rebuild(self.ctx, C.byref(f)))
+        return bool(f.value)
+
+    def build_nlist(self):
+        self._c(self.L.sg_nlist_build(self.ctx))
+
+    def update_nlist(self):
+        self._c(self.L.sg_nlist_update(self.ctx))
+
+    def npairs(self):
+        k = C.c_int64(0)
+        self._c(self.L.sg_nlist_count(self.ctx, C.byref(k)))
+        return k.value
+
+    def nlist_builds(self):
+        k = C.c_int64(0)
+        self._c(self.L.sg_nlist_builds(self.ctx, C.byref(k)))
+        return k.value
+
+    def export_nlist(self, one_based=False):
+        k = self.npairs()
+        nl = np.zeros(max(k, 1), dtype=np.int32)
+        off = np.zeros(self.n + 1, dtype=np.int32)
+        kk = C.c_int64(0)
+        self._c(self.L.sg_nlist_export(self.ctx, nl.ctypes.data_as(C.POINTER(C.c_int32)), len(nl),
+                                       off.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(kk), 1 if one_based else 0))
+        return nl[:k], (off[: self.n] if one_based else off)
+
+    def raw_pairs(self):
+        """Listed pairs in the device's internal order (the order of per-pair outputs)."""
+        k = self.npairs()
+        pi = np.zeros(max(k, 1), dtype=np.int32)
+        pj = np.zeros(max(k, 1), dtype=np.int32)
+        kk = C.c_int64(0)
+        P = C.POINTER(C.c_int32)
+        self._c(self.L.sg_nlist_pairs(self.ctx, pi.ctypes.data_as(P), pj.ctypes.data_as(P), len(pi), C.byref(kk)))
+        return pi[:k], pj[:k]
+
+    def pairs(self):
+        """Listed pairs as (i, j) arrays, 0-based, i < j, rows ascending."""
+        nl, off = self.export_nlist()
+        counts = np.diff(off)
+        return np.repeat(np.arange(self.n, dtype=np.int32), counts), nl
+
+    # ---- pair forces ------------------------------------------------------------
+    @staticmethod
+    def params(kind, sigma=1.0, epsilon=1.0, cutoff=2.5, wf=0.0, chirality=0.0, mu=0, nu=0,
+               solver=capi.SOLVER_NEWTON, newton_tol=1e-6, newton_max_iter=20, fp64_check=1):
+        return PairParams(kind, mu, nu, solver, sigma, epsilon, cutoff, wf, chirality, newton_tol, newton_max_iter,
+                          fp64_check)
+
+    def pair_forces(self, params, want_stats=False, allow=()):
+        pe = C.c_double(0.0)
+        vir = C.c_double(0.0)
+        st = EcpStats()
+        rc = self.L.sg_pair_forces(self.ctx, C.byref(params), C.byref(pe), C.byref(vir), C.byref(st))
+        if rc not in allow:
+            self._c(rc)
+        if want_stats:
+            return pe.value, vir.value, st
+        return pe.value, vir.value
+
+    def pair_forces_async(self, params):
+        self._c(self.L.sg_pair_forces_async(self.ctx, C.byref(params)))
+
+    def energies(self):
+        out = np.zeros(4)
+        self._c(self.L.sg_read_energies(self.ctx, _dp(out)))
+        return out
+
+    def ecp_lambda(self):
+        k = self.npairs()
+        lam = np.zeros(max(k, 1), dtype=np.float32)
+        self._c(self.L.sg_ecp_lambda(self.ctx, lam.ctypes.data_as(C.POINTER(C.c_float)), len(lam)))
+        return lam[:k]
+
+    # ---- integrators --------------------------------------------------------------
+    def vv_initial(self, dt):
+        self._c(self.L.sg_vv_initial(self.ctx, dt))
+
+    def vv_final(self, dt):
+        ke = C.c_double(0.0)
+        self._c(self.L.sg_vv_final(self.ctx, dt, C.byref(ke)))
+        return ke.value
+
+    def qq_initial(self, dt):
+        self._c(self.L.sg_qq_initial(self.ctx, dt))
+
+    def qq_final(self, dt):
+        kr = C.c_double(0.0)
+        self._c(self.L.sg_qq_final(self.ctx, dt, C.byref(kr)))
+        return kr.value
+
+    def lgv_initial(self, dt, step, damping=1.0, target_temp=1.0, key=None):
+        k = None if key is None else np.asarray(key, dtype=np.uint32)
+        self._c(self.L.sg_lgv_initial(self.ctx, dt, int(step), damping, target_temp,
+                                      None if k is None else k.ctypes.data_as(C.POINTER(C.c_uint32))))
+
+    def lgv_final(self, dt, damping=1.0):
+        ke = C.c_double(0.0)
+        kr = C.c_double(0.0)
+        self._c(self.L.sg_lgv_final(self.ctx, dt, damping, C.byref(ke), C.byref(kr)))
+        return ke.value, kr.value
+
+    def nht_initial(self, dt, target_temp, coupling=0.0, mode=1, rot_chain=0):
+        self._c(self.L.sg_nht_initial(self.ctx, dt, target_temp, coupling, mode, rot_chain))
+
+    def nht_final(self, dt, target_temp, coupling=0.0, mode=1, rot_chain=0):
+        ke = C.c_double(0.0)
+        self._c(self.L.sg_nht_final(self.ctx, dt, target_temp, coupling, mode, rot_chain, C.byref(ke)))
+        return ke.value
+
+    def nht_state(self, set_values=None):
+        out = np.zeros(12)
+        s = None if set_values is None else np.ascontiguousarray(set_values, dtype=np.float64)
+        self._c(self.L.sg_nht_state(self.ctx, _dp(out), _dp(s)))
+        return out
+
+    def thermo(self, dof, density, nrigid=1):
+        out = np.zeros(3)
+        self._c(self.L.sg_thermo(self.ctx, int(dof), float(density), int(nrigid), _dp(out)))
+        return out
+
+    def synchronize(self):
+        self._c(self.L.sg_synchronize(self.ctx))
+
+    # ---- captured timestep -------------------------------------------------------------
+    def configure_step(self, pair, integrator=capi.INT_NVE, dt=0.001, target_temp=1.0, damping=1.0, coupling=0.0,
+                       rotations=0, rot_chain=0, first_step=1, key=None):
+        cfg = capi.StepConfig()
+        cfg.integrator, cfg.rotations, cfg.rot_chain, cfg.first_step = integrator, rotations, rot_chain, first_step
+        cfg.dt, cfg.target_temp, cfg.damping, cfg.coupling = dt, target_temp, damping, coupling
+        if key is not None:
+            cfg.key[0], cfg.key[1] = int(key[0]), int(key[1])
+            cfg.has_key = 1
+        cfg.pair = pair
+        self._step_cfg = cfg
+        self._c(self.L.sg_step_configure(self.ctx, C.byref(cfg)))
+
+    def step(self, nsteps=1):
+        self._c(self.L.sg_step(self.ctx, int(nsteps)))
+
+    def step_check(self):
+        self._c(self.L.sg_step_check(self.ctx))
+
+    def step_kernel_count(self):
+        k = C.c_int64(0)
+        self._c(self.L.sg_step_kernel_count(self.ctx, C.byref(k)))
+        return k.value
+
+    def peak_fma(self, fp64=False):
+        t = C.c_double(0.0)
+        self._c(self.L.sg_peak_fma(self.ctx, 1 if fp64 else 0, C.byref(t)))
+        return t.value
+
+    def stream_ptr(self):
+        return self.L.sg_stream(self.ctx)
+
+    # ---- Philox ---------------------------------------------------------------------
+    def philox(self, ctr, key=(0x6D2B79F5, 0x1B873593)):
+        c = np.ascontiguousarray(ctr, dtype=np.uint32).reshape(-1, 4)
+        k = np.asarray(key, dtype=np.uint32)
+        out = np.zeros_like(c)
+        P = C.POINTER(C.c_uint32)
+        self._c(self.L.sg_philox4x32_device(self.ctx, len(c), c.ctypes.data_as(P), k.ctypes.data_as(P),
+                                            out.ctypes.data_as(P)))
+        return out
+
+    def normal_3seq(self, ctr):
+        c = np.ascontiguousarray(ctr, dtype=np.int32).reshape(-1, 4)
+        out = np.zeros((len(c), 3))
+        self._c(self.L.sg_philox_normal_3seq_device(self.ctx, len(c), c.ctypes.data_as(C.POINTER(C.c_int32)), _dp(out)))
+        return out
+
+    # ---- MLP ---------------------------------------------------------------------------
+    def set_mlp_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._c(self.L.sg_mlp_set_weights(self.ctx, w.ctypes.data_as(C.POINTER(C.c_float)), len(w)))
+
+    def get_mlp_weights(self):
+        n = self.L.sg_mlp_weight_count()
+        w = np.zeros(n, dtype=np.float32)
+        self._c(self.L.sg_mlp_get_weights(self.ctx, w.ctypes.data_as(C.POINTER(C.c_float)), n))
+        return w

@@ -1,0 +1,123 @@
+"""One step of each integrator on the device against the oracle, same state."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import Pair, ellipsoids, jittered_fcc, rel, f32
+from sucrose_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+SIG = (3.0, 2.0, 1.0)
+
+
+def state(seed=2):
+    r, q, box = ellipsoids((6, 8, 12), SIG, 0.1114, seed=seed, tilt=0.4)
+    n = len(r)
+    v = configs.velocities_to_temperature(n, 1.2, seed)
+    I = configs.default_inertia(SIG)
+    l = configs.angular_momenta(q, I, 1.2, seed)
+    P = Pair(r, q, box, sig=SIG, v=v, l=l)
+    rng = np.random.default_rng(seed)
+    F = f32(rng.normal(size=(n, 3)) * 5.0)
+    T = f32(rng.normal(size=(n, 3)) * 2.0)
+    P.g.set_forces(F, T)
+    P.set_oracle_forces(F, T)
+    return P
+
+
+def compare_state(P, tol=2e-6):
+    r, q, v, l = P.g.download()
+    o = P.o
+    ro = np.stack([o.rx, o.ry, o.rz], 1)
+    dr = r - ro
+    dr -= P.box * np.round(dr / P.box)
+    assert np.max(np.abs(dr)) < tol * np.max(P.box)
+    assert rel(v, np.stack([o.vx, o.vy, o.vz], 1)) < tol
+    assert rel(q, np.stack([o.qw, o.qx, o.qy, o.qz], 1)) < tol
+    lo = np.stack([o.lx, o.ly, o.lz], 1)
+    if np.linalg.norm(lo) > 0:
+        assert rel(l, lo) < tol
+
+
+def test_vv(lib):
+    P = state()
+    P.g.vv_initial(0.001)
+    P.o.vv_initial(0.001)
+    compare_state(P)
+    ke = P.g.vv_final(0.001)
+    P.o.vv_final(0.001)
+    compare_state(P)
+    assert abs(ke - P.o.s.kin_eng) < 1e-6 * P.o.s.kin_eng
+
+
+def test_quaternion(lib):
+    P = state(3)
+    P.g.qq_initial(0.001)
+    P.o.qq_initial(0.001)
+    compare_state(P)
+    kr = P.g.qq_final(0.001)
+    P.o.qq_final(0.001)
+    compare_state(P)
+    assert abs(kr - P.o.s.kin_rot) < 1e-5 * P.o.s.kin_rot
+
+
+def test_langevin(lib):
+    P = state(4)
+    P.o.s.target_temp = 1.0
+    P.g.lgv_initial(0.002, 17, damping=1.0, target_temp=1.0)
+    P.o.lgv_initial(0.002, 17, damping=1.0)
+    compare_state(P, tol=5e-6)
+    ke, kr = P.g.lgv_final(0.002, 1.0)
+    P.o.lgv_final(0.002)
+    compare_state(P, tol=5e-6)
+    assert abs(ke - P.o.s.kin_eng) < 1e-5 * P.o.s.kin_eng
+    assert abs(kr - P.o.s.kin_rot) < 1e-5 * P.o.s.kin_rot
+
+
+def test_langevin_replica_key(lib):
+    P = state(5)
+    key = (0x1234ABCD, 0x0BADF00D)
+    P.o.s.target_temp = 1.0
+    P.g.lgv_initial(0.002, 3, damping=1.0, target_temp=1.0, key=key)
+    P.o.lgv_initial(0.002, 3, damping=1.0, key=key)
+    compare_state(P, tol=5e-6)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_nose_hoover(lib, mode):
+    P = state(6)
+    P.o.s.target_temp = 1.2
+    # non-zero chain momenta so the thermostat acts
+    chain = np.array([0.0, 0.0, 0.0, 0.3, -0.2, 0.1, 0, 0, 0, 0, 0, 0])
+    P.g.nht_state(chain)
+    P.o.s.p_eta[0], P.o.s.p_eta[1], P.o.s.p_eta[2] = 0.3, -0.2, 0.1
+    P.g.nht_initial(0.001, 1.2, mode=mode)
+    P.o.nht_initial(0.001, mode=mode)
+    compare_state(P, tol=5e-6)
+    st = P.g.nht_state()
+    np.testing.assert_allclose(st[:6], list(P.o.s.eta) + list(P.o.s.p_eta), rtol=1e-6, atol=1e-9)
+    ke = P.g.nht_final(0.001, 1.2, mode=mode)
+    P.o.nht_final(0.001, mode=mode)
+    compare_state(P, tol=5e-6)
+    assert abs(ke - P.o.s.kin_eng) < 1e-5 * P.o.s.kin_eng
+    st = P.g.nht_state()
+    np.testing.assert_allclose(st[:6], list(P.o.s.eta) + list(P.o.s.p_eta), rtol=1e-6, atol=1e-9)
+
+
+def test_thermo(lib):
+    r, q, box = jittered_fcc(3, 0.8442, seed=1)
+    v = configs.velocities_to_temperature(108, 0.722, 15)
+    P = Pair(r, q, box, v=v)
+    rng = np.random.default_rng(1)
+    F = f32(rng.normal(size=(108, 3)))
+    P.g.set_forces(F, np.zeros((108, 3)))
+    P.set_oracle_forces(F, np.zeros((108, 3)))
+    P.g.vv_final(0.0)
+    P.o.vv_final(0.0)
+    P.o.s.dof = 6 * 108 - 3
+    P.o.s.density = 0.8442
+    P.o.thermo()
+    t = P.g.thermo(6 * 108 - 3, 0.8442)
+    assert abs(t[0] - P.o.s.temp) < 1e-6 * P.o.s.temp
+    assert abs(t[1] - P.o.s.virial) < 1e-5 * max(1.0, abs(P.o.s.virial))
+    assert abs(t[2] - P.o.s.pressure) < 1e-5 * max(1.0, abs(P.o.s.pressure))

@@ -1,0 +1,134 @@
+"""Device Philox words and Verlet-list pair sets against the oracle (bit-exact)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import Pair, lj_fcc, jittered_fcc, ellipsoids
+from sucrose_gb300 import GpuSystem, SgError, capi
+
+pytestmark = pytest.mark.gpu
+
+
+def test_philox_words_bit_exact(lib):
+    g = GpuSystem(4, 10.0)
+    rng = np.random.default_rng(7)
+    ctr = rng.integers(0, 2 ** 32, size=(1 << 20, 4), dtype=np.uint64).astype(np.uint32)
+    ctr[:4] = [[0, 0, 0, 0], [0xFFFFFFFF] * 4, [1, 2, 3, 4], [108, 20000, 722, 1]]
+    for key in ((0x6D2B79F5, 0x1B873593), (0xDEADBEEF, 0x12345678)):
+        assert np.array_equal(g.philox(ctr, key), O.philox4x32(ctr, key))
+
+
+def test_philox_normals(lib):
+    g = GpuSystem(4, 10.0)
+    idx = np.arange(1, 5001)
+    ctr = np.stack([idx, np.full_like(idx, 17), np.full_like(idx, 1000), idx % 2], 1)
+    dev = g.normal_3seq(ctr)
+    ref = np.array([O.philox_normal_3seq(*c) for c in ctr])
+    np.testing.assert_allclose(dev, ref, rtol=1e-13, atol=1e-13)
+
+
+def _pairs_equal(P, cutoff, skin):
+    opi, opj = P.o.pairs(cutoff, skin)
+    gpi, gpj = P.g.pairs()
+    assert len(gpi) == len(opi)
+    assert np.array_equal(gpi, opi) and np.array_equal(gpj, opj)
+    return len(opi)
+
+
+def test_nlist_readme_fcc(lib):
+    r, q, box, v = lj_fcc()
+    P = Pair(r, q, box)
+    P.g.init_nlist(0.3, 2.5)
+    assert _pairs_equal(P, 2.5, 0.3) == 3564
+    # reference CSR, 1-based, exactly as build_nlist leaves nlist/offset
+    onl, ooff = P.o.nlist(2.5, 0.3, one_based=True)
+    gnl, goff = P.g.export_nlist(one_based=True)
+    assert np.array_equal(onl, gnl) and np.array_equal(ooff, goff)
+    assert goff[-1] == len(gnl) + 1
+
+
+@pytest.mark.parametrize("cells,density", [(6, 0.8), (10, 0.7)])
+def test_nlist_cells_jittered(lib, cells, density):
+    r, q, box = jittered_fcc(cells, density, seed=cells)
+    P = Pair(r, q, box)
+    P.g.init_nlist(0.3, 2.5)
+    assert _pairs_equal(P, 2.5, 0.3) > 0
+
+
+def test_nlist_threshold_pairs(lib):
+    # pairs placed within a few ulps of (rc+skin) on both sides, across the
+    # periodic boundary: the FP64 re-test must decide them like the reference
+    rng = np.random.default_rng(3)
+    box = 20.0
+    rl = 2.8
+    base = rng.uniform(-box / 2, box / 2, size=(200, 3))
+    d = rng.normal(size=(200, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    eps = rng.uniform(-3e-6, 3e-6, size=(200, 1))
+    partner = base + d * (rl + eps)
+    partner -= box * np.round(partner / box)
+    r = np.concatenate([base, partner])
+    P = Pair(r, None, box)
+    P.g.init_nlist(0.3, 2.5)
+    _pairs_equal(P, 2.5, 0.3)
+
+
+def test_nlist_ellipsoid_cells(lib):
+    r, q, box = ellipsoids((12, 16, 24), (3.0, 2.0, 1.0), 0.1114, seed=5, tilt=0.4)
+    P = Pair(r, q, box, sig=(3.0, 2.0, 1.0))
+    P.g.init_nlist(0.3, 3.0)
+    _pairs_equal(P, 3.0, 0.3)
+
+
+def test_nlist_open_boundaries(lib):
+    rng = np.random.default_rng(11)
+    r = rng.uniform(-6, 6, size=(300, 3))
+    P = Pair(r, None, 100.0, periodic=False)
+    P.g.init_nlist(0.3, 2.5)
+    _pairs_equal(P, 2.5, 0.3)
+
+
+def test_nlist_small_and_empty(lib):
+    for n in (1, 2, 3, 8):
+        r = np.arange(3 * n, dtype=np.float64).reshape(n, 3) * 0.7
+        P = Pair(r, None, 30.0)
+        P.g.init_nlist(0.3, 2.5)
+        _pairs_equal(P, 2.5, 0.3)
+    P = Pair(np.array([[0.0, 0, 0], [10.0, 0, 0]]), None, 30.0)
+    P.g.init_nlist(0.3, 2.5)
+    assert P.g.npairs() == 0
+
+
+def test_nlist_cutoff_guard(lib):
+    P = Pair(np.zeros((4, 3)) + np.arange(4)[:, None], None, 4.0)
+    with pytest.raises(SgError) as e:
+        P.g.init_nlist(0.3, 2.5)
+    assert e.value.code == capi.SG_ECUTOFF_GT_HALFBOX
+
+
+def test_nlist_trigger_matches_reference(lib):
+    r, q, box = jittered_fcc(6, 0.8, seed=2)
+    P = Pair(r, q, box)
+    P.g.init_nlist(0.3, 2.5, trigger_mode=0)
+    last = P.r.copy()
+    for amp in (0.1, 0.5, 1.3, 1.5):
+        d = np.zeros_like(P.r)
+        d[7, 0] = amp
+        rn = P.r + d
+        P.g.upload(r=rn)
+        P.o.rx[:], P.o.ry[:], P.o.rz[:] = rn.T
+        expect = P.o.needs_rebuild(last[:, 0].copy(), last[:, 1].copy(), last[:, 2].copy(), 2.5, 0.3, 0)
+        assert P.g.needs_rebuild() == expect
+    # skin trigger
+    P.g.init_nlist(0.3, 2.5, trigger_mode=1)
+    P.g.upload(r=P.r + np.array([0.16, 0, 0]) * (np.arange(P.n)[:, None] == 0))
+    assert P.g.needs_rebuild()
+
+
+def test_nlist_regrows_capacity(lib):
+    # a dense blob forces rows far above the density estimate
+    rng = np.random.default_rng(5)
+    r = np.concatenate([rng.uniform(-1.0, 1.0, size=(400, 3)), rng.uniform(-15, 15, size=(200, 3))])
+    P = Pair(r, None, 30.0)
+    P.g.init_nlist(0.3, 2.5)
+    _pairs_equal(P, 2.5, 0.3)
