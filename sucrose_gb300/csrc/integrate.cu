@@ -149,6 +149,8 @@ struct LgvConst {
     float dt, ed, kk12, T;
     double c2;          // 1 - exp(-2 gamma dt)
     double rot_amp;     // 2 gamma T dt
+    float Tc2;          // T (1 - exp(-2 gamma dt))
+    float rot_ampf;
     float kk2;
     uint32_t step, temp_int, k0, k1;
 };
@@ -164,15 +166,15 @@ __global__ void k_lgv_initial(int n, LgvConst c, Geo g, float4* __restrict__ pos
     const float im = v.w;
     v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
     float3 p = make_float3(r.x + h * v.x, r.y + h * v.y, r.z + h * v.z);
-    double n1a, n1b, n1c, n2a = 0.0, n2b = 0.0, n2c = 0.0;
+    float n1a, n1b, n1c, n2a = 0.f, n2b = 0.f, n2c = 0.f;
     // counters (I, step, int(T*1000), stream) with I 1-based (integrators.f90:546-547)
     const uint32_t step = c.step_dev ? (uint32_t)*c.step_dev : c.step;
-    sg_normal_3seq((uint32_t)(i + 1), step, c.temp_int, 0u, c.k0, c.k1, n1a, n1b, n1c);
-    if (rotations) sg_normal_3seq((uint32_t)(i + 1), step, c.temp_int, 1u, c.k0, c.k1, n2a, n2b, n2c);
-    const float amp = (float)sqrt((double)c.T * (double)im * c.c2);
-    v.x = c.ed * v.x + amp * (float)n1a;
-    v.y = c.ed * v.y + amp * (float)n1b;
-    v.z = c.ed * v.z + amp * (float)n1c;
+    sg_normal_3seq_f32((uint32_t)(i + 1), step, c.temp_int, 0u, c.k0, c.k1, n1a, n1b, n1c);
+    if (rotations) sg_normal_3seq_f32((uint32_t)(i + 1), step, c.temp_int, 1u, c.k0, c.k1, n2a, n2b, n2c);
+    const float amp = sqrtf(c.Tc2 * im);
+    v.x = c.ed * v.x + amp * n1a;
+    v.y = c.ed * v.y + amp * n1b;
+    v.z = c.ed * v.z + amp * n1c;
     p = wrap_pos(make_float3(p.x + h * v.x, p.y + h * v.y, p.z + h * v.z), g);
     vel[i] = v;
     pos[i] = make_float4(p.x, p.y, p.z, r.w);
@@ -183,9 +185,9 @@ __global__ void k_lgv_initial(int n, LgvConst c, Geo g, float4* __restrict__ pos
     float3 Lb;
     const float4 q = quat[i];
     float4 qd = q_midpoint(q, L, make_float3(Ii.x, Ii.y, Ii.z), c.dt, rm, Lb);
-    Lb.x = c.kk12 * Lb.x + c.kk2 * (float)sqrt(c.rot_amp * I4.x) * (float)n2a;
-    Lb.y = c.kk12 * Lb.y + c.kk2 * (float)sqrt(c.rot_amp * I4.y) * (float)n2b;
-    Lb.z = c.kk12 * Lb.z + c.kk2 * (float)sqrt(c.rot_amp * I4.z) * (float)n2c;
+    Lb.x = c.kk12 * Lb.x + c.kk2 * sqrtf(c.rot_ampf * I4.x) * n2a;
+    Lb.y = c.kk12 * Lb.y + c.kk2 * sqrtf(c.rot_ampf * I4.y) * n2b;
+    Lb.z = c.kk12 * Lb.z + c.kk2 * sqrtf(c.rot_ampf * I4.z) * n2c;
     L = rot_apply_t(rm, Lb);
     angm[i] = make_float4(L.x, L.y, L.z, 0.f);
     quat[i] = q_advance(q, qd, c.dt);
@@ -466,6 +468,8 @@ int sg_lgv_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double 
     c.kk12 = (float)(kk2 * kk1);
     c.kk2 = (float)kk2;
     c.rot_amp = 2.0 * damping * target_temp * dt;
+    c.Tc2 = (float)(target_temp * c.c2);
+    c.rot_ampf = (float)c.rot_amp;
     c.T = (float)target_temp;
     c.step = (uint32_t)step;
     c.temp_int = (uint32_t)(int32_t)(target_temp * 1000.0);

@@ -95,6 +95,19 @@ __global__ void k_check(int n, const float4* __restrict__ pos, const float4* __r
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 a = pos[i], b = last[i];
+    {
+        // FP32 screen: decide in FP32 when clear of the bound by 1e-3 relative
+        float fx = a.x - b.x, fy = a.y - b.y, fz = a.z - b.z;
+        if (g.periodic) {
+            fx -= roundf(fx * g.inv_box.x) * g.box.x;
+            fy -= roundf(fy * g.inv_box.y) * g.box.y;
+            fz -= roundf(fz * g.inv_box.z) * g.box.z;
+        }
+        const float f4 = 4.f * (fx * fx + fy * fy + fz * fz);
+        if (f4 < (float)trigger_sq * 0.999f && fabsf(fx) < 0.25f * g.box.x && fabsf(fy) < 0.25f * g.box.y &&
+            fabsf(fz) < 0.25f * g.box.z)
+            return;
+    }
     double dx = __dsub_rn((double)a.x, (double)b.x), dy = __dsub_rn((double)a.y, (double)b.y),
            dz = __dsub_rn((double)a.z, (double)b.z);
     if (g.periodic) {

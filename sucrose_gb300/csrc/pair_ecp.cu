@@ -250,10 +250,18 @@ SG_DEV NewtonResult newton_solve(const float* A, const float* D, float3 r, float
         const float s1 = (1.f - 2.f * lam) * rK - l1 * KDK;
         const float s2 = -2.f * rK - 2.f * (1.f - 2.f * lam) * KDK + 2.f * l1 * DKZ;
         if (s1 == 0.f) { res.converged = true; break; }
-        if (s1 > 0.f) lo = lam; else hi = lam;
-        float ln = (s2 < 0.f) ? lam - s1 / s2 : 0.5f * (lo + hi);
-        if (!(ln > lo && ln < hi)) ln = 0.5f * (lo + hi);
-        const bool last = fabsf(ln - lam) < step_tol;
+        const float dl = (s2 < 0.f) ? -s1 / s2 : 1.f;
+        // a Newton step below step_tol lands at the FP32 noise floor: take it
+        // unbracketed (it may be below the resolution of lambda) and stop
+        const bool last = fabsf(dl) < step_tol;
+        float ln;
+        if (last) {
+            ln = fminf(fmaxf(lam + dl, 1e-6f), 1.f - 1e-6f);
+        } else {
+            if (s1 > 0.f) lo = lam; else hi = lam;
+            ln = (s2 < 0.f) ? lam + dl : 0.5f * (lo + hi);
+            if (!(ln > lo && ln < hi)) ln = 0.5f * (lo + hi);
+        }
         lam = ln;
         if (last) {
 #pragma unroll
@@ -268,31 +276,31 @@ SG_DEV NewtonResult newton_solve(const float* A, const float* D, float3 r, float
     return res;
 }
 
-// Normalised FP64 residual S'(lambda) / (r.K), with one step of FP64
-// iterative refinement of K = G^-1 r (G and the residual r - G K in FP64,
-// the correction solved with the FP32 factor). Also returns S'' from FP32.
+// Normalised residual S'(lambda) / (r.K) with K refined once in FP64: the
+// matrix G = A + lambda D and the linear-system residual e = r - G K are
+// formed in FP64 (15 DFMA), the correction G^-1 e is solved with the FP32
+// factor, and the two terms of S' are then formed from the refined K. With K
+// accurate to ~1e-13, the FP32 products contribute ~1e-7 of r.K to S' (well
+// under the 1e-6 bound); without the refinement the FP32 solve alone leaves an
+// error of the order of the bound. Also returns S'' from FP32.
 SG_DEV double residual64(const float* A, const float* D, float3 r, float lam, const Chol& c, float3 K, float& s2) {
     const double L = lam;
     double g[6];
 #pragma unroll
-    for (int m = 0; m < 6; ++m) g[m] = (double)A[m] + L * (double)D[m];
+    for (int m = 0; m < 6; ++m) g[m] = fma(L, (double)D[m], (double)A[m]);
     const double kx = K.x, ky = K.y, kz = K.z;
-    const double ex = (double)r.x - (g[0] * kx + g[1] * ky + g[2] * kz);
-    const double ey = (double)r.y - (g[1] * kx + g[3] * ky + g[4] * kz);
-    const double ez = (double)r.z - (g[2] * kx + g[4] * ky + g[5] * kz);
+    const double ex = (double)r.x - fma(g[0], kx, fma(g[1], ky, g[2] * kz));
+    const double ey = (double)r.y - fma(g[1], kx, fma(g[3], ky, g[4] * kz));
+    const double ez = (double)r.z - fma(g[2], kx, fma(g[4], ky, g[5] * kz));
     const float3 dk = chol_solve(c, make_float3((float)ex, (float)ey, (float)ez));
-    const double Kx = kx + dk.x, Ky = ky + dk.y, Kz = kz + dk.z;
-    const double dkx = D[0] * Kx + D[1] * Ky + D[2] * Kz;
-    const double dky = D[1] * Kx + D[3] * Ky + D[4] * Kz;
-    const double dkz = D[2] * Kx + D[4] * Ky + D[5] * Kz;
-    const double rK = r.x * Kx + r.y * Ky + r.z * Kz;
-    const double KDK = Kx * dkx + Ky * dky + Kz * dkz;
-    const float3 DK = symv(D, K);
+    const float3 Kr = make_float3(K.x + dk.x, K.y + dk.y, K.z + dk.z);
+    const float3 DK = symv(D, Kr);
+    const float rK = dot3(r, Kr), KDK = dot3(Kr, DK);
     const float3 Z = chol_solve(c, DK);
     const float l1 = lam * (1.f - lam);
-    s2 = -2.f * dot3(r, K) - 2.f * (1.f - 2.f * lam) * dot3(K, DK) + 2.f * l1 * dot3(DK, Z);
-    const double s1 = (1.0 - 2.0 * L) * rK - L * (1.0 - L) * KDK;
-    return s1 / fmax(rK, 1e-30);
+    s2 = -2.f * rK - 2.f * (1.f - 2.f * lam) * KDK + 2.f * l1 * dot3(DK, Z);
+    const double s1 = (1.0 - 2.0 * L) * (double)rK - L * (1.0 - L) * (double)KDK;
+    return s1 / fmax((double)rK, 1e-30);
 }
 
 template <int SOLVER>

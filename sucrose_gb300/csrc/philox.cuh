@@ -50,3 +50,23 @@ __device__ __forceinline__ void sg_normal_3seq(uint32_t c0, uint32_t c1, uint32_
     n2 = r1 * s1;
     n3 = r2 * cos(TWOPI * u4);
 }
+
+// The same three variates evaluated in FP32 from the same Philox words, for
+// kernels whose state is FP32: the words are the reference's bit for bit; the
+// variates agree with the FP64 ones to FP32 rounding (~1e-7 relative).
+__device__ __forceinline__ void sg_normal_3seq_f32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                                   uint32_t k1, float& n1, float& n2, float& n3) {
+    sg_u4 w = sg_philox(c0, c1, c2, c3, k0, k1);
+    const float s = 2.3283064365386963e-10f;   // 2^-32
+    const float u1 = fmaxf((float)w.x * s, 1.0e-35f);
+    const float u2 = (float)w.y * s;
+    const float u3 = fmaxf((float)w.z * s, 1.0e-35f);
+    const float u4 = (float)w.w * s;
+    const float r1 = sqrtf(-2.0f * logf(u1));
+    const float r2 = sqrtf(-2.0f * logf(u3));
+    float s1, c1v;
+    sincospif(2.0f * u2, &s1, &c1v);
+    n1 = r1 * c1v;
+    n2 = r1 * s1;
+    n3 = r2 * cospif(2.0f * u4);
+}
