@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--equil", type=int, default=1500, help="untimed Langevin equilibration steps")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary measurements")
+    ap.add_argument("--no-mlp", action="store_true", help="skip the learned-guess leg")
+    ap.add_argument("--mlp-samples", type=int, default=10_000_000)
+    ap.add_argument("--mlp-epochs", type=int, default=3)
     return ap.parse_args()
 
 
@@ -198,6 +201,73 @@ def cpu_baseline(g, w, seconds, nthreads=1):
     return m / dt, m
 
 
+def force_error_vs_fp64(g, w, pp, nthreads=None):
+    """Norm-wise relative error of the device forces and torques against the
+    oracle's FP64 evaluation with the tightly converged contact parameter, on
+    the same FP32 state and list."""
+    import oracle as O
+    r, q, v, l = g.download()
+    pi, pj = g.pairs()
+    g.zero_forces()
+    pe, _ = g.pair_forces(pp)
+    F, T = g.forces()
+    s = O.System(g.n, g.box, fast=True)
+    s.set_defaults(sig=w["sig"], eps=w["eps"])
+    s.rx[:], s.ry[:], s.rz[:] = r.T
+    s.qw[:], s.qx[:], s.qy[:], s.qz[:] = q.T
+    kind = getattr(O, w["kind"])
+    out = s.pair_batch(O.pair_params(kind, cutoff=w["cutoff"], solver=O.SOLVER_TIGHT), pi, pj,
+                       nthreads or os.cpu_count() or 1)
+    Fo = np.zeros((g.n, 3))
+    To = np.zeros((g.n, 3))
+    np.add.at(Fo, pi, out[:, 1:4])
+    np.add.at(Fo, pj, -out[:, 1:4])
+    np.add.at(To, pi, out[:, 4:7])
+    np.add.at(To, pj, out[:, 7:10])
+    peo = out[:, 0].sum()
+    nf = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    return {"force": nf(F, Fo), "torque": nf(T, To), "pot_eng": abs(pe - peo) / max(abs(peo), 1e-300)}
+
+
+def mlp_leg(a, g, w, torch, stream, flush, npairs):
+    """Train the learned guess on plain-Newton samples at T* 0.8, 1.2, 1.6 and
+    time the MLP-guess path against the plain path on the same state."""
+    from sucrose_gb300 import capi, mlp
+    r, q, v, l = g.download()          # restore the timed state afterwards
+    newton = pair_params(g, w, "newton")
+
+    def langevin(T):
+        g.configure_step(newton, integrator=capi.INT_LANGEVIN, dt=w["dt"], target_temp=T, damping=1.0, rotations=1)
+
+    t0 = time.perf_counter()
+    X, y = mlp.generate(g, newton, langevin, samples=a.mlp_samples, every=25, equil=200)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    hist = mlp.train(g, X, y, epochs=a.mlp_epochs, batch=65536, lr=2e-3, seed=1)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del X, y
+    g.upload(r=r, q=q, v=v, l=l)
+    g.build_nlist()
+    pm = pair_params(g, w, "mlp")
+    _, _, sm = g.pair_forces(pm, want_stats=True)
+    _, _, sp = g.pair_forces(newton, want_stats=True)
+    tm = statistics.median(timed_forces(g, torch, stream, pm, 10, flush))
+    tp = statistics.median(timed_forces(g, torch, stream, newton, 10, flush))
+    configure(g, w, pm)
+    g.step(5)
+    g.step_check()
+    t_step = timed_steps(g, torch, stream, 50, flush)
+    return {"samples": a.mlp_samples, "epochs": a.mlp_epochs, "train_mse": hist, "gen_s": t_gen, "train_s": t_train,
+            "force_kernel_ms": 1e3 * tm, "pair_evals_per_s_force_kernel": npairs / tm,
+            "plain_force_kernel_ms_same_state": 1e3 * tp, "speedup_vs_plain_force_kernel": tp / tm,
+            "full_step_pair_evals_per_s": npairs * 50 / t_step,
+            "mean_evals_per_pair": sm.solver_evals / max(sm.pairs, 1),
+            "plain_mean_evals_per_pair": sp.solver_evals / max(sp.pairs, 1),
+            "fallback_rate": sm.fallbacks / max(sm.pairs, 1), "nonconverged": int(sm.nonconverged),
+            "iter_hist": [int(x) for x in sm.iter_hist], "force_error_vs_fp64": force_error_vs_fp64(g, w, pm)}
+
+
 # -------------------------------------------------------------------- ours ---
 def run_ours(a):
     import torch
@@ -297,13 +367,22 @@ def run_ours(a):
         extras["fp64_peak_tflops_measured"] = g.peak_fma(True)
         extras["list_rebuilds_in_timed_region"] = int(builds)
         if a.config == "ecp" and a.solver == "newton":
+            # residual check variants of the same kernel
+            for mode, name in ((2, "double_float"), (0, "none")):
+                pv = pair_params(g, w, "newton")
+                pv.fp64_check = mode
+                tv = statistics.median(timed_forces(g, torch, stream, pv, 10, flush))
+                extras[f"newton_check_{name}_force_kernel_ms"] = 1e3 * tv
+                extras[f"newton_check_{name}_pair_evals_per_s"] = npairs / tv
             pb = pair_params(g, w, "brent")
             _, _, stb = g.pair_forces(pb, want_stats=True)
             tb = statistics.median(timed_forces(g, torch, stream, pb, 5, flush))
             extras["brent_compat_force_kernel_ms"] = 1e3 * tb
             extras["brent_compat_pair_evals_per_s"] = npairs / tb
             extras["brent_mean_evals_per_pair"] = stb.solver_evals / max(stb.pairs, 1)
-            extras["mlp"] = "not measured: no trained weights in this run"
+            extras["force_error_vs_fp64"] = force_error_vs_fp64(g, w, pp)
+            if not a.no_mlp:
+                extras["mlp"] = mlp_leg(a, g, w, torch, stream, flush, npairs)
 
     cpu = None
     if rank == 0:

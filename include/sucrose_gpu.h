@@ -78,7 +78,8 @@ typedef struct {
     double chirality;   /* gbc, gbwc, ecpc, ecpwc                                   */
     double newton_tol;  /* bound on |S'(lambda)| / (r.K) checked in FP64; 0 selects 1e-6 */
     int32_t newton_max_iter;  /* 0 selects 20                                       */
-    int32_t fp64_check; /* Newton: 1 = FP64 residual check (default), 0 = FP32 step-size test only */
+    int32_t fp64_check; /* Newton residual check: 1 = FP64 (default), 2 = double-float on the FP32 pipe,
+                           0 = none (FP32 step-size test only) */
 } sg_pair_params;
 
 /* Per-call statistics of an ECP force evaluation. */
@@ -243,6 +244,21 @@ int sg_philox_normal_3seq_device(sg_ctx* ctx, int64_t n, const int32_t* ctr, dou
 int sg_mlp_set_weights(sg_ctx* ctx, const float* w, int64_t count);
 int sg_mlp_get_weights(sg_ctx* ctx, float* w, int64_t count);
 int64_t sg_mlp_weight_count(void);
+/* Seeded Kaiming-uniform initialisation; resets the Adam state. */
+int sg_mlp_init(sg_ctx* ctx, uint64_t seed);
+/* Features (BF16, 16 per pair, x_bf16 is a DEVICE buffer) and labels (the
+ * lambda of the last ECP call, FP32, DEVICE) for the current list. */
+int sg_mlp_features(sg_ctx* ctx, void* x_bf16, float* y, int64_t capacity, int64_t* count);
+/* Tensor-core training: one Adam step on a minibatch (DEVICE x_bf16 rows x 16,
+ * y rows), MSE on the sigmoid output; loss_host may be NULL. */
+int sg_mlp_train_step(sg_ctx* ctx, const void* x_bf16, const float* y, int64_t rows, float lr, float* loss_host);
+/* Gradients of the MSE loss (packed like the weights) without an update. */
+int sg_mlp_grad(sg_ctx* ctx, const void* x_bf16, const float* y, int64_t rows, float* grad_host, float* loss_host);
+/* The in-kernel guess (warp-level MMA inference, clamped to [0.02, 0.98]) for
+ * every listed pair, in sg_nlist_pairs order, into a DEVICE buffer. */
+int sg_mlp_guess(sg_ctx* ctx, float* out_dev, int64_t capacity);
+/* Forward pass of the training path: yhat (DEVICE, rows). */
+int sg_mlp_predict(sg_ctx* ctx, const void* x_bf16, int64_t rows, float* yhat_dev);
 
 #ifdef __cplusplus
 }

@@ -96,6 +96,12 @@ SIGNATURES = [
     ("sg_mlp_set_weights", C.c_int, [_P, _F, C.c_int64]),
     ("sg_mlp_get_weights", C.c_int, [_P, _F, C.c_int64]),
     ("sg_mlp_weight_count", C.c_int64, []),
+    ("sg_mlp_init", C.c_int, [_P, C.c_uint64]),
+    ("sg_mlp_features", C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_int64, _I64]),
+    ("sg_mlp_train_step", C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, _F]),
+    ("sg_mlp_grad", C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_int64, _F, _F]),
+    ("sg_mlp_predict", C.c_int, [_P, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("sg_mlp_guess", C.c_int, [_P, C.c_void_p, C.c_int64]),
 ]
 
 _lib = None

@@ -276,14 +276,24 @@ SG_DEV NewtonResult newton_solve(const float* A, const float* D, float3 r, float
     return res;
 }
 
-// Normalised residual S'(lambda) / (r.K) with K refined once in FP64: the
-// matrix G = A + lambda D and the linear-system residual e = r - G K are
-// formed in FP64 (15 DFMA), the correction G^-1 e is solved with the FP32
-// factor, and the two terms of S' are then formed from the refined K. With K
-// accurate to ~1e-13, the FP32 products contribute ~1e-7 of r.K to S' (well
-// under the 1e-6 bound); without the refinement the FP32 solve alone leaves an
-// error of the order of the bound. Also returns S'' from FP32.
-SG_DEV double residual64(const float* A, const float* D, float3 r, float lam, const Chol& c, float3 K, float& s2) {
+// Residual check of the contact solve. The linear-system residual
+// e = r - G K of the FP32 solution K, with G = A + lambda D formed exactly, is
+// evaluated in extended precision, the correction G^-1 e is solved with the
+// FP32 factor, and S'(lambda) = (1-2l) r.K - l(1-l) K.D.K is formed from the
+// refined K. With K accurate to ~1e-13 the FP32 dot products contribute
+// ~1e-7 of r.K to S' (ten times under the 1e-6 bound); without the refinement
+// the FP32 solve alone leaves an error of the order of the bound.
+//   mode 1: e in FP64 (6 + 12 DFMA, no division);
+//   mode 2: e in double-float arithmetic on the FP32 pipe (error-free
+//           products and sums, ~48-bit significand), no FP64 instruction.
+// Returns s1 = S' and rK = r.K (the check is |s1| <= tol rK) and S'' (FP32).
+SG_DEV void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+SG_DEV float3 lin_residual_fp64(const float* A, const float* D, float3 r, float lam, float3 K) {
     const double L = lam;
     double g[6];
 #pragma unroll
@@ -292,15 +302,56 @@ SG_DEV double residual64(const float* A, const float* D, float3 r, float lam, co
     const double ex = (double)r.x - fma(g[0], kx, fma(g[1], ky, g[2] * kz));
     const double ey = (double)r.y - fma(g[1], kx, fma(g[3], ky, g[4] * kz));
     const double ez = (double)r.z - fma(g[2], kx, fma(g[4], ky, g[5] * kz));
-    const float3 dk = chol_solve(c, make_float3((float)ex, (float)ey, (float)ez));
+    return make_float3((float)ex, (float)ey, (float)ez);
+}
+
+SG_DEV float3 lin_residual_df(const float* A, const float* D, float3 r, float lam, float3 K) {
+    // G = A + lam D as hi + lo (exact up to the lo rounding)
+    float gh[6], gl[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+        const float p = lam * D[m];
+        const float pe = fmaf(lam, D[m], -p);
+        float sh, se;
+        two_sum(A[m], p, sh, se);
+        gh[m] = sh;
+        gl[m] = se + pe;
+    }
+    const float kv[3] = {K.x, K.y, K.z};
+    const float rv[3] = {r.x, r.y, r.z};
+    const int row[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    float out[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        // e_i = r_i - sum_j G_ij K_j, accumulated as hi + lo
+        float hi = rv[i], lo = 0.f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int m = row[i][j];
+            const float t = gh[m] * kv[j];
+            const float te = fmaf(gh[m], kv[j], -t);
+            float sh, se;
+            two_sum(hi, -t, sh, se);
+            hi = sh;
+            lo += se - te - gl[m] * kv[j];
+        }
+        out[i] = hi + lo;
+    }
+    return make_float3(out[0], out[1], out[2]);
+}
+
+SG_DEV float residual_check(int mode, const float* A, const float* D, float3 r, float lam, const Chol& c, float3 K,
+                            float& rK_out, float& s2) {
+    const float3 e = mode == 2 ? lin_residual_df(A, D, r, lam, K) : lin_residual_fp64(A, D, r, lam, K);
+    const float3 dk = chol_solve(c, e);
     const float3 Kr = make_float3(K.x + dk.x, K.y + dk.y, K.z + dk.z);
     const float3 DK = symv(D, Kr);
     const float rK = dot3(r, Kr), KDK = dot3(Kr, DK);
     const float3 Z = chol_solve(c, DK);
     const float l1 = lam * (1.f - lam);
     s2 = -2.f * rK - 2.f * (1.f - 2.f * lam) * KDK + 2.f * l1 * dot3(DK, Z);
-    const double s1 = (1.0 - 2.0 * L) * (double)rK - L * (1.0 - L) * (double)KDK;
-    return s1 / fmax((double)rK, 1e-30);
+    rK_out = rK;
+    return (1.f - 2.f * lam) * rK - l1 * KDK;
 }
 
 template <int SOLVER>
@@ -370,15 +421,14 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
     lam = nr.lam;
     nonconv = !nr.converged;
     if (fp64_check) {
-        float s2;
-        const double rho = residual64(A, D, r, lam, nr.c, nr.K, s2);
-        if (fabs(rho) > (double)tol) {
-            // one Newton step driven by the FP64 residual
+        float s2, rK;
+        const float s1 = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2);
+        if (!(fabsf(s1) <= tol * rK)) {
+            // one Newton step driven by the extended-precision residual
             refined = true;
             evals += 1;
             if (s2 < 0.f) {
-                const double rK = dot3(r, nr.K);
-                const float ln = lam - (float)(rho * rK / (double)s2);
+                const float ln = lam - s1 / s2;
                 if (ln > 0.f && ln < 1.f) {
                     lam = ln;
                     float g[6];
@@ -388,7 +438,8 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
                     nr.K = chol_solve(nr.c, r);
                 }
             }
-            if (fabs(residual64(A, D, r, lam, nr.c, nr.K, s2)) > (double)tol) nonconv = true;
+            const float s1b = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2);
+            if (!(fabsf(s1b) <= tol * rK)) nonconv = true;
         }
     }
     cR = nr.c;

@@ -82,6 +82,8 @@ struct sg_ctx {
     void* mlp_wbf16 = nullptr;       // device: bf16 W1 W2 W3 then f32 b1 b2 b3 w4
     unsigned char mlp_host_desc[128];  // host copy of the MlpDev descriptor (device pointers)
     int mlp_ready = 0;
+    void* mlp_work = nullptr;        // training workspace (mlp_train.cu)
+    int mlp_adam_t = 0;
 
     // staging (pinned host) for uploads / downloads
     float4* h_stage = nullptr;
@@ -186,3 +188,4 @@ int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p);
 int sg_nlist_free(sg_ctx* ctx);
+void sg_mlp_free(sg_ctx* ctx);

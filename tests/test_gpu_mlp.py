@@ -1,0 +1,87 @@
+"""The learned contact-parameter guess: device training gradients against the
+numpy reference, in-kernel inference against the training forward pass, and
+what a trained network gains over the plain Newton start."""
+import numpy as np
+import pytest
+
+from helpers import Pair, ellipsoids
+from oracle import mlp_ref as M
+from sucrose_gb300 import capi, mlp
+
+pytestmark = pytest.mark.gpu
+SIG = (3.0, 2.0, 1.0)
+
+
+def small_ecp(counts=(8, 12, 16), seed=3):
+    r, q, box = ellipsoids(counts, SIG, 0.1114, seed=seed, tilt=0.5)
+    P = Pair(r, q, box, sig=SIG)
+    P.g.init_nlist(0.3, 3.0, trigger_mode=1)
+    return P
+
+
+def test_mlp_gradients_match_reference(lib):
+    import torch
+    P = small_ecp()
+    g = P.g
+    capi.check(g.ctx, g.L.sg_mlp_init(g.ctx, 7))
+    rng = np.random.default_rng(1)
+    Xf = rng.normal(size=(512, 16)).astype(np.float32) * 0.7
+    Xf[:, 14:] = 0.0
+    y = rng.uniform(0.2, 0.8, size=512).astype(np.float32)
+    X = torch.tensor(Xf, device="cuda").to(torch.bfloat16)
+    yt = torch.tensor(y, device="cuda")
+    gd, loss = mlp.grad(g, X, yt)
+    w = g.get_mlp_weights()
+    lref, gref, _ = M.forward_backward(w, X.float().cpu().numpy(), y.astype(np.float64), bf=True)
+    assert abs(loss - lref) <= 1e-5 * abs(lref)
+    blocks = [(M.OFF_W1, M.OFF_B1), (M.OFF_B1, M.OFF_W2), (M.OFF_W2, M.OFF_B2), (M.OFF_B2, M.OFF_W3),
+              (M.OFF_W3, M.OFF_B3), (M.OFF_B3, M.OFF_W4), (M.OFF_W4, M.OFF_B4), (M.OFF_B4, M.NPARAM)]
+    for a, b in blocks:
+        e = np.linalg.norm(gd[a:b] - gref[a:b]) / max(np.linalg.norm(gref[a:b]), 1e-30)
+        # BF16 rounding of intermediate gradients may round differently when
+        # their FP32 inputs differ in the last bit: 1e-2 norm-wise per block
+        assert e < 1e-2, (a, b, e)
+
+
+def test_inference_kernel_matches_training_forward(lib):
+    import torch
+    P = small_ecp(seed=4)
+    g = P.g
+    capi.check(g.ctx, g.L.sg_mlp_init(g.ctx, 11))
+    g.zero_forces()
+    g.pair_forces(g.params(capi.ECPR, solver=capi.SOLVER_NEWTON))
+    k = g.npairs()
+    X = torch.empty((k, 16), dtype=torch.bfloat16, device="cuda")
+    y = torch.empty(k, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    import ctypes as C
+    cnt = C.c_int64(0)
+    capi.check(g.ctx, g.L.sg_mlp_features(g.ctx, C.c_void_p(X.data_ptr()), C.c_void_p(y.data_ptr()), k, C.byref(cnt)))
+    assert cnt.value == k
+    pred = mlp.predict(g, X).clamp(0.02, 0.98).cpu().numpy()
+    inf = mlp.guess(g).cpu().numpy()
+    assert np.max(np.abs(pred - inf)) < 2e-3
+
+
+def test_trained_guess_cuts_newton_iterations(lib):
+    P = small_ecp(counts=(12, 16, 24), seed=5)
+    g = P.g
+    newton = g.params(capi.ECPR, solver=capi.SOLVER_NEWTON)
+
+    def langevin(T):
+        g.configure_step(newton, integrator=capi.INT_LANGEVIN, dt=0.001, target_temp=T, damping=1.0, rotations=1)
+
+    X, y = mlp.generate(g, newton, langevin, samples=400_000, every=20, equil=100)
+    hist = mlp.train(g, X, y, epochs=12, batch=8192, lr=3e-3, seed=2)
+    assert hist[-1] < 0.2 * hist[0]
+    g.zero_forces()
+    _, _, plain = g.pair_forces(newton, want_stats=True)
+    g.zero_forces()
+    _, _, learned = g.pair_forces(g.params(capi.ECPR, solver=capi.SOLVER_MLP_NEWTON), want_stats=True)
+    mean_plain = plain.solver_evals / plain.pairs
+    mean_mlp = learned.solver_evals / learned.pairs
+    print(f"Newton evaluations per pair: plain {mean_plain:.3f}, learned guess {mean_mlp:.3f}, "
+          f"fallbacks {learned.fallbacks / learned.pairs:.4f}, final mse {hist[-1]:.2e}")
+    assert learned.nonconverged == 0
+    assert mean_mlp < mean_plain
+    assert learned.fallbacks < 0.01 * learned.pairs
