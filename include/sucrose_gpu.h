@@ -230,6 +230,34 @@ int sg_step_kernel_count(sg_ctx* ctx, int64_t* count);
  * TFLOP/s: the roofline denominator of the FP32-pipe pair kernels. */
 int sg_peak_fma(sg_ctx* ctx, int32_t fp64, double* tflops);
 
+/* ---- pair forces without any allocation -------------------------------------- */
+/* No counterpart in the reference. For callers that keep their particle data
+ * in device memory and cannot call cudaMalloc where they call this: code that
+ * runs while another library captures the stream into a CUDA graph, hosts
+ * whose device memory comes from their own pool, OpenACC / CUDA Fortran
+ * programs that keep RX, RY, RZ and FX, FY, FZ resident on the device.
+ *
+ * Evaluates lj_ / lj12_ / ljw_ / wca_ (params->kind) over the half list
+ * (pair_i[k] < pair_j[k], 0-based) and ADDS the forces into fx, fy, fz and
+ * {pot_eng, pair virial} into pot_virial[0..1], like the reference's pair
+ * loop (README.md:86-103). rx..rz, pair_i, pair_j, fx..fz and pot_virial are
+ * DEVICE pointers owned by the caller; box and params are host memory; the
+ * work is enqueued on `stream` (a cudaStream_t, NULL for the default stream)
+ * and the call returns without waiting.
+ *
+ * It allocates nothing: its scratch is a fixed device array inside the
+ * library (about 2.1 MiB, held by every GPU that loads the library until the
+ * process exits), which limits n to 131072 particles; larger n returns
+ * SG_EINVAL with a message in err. The first call on a device looks the
+ * scratch up for that device, so make that first call before any stream
+ * capture. All calls share the scratch: calls whose work overlaps on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller. err (may be NULL) receives a message on failure. */
+int sg_lj_forces_noalloc(int32_t n, const double* rx, const double* ry, const double* rz, const int32_t* pair_i,
+                         const int32_t* pair_j, int64_t npairs, const double box[3], int32_t periodic,
+                         const sg_pair_params* params, double* fx, double* fy, double* fz, double* pot_virial,
+                         void* stream, char* err, int32_t err_len);
+
 /* ---- Philox4x32-10 (fortran/xmath.f90:42-113) -------------------------------- */
 /* Host-side single block, for callers that mirror philox_uniform. */
 void sg_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
