@@ -45,7 +45,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="ecp", choices=sorted(WORKLOADS))
+    ap.add_argument("--config", default="ecp", choices=sorted(WORKLOADS) + ["replicas"])
+    ap.add_argument("--nrep", type=int, default=4096, help="replicas (config replicas)")
+    ap.add_argument("--rep-equil", type=int, default=300, help="untimed equilibration steps (config replicas)")
     ap.add_argument("--solver", default="newton", choices=["newton", "brent", "mlp"])
     ap.add_argument("--equil", type=int, default=1500, help="untimed Langevin equilibration steps")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU-baseline sample")
@@ -139,6 +141,18 @@ def configure(g, w, pp, langevin=False, first_step=1):
                          rotations=1, first_step=first_step)
     else:
         g.configure_step(pp, integrator=capi.INT_NH, dt=w["dt"], target_temp=w["T"], rotations=1, rot_chain=1)
+
+
+def pair_flops(kind, listed, in_range, mean_evals=0.0):
+    """Algorithmic FP32 flops of one pair-force launch, counted from the kernel
+    sources (FMA = 2 flops, sqrt / rsqrt / division = 1). Every listed pair
+    pays the distance and, for Gay-Berne, the orientation terms up to the range
+    test; pairs in range pay the force and torque terms."""
+    if kind.startswith("ECP"):
+        return ecp_flops_per_pair(mean_evals) * listed
+    if kind.startswith("GB"):
+        return 80.0 * listed + 240.0 * in_range
+    return 20.0 * listed + 20.0 * in_range
 
 
 def ecp_flops_per_pair(mean_evals):
@@ -275,12 +289,12 @@ def run_ours(a):
     __graft_entry__.build_library()
     from sucrose_gb300 import capi
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from sucrose_gb300 import ranks
+    rank, world, local = ranks.rank_info()
     torch.cuda.set_device(local)
     w = WORKLOADS[a.config]
-    g, box = make_system(w, seed=1003 + rank)
+    # replicas only: every rank runs its own independent system
+    g, box = make_system(w, seed=ranks.replica_seed(1003, rank))
     stream = torch.cuda.ExternalStream(g.stream_ptr())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     pp = pair_params(g, w, a.solver)
@@ -310,9 +324,7 @@ def run_ours(a):
     builds = g.nlist_builds() - builds0
     npairs = 0.5 * (p_before + p_after)
     if dist is not None:
-        tt = torch.tensor([t_dev], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
+        t_dev = ranks.max_over_ranks(t_dev, device="cuda")
     ms_per_step = 1e3 * t_dev / a.steps
     value = npairs * a.steps * world / t_dev
     steps_per_s = a.steps / t_dev
@@ -324,7 +336,7 @@ def run_ours(a):
     tf = timed_forces(g, torch, stream, pp, 20, flush)
     t_force = statistics.median(tf)
     peak32 = g.peak_fma(False)
-    flops = ecp_flops_per_pair(mean_evals) * npairs
+    flops = pair_flops(w["kind"], st.pairs, st.solver_evals, mean_evals)
     achieved = flops / t_force / 1e12
 
     # e2e: FP64 host arrays in and out through the C ABI every step
@@ -360,7 +372,10 @@ def run_ours(a):
     if not a.no_extras and rank == 0:
         extras["force_kernel_pair_evals_per_s"] = npairs / t_force
         extras["force_kernel_ms"] = 1e3 * t_force
-        extras["newton_mean_evals_per_pair"] = mean_evals
+        if w["kind"].startswith("ECP"):
+            extras["newton_mean_evals_per_pair"] = mean_evals
+        else:
+            extras["pairs_in_range_frac"] = st.solver_evals / max(st.pairs, 1)
         extras["newton_iter_hist"] = [int(x) for x in st.iter_hist]
         extras["newton_fp64_refined_frac"] = st.fp64_refined / max(st.pairs, 1)
         extras["nonconverged"] = int(st.nonconverged)
@@ -403,7 +418,8 @@ def run_ours(a):
             "ns_per_day": ns_day, "tau_per_day": steps_per_s * w["dt"] * 86400.0,
             "e2e": {"value": e2e_value, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(kernels_per_step * a.steps),
-            "roofline": {"bound": "fp32", "kernel": "k_pair<PotECP>", "achieved": achieved, "peak": peak32,
+            "roofline": {"bound": "fp32", "kernel": "k_pair<PotECP>" if w["kind"].startswith("ECP") else "k_pair<PotGB>",
+                         "achieved": achieved, "peak": peak32,
                          "unit": "TFLOP/s", "frac": achieved / peak32,
                          "peak_source": "measured FMA throughput (sg_peak_fma) on this GPU",
                          "traffic": None},
@@ -416,6 +432,277 @@ def run_ours(a):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------- replicas ---
+REPLICAS = dict(workload="replicas_4096_lj_gb_langevin_n64to2048", nrep=4096, seed=1005, dt=0.002, damping=1.0)
+
+
+def replica_arrays(e):
+    """Per-particle constants and initial velocities / angular momenta of an
+    ensemble from configs.replica_ensemble (seeded per replica)."""
+    from sucrose_gb300 import configs
+    fams = (configs.LJ_REPLICA, configs.GB_REPLICA)
+    sig, eps, inert, v, l = [], [], [], [], []
+    for k in range(len(e["n"])):
+        n = int(e["n"][k])
+        p = fams[e["family"][k]]
+        I = configs.default_inertia(p["sig"])
+        sig.append(np.tile(p["sig"], (n, 1)))
+        eps.append(np.tile(p["eps"], (n, 1)))
+        inert.append(np.tile(I, (n, 1)))
+        v.append(configs.velocities_to_temperature(n, e["temp"][k], 1 + k))
+        a, b = e["off"][k], e["off"][k + 1]
+        l.append(configs.angular_momenta(e["q"][a:b], I, e["temp"][k], 1 + k) if e["family"][k] == 1
+                 else np.zeros((n, 3)))
+    return [np.concatenate(x) for x in (sig, eps, inert, v, l)]
+
+
+def replica_pair_params():
+    from sucrose_gb300 import GpuSystem, capi, configs
+    return [GpuSystem.params(capi.LJ, cutoff=configs.LJ_REPLICA["cutoff"]),
+            GpuSystem.params(capi.GB, cutoff=configs.GB_REPLICA["cutoff"], mu=2, nu=1)]
+
+
+def run_replicas(a):
+    """Batched replicas: one captured step advances all 4096 replicas; the
+    same replicas as 4096 single-system contexts, each stepped by its own
+    captured graph one after another, give the sequential-launch comparison."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from sucrose_gb300 import GpuSystem, capi, configs, ranks
+    rank, world, local = ranks.rank_info()
+    torch.cuda.set_device(local)
+    W = REPLICAS
+    t0 = time.perf_counter()
+    e = configs.replica_ensemble(a.nrep, seed=ranks.replica_seed(W["seed"], rank))
+    sig, eps, inert, v0, l0 = replica_arrays(e)
+    t_setup_host = time.perf_counter() - t0
+    LJ, GB = configs.LJ_REPLICA, configs.GB_REPLICA
+    skins = [LJ["skin"], GB["skin"], 0.3]
+    cuts = [LJ["list_cutoff"], GB["list_cutoff"], 3.0]
+    g = GpuSystem.replicas(e["n"], e["box"], e["family"], e["temp"], e["key"])
+    g.set_particles(mass=1.0, sig=sig, eps=eps, inertia=inert)
+    g.upload(r=e["r"], q=e["q"], v=v0, l=l0)
+    g.init_rep_nlist(skins, cuts, trigger_mode=1)
+    pairs = replica_pair_params()
+    stream = torch.cuda.ExternalStream(g.stream_ptr())
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    dt = W["dt"]
+
+    def configure(step_dt, first):
+        g.configure_step_pairs(pairs, integrator=capi.INT_LANGEVIN, dt=step_dt, damping=W["damping"], rotations=1,
+                               first_step=first)
+
+    # untimed equilibration from the lattice: short steps first
+    configure(dt / 4, 1)
+    g.step(a.rep_equil // 2)
+    g.step_check()
+    configure(dt, 1 + a.rep_equil // 2)
+    g.step(a.rep_equil - a.rep_equil // 2)
+    g.step_check()
+    g.step(max(a.warmup, 3))
+    g.step_check()
+    kernels_per_step = g.step_kernel_count()
+    p_before = g.npairs()
+    builds0 = g.nlist_builds()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_dev = timed_steps(g, torch, stream, a.steps, flush)
+    g.step_check()
+    npairs = 0.5 * (p_before + g.npairs())
+    builds = g.nlist_builds() - builds0
+    if world > 1:
+        t_dev = ranks.max_over_ranks(t_dev, device="cuda")
+    ms_per_step = 1e3 * t_dev / a.steps
+    value = npairs * a.steps * world / t_dev
+
+    # dominant kernels: each family's pair launch timed alone
+    fam = {}
+    peak32 = g.peak_fma(False)
+    for pp, name in zip(pairs, ("LJ", "GB")):
+        _, _, st = g.pair_forces(pp, want_stats=True)
+        tk = statistics.median(timed_forces(g, torch, stream, pp, 10, flush))
+        fl = pair_flops(name, st.pairs, st.solver_evals)
+        fam[name] = {"listed_pairs": int(st.pairs), "in_range": int(st.solver_evals), "force_kernel_ms": 1e3 * tk,
+                     "tflops": fl / tk / 1e12}
+    top = max(fam, key=lambda k: fam[k]["force_kernel_ms"])
+
+    # e2e through the C ABI: FP64 host state in and out every step
+    n = g.n
+    host = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(13)]
+    import ctypes as C
+    D = C.POINTER(C.c_double)
+    r, q, v, l = g.download()
+    for k in range(3):
+        host[k][:], host[7 + k][:], host[10 + k][:] = r[:, k], v[:, k], l[:, k]
+    for k in range(4):
+        host[3 + k][:] = q[:, k]
+    ptrs = [h.ctypes.data_as(D) for h in host]
+    energies = np.zeros(4)
+    e_steps = 10
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e_steps):
+        capi.check(g.ctx, g.L.sg_upload_state(g.ctx, *ptrs))
+        g.step(1)
+        capi.check(g.ctx, g.L.sg_download_state(g.ctx, *ptrs))
+        capi.check(g.ctx, g.L.sg_read_energies(g.ctx, energies.ctypes.data_as(D)))
+    t_e2e = time.perf_counter() - t0
+
+    # the same replicas one context each, stepped one after another
+    seq = None
+    if rank == 0 and not a.no_extras:
+        r, q, v, l = g.download()
+        t0 = time.perf_counter()
+        singles = []
+        fams = (LJ, GB)
+        for k in range(len(e["n"])):
+            lo, hi = e["off"][k], e["off"][k + 1]
+            f = int(e["family"][k])
+            s = GpuSystem(int(e["n"][k]), e["box"][k])
+            s.set_particles(mass=1.0, sig=sig[lo:hi], eps=eps[lo:hi], inertia=inert[lo:hi])
+            s.upload(r=r[lo:hi], q=q[lo:hi], v=v[lo:hi], l=l[lo:hi])
+            s.init_nlist(fams[f]["skin"], fams[f]["list_cutoff"], trigger_mode=1)
+            s.configure_step(pairs[f], integrator=capi.INT_LANGEVIN, dt=dt, damping=W["damping"], rotations=1,
+                             target_temp=e["temp"][k], key=e["key"][k], first_step=1000)
+            s.step(1)          # eager step + capture of the single-system graph
+            singles.append(s)
+        torch.cuda.synchronize()
+        t_seq_setup = time.perf_counter() - t0
+        seq_steps = 3
+        t0 = time.perf_counter()
+        for _ in range(seq_steps):
+            for s in singles:
+                s.step(1)
+        torch.cuda.synchronize()
+        t_seq = (time.perf_counter() - t0) / seq_steps
+        for s in singles:
+            s.step_check()
+            s.close()
+        seq = {"ms_per_step": 1e3 * t_seq, "contexts": len(singles), "setup_s": t_seq_setup,
+               "batched_speedup": t_seq / (t_dev / a.steps),
+               "how": "one context and one captured step graph per replica, launched one after another from the "
+                      "host each step (each context on its own stream); host wall clock over 3 steps with device "
+                      "synchronisation at both ends"}
+
+    cpu = None
+    if rank == 0:
+        cpu = replica_cpu_sample(e, a.cpu_seconds, nthreads=1)
+    if rank == 0:
+        nrep_total = len(e["n"]) * world
+        line = {
+            "metric": "replica-ensemble pair-evals/s (4096 LJ + GB replicas, one captured step for all)",
+            "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (fp64 sums)", "data": "synthetic (seeded replica ensemble, device-equilibrated)",
+            "config": {"workload": W["workload"], "replicas": len(e["n"]), "particles": int(n),
+                       "listed_pairs": npairs, "lj_replicas": int(np.sum(e["family"] == 0)),
+                       "gb_replicas": int(np.sum(e["family"] == 1)), "count_redraws": int(e["redraws"]),
+                       "dt": dt, "integrator": "Langevin (translation + rotation), per-replica T and Philox key",
+                       "l2": "inputs larger than L2 (and a 256 MB write between timed steps)",
+                       "parallelism": "replicas only" if world > 1 else "single GPU"},
+            "replica_steps_per_s": nrep_total * a.steps / t_dev,
+            "e2e": {"value": npairs * e_steps / t_e2e, "unit": "pair-evals/s", "h2d_bytes_per_step": 13 * 8 * n,
+                    "d2h_bytes_per_step": 13 * 8 * n + 32},
+            "gpu_launches": int(kernels_per_step * a.steps),
+            "roofline": {"bound": "fp32", "kernel": f"k_pair<Pot{top}> (replica family range)",
+                         "achieved": fam[top]["tflops"], "peak": peak32, "unit": "TFLOP/s",
+                         "frac": fam[top]["tflops"] / peak32,
+                         "peak_source": "measured FMA throughput (sg_peak_fma) on this GPU", "traffic": None},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "families": fam,
+            "list_rebuilds_in_timed_region": int(builds),
+            "sequential_single_system": seq,
+            "host_setup_s": t_setup_host,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def replica_cpu_systems(e, stride=97):
+    """Oracle systems and k-d-tree lists (the reference's list contents) for
+    every stride-th LJ and GB replica, interleaved."""
+    import oracle as O
+    from scipy.spatial import cKDTree
+    from sucrose_gb300 import configs
+    fams = (configs.LJ_REPLICA, configs.GB_REPLICA)
+    R = len(e["n"])
+    lj, gb = list(range(0, R // 2, stride)), list(range(R // 2, R, stride))
+    idx = [k for pair in zip(lj, gb) for k in pair] + lj[len(gb):] + gb[len(lj):]
+    out = []
+    for k in idx:
+        f = int(e["family"][k])
+        p = fams[f]
+        lo, hi = e["off"][k], e["off"][k + 1]
+        box = e["box"][k]
+        r = e["r"][lo:hi]
+        t = cKDTree((r + box / 2) % box, boxsize=box)
+        pr = t.query_pairs(p["list_cutoff"] + p["skin"], output_type="ndarray")
+        if len(pr) == 0:
+            continue
+        pr.sort(axis=1)
+        s = O.System(hi - lo, box, fast=True)
+        s.set_defaults(sig=p["sig"], eps=p["eps"])
+        s.rx[:], s.ry[:], s.rz[:] = r.T
+        s.qw[:], s.qx[:], s.qy[:], s.qz[:] = e["q"][lo:hi].T
+        pp = O.pair_params(O.LJ if f == 0 else O.GB, cutoff=p["cutoff"], mu=2 if f else None, nu=1 if f else None)
+        out.append((s, pp, pr[:, 0].astype(np.int32).copy(), pr[:, 1].astype(np.int32).copy()))
+    return out
+
+
+def replica_cpu_sample(e, seconds, nthreads=1):
+    """The oracle's restatement of the reference pair routines (lj_, gb_) on
+    whole replicas, one after another, until about `seconds` have passed."""
+    done, spent, reps = 0, 0.0, 0
+    for s, pp, pi, pj in replica_cpu_systems(e):
+        t0 = time.perf_counter()
+        s.pair_batch(pp, pi, pj, nthreads)
+        spent += time.perf_counter() - t0
+        done += len(pi)
+        reps += 1
+        if spent > seconds:
+            break
+    return {"value": done / max(spent, 1e-9), "unit": "pair-evals/s", "cores": nthreads, "kind": "port",
+            "sample": f"{reps} whole replicas (every 97th LJ and GB replica, interleaved), {done} listed pairs, the "
+                      "reference's lj_ / gb_ restated in C++ (FP64), oracle built -O3 -ffast-math"}
+
+
+def run_reference_replicas(a):
+    """Reference arm for the replica ensemble: the restated lj_ / gb_ on the
+    host cores (OpenMP), each step one pass over a fixed sample of whole
+    replicas."""
+    from sucrose_gb300 import configs
+    e = configs.replica_ensemble(a.nrep, seed=REPLICAS["seed"])
+    systems = replica_cpu_systems(e)
+    nth = os.cpu_count() or 1
+    per_step = 0
+    chosen = []
+    for sy in systems:          # about 2M pairs per step
+        chosen.append(sy)
+        per_step += len(sy[2])
+        if per_step > 2000000:
+            break
+    for _ in range(a.warmup):
+        for s, pp, pi, pj in chosen[:2]:
+            s.pair_batch(pp, pi, pj, nth)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        for s, pp, pi, pj in chosen:
+            s.pair_batch(pp, pi, pj, nth)
+    dt = time.perf_counter() - t0
+    value = per_step * a.steps / dt
+    line = {"impl": "reference", "metric": "replica-ensemble pair-evals/s (4096 LJ + GB replicas, one captured step for all)",
+            "value": value, "unit": "pair-evals/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * dt / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64", "data": "synthetic (seeded replica ensemble, lattice state)",
+            "config": {"workload": REPLICAS["workload"], "replicas_sampled": len(chosen), "per_step_pairs": per_step},
+            "cpu_baseline": {"value": value, "unit": "pair-evals/s", "cores": nth, "kind": "port",
+                             "sample": f"{len(chosen)} whole replicas per step ({per_step} pairs); the reference "
+                                       "lj_ / gb_ restated in C++, OpenMP"},
+            "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 # --------------------------------------------------------------- reference ---
 def run_reference(a):
     """The reference's pair routine restated on the CPU (its Fortran has no
@@ -423,6 +710,8 @@ def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if a.config == "replicas":
+        return run_reference_replicas(a)
     import oracle as O
     from scipy.spatial import cKDTree
     from sucrose_gb300 import configs
@@ -467,5 +756,7 @@ if __name__ == "__main__":
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "replicas":
+        run_replicas(args)
     else:
         run_ours(args)

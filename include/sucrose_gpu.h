@@ -82,10 +82,12 @@ typedef struct {
                            0 = none (FP32 step-size test only) */
 } sg_pair_params;
 
-/* Per-call statistics of an ECP force evaluation. */
+/* Per-call statistics of a pair-force evaluation. ECP kinds fill every field;
+ * LJ and GB kinds fill pairs and, in solver_evals, the pairs that were inside
+ * the potential's range (the rest were listed but out of range). */
 typedef struct {
     int64_t pairs;          /* pairs evaluated                                      */
-    int64_t solver_evals;   /* total objective / Newton evaluations                 */
+    int64_t solver_evals;   /* ECP: total objective / Newton evaluations; LJ, GB: pairs in range */
     int64_t nonconverged;   /* pairs whose solve hit its iteration cap              */
     int64_t fallbacks;      /* MLP path: pairs that fell back to the plain Newton   */
     int64_t iter_hist[24];  /* Newton iterations per pair (last bin: >= 23)         */
@@ -191,6 +193,26 @@ int sg_nht_state(sg_ctx* ctx, double* get12, const double* set12);
  * dof and density as in initialize_system; kin_eng/kin_rot from the last integrator call. */
 int sg_thermo(sg_ctx* ctx, int32_t dof, double density, int32_t nrigid, double* out3);
 
+/* ---- batched replicas (no counterpart in the reference: its state is one
+ * global system, fortran/system.f90:7-39) ------------------------------------ */
+/* nrep independent periodic systems of uneven size in one context: replica r
+ * holds n_per_rep[r] particles, box boxes[3r..3r+2], potential family
+ * family[r] (0 = LJ kinds, 1 = GB kinds, 2 = ECP kinds; replicas grouped by
+ * family in increasing order), Langevin temperature temps[r] and Philox key
+ * keys[2r..2r+1] (NULL: the reference key). State arrays are the replicas'
+ * arrays concatenated, each in its own box centred on the origin. Every other
+ * entry point then acts on all replicas at once: pair calls evaluate the
+ * replicas of the params' family, Langevin uses each replica's T and key with
+ * the particle's index within its replica in the counter, so a replica draws
+ * the numbers of its own single-system run. Nose-Hoover is per system and not
+ * available here. */
+int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, const double* boxes,
+                       const int32_t* family, const double* temps, const uint32_t* keys, int32_t device);
+/* Verlet lists of every replica; skin[f], cutoff[f] per family f (3 each). */
+int sg_rep_nlist_init(sg_ctx* ctx, const double* skin, const double* cutoff, int32_t trigger_mode);
+/* Per-replica kinetic energies: ke2[2r] translational, ke2[2r+1] rotational (FP64). */
+int sg_rep_kinetic(sg_ctx* ctx, double* ke2);
+
 /* ---- whole timestep, captured in a CUDA graph ------------------------------- */
 /* One timestep in the reference's README order (README.md:83-115, with the
  * Verlet list of fortran/system.f90:1005 and :966): integrator initial half
@@ -219,6 +241,10 @@ typedef struct {
  * allocates every buffer), then captures one step as a CUDA graph; later
  * steps launch the graph. Reallocation (list regrowth) forces a re-capture. */
 int sg_step_configure(sg_ctx* ctx, const sg_step_config* cfg);
+/* Same, with the step's pair stage given as npairs (1..3) parameter sets run in
+ * order, at most one per potential family: a replica context holding LJ and
+ * GB replicas passes one LJ and one GB set. cfg->pair is ignored. */
+int sg_step_configure_pairs(sg_ctx* ctx, const sg_step_config* cfg, const sg_pair_params* pairs, int32_t npairs);
 /* Enqueue nsteps timesteps on the context stream; returns without waiting. */
 int sg_step(sg_ctx* ctx, int32_t nsteps);
 /* Wait, then report list overflow (SG_ECAPACITY) or a non-finite energy (SG_ENAN). */

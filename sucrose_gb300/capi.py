@@ -85,7 +85,11 @@ SIGNATURES = [
     ("sg_nht_final", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, _D]),
     ("sg_nht_state", C.c_int, [_P, _D, _D]),
     ("sg_thermo", C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
+    ("sg_create_replicas", C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _I32, _D, _U32, C.c_int32]),
+    ("sg_rep_nlist_init", C.c_int, [_P, _D, _D, C.c_int32]),
+    ("sg_rep_kinetic", C.c_int, [_P, _D]),
     ("sg_step_configure", C.c_int, [_P, C.POINTER(StepConfig)]),
+    ("sg_step_configure_pairs", C.c_int, [_P, C.POINTER(StepConfig), C.POINTER(PairParams), C.c_int32]),
     ("sg_step", C.c_int, [_P, C.c_int32]),
     ("sg_step_check", C.c_int, [_P]),
     ("sg_step_kernel_count", C.c_int, [_P, _I64]),

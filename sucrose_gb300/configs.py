@@ -158,3 +158,77 @@ def default_inertia(sig, mass=1.0):
     """initialize_system default (system.f90:619-621): I_x = (s_y^2 + s_z^2)/20 ..."""
     sx, sy, sz = sig
     return np.array([(sy ** 2 + sz ** 2) / 20.0, (sx ** 2 + sz ** 2) / 20.0, (sx ** 2 + sy ** 2) / 20.0]) * mass
+
+
+# ---------------------------------------------------------------- replicas ---
+LJ_REPLICA = dict(family=0, cutoff=2.5, list_cutoff=2.5, skin=0.3, rho=(0.7, 0.9), T=(0.7, 1.5),
+                  sig=(1.0, 1.0, 1.0), eps=(1.0, 1.0, 1.0))
+GB_REPLICA = dict(family=1, cutoff=4.0, list_cutoff=6.0, skin=0.4, rho=(0.2, 0.35), T=(0.8, 1.6),
+                  sig=(1.0, 1.0, 3.0), eps=(1.0, 1.0, 0.2))
+
+
+def _replica_lattice(n, sig, density, seed, rng, tilt):
+    """n particles on an orthorhombic lattice of cell s*sig with about three
+    times as many cells across x and y as along the long axis, seeded
+    vacancies removed; box fixed by the density. Returns r, q, box."""
+    sx, sy, sz = sig
+    aspect = sz / sx
+    nz = max(1, int(round((n / aspect ** 2) ** (1.0 / 3.0))))
+    nxy = int(np.ceil(np.sqrt(n / nz)))
+    m = nxy * nxy * nz
+    s = (n / (density * m * sx * sy * sz)) ** (1.0 / 3.0)
+    cell = s * np.array([sx, sy, sz])
+    box = cell * np.array([nxy, nxy, nz], dtype=np.float64)
+    g = np.stack(np.meshgrid(np.arange(nxy), np.arange(nxy), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    keep = np.sort(rng.choice(m, size=n, replace=False))
+    r = (g[keep] + 0.5) * cell - box / 2.0
+    r = r + 0.02 * np.clip(rng.standard_normal((n, 3)), -2.0, 2.0) * cell.min()
+    q = _small_rotations(n, seed, tilt) if tilt > 0 else np.tile([1.0, 0.0, 0.0, 0.0], (n, 1))
+    return r, q, box
+
+
+def replica_ensemble(nrep=4096, seed=1005, nmin=64, nmax=2048, lj=LJ_REPLICA, gb=GB_REPLICA, max_redraw=1000):
+    """Seeded ensemble of nrep independent periodic replicas: the first half
+    Lennard-Jones point fluids, the second half Gay-Berne (3, 5, 2, 1)
+    ellipsoid fluids. Particle counts are log-uniform in [nmin, nmax]; a
+    count whose box would be narrower than twice its list cut-off (the
+    reference's init_nlist guard, fortran/system.f90:902-906) is redrawn from
+    the same stream. Each replica has its own density, temperature and
+    Philox key (two words derived from (seed, replica)).
+
+    Returns a dict of per-replica arrays (n, box, family, temp, key, density)
+    and the concatenated r, q (each replica centred in its own box)."""
+    rng = np.random.default_rng(seed)
+    fams = [lj] * (nrep // 2) + [gb] * (nrep - nrep // 2)
+    out = dict(n=[], box=[], family=[], temp=[], density=[], redraws=0)
+    rs, qs = [], []
+    for k, p in enumerate(fams):
+        rho = rng.uniform(*p["rho"])
+        T = rng.uniform(*p["T"])
+        for attempt in range(max_redraw):
+            n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+            r, q, box = _replica_lattice(n, p["sig"], rho, seed * 7919 + k, rng, 0.1 if p["family"] == 1 else 0.0)
+            if box.min() >= 2.0 * p["list_cutoff"]:
+                break
+            out["redraws"] += 1
+        else:
+            raise RuntimeError("replica %d: no count in range fits the cut-off" % k)
+        out["n"].append(n)
+        out["box"].append(box)
+        out["family"].append(p["family"])
+        out["temp"].append(T)
+        out["density"].append(rho)
+        rs.append(r)
+        qs.append(q)
+    R = np.arange(nrep, dtype=np.int64)
+    words = philox4x32(np.stack([R, np.full(nrep, seed), np.full(nrep, 0x5EED), np.zeros(nrep)], 1).astype(np.uint32))
+    out["key"] = words[:, :2].copy()
+    for k in ("n", "family"):
+        out[k] = np.asarray(out[k], dtype=np.int32)
+    for k in ("temp", "density"):
+        out[k] = np.asarray(out[k], dtype=np.float64)
+    out["box"] = np.asarray(out["box"])
+    out["r"] = np.concatenate(rs)
+    out["q"] = np.concatenate(qs)
+    out["off"] = np.concatenate([[0], np.cumsum(out["n"])]).astype(np.int64)
+    return out

@@ -32,9 +32,6 @@ int sg_ensure_partials(sg_ctx* ctx, int slots) {
 int sg_ensure_stage(sg_ctx* ctx, size_t bytes) {
     if (bytes <= ctx->h_stage_bytes) return SG_OK;
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
-    if (ctx->d_stage) cudaFree(ctx->d_stage);
-    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
-    if (ctx->step_dev) cudaFree(ctx->step_dev);
     ctx->h_stage = nullptr;
     SG_CUDA(ctx, cudaMallocHost(&ctx->h_stage, bytes));
     ctx->h_stage_bytes = bytes;
@@ -114,8 +111,10 @@ int sg_destroy(sg_ctx* ctx) {
         if (b) cudaFree(b);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->d_stage) cudaFree(ctx->d_stage);
+    if (ctx->rep_alloc) cudaFree(ctx->rep_alloc);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->step_dev) cudaFree(ctx->step_dev);
+    if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SG_OK;
@@ -133,6 +132,7 @@ int sg_synchronize(sg_ctx* ctx) {
 
 int sg_set_box(sg_ctx* ctx, const double box[3], int32_t periodic) {
     if (!ctx || !box) return SG_EINVAL;
+    if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "replica boxes are fixed by sg_create_replicas");
     for (int d = 0; d < 3; ++d)
         if (!(box[d] > 0.0)) return sg_fail(ctx, SG_EINVAL, "box dimensions must be positive");
     for (int d = 0; d < 3; ++d) ctx->box[d] = box[d];

@@ -117,18 +117,22 @@ __device__ __forceinline__ float mlp_warp_guess(const MlpDev& m, const float (&f
     float out_rows[2][2];  // [m-tile][row g / g+8]
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
-        // A fragment of layer 1 (16 pairs x 16 features): gather features of
-        // rows g and g+8 of this m-tile from their lanes.
+        // A fragment of layer 1 (16 pairs x 16 features): rows g and g+8 of
+        // this m-tile live in lanes ra and rb. A shuffle delivers the source
+        // lane's register, so every feature index is shuffled uniformly and
+        // each lane keeps the columns (c, c+1, 8+c, 9+c) it needs.
         uint32_t a1[4];
         {
             const int ra = mt * 16 + g, rb = mt * 16 + g + 8;
-            float v[8];
+            float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                v[q] = __shfl_sync(0xffffffffu, f[c + q], ra);
-                v[2 + q] = __shfl_sync(0xffffffffu, f[c + q], rb);
-                v[4 + q] = __shfl_sync(0xffffffffu, f[8 + c + q], ra);
-                v[6 + q] = __shfl_sync(0xffffffffu, f[8 + c + q], rb);
+            for (int k = 0; k < 16; ++k) {
+                const float xa = __shfl_sync(0xffffffffu, f[k], ra);
+                const float xb = __shfl_sync(0xffffffffu, f[k], rb);
+                if (k == c) { v[0] = xa; v[2] = xb; }
+                if (k == c + 1) { v[1] = xa; v[3] = xb; }
+                if (k == 8 + c) { v[4] = xa; v[6] = xb; }
+                if (k == 9 + c) { v[5] = xa; v[7] = xb; }
             }
             a1[0] = pack_bf16(v[0], v[1]);
             a1[1] = pack_bf16(v[2], v[3]);

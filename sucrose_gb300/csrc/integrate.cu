@@ -12,17 +12,27 @@ namespace {
 struct Geo {
     float3 box, inv_box;
     int periodic;
+    RepDev rp;
 };
 
 Geo make_geo(const sg_ctx* ctx) {
     Geo g;
+    g.rp = ctx->rep;
     g.box = make_float3((float)ctx->box[0], (float)ctx->box[1], (float)ctx->box[2]);
     g.inv_box = make_float3((float)(1.0 / ctx->box[0]), (float)(1.0 / ctx->box[1]), (float)(1.0 / ctx->box[2]));
     g.periodic = ctx->periodic;
     return g;
 }
 
-SG_DEV float3 wrap_pos(float3 r, const Geo& g) {
+SG_DEV float3 wrap_pos(float3 r, const Geo& g, int i) {
+    if (g.rp.rep_of) {
+        const int k = g.rp.rep_of[i];
+        const float4 b = g.rp.box[k], ib = g.rp.inv_box[k];
+        r.x -= roundf(r.x * ib.x) * b.x;
+        r.y -= roundf(r.y * ib.y) * b.y;
+        r.z -= roundf(r.z * ib.z) * b.z;
+        return r;
+    }
     if (g.periodic) {
         r.x -= roundf(r.x * g.inv_box.x) * g.box.x;
         r.y -= roundf(r.y * g.inv_box.y) * g.box.y;
@@ -94,7 +104,7 @@ __global__ void k_vv_initial(int n, float dt, Geo g, float4* __restrict__ pos, f
     float4 v = vel[i], f = force[i], r = pos[i];
     const float h = 0.5f * dt, im = v.w;
     v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
-    float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g);
+    float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g, i);
     vel[i] = v;
     pos[i] = make_float4(p.x, p.y, p.z, r.w);
 }
@@ -151,6 +161,7 @@ struct LgvConst {
     double rot_amp;     // 2 gamma T dt
     float Tc2;          // T (1 - exp(-2 gamma dt))
     float rot_ampf;
+    double g2, dtd;     // 2 gamma and dt: per-replica 2 gamma T dt, evaluated in the host's order
     float kk2;
     uint32_t step, temp_int, k0, k1;
 };
@@ -169,13 +180,27 @@ __global__ void k_lgv_initial(int n, LgvConst c, Geo g, float4* __restrict__ pos
     float n1a, n1b, n1c, n2a = 0.f, n2b = 0.f, n2c = 0.f;
     // counters (I, step, int(T*1000), stream) with I 1-based (integrators.f90:546-547)
     const uint32_t step = c.step_dev ? (uint32_t)*c.step_dev : c.step;
-    sg_normal_3seq_f32((uint32_t)(i + 1), step, c.temp_int, 0u, c.k0, c.k1, n1a, n1b, n1c);
-    if (rotations) sg_normal_3seq_f32((uint32_t)(i + 1), step, c.temp_int, 1u, c.k0, c.k1, n2a, n2b, n2c);
-    const float amp = sqrtf(c.Tc2 * im);
+    // counter index, temperature and key: the replica's own in a batched context,
+    // so a replica draws exactly the numbers of its single-system run
+    uint32_t idx = (uint32_t)(i + 1), tint = c.temp_int, k0 = c.k0, k1 = c.k1;
+    float Tc2 = c.Tc2, rot_ampf = c.rot_ampf;
+    if (g.rp.rep_of) {
+        const int k = g.rp.rep_of[i];
+        idx = (uint32_t)(i - g.rp.off[k] + 1);
+        tint = (uint32_t)g.rp.temp_int[k];
+        k0 = g.rp.key[k].x;
+        k1 = g.rp.key[k].y;
+        const double T = g.rp.temp[k];
+        Tc2 = (float)(T * c.c2);
+        rot_ampf = (float)(c.g2 * T * c.dtd);
+    }
+    sg_normal_3seq_f32(idx, step, tint, 0u, k0, k1, n1a, n1b, n1c);
+    if (rotations) sg_normal_3seq_f32(idx, step, tint, 1u, k0, k1, n2a, n2b, n2c);
+    const float amp = sqrtf(Tc2 * im);
     v.x = c.ed * v.x + amp * n1a;
     v.y = c.ed * v.y + amp * n1b;
     v.z = c.ed * v.z + amp * n1c;
-    p = wrap_pos(make_float3(p.x + h * v.x, p.y + h * v.y, p.z + h * v.z), g);
+    p = wrap_pos(make_float3(p.x + h * v.x, p.y + h * v.y, p.z + h * v.z), g, i);
     vel[i] = v;
     pos[i] = make_float4(p.x, p.y, p.z, r.w);
     if (!rotations) return;
@@ -185,9 +210,9 @@ __global__ void k_lgv_initial(int n, LgvConst c, Geo g, float4* __restrict__ pos
     float3 Lb;
     const float4 q = quat[i];
     float4 qd = q_midpoint(q, L, make_float3(Ii.x, Ii.y, Ii.z), c.dt, rm, Lb);
-    Lb.x = c.kk12 * Lb.x + c.kk2 * sqrtf(c.rot_ampf * I4.x) * n2a;
-    Lb.y = c.kk12 * Lb.y + c.kk2 * sqrtf(c.rot_ampf * I4.y) * n2b;
-    Lb.z = c.kk12 * Lb.z + c.kk2 * sqrtf(c.rot_ampf * I4.z) * n2c;
+    Lb.x = c.kk12 * Lb.x + c.kk2 * sqrtf(rot_ampf * I4.x) * n2a;
+    Lb.y = c.kk12 * Lb.y + c.kk2 * sqrtf(rot_ampf * I4.y) * n2b;
+    Lb.z = c.kk12 * Lb.z + c.kk2 * sqrtf(rot_ampf * I4.z) * n2c;
     L = rot_apply_t(rm, Lb);
     angm[i] = make_float4(L.x, L.y, L.z, 0.f);
     quat[i] = q_advance(q, qd, c.dt);
@@ -310,7 +335,7 @@ __global__ void k_nhc_apply(int n, const double* nh, int do_vv, float dt, Geo g,
         const float4 f = force[i], r = pos[i];
         const float h = 0.5f * dt, im = v.w;
         v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
-        float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g);
+        float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g, i);
         pos[i] = make_float4(p.x, p.y, p.z, r.w);
     }
     vel[i] = v;
@@ -365,7 +390,7 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
             K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
             const float4 r = pos[i];
             float3 q = wrap_pos(make_float3(r.x + (float)c.dt * (float)vx, r.y + (float)c.dt * (float)vy,
-                                            r.z + (float)c.dt * (float)vz), g);
+                                            r.z + (float)c.dt * (float)vz), g, i);
             pos[i] = make_float4(q.x, q.y, q.z, r.w);
         } else {
             ke += 0.5 * m * (vx * vx + vy * vy + vz * vz);
@@ -469,6 +494,8 @@ int sg_lgv_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double 
     c.kk2 = (float)kk2;
     c.rot_amp = 2.0 * damping * target_temp * dt;
     c.Tc2 = (float)(target_temp * c.c2);
+    c.g2 = 2.0 * damping;
+    c.dtd = dt;
     c.rot_ampf = (float)c.rot_amp;
     c.T = (float)target_temp;
     c.step = (uint32_t)step;
@@ -498,6 +525,7 @@ int sg_lgv_final(sg_ctx* ctx, double dt, double damping, double* kin_eng, double
 
 int sg_nht_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain) {
     if (!ctx) return SG_EINVAL;
+    if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "Nose-Hoover chains are per system: not available on a replica context");
     if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
     NhConst c = nh_const(ctx, dt, target_temp, coupling);
     const int nb = (ctx->n + 255) / 256;
@@ -520,6 +548,7 @@ int sg_nht_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, 
 int sg_nht_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain,
                  double* kin_eng) {
     if (!ctx) return SG_EINVAL;
+    if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "Nose-Hoover chains are per system: not available on a replica context");
     if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
     NhConst c = nh_const(ctx, dt, target_temp, coupling);
     const int nb = (ctx->n + 255) / 256;

@@ -74,6 +74,25 @@ __device__ __forceinline__ bool accept_pair(float4 pi, float4 pj, const ListGeom
     return ref_accept(pi, pj, g);
 }
 
+// Geometry of replica r (batched contexts): its box, list radius and grid.
+__device__ __forceinline__ ListGeom geom_for(const ListGeom& base, const RepDev& rp, int r) {
+    ListGeom g = base;
+    const float4 b = rp.box[r], ib = rp.inv_box[r];
+    g.box = make_float3(b.x, b.y, b.z);
+    g.inv_box = make_float3(ib.x, ib.y, ib.z);
+    g.bx = rp.boxd[3 * r];
+    g.by = rp.boxd[3 * r + 1];
+    g.bz = rp.boxd[3 * r + 2];
+    g.rl2 = rp.rl2[r];
+    g.rl2_lo = (float)(g.rl2 * (1.0 - 1e-4));
+    g.rl2_hi = (float)(g.rl2 * (1.0 + 1e-4));
+    const int4 gr = rp.grid[r];
+    g.nc[0] = max(gr.x, 1);
+    g.nc[1] = max(gr.y, 1);
+    g.nc[2] = max(gr.z, 1);
+    return g;
+}
+
 __device__ __forceinline__ int wrapc(int c, int n) {
     c %= n;
     return c < 0 ? c + n : c;
@@ -90,10 +109,17 @@ __device__ __forceinline__ int cell_of(float4 p, const ListGeom& g, int& cx, int
 // needs_rebuild (system.f90:1005-1039) in FP64 on the FP32 state: any
 // particle with 4 |dr|^2 > trigger_sq requests a rebuild (the maximum over
 // particles exceeds the bound iff some particle does).
-__global__ void k_check(int n, const float4* __restrict__ pos, const float4* __restrict__ last, ListGeom g,
-                        double trigger_sq, int* flags) {
+__global__ void k_check(int n, const float4* __restrict__ pos, const float4* __restrict__ last, ListGeom g0,
+                        double trigger_sq, int* flags, RepDev rp, int* rep_flag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    ListGeom g = g0;
+    int r = 0;
+    if (rp.rep_of) {
+        r = rp.rep_of[i];
+        g = geom_for(g0, rp, r);
+        trigger_sq = rp.trig[r];
+    }
     float4 a = pos[i], b = last[i];
     {
         // FP32 screen: decide in FP32 when clear of the bound by 1e-3 relative
@@ -115,8 +141,12 @@ __global__ void k_check(int n, const float4* __restrict__ pos, const float4* __r
         dy = __dsub_rn(dy, __dmul_rn(round(__ddiv_rn(dy, g.by)), g.by));
         dz = __dsub_rn(dz, __dmul_rn(round(__ddiv_rn(dz, g.bz)), g.bz));
     }
-    double r = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    if (__dmul_rn(4.0, r) > trigger_sq) flags[F_REBUILD] = 1;
+    double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (__dmul_rn(4.0, rr) > trigger_sq) {
+        // a replica context rebuilds only the replicas whose particles moved
+        if (rp.rep_of) rep_flag[r] = 1;
+        flags[F_REBUILD] = 1;
+    }
 }
 
 __global__ void k_begin(int* flags, int* cell_count, int* cell_fill, int ncells) {
@@ -129,75 +159,145 @@ __global__ void k_begin(int* flags, int* cell_count, int* cell_fill, int ncells)
     if (t == 0) flags[F_OVERFLOW] = 0;
 }
 
-__global__ void k_bin(int n, const float4* __restrict__ pos, ListGeom g, int* particle_cell, int* cell_count,
-                      const int* flags) {
+__global__ void k_bin(int n, const float4* __restrict__ pos, ListGeom g0, int* particle_cell, int* cell_count,
+                      const int* flags, RepDev rp) {
     if (!flags[F_REBUILD]) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int cx, cy, cz;
-    int c = cell_of(pos[i], g, cx, cy, cz);
+    int c;
+    if (rp.rep_of) {
+        const int r = rp.rep_of[i];
+        const int4 gr = rp.grid[r];
+        if (!gr.x) {
+            // a replica under three cells per side is searched all-pairs, not binned
+            particle_cell[i] = -1;
+            return;
+        }
+        const ListGeom g = geom_for(g0, rp, r);
+        c = gr.w + cell_of(pos[i], g, cx, cy, cz);
+    } else {
+        c = cell_of(pos[i], g0, cx, cy, cz);
+    }
     particle_cell[i] = c;
     atomicAdd(&cell_count[c], 1);
 }
 
+// Cell members in arrival order (atomic slots) into the scratch array.
 __global__ void k_fill(int n, const int* __restrict__ particle_cell, const int* __restrict__ cell_start, int* cell_fill,
-                       int* cell_particles, const int* flags) {
+                       int* cell_unsorted, const int* flags) {
     if (!flags[F_REBUILD]) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int c = particle_cell[i];
+    if (c < 0) return;
     int s = atomicAdd(&cell_fill[c], 1);
-    cell_particles[cell_start[c] + s] = i;
+    cell_unsorted[cell_start[c] + s] = i;
 }
 
-// Order each cell's particles by index so that rows are deterministic.
-__global__ void k_sort_cells(int ncells, const int* __restrict__ cell_start, int* cell_particles, const int* flags) {
+// Order each cell's particles by index so that rows are deterministic: one
+// warp per cell, each member placed at its rank (the number of smaller
+// indices in the cell; indices are distinct).
+__global__ void k_sort_cells(int ncells, const int* __restrict__ cell_start, const int* __restrict__ cell_unsorted,
+                             int* cell_particles, const int* flags) {
     if (!flags[F_REBUILD]) return;
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (c >= ncells) return;
-    int b = cell_start[c], e = cell_start[c + 1];
-    for (int k = b + 1; k < e; ++k) {
-        int v = cell_particles[k];
-        int m = k - 1;
-        while (m >= b && cell_particles[m] > v) {
-            cell_particles[m + 1] = cell_particles[m];
-            --m;
-        }
-        cell_particles[m + 1] = v;
+    const int b = cell_start[c], e = cell_start[c + 1];
+    for (int k = b + lane; k < e; k += 32) {
+        const int v = cell_unsorted[k];
+        int rank = 0;
+        for (int t = b; t < e; ++t) rank += cell_unsorted[t] < v;
+        cell_particles[b + rank] = v;
     }
 }
 
-__global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g, const int* __restrict__ cell_start,
+// Padded-row addressing: slot k of particle i's row is nb_pad[base + k * stride].
+struct PadRep {
+    const int* max_nb;          // [R] row capacity of each replica
+    const long long* pad_off;   // [R] first slot of each replica's section
+    int* need;                  // [R] longest row seen on overflow
+};
+
+__device__ __forceinline__ void pad_slot(int n, int i, int max_nb, const RepDev& rp, const PadRep& pr, size_t& base,
+                                         size_t& stride, int& cap) {
+    if (rp.rep_of) {
+        const int r = rp.rep_of[i];
+        const int o = rp.off[r];
+        base = (size_t)pr.pad_off[r] + (size_t)(i - o);
+        stride = (size_t)(rp.off[r + 1] - o);
+        cap = pr.max_nb[r];
+    } else {
+        base = (size_t)i;
+        stride = (size_t)n;
+        cap = max_nb;
+    }
+}
+
+__device__ __forceinline__ void row_done(int i, int cnt, int cap, int* nb_count, int* flags, const RepDev& rp,
+                                         const PadRep& pr) {
+    nb_count[i] = min(cnt, cap);
+    if (cnt > cap) {
+        atomicMax(&flags[F_OVERFLOW], cnt);
+        if (rp.rep_of) atomicMax(&pr.need[rp.rep_of[i]], cnt);
+    }
+}
+
+__global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g0, const int* __restrict__ cell_start,
                              const int* __restrict__ cell_particles, int max_nb, int* nb_pad, int* nb_count,
-                             int* flags) {
+                             int* flags, RepDev rp, PadRep pr, const int* rep_flag) {
     if (!flags[F_REBUILD]) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (rp.rep_of && !rep_flag[rp.rep_of[i]]) return;   // this replica keeps its rows
     float4 pi = pos[i];
+    ListGeom g = g0;
+    int first_cell = 0;
+    int cnt = 0;
+    size_t base, stride;
+    int cap;
+    pad_slot(n, i, max_nb, rp, pr, base, stride, cap);
+    if (rp.rep_of) {
+        const int r = rp.rep_of[i];
+        const int4 gr = rp.grid[r];
+        g = geom_for(g0, rp, r);
+        first_cell = gr.w;
+        if (!gr.x) {
+            // box under three cells per side: every later particle of the replica
+            const int e = rp.off[r + 1];
+            for (int j = i + 1; j < e; ++j) {
+                if (accept_pair(pi, pos[j], g)) {
+                    if (cnt < cap) nb_pad[base + (size_t)cnt * stride] = j;
+                    ++cnt;
+                }
+            }
+            row_done(i, cnt, cap, nb_count, flags, rp, pr);
+            return;
+        }
+    }
     int cx, cy, cz;
     cell_of(pi, g, cx, cy, cz);
-    int cnt = 0;
     for (int dz = -1; dz <= 1; ++dz) {
         int zz = wrapc(cz + dz, g.nc[2]);
         for (int dy = -1; dy <= 1; ++dy) {
             int yy = wrapc(cy + dy, g.nc[1]);
             for (int dx = -1; dx <= 1; ++dx) {
                 int xx = wrapc(cx + dx, g.nc[0]);
-                int c = (zz * g.nc[1] + yy) * g.nc[0] + xx;
+                int c = first_cell + (zz * g.nc[1] + yy) * g.nc[0] + xx;
                 int b = cell_start[c], e = cell_start[c + 1];
                 for (int k = b; k < e; ++k) {
                     int j = cell_particles[k];
                     if (j <= i) continue;
                     if (accept_pair(pi, pos[j], g)) {
-                        if (cnt < max_nb) nb_pad[(size_t)cnt * n + i] = j;
+                        if (cnt < cap) nb_pad[base + (size_t)cnt * stride] = j;
                         ++cnt;
                     }
                 }
             }
         }
     }
-    nb_count[i] = min(cnt, max_nb);
-    if (cnt > max_nb) atomicMax(&flags[F_OVERFLOW], cnt);
+    row_done(i, cnt, cap, nb_count, flags, rp, pr);
 }
 
 // All-pairs variant for boxes with fewer than three cells per side and for
@@ -296,22 +396,27 @@ __global__ void k_scan_add(int* out, int m, const int* __restrict__ tile_sums, i
     }
 }
 
-__global__ void k_compact(int n, const int* __restrict__ nb_pad, const int* __restrict__ nb_count,
-                          const int* __restrict__ row_off, int* pair_i, int* pair_j, const int* flags) {
+__global__ void k_compact(int n, int max_nb, const int* __restrict__ nb_pad, const int* __restrict__ nb_count,
+                          const int* __restrict__ row_off, int* pair_i, int* pair_j, const int* flags, RepDev rp,
+                          PadRep pr) {
     if (!flags[F_REBUILD]) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    size_t base, stride;
+    int cap;
+    pad_slot(n, i, max_nb, rp, pr, base, stride, cap);
     int o = row_off[i], c = nb_count[i];
     for (int k = 0; k < c; ++k) {
         pair_i[o + k] = i;
-        pair_j[o + k] = nb_pad[(size_t)k * n + i];
+        pair_j[o + k] = nb_pad[base + (size_t)k * stride];
     }
 }
 
-__global__ void k_finish(int n, const float4* __restrict__ pos, float4* last, int* flags) {
+__global__ void k_finish(int n, const float4* __restrict__ pos, float4* last, int* flags, const int* rep_of,
+                         const int* rep_flag) {
     if (!flags[F_REBUILD]) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) last[i] = pos[i];
+    if (i < n && (!rep_of || rep_flag[rep_of[i]])) last[i] = pos[i];
     __syncthreads();
     // the last block clears the request; blocks only read the flag at entry
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
@@ -319,8 +424,17 @@ __global__ void k_finish(int n, const float4* __restrict__ pos, float4* last, in
     }
 }
 
-__global__ void k_clear_request(int* flags) { flags[F_REBUILD] = 0; }
-__global__ void k_set_request(int* flags) { flags[F_REBUILD] = 1; }
+// Request flags: the global one and, in a replica context, one per replica.
+__global__ void k_clear_request(int* flags, int* rep_flag, int R) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) flags[F_REBUILD] = 0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) rep_flag[r] = 0;
+}
+__global__ void k_set_request(int* flags, int* rep_flag, int R) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) flags[F_REBUILD] = 1;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) rep_flag[r] = 1;
+}
+
+int clear_grid(const sg_ctx* ctx) { return std::max(1, std::min(64, (ctx->nrep + 255) / 256)); }
 
 ListGeom make_geom(const sg_ctx* ctx) {
     ListGeom g;
@@ -354,6 +468,23 @@ int alloc_rows(sg_ctx* ctx, int max_nb) {
     ctx->graph_epoch++;
     nl.max_nb = max_nb;
     nl.pair_capacity = (int64_t)max_nb * ctx->n;
+    if (ctx->nrep) {
+        // each replica's rows in a section of their own, sized by its own capacity
+        const int R = ctx->nrep;
+        std::vector<long long> pad(R);
+        long long total = 0;
+        for (int r = 0; r < R; ++r) {
+            pad[r] = total;
+            total += (long long)nl.h_rep_max_nb[r] * (ctx->h_rep_off[r + 1] - ctx->h_rep_off[r]);
+        }
+        nl.pair_capacity = total;
+        nl.max_nb = *std::max_element(nl.h_rep_max_nb.begin(), nl.h_rep_max_nb.end());
+        if (total <= (long long)INT32_MAX) {
+            SG_CUDA(ctx, cudaMemcpy(nl.rep_max_nb, nl.h_rep_max_nb.data(), sizeof(int) * R, cudaMemcpyHostToDevice));
+            SG_CUDA(ctx, cudaMemcpy(nl.rep_pad_off, pad.data(), sizeof(long long) * R, cudaMemcpyHostToDevice));
+            SG_CUDA(ctx, cudaMemset(nl.rep_need, 0, sizeof(int) * R));
+        }
+    }
     if (nl.pair_capacity > (int64_t)INT32_MAX)
         return sg_fail(ctx, SG_ECAPACITY, "neighbour list capacity %lld exceeds 2^31", (long long)nl.pair_capacity);
     SG_CUDA(ctx, cudaMalloc(&nl.nb_pad, sizeof(int) * (size_t)nl.pair_capacity));
@@ -368,25 +499,27 @@ int enqueue_build(sg_ctx* ctx) {
     const int n = ctx->n;
     ListGeom g = make_geom(ctx);
     const int nb = (n + 255) / 256;
+    const PadRep pad{nl.rep_max_nb, nl.rep_pad_off, nl.rep_need};
     if (nl.use_cells) {
         k_begin<<<std::max(1, std::min(1024, (nl.ncells + 255) / 256)), 256, 0, ctx->stream>>>(nl.dev_flags, nl.cell_count,
                                                                                                 nl.cell_fill, nl.ncells);
-        k_bin<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.particle_cell, nl.cell_count, nl.dev_flags);
+        k_bin<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.particle_cell, nl.cell_count, nl.dev_flags, ctx->rep);
         if (int rc = scan(ctx, nl.cell_count, nl.ncells, nl.cell_start, nullptr, nl.dev_flags)) return rc;
-        k_fill<<<nb, 256, 0, ctx->stream>>>(n, nl.particle_cell, nl.cell_start, nl.cell_fill, nl.cell_particles,
+        k_fill<<<nb, 256, 0, ctx->stream>>>(n, nl.particle_cell, nl.cell_start, nl.cell_fill, nl.cell_unsorted,
                                             nl.dev_flags);
-        k_sort_cells<<<(nl.ncells + 255) / 256, 256, 0, ctx->stream>>>(nl.ncells, nl.cell_start, nl.cell_particles,
-                                                                       nl.dev_flags);
+        k_sort_cells<<<(nl.ncells + 7) / 8, 256, 0, ctx->stream>>>(nl.ncells, nl.cell_start, nl.cell_unsorted,
+                                                                    nl.cell_particles, nl.dev_flags);
         k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
-                                                  nl.nb_pad, nl.nb_count, nl.dev_flags);
+                                                  nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag);
     } else {
         k_begin<<<1, 32, 0, ctx->stream>>>(nl.dev_flags, nl.cell_count, nl.cell_fill, 0);
         k_rows_all<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
     }
     if (int rc = scan(ctx, nl.nb_count, n, nl.row_off, nl.dev_flags + F_NPAIRS, nl.dev_flags)) return rc;
-    k_compact<<<nb, 256, 0, ctx->stream>>>(n, nl.nb_pad, nl.nb_count, nl.row_off, nl.pair_i, nl.pair_j, nl.dev_flags);
-    k_finish<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, nl.pos_last, nl.dev_flags);
-    k_clear_request<<<1, 1, 0, ctx->stream>>>(nl.dev_flags);
+    k_compact<<<nb, 256, 0, ctx->stream>>>(n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off, nl.pair_i, nl.pair_j,
+                                           nl.dev_flags, ctx->rep, pad);
+    k_finish<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, nl.pos_last, nl.dev_flags, ctx->rep.rep_of, nl.rep_flag);
+    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(nl.dev_flags, nl.rep_flag, ctx->nrep);
     SG_LAUNCH_CHECK(ctx, "nlist build");
     return SG_OK;
 }
@@ -394,13 +527,23 @@ int enqueue_build(sg_ctx* ctx) {
 // Synchronous build with automatic regrowth on overflow.
 int build_sync(sg_ctx* ctx) {
     for (int attempt = 0; attempt < 8; ++attempt) {
-        k_set_request<<<1, 1, 0, ctx->stream>>>(ctx->nl.dev_flags);
+        k_set_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(ctx->nl.dev_flags, ctx->nl.rep_flag, ctx->nrep);
         if (int rc = enqueue_build(ctx)) return rc;
         int flags[4];
         SG_CUDA(ctx, cudaMemcpyAsync(flags, ctx->nl.dev_flags, sizeof(flags), cudaMemcpyDeviceToHost, ctx->stream));
         SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (flags[F_OVERFLOW] == 0) return SG_OK;
         int want = ((flags[F_OVERFLOW] * 5 / 4) + 31) / 32 * 32;
+        if (ctx->nrep) {
+            // grow only the replicas whose rows overflowed
+            const int R = ctx->nrep;
+            std::vector<int> need(R);
+            SG_CUDA(ctx, cudaMemcpy(need.data(), ctx->nl.rep_need, sizeof(int) * R, cudaMemcpyDeviceToHost));
+            for (int r = 0; r < R; ++r)
+                if (need[r] > ctx->nl.h_rep_max_nb[r])
+                    ctx->nl.h_rep_max_nb[r] = std::min(((need[r] * 5 / 4) + 31) / 32 * 32,
+                                                       ctx->h_rep_off[r + 1] - ctx->h_rep_off[r]);
+        }
         if (int rc = alloc_rows(ctx, want)) return rc;
     }
     return sg_fail(ctx, SG_ECAPACITY, "neighbour list did not fit after regrowth");
@@ -408,10 +551,21 @@ int build_sync(sg_ctx* ctx) {
 
 }  // namespace
 
+int sg_nlist_enqueue_check(sg_ctx* ctx) {
+    ListGeom g = make_geom(ctx);
+    k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->nl.pos_last, g, ctx->nl.trigger_sq,
+                                                           ctx->nl.dev_flags, ctx->rep, ctx->nl.rep_flag);
+    SG_LAUNCH_CHECK(ctx, "k_check");
+    return SG_OK;
+}
+
+int sg_nlist_enqueue_build(sg_ctx* ctx) { return enqueue_build(ctx); }
+
 int sg_nlist_free(sg_ctx* ctx) {
     sg_nlist_state& nl = ctx->nl;
     void* bufs[] = {nl.cell_count, nl.cell_start, nl.cell_fill, nl.cell_particles, nl.particle_cell, nl.nb_count,
-                    nl.nb_pad, nl.row_off, nl.scan_tmp, nl.pair_i, nl.pair_j, nl.dev_flags, nl.pos_last};
+                    nl.nb_pad, nl.row_off, nl.scan_tmp, nl.pair_i, nl.pair_j, nl.dev_flags, nl.pos_last,
+                    nl.rep_max_nb, nl.rep_pad_off, nl.rep_need, nl.rep_flag, nl.cell_unsorted};
     for (void* b : bufs)
         if (b) cudaFree(b);
     nl = sg_nlist_state();
@@ -420,8 +574,11 @@ int sg_nlist_free(sg_ctx* ctx) {
 
 extern "C" {
 
+static int alloc_list(sg_ctx* ctx, int max_nb);
+
 int sg_nlist_init(sg_ctx* ctx, double skin, double cutoff, int32_t trigger_mode) {
     if (!ctx) return SG_EINVAL;
+    if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "a replica context takes sg_rep_nlist_init");
     if (!(skin >= 0.0) || !(cutoff > 0.0)) return sg_fail(ctx, SG_EINVAL, "skin must be >= 0 and cutoff > 0");
     if (ctx->box[0] <= 0.0) return sg_fail(ctx, SG_ENOTREADY, "sg_set_box must precede sg_nlist_init");
     for (int d = 0; d < 3; ++d)
@@ -448,15 +605,25 @@ int sg_nlist_init(sg_ctx* ctx, double skin, double cutoff, int32_t trigger_mode)
     nl.ncells = nl.ncell[0] * nl.ncell[1] * nl.ncell[2];
     double vol = ctx->box[0] * ctx->box[1] * ctx->box[2];
     double rho = n / vol;
-    double expect = 0.5 * (4.0 / 3.0) * M_PI * rskin * rskin * rskin * rho;
-    int max_nb = (int)std::ceil(expect * 1.6 + 32.0);
+    // rows hold the j > i neighbours in index order, so a particle of low
+    // index can list nearly all of its neighbours: size for the full count
+    double expect = (4.0 / 3.0) * M_PI * rskin * rskin * rskin * rho;
+    int max_nb = (int)std::ceil(expect * 1.3 + 32.0);
     max_nb = (max_nb + 31) / 32 * 32;
     if (max_nb > n) max_nb = std::max(1, n);
+    return alloc_list(ctx, max_nb);
+}
+
+// Buffers of a list with nl.ncells cells and rows of max_nb, then a build.
+static int alloc_list(sg_ctx* ctx, int max_nb) {
+    sg_nlist_state& nl = ctx->nl;
+    const int n = ctx->n;
     int ntiles = std::max((n + SCAN_TILE - 1) / SCAN_TILE, (nl.ncells + SCAN_TILE - 1) / SCAN_TILE) + 2;
     SG_CUDA(ctx, cudaMalloc(&nl.cell_count, sizeof(int) * (size_t)nl.ncells));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_start, sizeof(int) * ((size_t)nl.ncells + 1)));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_fill, sizeof(int) * (size_t)nl.ncells));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_particles, sizeof(int) * (size_t)n));
+    SG_CUDA(ctx, cudaMalloc(&nl.cell_unsorted, sizeof(int) * (size_t)n));
     SG_CUDA(ctx, cudaMalloc(&nl.particle_cell, sizeof(int) * (size_t)n));
     SG_CUDA(ctx, cudaMalloc(&nl.nb_count, sizeof(int) * (size_t)n));
     SG_CUDA(ctx, cudaMalloc(&nl.row_off, sizeof(int) * ((size_t)n + 1)));
@@ -469,6 +636,63 @@ int sg_nlist_init(sg_ctx* ctx, double skin, double cutoff, int32_t trigger_mode)
     return build_sync(ctx);
 }
 
+// Per-replica lists of a batched context: each replica gets its own cell grid
+// (or one cell when its box is under three list radii per side), its own list
+// radius (cutoff[f] + skin[f] of its potential family f) and its own trigger.
+int sg_rep_nlist_init(sg_ctx* ctx, const double* skin, const double* cutoff, int32_t trigger_mode) {
+    if (!ctx || !skin || !cutoff) return SG_EINVAL;
+    if (!ctx->nrep) return sg_fail(ctx, SG_EINVAL, "not a replica context");
+    const int R = ctx->nrep;
+    std::vector<double> rl2(R), trig(R);
+    std::vector<int4> grid(R);
+    std::vector<int> max_nb_r(R);
+    int total_cells = 0;
+    for (int r = 0; r < R; ++r) {
+        const int f = ctx->h_rep_family[r];
+        const double* b = &ctx->h_rep_box[3 * r];
+        if (!(skin[f] >= 0.0) || !(cutoff[f] > 0.0)) return sg_fail(ctx, SG_EINVAL, "bad skin / cutoff for family %d", f);
+        for (int d = 0; d < 3; ++d)
+            if (cutoff[f] > b[d] / 2.0)
+                return sg_fail(ctx, SG_ECUTOFF_GT_HALFBOX, "replica %d: a cutoff of %.2f is too large for the box %.2f",
+                               r, cutoff[f], b[d]);
+        const double rs = cutoff[f] + skin[f];
+        rl2[r] = rs * rs;
+        trig[r] = trigger_mode == 0 ? rl2[r] : skin[f] * skin[f];
+        int nc[3];
+        bool cells = true;
+        for (int d = 0; d < 3; ++d) {
+            nc[d] = (int)std::floor(b[d] / (rs * (1.0 + 1e-4)));
+            if (nc[d] < 3) cells = false;
+        }
+        grid[r] = cells ? make_int4(nc[0], nc[1], nc[2], total_cells) : make_int4(0, 0, 0, total_cells);
+        total_cells += cells ? nc[0] * nc[1] * nc[2] : 1;
+        const int nr = ctx->h_rep_off[r + 1] - ctx->h_rep_off[r];
+        const double rho = nr / (b[0] * b[1] * b[2]);
+        // full neighbour count: index-ordered half rows of low index reach it
+        const double expect = (4.0 / 3.0) * M_PI * rs * rs * rs * rho;
+        int mnb = (int)std::ceil(expect * 1.3 + 32.0);
+        max_nb_r[r] = std::max(1, std::min((mnb + 31) / 32 * 32, nr));
+    }
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    sg_nlist_free(ctx);
+    ctx->graph_epoch++;
+    SG_CUDA(ctx, cudaMemcpy((void*)ctx->rep.rl2, rl2.data(), sizeof(double) * R, cudaMemcpyHostToDevice));
+    SG_CUDA(ctx, cudaMemcpy((void*)ctx->rep.trig, trig.data(), sizeof(double) * R, cudaMemcpyHostToDevice));
+    SG_CUDA(ctx, cudaMemcpy((void*)ctx->rep.grid, grid.data(), sizeof(int4) * R, cudaMemcpyHostToDevice));
+    sg_nlist_state& nl = ctx->nl;
+    nl.trigger_mode = trigger_mode;
+    nl.use_cells = 1;
+    nl.ncell[0] = nl.ncell[1] = nl.ncell[2] = 1;
+    nl.ncells = total_cells;
+    nl.h_rep_max_nb = max_nb_r;
+    SG_CUDA(ctx, cudaMalloc(&nl.rep_max_nb, sizeof(int) * R));
+    SG_CUDA(ctx, cudaMalloc(&nl.rep_pad_off, sizeof(long long) * R));
+    SG_CUDA(ctx, cudaMalloc(&nl.rep_need, sizeof(int) * R));
+    SG_CUDA(ctx, cudaMalloc(&nl.rep_flag, sizeof(int) * R));
+    SG_CUDA(ctx, cudaMemset(nl.rep_flag, 0, sizeof(int) * R));
+    return alloc_list(ctx, *std::max_element(max_nb_r.begin(), max_nb_r.end()));
+}
+
 int sg_nlist_build(sg_ctx* ctx) {
     if (!ctx) return SG_EINVAL;
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_nlist_build");
@@ -479,14 +703,14 @@ int sg_nlist_needs_rebuild(sg_ctx* ctx, int32_t* flag) {
     if (!ctx || !flag) return SG_EINVAL;
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_nlist_needs_rebuild");
     ListGeom g = make_geom(ctx);
-    k_clear_request<<<1, 1, 0, ctx->stream>>>(ctx->nl.dev_flags);
+    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(ctx->nl.dev_flags, ctx->nl.rep_flag, ctx->nrep);
     k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->nl.pos_last, g, ctx->nl.trigger_sq,
-                                                           ctx->nl.dev_flags);
+                                                           ctx->nl.dev_flags, ctx->rep, ctx->nl.rep_flag);
     SG_LAUNCH_CHECK(ctx, "k_check");
     int f = 0;
     SG_CUDA(ctx, cudaMemcpyAsync(&f, ctx->nl.dev_flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    k_clear_request<<<1, 1, 0, ctx->stream>>>(ctx->nl.dev_flags);
+    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(ctx->nl.dev_flags, ctx->nl.rep_flag, ctx->nrep);
     *flag = f;
     return SG_OK;
 }
@@ -496,7 +720,7 @@ int sg_nlist_update(sg_ctx* ctx) {
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_nlist_update");
     ListGeom g = make_geom(ctx);
     k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->nl.pos_last, g, ctx->nl.trigger_sq,
-                                                           ctx->nl.dev_flags);
+                                                           ctx->nl.dev_flags, ctx->rep, ctx->nl.rep_flag);
     SG_LAUNCH_CHECK(ctx, "k_check");
     return enqueue_build(ctx);
 }

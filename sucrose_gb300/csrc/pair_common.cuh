@@ -22,12 +22,14 @@ struct PairOut {
     float3 tj;   // torque on J (TXJ)
     float pe;
     float vir;
+    int act;     // the pair was inside the potential's range (counted for LJ / GB)
 };
 
 struct PairLaunch {
     const int* __restrict__ pair_i;
     const int* __restrict__ pair_j;
-    const int* npairs;           // device
+    const int* npairs;           // device: end of the range (pair count)
+    const int* begin;            // device: start of the range, or nullptr for 0
     float4* force;
     float4* torque;
     double* partials;
@@ -63,7 +65,9 @@ SG_DEV void segmented_scatter_i(const PairLaunch& L, int i, float3 f, float3 t) 
     }
     int inext = __shfl_down_sync(0xffffffffu, i, 1);
     bool last = (lane == 31) || (inext != i);
-    if (last && i >= 0) {
+    // a run of pairs that all lay out of range sums to exact zeros: no atomic
+    const bool zero = f.x == 0.f && f.y == 0.f && f.z == 0.f && (!TORQUE || (t.x == 0.f && t.y == 0.f && t.z == 0.f));
+    if (last && i >= 0 && !zero) {
         atomic_add_f3(&L.force[i], f);
         if (TORQUE) atomic_add_f3(&L.torque[i], t);
     }
@@ -74,7 +78,8 @@ SG_DEV void segmented_scatter_i(const PairLaunch& L, int i, float3 f, float3 t) 
 template <class Pot>
 __global__ void __launch_bounds__(256) k_pair(PairLaunch L, Pot pot) {
     __shared__ unsigned long long sh_stats[SG_NSTATS];
-    if (Pot::kStats) {
+    constexpr bool kSh = Pot::kStats || Pot::kCountActive;
+    if (kSh) {
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x) sh_stats[k] = 0ull;
         __syncthreads();
     }
@@ -82,8 +87,9 @@ __global__ void __launch_bounds__(256) k_pair(PairLaunch L, Pot pot) {
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int np = *L.npairs;
+    const int b0 = L.begin ? *L.begin : 0;
     float pe = 0.f, vir = 0.f;
-    for (int base = gwarp * 32; base < np; base += nwarps * 32) {
+    for (int base = b0 + gwarp * 32; base < np; base += nwarps * 32) {
         const int t = base + lane;
         const bool valid = t < np;
         int i = -1, j = 0;
@@ -93,13 +99,22 @@ __global__ void __launch_bounds__(256) k_pair(PairLaunch L, Pot pot) {
         o.tj = o.f;
         o.pe = 0.f;
         o.vir = 0.f;
+        o.act = 0;
         if (valid) {
             i = L.pair_i[t];
             j = L.pair_j[t];
         }
         // called by every lane (warp-cooperative potentials need all 32)
         pot.eval(valid, valid ? i : 0, j, t, o, sh_stats);
-        if (valid) {
+        if (Pot::kCountActive) {
+            // stats[0] listed pairs, stats[1] pairs inside the range
+            const unsigned va = __ballot_sync(0xffffffffu, valid), ac = __ballot_sync(0xffffffffu, o.act != 0);
+            if (lane == 0) {
+                atomicAdd(&sh_stats[0], (unsigned long long)__popc(va));
+                if (ac) atomicAdd(&sh_stats[1], (unsigned long long)__popc(ac));
+            }
+        }
+        if (valid && (!Pot::kCountActive || o.act)) {   // out-of-range pairs add nothing
             atomic_add_f3(&L.force[j], make_float3(-o.f.x, -o.f.y, -o.f.z));
             if (Pot::kTorque) atomic_add_f3(&L.torque[j], o.tj);
         }
@@ -107,7 +122,7 @@ __global__ void __launch_bounds__(256) k_pair(PairLaunch L, Pot pot) {
         vir += o.vir;
         segmented_scatter_i<Pot::kTorque>(L, i, o.f, o.ti);
     }
-    if (Pot::kStats) {
+    if (kSh) {
         __syncthreads();
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x)
             if (sh_stats[k]) atomicAdd(&L.stats[k], sh_stats[k]);
@@ -124,6 +139,13 @@ int launch_pair(sg_ctx* ctx, const Pot& pot) {
     L.pair_i = ctx->nl.pair_i;
     L.pair_j = ctx->nl.pair_j;
     L.npairs = ctx->nl.dev_flags + 2;
+    L.begin = nullptr;
+    if (ctx->nrep) {
+        // pairs of one potential family: rows of the family's particle range
+        const int f = ctx->launch_family;
+        L.begin = ctx->nl.row_off + ctx->fam_pstart[f];
+        L.npairs = ctx->nl.row_off + ctx->fam_pstart[f + 1];
+    }
     L.force = ctx->force;
     L.torque = ctx->torque;
     L.done = ctx->done_counter;
@@ -143,10 +165,16 @@ int launch_pair(sg_ctx* ctx, const Pot& pot) {
 struct BoxF {
     float3 box, inv_box;
     int periodic;
+    const int* rep_of;          // batched replicas: per-particle replica, else nullptr
+    const float4* rbox;
+    const float4* rinv;
 };
 
 inline BoxF make_boxf(const sg_ctx* ctx) {
     BoxF b;
+    b.rep_of = ctx->rep.rep_of;
+    b.rbox = ctx->rep.box;
+    b.rinv = ctx->rep.inv_box;
     b.box = make_float3((float)ctx->box[0], (float)ctx->box[1], (float)ctx->box[2]);
     b.inv_box = make_float3((float)(1.0 / ctx->box[0]), (float)(1.0 / ctx->box[1]), (float)(1.0 / ctx->box[2]));
     b.periodic = ctx->periodic;
@@ -155,6 +183,13 @@ inline BoxF make_boxf(const sg_ctx* ctx) {
 
 SG_DEV float3 pair_rij(const float4* __restrict__ pos, int i, int j, const BoxF& b) {
     float4 a = pos[i], c = pos[j];
+    if (b.rep_of) {
+        // pairs never cross replicas: the replica of i gives the box
+        const int r = b.rep_of[i];
+        const float4 bx = b.rbox[r], ib = b.rinv[r];
+        return min_image(make_float3(a.x - c.x, a.y - c.y, a.z - c.z), make_float3(bx.x, bx.y, bx.z),
+                         make_float3(ib.x, ib.y, ib.z), 1);
+    }
     return min_image(make_float3(a.x - c.x, a.y - c.y, a.z - c.z), b.box, b.inv_box, b.periodic);
 }
 

@@ -341,10 +341,10 @@ SG_DEV float3 lin_residual_df(const float* A, const float* D, float3 r, float la
 }
 
 SG_DEV float residual_check(int mode, const float* A, const float* D, float3 r, float lam, const Chol& c, float3 K,
-                            float& rK_out, float& s2) {
+                            float& rK_out, float& s2, float3& Kr) {
     const float3 e = mode == 2 ? lin_residual_df(A, D, r, lam, K) : lin_residual_fp64(A, D, r, lam, K);
     const float3 dk = chol_solve(c, e);
-    const float3 Kr = make_float3(K.x + dk.x, K.y + dk.y, K.z + dk.z);
+    Kr = make_float3(K.x + dk.x, K.y + dk.y, K.z + dk.z);
     const float3 DK = symv(D, Kr);
     const float rK = dot3(r, Kr), KDK = dot3(Kr, DK);
     const float3 Z = chol_solve(c, DK);
@@ -358,6 +358,7 @@ template <int SOLVER>
 struct PotECP {
     static constexpr bool kTorque = true;
     static constexpr bool kStats = true;
+    static constexpr bool kCountActive = false;
     const float4* __restrict__ pos;
     const float4* __restrict__ quat;
     const float4* __restrict__ shape;
@@ -407,6 +408,12 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
         for (int m = 0; m < 6; ++m) g[m] = fmaf(lam, D[m], A[m]);
         cR = chol(g);
         KR = chol_solve(cR, r);
+        if (fp64_check) {
+            // refine K_R against the exact G(lambda): it sets the contact distance
+            const float3 e = fp64_check == 2 ? lin_residual_df(A, D, r, lam, KR) : lin_residual_fp64(A, D, r, lam, KR);
+            const float3 dk = chol_solve(cR, e);
+            KR = make_float3(KR.x + dk.x, KR.y + dk.y, KR.z + dk.z);
+        }
         return lam;
     }
     const int budget = (SOLVER == SG_SOLVER_MLP_NEWTON) ? 3 : max_iter;
@@ -422,7 +429,8 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
     nonconv = !nr.converged;
     if (fp64_check) {
         float s2, rK;
-        const float s1 = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2);
+        float3 Kr;
+        const float s1 = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2, Kr);
         if (!(fabsf(s1) <= tol * rK)) {
             // one Newton step driven by the extended-precision residual
             refined = true;
@@ -438,9 +446,10 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
                     nr.K = chol_solve(nr.c, r);
                 }
             }
-            const float s1b = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2);
+            const float s1b = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2, Kr);
             if (!(fabsf(s1b) <= tol * rK)) nonconv = true;
         }
+        nr.K = Kr;   // the refined K feeds the force terms
     }
     cR = nr.c;
     KR = nr.K;
@@ -512,25 +521,30 @@ SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, un
 #pragma unroll
     for (int m = 0; m < 6; ++m) GE[m] = oml * AE[m] + lam * BE[m];
     const Chol cE = chol(GE);
-    const float3 KE = chol_solve(cE, r);
+    const float3 KE = chol_solve(cE, r);   // enters eps2^mu only: FP32 suffices
     const float l1 = lam * oml;
     const float rKE = dot3(r, KE), rKR = dot3(r, KR);
-    const float inv_rsq = rinv * rinv;
+    const float inv_rsq = 1.f / rsq;
     const float eps2 = l1 * rKE * inv_rsq;
-    const float phi = l1 * rKR * inv_rsq;
-    const float sigma = rsqrtf(phi);
+    // contact distance sigma = r / sqrt(S), S = l(1-l) r.K_R (force.f90:1316-1317); the
+    // envelope needs r - sigma, formed without cancellation as r (S-1) / (sqrt S (sqrt S + 1))
+    const float Sc = l1 * rKR;
+    const float sqS = sqrtf(Sc);
+    const float rexact = sqrtf(rsq);
+    const float rms = rexact * (Sc - 1.f) / (sqS * (sqS + 1.f));   // r - sigma
+    const float sigma = rexact / sqS;
     const float fac = 2.f * l1 * inv_rsq;   // efac = rfac (lambda_E = lambda_R, force.f90:1308)
     const float pi32 = sigma * sigma * sigma;
     const float reach = weld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
-    const bool active = rep ? (rmag <= sigma) : (rmag < reach);
+    const bool active = rep ? (rms <= 0.f) : (rmag < reach);
     if (!active) return;
     float sr;
     if (weld) {
-        if (rmag < sigma) sr = 1.f / (rmag - sigma + 1.f);
-        else if (rmag <= sigma + wf) sr = 1.f;
-        else sr = 1.f / (rmag - sigma + 1.f - wf);
+        if (rms < 0.f) sr = 1.f / (rms + 1.f);
+        else if (rms <= wf) sr = 1.f;
+        else sr = 1.f / (rms + 1.f - wf);
     } else {
-        sr = 1.f / (rmag - sigma + 1.f);
+        sr = 1.f / (rms + 1.f);
     }
     const float sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
     float srx = sr12 - 2.f * sr6;

@@ -45,6 +45,7 @@ template <int KIND>
 struct PotGB {
     static constexpr bool kTorque = true;
     static constexpr bool kStats = false;
+    static constexpr bool kCountActive = true;
     static constexpr bool kWeld = (KIND == SG_GBW || KIND == SG_GBWC);
     static constexpr bool kTaper = (KIND != SG_GBR);
     static constexpr bool kChiral = (KIND == SG_GBC || KIND == SG_GBWC);
@@ -69,11 +70,12 @@ struct PotGB {
         const GTerms gx = gterms(xhi, ru1, ru2, uu, rsq);
         const float eps1 = rsqrtf(1.f - (chi * uu) * (chi * uu));
         const float eps2 = gx.g * inv_ez;
-        const float sigma = lprp * rsqrtf(gc.g);
+        const float sigma = lprp / sqrtf(gc.g);   // correctly rounded: r - sigma sets the envelope
         const float ginv = sigma / gc.g;
         const float reach = kWeld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
         const bool active = (KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach);
         if (!active) return;
+        o.act = 1;
         float sr;
         if (kWeld) {
             if (rmag < sigma) sr = 1.f / (rmag - sigma + 1.f);

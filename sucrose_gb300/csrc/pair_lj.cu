@@ -9,6 +9,7 @@ namespace {
 struct PotLJ {
     static constexpr bool kTorque = false;
     static constexpr bool kStats = false;
+    static constexpr bool kCountActive = true;
     const float4* __restrict__ pos;
     BoxF b;
     int kind;
@@ -27,6 +28,7 @@ struct PotLJ {
                 float coeff = 24.f * eps * (2.f * sr12 - sr6) * inv;
                 o.f = coeff * r;
                 o.vir = coeff * rsq;
+                o.act = 1;
             }
         } else if (kind == SG_LJ12) {                // force.f90:72-91
             if (rsq < rc2) {
@@ -36,6 +38,7 @@ struct PotLJ {
                 float coeff = 12.f * eps * (sr12 - sr6) * inv;
                 o.f = coeff * r;
                 o.vir = coeff * rsq;
+                o.act = 1;
             }
         } else if (kind == SG_LJW) {                 // force.f90:116-144
             float rmag = sqrtf(rsq);
@@ -49,6 +52,7 @@ struct PotLJ {
                 float coeff = 12.f * eps * (sr12 - sr6) * (sr / sigma) / rmag;
                 o.f = coeff * r;
                 o.vir = coeff * rsq;
+                o.act = 1;
             }
         } else {                                      // SG_WCA, force.f90:175-188
             if (rsq <= sig2) {
@@ -58,6 +62,7 @@ struct PotLJ {
                 float coeff = 12.f * eps * (sr12 - sr6) * inv;
                 o.f = coeff * r;
                 o.vir = coeff * rsq;
+                o.act = 1;
             }
         }
     }

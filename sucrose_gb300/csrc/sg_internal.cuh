@@ -13,6 +13,23 @@
 #define SG_DEV __device__ __forceinline__
 
 // ------------------------------------------------------------------ context --
+// Per-replica tables of a batched context (sg_create_replicas). A context
+// without replicas has rep_of == nullptr and every kernel uses the single
+// box of the context.
+struct RepDev {
+    const int* rep_of = nullptr;      // [n] replica of each particle
+    const int* off = nullptr;         // [R+1] first particle of each replica
+    const float4* box = nullptr;      // [R] box lengths (x, y, z, 0)
+    const float4* inv_box = nullptr;  // [R] 1 / box
+    const double* boxd = nullptr;     // [3R] box lengths in FP64
+    const double* rl2 = nullptr;      // [R] (rc + skin)^2 of the replica's list
+    const double* trig = nullptr;     // [R] rebuild bound on 4 |dr|^2
+    const int4* grid = nullptr;       // [R] cells per side (x, y, z) and first global cell; x = 0: one cell
+    const double* temp = nullptr;     // [R] target temperature
+    const int* temp_int = nullptr;    // [R] int(T * 1000) for the Philox counter
+    const uint2* key = nullptr;       // [R] Philox key
+};
+
 struct sg_nlist_state {
     int initialized = 0;
     int trigger_mode = 0;
@@ -37,6 +54,14 @@ struct sg_nlist_state {
     int* pair_j = nullptr;           // [pair_capacity]
     int* dev_flags = nullptr;        // [0] rebuild requested, [1] overflow (max row seen), [2] npairs, [3] builds
     float4* pos_last = nullptr;      // positions at the last build
+    // replica contexts: rows of replica r have their own capacity max_nb[r] and
+    // sit column-major in their own section of nb_pad, starting at pad_off[r]
+    int* rep_max_nb = nullptr;       // [R]
+    long long* rep_pad_off = nullptr;// [R]
+    int* rep_need = nullptr;         // [R] longest row seen when a row overflowed
+    int* rep_flag = nullptr;         // [R] rebuild requested for this replica
+    int* cell_unsorted = nullptr;    // [n] cell members before ordering
+    std::vector<int> h_rep_max_nb;
 };
 
 struct sg_ctx {
@@ -99,10 +124,23 @@ struct sg_ctx {
     unsigned graph_epoch = 0;        // bumped whenever a buffer a captured graph uses is reallocated
     unsigned graph_epoch_captured = 0;
     int graph_kernels = 0;
+    cudaStream_t aux_stream = nullptr;   // used to capture conditional graph bodies
     unsigned char step_cfg[256];     // copy of the sg_step_config the graph was captured with
+    sg_pair_params step_pairs[3];    // pair stage of the step: cfg.pair, or one set per family
+    int step_npairs = 1;
     int step_ready = 0;
 
     sg_nlist_state nl;
+
+    // batched replicas (sg_create_replicas); rep.rep_of == nullptr otherwise
+    RepDev rep;
+    int nrep = 0;
+    int fam_pstart[4] = {0, 0, 0, 0};  // particle ranges of the LJ / GB / ECP families
+    int launch_family = 0;             // family of the pair launch being enqueued
+    void* rep_alloc = nullptr;         // one device allocation backing the tables
+    std::vector<int> h_rep_off;        // host copies
+    std::vector<double> h_rep_box;
+    std::vector<int> h_rep_family;
 };
 
 // --------------------------------------------------------------- errors ----
@@ -188,4 +226,6 @@ int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p);
 int sg_nlist_free(sg_ctx* ctx);
+int sg_nlist_enqueue_check(sg_ctx* ctx);   // rebuild request flag from the displacement test
+int sg_nlist_enqueue_build(sg_ctx* ctx);   // the flag-gated build kernels
 void sg_mlp_free(sg_ctx* ctx);

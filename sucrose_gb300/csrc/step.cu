@@ -10,6 +10,52 @@ namespace {
 
 __global__ void k_step_incr(int* step) { *step += 1; }
 
+__global__ void k_set_rebuild_condition(cudaGraphConditionalHandle h, const int* flags) {
+    cudaGraphSetConditional(h, flags[0] ? 1u : 0u);
+}
+
+// List maintenance inside a captured step: the displacement test runs every
+// step; the build kernels sit in the body of a conditional graph node that
+// executes only when a rebuild was requested, so a step without a rebuild
+// launches none of them. Outside capture the flag-gated kernels are enqueued.
+int enqueue_list_update(sg_ctx* ctx) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t nd = 0;
+    SG_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &edges, &nd));
+    if (st != cudaStreamCaptureStatusActive) return sg_nlist_update(ctx);
+    if (int rc = sg_nlist_enqueue_check(ctx)) return rc;
+    cudaGraphConditionalHandle h;
+    SG_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &edges, &nd));
+    SG_CUDA(ctx, cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault));
+    k_set_rebuild_condition<<<1, 1, 0, ctx->stream>>>(h, ctx->nl.dev_flags);
+    SG_LAUNCH_CHECK(ctx, "k_set_rebuild_condition");
+    SG_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &edges, &nd));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    SG_CUDA(ctx, cudaGraphAddNode(&node, cg, deps, edges, nd, &cp));
+    SG_CUDA(ctx, cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if (!ctx->aux_stream) SG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+    SG_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->aux_stream, body, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+    cudaStream_t main = ctx->stream;
+    ctx->stream = ctx->aux_stream;
+    int rc = sg_nlist_enqueue_build(ctx);
+    ctx->stream = main;
+    cudaGraph_t out = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->aux_stream, &out);
+    if (rc) return rc;
+    if (e != cudaSuccess) return sg_cuda_check(ctx, e, "capture of the rebuild body");
+    return SG_OK;
+}
+
 int enqueue_step(sg_ctx* ctx, const sg_step_config& c) {
     const double dt = c.dt;
     ctx->lgv_step_dev = ctx->step_dev;
@@ -28,9 +74,9 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c) {
             break;
         default: rc = sg_fail(ctx, SG_EINVAL, "unknown integrator %d", c.integrator);
     }
-    if (!rc) rc = sg_nlist_update(ctx);
+    if (!rc) rc = enqueue_list_update(ctx);
     if (!rc) rc = sg_zero_forces(ctx);
-    if (!rc) rc = sg_pair_forces_async(ctx, &c.pair);
+    for (int k = 0; !rc && k < ctx->step_npairs; ++k) rc = sg_pair_forces_async(ctx, &ctx->step_pairs[k]);
     if (!rc) {
         switch (c.integrator) {
             case SG_INT_NVE: rc = sg_vv_final(ctx, dt, nullptr); if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr); break;
@@ -60,6 +106,8 @@ int sg_step_configure(sg_ctx* ctx, const sg_step_config* cfg) {
     static_assert(sizeof(sg_step_config) <= sizeof(ctx->step_cfg), "config size");
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_step_configure");
     memcpy(ctx->step_cfg, cfg, sizeof(sg_step_config));
+    ctx->step_pairs[0] = cfg->pair;
+    ctx->step_npairs = 1;
     if (!ctx->step_dev) SG_CUDA(ctx, cudaMalloc(&ctx->step_dev, sizeof(int)));
     SG_CUDA(ctx, cudaMemcpyAsync(ctx->step_dev, &cfg->first_step, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -68,6 +116,21 @@ int sg_step_configure(sg_ctx* ctx, const sg_step_config* cfg) {
         ctx->graph_exec = nullptr;
     }
     ctx->step_ready = 1;
+    return SG_OK;
+}
+
+int sg_step_configure_pairs(sg_ctx* ctx, const sg_step_config* cfg, const sg_pair_params* pairs, int32_t npairs) {
+    if (!ctx || !cfg || !pairs || npairs < 1 || npairs > 3) return SG_EINVAL;
+    int seen = 0;
+    for (int k = 0; k < npairs; ++k) {
+        const int f = pairs[k].kind < 10 ? 0 : (pairs[k].kind < 20 ? 1 : 2);
+        if (seen & (1 << f)) return sg_fail(ctx, SG_EINVAL, "two pair sets of the same potential family");
+        seen |= 1 << f;
+    }
+    if (npairs > 1 && !ctx->nrep) return sg_fail(ctx, SG_EINVAL, "several pair sets need a replica context");
+    if (int rc = sg_step_configure(ctx, cfg)) return rc;
+    for (int k = 0; k < npairs; ++k) ctx->step_pairs[k] = pairs[k];
+    ctx->step_npairs = npairs;
     return SG_OK;
 }
 
@@ -103,7 +166,7 @@ int sg_step(sg_ctx* ctx, int32_t nsteps) {
         cudaGraphGetNodes(graph, nullptr, &nn);
         std::vector<cudaGraphNode_t> nodes(nn);
         if (nn) cudaGraphGetNodes(graph, nodes.data(), &nn);
-        int kernels = 0;
+        int kernels = 0;   // kernels launched by a step without a rebuild
         for (size_t k = 0; k < nn; ++k) {
             cudaGraphNodeType t;
             if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;

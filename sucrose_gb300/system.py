@@ -38,6 +38,46 @@ class GpuSystem:
         check(ctx, rc)
         self.set_box(box, periodic)
 
+    @classmethod
+    def replicas(cls, n_per_rep, boxes, family, temps=None, keys=None, device=0):
+        """A batched context of independent periodic replicas (sg_create_replicas):
+        replica r has n_per_rep[r] particles in box boxes[r] (3 lengths) and
+        potential family family[r] (0 LJ, 1 GB, 2 ECP; non-decreasing)."""
+        self = cls.__new__(cls)
+        self.L = capi.load()
+        npr = np.ascontiguousarray(n_per_rep, dtype=np.int32)
+        bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.float64).reshape(-1, 3))
+        fam = np.ascontiguousarray(family, dtype=np.int32)
+        R = len(npr)
+        T = None if temps is None else np.ascontiguousarray(temps, dtype=np.float64)
+        K = None if keys is None else np.ascontiguousarray(np.asarray(keys, dtype=np.uint32).reshape(R, 2))
+        self.n = int(npr.sum())
+        self.nrep = R
+        self.rep_off = np.concatenate([[0], np.cumsum(npr)]).astype(np.int64)
+        self.rep_box = bx.copy()
+        self.box = bx.max(axis=0)
+        self.periodic = True
+        ctx = C.c_void_p()
+        P32 = C.POINTER(C.c_int32)
+        rc = self.L.sg_create_replicas(C.byref(ctx), R, npr.ctypes.data_as(P32), _dp(bx), fam.ctypes.data_as(P32),
+                                       _dp(T), None if K is None else K.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                       int(device))
+        self.ctx = ctx
+        check(ctx, rc)
+        return self
+
+    def init_rep_nlist(self, skin, cutoff, trigger_mode=0):
+        """Lists of every replica; skin and cutoff are 3-vectors indexed by family."""
+        s = np.ascontiguousarray(np.broadcast_to(np.asarray(skin, dtype=np.float64), (3,)))
+        c = np.ascontiguousarray(np.broadcast_to(np.asarray(cutoff, dtype=np.float64), (3,)))
+        self._c(self.L.sg_rep_nlist_init(self.ctx, _dp(s), _dp(c), int(trigger_mode)))
+
+    def rep_kinetic(self):
+        """Per-replica (KE, KE_rot), FP64, shape (nrep, 2)."""
+        out = np.zeros((self.nrep, 2))
+        self._c(self.L.sg_rep_kinetic(self.ctx, _dp(out)))
+        return out
+
     def close(self):
         if getattr(self, "ctx", None):
             self.L.sg_destroy(self.ctx)
@@ -260,6 +300,20 @@ class GpuSystem:
         cfg.pair = pair
         self._step_cfg = cfg
         self._c(self.L.sg_step_configure(self.ctx, C.byref(cfg)))
+
+    def configure_step_pairs(self, pairs, integrator=capi.INT_NVE, dt=0.001, target_temp=1.0, damping=1.0,
+                             coupling=0.0, rotations=0, rot_chain=0, first_step=1, key=None):
+        """Step whose pair stage runs several parameter sets in order, one per
+        potential family (replica contexts)."""
+        cfg = capi.StepConfig()
+        cfg.integrator, cfg.rotations, cfg.rot_chain, cfg.first_step = integrator, rotations, rot_chain, first_step
+        cfg.dt, cfg.target_temp, cfg.damping, cfg.coupling = dt, target_temp, damping, coupling
+        if key is not None:
+            cfg.key[0], cfg.key[1] = int(key[0]), int(key[1])
+            cfg.has_key = 1
+        arr = (PairParams * len(pairs))(*pairs)
+        self._step_cfg = (cfg, arr)
+        self._c(self.L.sg_step_configure_pairs(self.ctx, C.byref(cfg), arr, len(pairs)))
 
     def step(self, nsteps=1):
         self._c(self.L.sg_step(self.ctx, int(nsteps)))
