@@ -304,6 +304,7 @@ def run_ours(a):
     configure(g, w, pp_eq, langevin=True, first_step=1)
     g.step(a.equil)
     g.step_check()
+    tune = g.autotune(pp, reps=5)      # launch shape of the pair kernel on the equilibrated list
     configure(g, w, pp)
     g.step(max(a.warmup, 3))
     g.step_check()
@@ -381,6 +382,9 @@ def run_ours(a):
         extras["nonconverged"] = int(st.nonconverged)
         extras["fp64_peak_tflops_measured"] = g.peak_fma(True)
         extras["list_rebuilds_in_timed_region"] = int(builds)
+        extras["autotune"] = {"block": tune.block, "filter": tune.filter,
+                              "variant_ms": {f"b{b}_f{f}": float(tune.ms[k]) for k, (b, f) in
+                                             enumerate(((256, 0), (128, 0), (256, 1), (128, 1))[:tune.candidates])}}
         if a.config == "ecp" and a.solver == "newton":
             # residual check variants of the same kernel
             for mode, name in ((2, "double_float"), (0, "none")):
@@ -500,6 +504,10 @@ def run_replicas(a):
     configure(dt, 1 + a.rep_equil // 2)
     g.step(a.rep_equil - a.rep_equil // 2)
     g.step_check()
+    tunes = {}
+    for pp, name in zip(pairs, ("LJ", "GB")):
+        t = g.autotune(pp, reps=3)
+        tunes[name] = {"block": t.block, "filter": t.filter, "variant_ms": [float(t.ms[k]) for k in range(t.candidates)]}
     g.step(max(a.warmup, 3))
     g.step_check()
     kernels_per_step = g.step_kernel_count()
@@ -515,6 +523,32 @@ def run_replicas(a):
         t_dev = ranks.max_over_ranks(t_dev, device="cuda")
     ms_per_step = 1e3 * t_dev / a.steps
     value = npairs * a.steps * world / t_dev
+
+    # where a step's time goes: the same step enqueued stage by stage (no graph)
+    stages = ("lgv_initial", "list_check_and_rebuild", "zero_forces", "pair_LJ", "pair_GB", "lgv_final")
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)] for _ in range(10)]
+    builds_b = g.nlist_builds()
+    with torch.cuda.stream(stream):
+        for k in range(10):
+            evk = ev[k]
+            evk[0].record(stream)
+            g.lgv_initial(dt, 10_000 + k, damping=W["damping"])
+            evk[1].record(stream)
+            g.update_nlist()
+            evk[2].record(stream)
+            g.zero_forces()
+            evk[3].record(stream)
+            g.pair_forces_async(pairs[0])
+            evk[4].record(stream)
+            g.pair_forces_async(pairs[1])
+            evk[5].record(stream)
+            g.L.sg_lgv_final(g.ctx, dt, W["damping"], None, None)
+            evk[6].record(stream)
+    torch.cuda.synchronize()
+    g.step_check()
+    breakdown = {name: statistics.mean(ev[k][s].elapsed_time(ev[k][s + 1]) for k in range(10))
+                 for s, name in enumerate(stages)}
+    breakdown["rebuilds_in_10_steps"] = int(g.nlist_builds() - builds_b)
 
     # dominant kernels: each family's pair launch timed alone
     fam = {}
@@ -612,6 +646,8 @@ def run_replicas(a):
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "families": fam,
+            "autotune": tunes,
+            "stage_ms_eager": breakdown,
             "list_rebuilds_in_timed_region": int(builds),
             "sequential_single_system": seq,
             "host_setup_s": t_setup_host,

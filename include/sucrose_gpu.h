@@ -252,6 +252,22 @@ int sg_step_check(sg_ctx* ctx);
 /* Kernel launches in one captured step (after the first sg_step call). */
 int sg_step_kernel_count(sg_ctx* ctx, int64_t* count);
 
+/* ---- autotuner of the pair kernels (no counterpart in the reference) ------- */
+typedef struct {
+    int32_t block;       /* chosen threads per block                            */
+    int32_t filter;      /* chosen: 1 = range filter + per-warp in-range queue   */
+    int32_t candidates;  /* variants timed (ms[0..candidates-1])                 */
+    int32_t reserved;
+    float ms[4];         /* mean launch time of (256,0) (128,0) (256,1) (128,1)  */
+} sg_tune_result;
+/* Time each launch variant of the params' pair kernel on the current list
+ * (reps launches each), keep the fastest for this context's (kind, size,
+ * density) bucket. Forces, torques and energy accumulators are restored.
+ * Captured steps are re-captured at their next sg_step. */
+int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* params, int32_t reps, sg_tune_result* out);
+/* Set a launch variant by hand (block 128 or 256; filter ignored for ECP). */
+int sg_pair_set_launch(sg_ctx* ctx, int32_t kind, int32_t block, int32_t filter);
+
 /* Measured FP32 (fp64 = 0) or FP64 (fp64 = 1) FMA throughput of this GPU in
  * TFLOP/s: the roofline denominator of the FP32-pipe pair kernels. */
 int sg_peak_fma(sg_ctx* ctx, int32_t fp64, double* tflops);

@@ -37,6 +37,11 @@ class StepConfig(C.Structure):
 INT_NVE, INT_LANGEVIN, INT_NH, INT_NH_REF = 0, 1, 2, 3
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("block", C.c_int32), ("filter", C.c_int32), ("candidates", C.c_int32), ("reserved", C.c_int32),
+                ("ms", C.c_float * 4)]
+
+
 class EcpStats(C.Structure):
     _fields_ = [("pairs", C.c_int64), ("solver_evals", C.c_int64), ("nonconverged", C.c_int64),
                 ("fallbacks", C.c_int64), ("iter_hist", C.c_int64 * 24), ("fp64_refined", C.c_int64)]
@@ -88,6 +93,8 @@ SIGNATURES = [
     ("sg_create_replicas", C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _I32, _D, _U32, C.c_int32]),
     ("sg_rep_nlist_init", C.c_int, [_P, _D, _D, C.c_int32]),
     ("sg_rep_kinetic", C.c_int, [_P, _D]),
+    ("sg_pair_autotune", C.c_int, [_P, C.POINTER(PairParams), C.c_int32, C.POINTER(TuneResult)]),
+    ("sg_pair_set_launch", C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     ("sg_step_configure", C.c_int, [_P, C.POINTER(StepConfig)]),
     ("sg_step_configure_pairs", C.c_int, [_P, C.POINTER(StepConfig), C.POINTER(PairParams), C.c_int32]),
     ("sg_step", C.c_int, [_P, C.c_int32]),

@@ -67,9 +67,7 @@ int sg_ecp_lambda(sg_ctx* ctx, float* lam, int64_t capacity) {
     if (int rc = sg_nlist_count(ctx, &k)) return rc;
     if (!ctx->ecp_lambda) return sg_fail(ctx, SG_ENOTREADY, "no ECP call yet");
     if (capacity < k) return sg_fail(ctx, SG_ECAPACITY, "lambda capacity too small");
-    SG_CUDA(ctx, cudaMemcpyAsync(lam, ctx->ecp_lambda, sizeof(float) * k, cudaMemcpyDeviceToHost, ctx->stream));
-    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return SG_OK;
+    return sg_gather_pair_floats(ctx, ctx->ecp_lambda, k, lam);
 }
 
 int64_t sg_mlp_weight_count(void) { return SG_MLP_NPARAM; }

@@ -292,8 +292,7 @@ __global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* _
 
 // Standard NHC half step on the chain(s): nh[14], nh[15] hold the sums on
 // entry (zeroed by the host before the reduction). Writes the scale factors.
-__global__ void k_nhc_chain(NhConst c, double* nh, int rot) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void nhc_chain(const NhConst& c, double* nh, int rot) {
     double* eta = nh;
     double* p = nh + 3;
     double K = nh[14];
@@ -315,6 +314,114 @@ __global__ void k_nhc_chain(NhConst c, double* nh, int rot) {
     } else {
         nh[13] = 1.0;
     }
+}
+
+__global__ void k_nhc_chain(NhConst c, double* nh, int rot) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    nhc_chain(c, nh, rot);
+}
+
+// ---- fused Nose-Hoover step (the captured step's form) -----------------------
+// The same arithmetic as the separate entry points, in fewer passes:
+//   initial: [sum m v^2, L_b^2/I -> chain in the finishing block] [scale, kick, drift, rotate]
+//   final:   [kick, sums -> chain in the finishing block] [scale, rotational kick, KE, KE_rot]
+
+// Sums of m v^2 and 2 KE_rot (after an optional half kick of v), then the
+// chain update in the block that finishes the sums.
+__global__ void k_nhc_sum_chain(int n, float dt, int kick, float4* __restrict__ vel, const float4* __restrict__ force,
+                                const float4* __restrict__ shape, const float4* __restrict__ quat,
+                                const float4* __restrict__ angm, const float4* __restrict__ inert_inv, int rot,
+                                NhConst c, double* partials, unsigned int* done, double* nh) {
+    double e[2] = {0.0, 0.0};
+    const float h = 0.5f * dt;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 v = vel[i];
+        if (kick) {
+            const float4 f = force[i];
+            const float im = v.w;
+            v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
+            vel[i] = v;
+        }
+        e[0] += (double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        if (rot) {
+            float4 L = angm[i], Ii = inert_inv[i];
+            e[1] += 2.0 * kin_rot_of(quat[i], make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z));
+        }
+    }
+    if (block_reduce_finish<2>(e, partials, done, nh + 14)) {
+        __syncthreads();
+        __threadfence_block();
+        if (threadIdx.x == 0) nhc_chain(c, nh, rot);
+    }
+}
+
+// Chain scaling, half kick and drift, then the quaternion update with the
+// rotational half kick (k_nhc_apply(do_vv = 1) followed by k_qq_initial).
+__global__ void k_nhc_initial_fused(int n, const double* nh, float dt, Geo g, float4* __restrict__ pos,
+                                    float4* __restrict__ vel, const float4* __restrict__ force,
+                                    float4* __restrict__ quat, float4* __restrict__ angm,
+                                    const float4* __restrict__ torque, const float4* __restrict__ inert_inv,
+                                    int rot_chain, int rotations) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float sc = (float)nh[12];
+    float4 v = vel[i];
+    v.x *= sc; v.y *= sc; v.z *= sc;
+    float4 L4 = angm[i];
+    if (rot_chain) {
+        const float sr = (float)nh[13];
+        L4 = make_float4(L4.x * sr, L4.y * sr, L4.z * sr, L4.w);
+    }
+    const float4 f = force[i], r = pos[i];
+    const float h = 0.5f * dt, im = v.w;
+    v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
+    float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g, i);
+    pos[i] = make_float4(p.x, p.y, p.z, r.w);
+    vel[i] = v;
+    if (rotations) {
+        const float4 T = torque[i], Ii = inert_inv[i];
+        float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
+        Rot rm;
+        float3 Lb;
+        const float4 q = quat[i];
+        float4 qd = q_midpoint(q, L, make_float3(Ii.x, Ii.y, Ii.z), dt, rm, Lb);
+        quat[i] = q_advance(q, qd, dt);
+        angm[i] = make_float4(L.x, L.y, L.z, 0.f);
+    } else if (rot_chain) {
+        angm[i] = L4;
+    }
+}
+
+// Chain scaling, then the rotational half kick; KE = sum 0.5 m v^2 and KE_rot
+// into acc[0], acc[1] (k_nhc_apply(do_vv = 0), the KE sum and k_qq_final).
+__global__ void k_nhc_final_fused(int n, const double* nh, float dt, float4* __restrict__ vel,
+                                  const float4* __restrict__ shape, const float4* __restrict__ quat,
+                                  float4* __restrict__ angm, const float4* __restrict__ torque,
+                                  const float4* __restrict__ inert_inv, int rot_chain, int rotations, double* partials,
+                                  unsigned int* done, double* acc) {
+    double e[2] = {0.0, 0.0};
+    const float h = 0.5f * dt;
+    const float sc = (float)nh[12];
+    const float sr = rot_chain ? (float)nh[13] : 1.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 v = vel[i];
+        v.x *= sc; v.y *= sc; v.z *= sc;
+        vel[i] = v;
+        e[0] += 0.5 * ((double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z));
+        if (rot_chain || rotations) {
+            float4 L4 = angm[i];
+            if (rot_chain) L4 = make_float4(L4.x * sr, L4.y * sr, L4.z * sr, L4.w);
+            if (rotations) {
+                const float4 T = torque[i], Ii = inert_inv[i];
+                const float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
+                angm[i] = make_float4(L.x, L.y, L.z, 0.f);
+                e[1] += kin_rot_of(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z));
+            } else {
+                angm[i] = L4;
+            }
+        }
+    }
+    block_reduce_finish<2>(e, partials, done, acc);
 }
 
 // scale v (and L), then optionally the VV kick + drift (initial step)
@@ -573,6 +680,51 @@ int sg_nht_final(sg_ctx* ctx, double dt, double target_temp, double coupling, in
     SG_LAUNCH_CHECK(ctx, "k_half_into");
     return read_acc(ctx, 2, kin_eng);
 }
+
+}  // extern "C"
+
+// Nose-Hoover (standard chain) halves of the captured step, fused kernels.
+int sg_nhc_step_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t rot_chain,
+                        int32_t rotations) {
+    if (!ctx) return SG_EINVAL;
+    if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "Nose-Hoover chains are per system: not available on a replica context");
+    if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
+    NhConst c = nh_const(ctx, dt, target_temp, coupling);
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->nh + 14, 0, sizeof(double) * 2, ctx->stream));
+    int grid = reduce_grid(ctx);
+    if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
+    k_nhc_sum_chain<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, 0, ctx->vel, ctx->force, ctx->shape, ctx->quat,
+                                                  ctx->angm, ctx->inert_inv, rot_chain, c, ctx->partials,
+                                                  ctx->done_counter, ctx->nh);
+    k_nhc_initial_fused<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, (float)dt, make_geo(ctx),
+                                                                       ctx->pos, ctx->vel, ctx->force, ctx->quat,
+                                                                       ctx->angm, ctx->torque, ctx->inert_inv,
+                                                                       rot_chain, rotations);
+    SG_LAUNCH_CHECK(ctx, "k_nhc_initial_fused");
+    return SG_OK;
+}
+
+int sg_nhc_step_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t rot_chain,
+                      int32_t rotations) {
+    if (!ctx) return SG_EINVAL;
+    if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "Nose-Hoover chains are per system: not available on a replica context");
+    if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
+    NhConst c = nh_const(ctx, dt, target_temp, coupling);
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->nh + 14, 0, sizeof(double) * 2, ctx->stream));
+    int grid = reduce_grid(ctx);
+    if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
+    k_nhc_sum_chain<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, 1, ctx->vel, ctx->force, ctx->shape, ctx->quat,
+                                                  ctx->angm, ctx->inert_inv, rot_chain, c, ctx->partials,
+                                                  ctx->done_counter, ctx->nh);
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double) * 2, ctx->stream));
+    k_nhc_final_fused<<<grid, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, (float)dt, ctx->vel, ctx->shape, ctx->quat,
+                                                    ctx->angm, ctx->torque, ctx->inert_inv, rot_chain, rotations,
+                                                    ctx->partials, ctx->done_counter, ctx->acc + 2);
+    SG_LAUNCH_CHECK(ctx, "k_nhc_final_fused");
+    return SG_OK;
+}
+
+extern "C" {
 
 int sg_nht_state(sg_ctx* ctx, double* get12, const double* set12) {
     if (!ctx) return SG_EINVAL;

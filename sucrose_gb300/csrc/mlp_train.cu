@@ -407,6 +407,7 @@ int sg_mlp_init(sg_ctx* ctx, uint64_t seed) {
 }
 
 int sg_mlp_features(sg_ctx* ctx, void* x_bf16, float* y, int64_t capacity, int64_t* count) {
+    if (ctx && ctx->nrep) return sg_fail(ctx, SG_EINVAL, "learned-guess data comes from single-system contexts");
     if (!ctx || !x_bf16 || !y || !count) return SG_EINVAL;
     int64_t k = 0;
     if (int rc = sg_nlist_count(ctx, &k)) return rc;
@@ -427,6 +428,7 @@ int sg_mlp_features(sg_ctx* ctx, void* x_bf16, float* y, int64_t capacity, int64
 }
 
 int sg_mlp_guess(sg_ctx* ctx, float* out_dev, int64_t capacity) {
+    if (ctx && ctx->nrep) return sg_fail(ctx, SG_EINVAL, "learned-guess data comes from single-system contexts");
     if (!ctx || !out_dev) return SG_EINVAL;
     if (!ctx->mlp_ready) return sg_fail(ctx, SG_ENOTREADY, "MLP weights are not set");
     int64_t k = 0;

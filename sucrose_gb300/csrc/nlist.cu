@@ -396,16 +396,46 @@ __global__ void k_scan_add(int* out, int m, const int* __restrict__ tile_sums, i
     }
 }
 
+// Replica of the first pair of every 32-pair chunk of the row order: the
+// largest r with row_off[off[r]] <= 32 c (pair kernels start their search there).
+__global__ void k_chunk_rep(const int* __restrict__ row_off, const int* __restrict__ rep_off, int R,
+                            const int* flags, int* chunk_rep) {
+    if (!flags[F_REBUILD]) return;
+    const int total = flags[F_NPAIRS];
+    const int nchunks = (total + 31) >> 5;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += gridDim.x * blockDim.x) {
+        const int v = c << 5;
+        int lo = 0, hi = R;   // row_off[off[lo]] <= v < row_off[off[hi]] (hi = R: past the end)
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (row_off[rep_off[mid]] <= v) lo = mid;
+            else hi = mid;
+        }
+        chunk_rep[c] = lo;
+    }
+}
+
+// Rows into the flat pair arrays. A single system stores them in row order
+// (pair index = row_off[i] + k). A replica context stores each replica's rows
+// in the replica's own section (it starts where the replica's padded rows
+// start), so only replicas that rebuilt are rewritten: the pair at row-order
+// index v of replica r sits at pad_off[r] + v - row_off[off[r]].
 __global__ void k_compact(int n, int max_nb, const int* __restrict__ nb_pad, const int* __restrict__ nb_count,
                           const int* __restrict__ row_off, int* pair_i, int* pair_j, const int* flags, RepDev rp,
-                          PadRep pr) {
+                          PadRep pr, const int* rep_flag) {
     if (!flags[F_REBUILD]) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     size_t base, stride;
     int cap;
     pad_slot(n, i, max_nb, rp, pr, base, stride, cap);
-    int o = row_off[i], c = nb_count[i];
+    size_t o = (size_t)row_off[i];
+    if (rp.rep_of) {
+        const int r = rp.rep_of[i];
+        if (!rep_flag[r]) return;
+        o = (size_t)pr.pad_off[r] + (size_t)(row_off[i] - row_off[rp.off[r]]);
+    }
+    const int c = nb_count[i];
     for (int k = 0; k < c; ++k) {
         pair_i[o + k] = i;
         pair_j[o + k] = nb_pad[base + (size_t)k * stride];
@@ -464,7 +494,8 @@ int alloc_rows(sg_ctx* ctx, int max_nb) {
     if (nl.nb_pad) cudaFree(nl.nb_pad);
     if (nl.pair_i) cudaFree(nl.pair_i);
     if (nl.pair_j) cudaFree(nl.pair_j);
-    nl.nb_pad = nl.pair_i = nl.pair_j = nullptr;
+    if (nl.chunk_rep) cudaFree(nl.chunk_rep);
+    nl.nb_pad = nl.pair_i = nl.pair_j = nl.chunk_rep = nullptr;
     ctx->graph_epoch++;
     nl.max_nb = max_nb;
     nl.pair_capacity = (int64_t)max_nb * ctx->n;
@@ -478,6 +509,7 @@ int alloc_rows(sg_ctx* ctx, int max_nb) {
             total += (long long)nl.h_rep_max_nb[r] * (ctx->h_rep_off[r + 1] - ctx->h_rep_off[r]);
         }
         nl.pair_capacity = total;
+        nl.h_rep_pad_off = pad;
         nl.max_nb = *std::max_element(nl.h_rep_max_nb.begin(), nl.h_rep_max_nb.end());
         if (total <= (long long)INT32_MAX) {
             SG_CUDA(ctx, cudaMemcpy(nl.rep_max_nb, nl.h_rep_max_nb.data(), sizeof(int) * R, cudaMemcpyHostToDevice));
@@ -490,6 +522,7 @@ int alloc_rows(sg_ctx* ctx, int max_nb) {
     SG_CUDA(ctx, cudaMalloc(&nl.nb_pad, sizeof(int) * (size_t)nl.pair_capacity));
     SG_CUDA(ctx, cudaMalloc(&nl.pair_i, sizeof(int) * (size_t)nl.pair_capacity));
     SG_CUDA(ctx, cudaMalloc(&nl.pair_j, sizeof(int) * (size_t)nl.pair_capacity));
+    if (ctx->nrep) SG_CUDA(ctx, cudaMalloc(&nl.chunk_rep, sizeof(int) * (size_t)(nl.pair_capacity / 32 + 2)));
     return SG_OK;
 }
 
@@ -517,7 +550,10 @@ int enqueue_build(sg_ctx* ctx) {
     }
     if (int rc = scan(ctx, nl.nb_count, n, nl.row_off, nl.dev_flags + F_NPAIRS, nl.dev_flags)) return rc;
     k_compact<<<nb, 256, 0, ctx->stream>>>(n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off, nl.pair_i, nl.pair_j,
-                                           nl.dev_flags, ctx->rep, pad);
+                                           nl.dev_flags, ctx->rep, pad, nl.rep_flag);
+    if (ctx->nrep)
+        k_chunk_rep<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(nl.row_off, ctx->rep.off, ctx->nrep, nl.dev_flags,
+                                                              nl.chunk_rep);
     k_finish<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, nl.pos_last, nl.dev_flags, ctx->rep.rep_of, nl.rep_flag);
     k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(nl.dev_flags, nl.rep_flag, ctx->nrep);
     SG_LAUNCH_CHECK(ctx, "nlist build");
@@ -565,7 +601,7 @@ int sg_nlist_free(sg_ctx* ctx) {
     sg_nlist_state& nl = ctx->nl;
     void* bufs[] = {nl.cell_count, nl.cell_start, nl.cell_fill, nl.cell_particles, nl.particle_cell, nl.nb_count,
                     nl.nb_pad, nl.row_off, nl.scan_tmp, nl.pair_i, nl.pair_j, nl.dev_flags, nl.pos_last,
-                    nl.rep_max_nb, nl.rep_pad_off, nl.rep_need, nl.rep_flag, nl.cell_unsorted};
+                    nl.rep_max_nb, nl.rep_pad_off, nl.rep_need, nl.rep_flag, nl.cell_unsorted, nl.chunk_rep};
     for (void* b : bufs)
         if (b) cudaFree(b);
     nl = sg_nlist_state();
@@ -746,18 +782,58 @@ int sg_nlist_builds(sg_ctx* ctx, int64_t* builds) {
     return SG_OK;
 }
 
+}  // extern "C"
+
+// Storage index of every pair in row order (identity for a single system;
+// replica sections otherwise), with the row offsets.
+int sg_pair_storage_index(sg_ctx* ctx, int64_t k, std::vector<int>& off, std::vector<int64_t>& where) {
+    const int n = ctx->n;
+    off.assign(n + 1, 0);
+    SG_CUDA(ctx, cudaMemcpyAsync(off.data(), ctx->nl.row_off, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    where.resize(k);
+    if (!ctx->nrep) {
+        for (int64_t v = 0; v < k; ++v) where[v] = v;
+        return SG_OK;
+    }
+    for (int r = 0; r < ctx->nrep; ++r) {
+        const int64_t v0 = off[ctx->h_rep_off[r]], v1 = off[ctx->h_rep_off[r + 1]];
+        for (int64_t v = v0; v < v1; ++v) where[v] = ctx->nl.h_rep_pad_off[r] + (v - v0);
+    }
+    return SG_OK;
+}
+
+// Row-order copy of a device array of per-pair values.
+template <class T>
+static int gather_pairs(sg_ctx* ctx, const T* dev, int64_t k, T* out) {
+    if (k <= 0) return SG_OK;
+    if (!ctx->nrep) {
+        SG_CUDA(ctx, cudaMemcpyAsync(out, dev, sizeof(T) * k, cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return SG_OK;
+    }
+    std::vector<int> off;
+    std::vector<int64_t> where;
+    if (int rc = sg_pair_storage_index(ctx, k, off, where)) return rc;
+    std::vector<T> all((size_t)ctx->nl.pair_capacity);
+    SG_CUDA(ctx, cudaMemcpyAsync(all.data(), dev, sizeof(T) * all.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t v = 0; v < k; ++v) out[v] = all[where[v]];
+    return SG_OK;
+}
+
+int sg_gather_pair_floats(sg_ctx* ctx, const float* dev, int64_t k, float* out) { return gather_pairs(ctx, dev, k, out); }
+
+extern "C" {
+
 int sg_nlist_pairs(sg_ctx* ctx, int32_t* pi, int32_t* pj, int64_t capacity, int64_t* npairs) {
     if (!ctx || !npairs) return SG_EINVAL;
     int64_t k = 0;
     if (int rc = sg_nlist_count(ctx, &k)) return rc;
     *npairs = k;
     if (k > capacity || (k > 0 && (!pi || !pj))) return sg_fail(ctx, SG_ECAPACITY, "pair capacity too small");
-    if (k > 0) {
-        SG_CUDA(ctx, cudaMemcpyAsync(pi, ctx->nl.pair_i, sizeof(int) * k, cudaMemcpyDeviceToHost, ctx->stream));
-        SG_CUDA(ctx, cudaMemcpyAsync(pj, ctx->nl.pair_j, sizeof(int) * k, cudaMemcpyDeviceToHost, ctx->stream));
-    }
-    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return SG_OK;
+    if (int rc = gather_pairs(ctx, ctx->nl.pair_i, k, pi)) return rc;
+    return gather_pairs(ctx, ctx->nl.pair_j, k, pj);
 }
 
 int sg_nlist_export(sg_ctx* ctx, int32_t* nlist, int64_t capacity, int32_t* offset, int64_t* npairs, int32_t one_based) {
@@ -770,9 +846,8 @@ int sg_nlist_export(sg_ctx* ctx, int32_t* nlist, int64_t capacity, int32_t* offs
     const int n = ctx->n;
     std::vector<int> off(n + 1), pj(k > 0 ? k : 1);
     SG_CUDA(ctx, cudaMemcpyAsync(off.data(), ctx->nl.row_off, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, ctx->stream));
-    if (k > 0)
-        SG_CUDA(ctx, cudaMemcpyAsync(pj.data(), ctx->nl.pair_j, sizeof(int) * k, cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (int rc = gather_pairs(ctx, ctx->nl.pair_j, k, pj.data())) return rc;
     for (int i = 0; i < n; ++i) std::sort(pj.begin() + off[i], pj.begin() + off[i + 1]);
     for (int64_t t = 0; t < k; ++t) nlist[t] = pj[t] + (one_based ? 1 : 0);
     if (one_based) {

@@ -28,15 +28,23 @@ struct PairOut {
 struct PairLaunch {
     const int* __restrict__ pair_i;
     const int* __restrict__ pair_j;
-    const int* npairs;           // device: end of the range (pair count)
+    const int* npairs;           // device: end of the (row-order) range
     const int* begin;            // device: start of the range, or nullptr for 0
+    // Replica contexts keep each replica's pairs in a section of their own:
+    // the pair at row-order index v of replica r sits at
+    // sec[r] + v - row_off[rep_off[r]]. sec == nullptr: storage is row order.
+    const int* row_off;
+    const int* rep_off;
+    const long long* sec;
+    const int* chunk_rep;        // replica holding pair index 32 c, for every chunk c
+    int nrep;
     float4* force;
     float4* torque;
     double* partials;
     unsigned int* done;
     double* acc;                 // per-call sums: acc[0] += PE, acc[1] += virial
     double* acc_total;           // running sums since the last zero_forces
-    unsigned long long* stats;   // solver statistics (ECP)
+    unsigned long long* stats;   // solver statistics (ECP) or listed / in-range counts (LJ, GB)
 };
 
 SG_DEV void atomic_add_f3(float4* p, float3 v) {
@@ -74,10 +82,51 @@ SG_DEV void segmented_scatter_i(const PairLaunch& L, int i, float3 f, float3 t) 
 }
 
 #define SG_NSTATS 32
+#define SG_PAIR_MAX_BLOCK 256
 
-template <class Pot>
-__global__ void __launch_bounds__(256) k_pair(PairLaunch L, Pot pot) {
+// One pair per lane, evaluated and scattered (all 32 lanes call it).
+template <class Pot, bool COUNT>
+SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, bool valid, float& pe, float& vir,
+                         unsigned long long* sh_stats) {
+    const int lane = threadIdx.x & 31;
+    int i = -1, j = 0;
+    PairOut o;
+    o.f = make_float3(0.f, 0.f, 0.f);
+    o.ti = o.f;
+    o.tj = o.f;
+    o.pe = 0.f;
+    o.vir = 0.f;
+    o.act = 0;
+    if (valid) {
+        i = L.pair_i[t];
+        j = L.pair_j[t];
+    }
+    // called by every lane (warp-cooperative potentials need all 32)
+    pot.eval(valid, valid ? i : 0, j, t, o, sh_stats);
+    if (COUNT) {
+        // stats[0] listed pairs, stats[1] pairs inside the range
+        const unsigned va = __ballot_sync(0xffffffffu, valid), ac = __ballot_sync(0xffffffffu, o.act != 0);
+        if (lane == 0) {
+            atomicAdd(&sh_stats[0], (unsigned long long)__popc(va));
+            if (ac) atomicAdd(&sh_stats[1], (unsigned long long)__popc(ac));
+        }
+    }
+    if (valid && (!Pot::kCountActive || o.act)) {   // out-of-range pairs add nothing
+        atomic_add_f3(&L.force[j], make_float3(-o.f.x, -o.f.y, -o.f.z));
+        if (Pot::kTorque) atomic_add_f3(&L.torque[j], o.tj);
+    }
+    pe += o.pe;
+    vir += o.vir;
+    segmented_scatter_i<Pot::kTorque>(L, i, o.f, o.ti);
+}
+
+// FILTER: a cheap range test runs on every listed pair first; the pairs in
+// range queue up per warp (in list order, so rows stay contiguous) and are
+// evaluated 32 at a time, so no lane idles on an out-of-range pair.
+template <class Pot, bool FILTER>
+__global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK) k_pair(PairLaunch L, Pot pot) {
     __shared__ unsigned long long sh_stats[SG_NSTATS];
+    __shared__ int sh_queue[FILTER ? SG_PAIR_MAX_BLOCK * 2 : 1];
     constexpr bool kSh = Pot::kStats || Pot::kCountActive;
     if (kSh) {
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x) sh_stats[k] = 0ull;
@@ -89,38 +138,45 @@ __global__ void __launch_bounds__(256) k_pair(PairLaunch L, Pot pot) {
     const int np = *L.npairs;
     const int b0 = L.begin ? *L.begin : 0;
     float pe = 0.f, vir = 0.f;
-    for (int base = b0 + gwarp * 32; base < np; base += nwarps * 32) {
-        const int t = base + lane;
-        const bool valid = t < np;
-        int i = -1, j = 0;
-        PairOut o;
-        o.f = make_float3(0.f, 0.f, 0.f);
-        o.ti = o.f;
-        o.tj = o.f;
-        o.pe = 0.f;
-        o.vir = 0.f;
-        o.act = 0;
-        if (valid) {
-            i = L.pair_i[t];
-            j = L.pair_j[t];
+    int* q = sh_queue + (FILTER ? (threadIdx.x >> 5) * 64 : 0);
+    int qn = 0;
+    // replica sections: warps walk whole 32-pair chunks, whose first replica is tabulated
+    const int bstart = L.sec ? (b0 & ~31) : b0;
+    for (int base = bstart + gwarp * 32; base < np; base += nwarps * 32) {
+        const int v = base + lane;
+        const bool valid = v < np && v >= b0;
+        int t = v;
+        if (L.sec && valid) {
+            int r = L.chunk_rep[base >> 5];
+            while (r + 1 < L.nrep && L.row_off[L.rep_off[r + 1]] <= v) ++r;
+            t = (int)(L.sec[r] + (long long)(v - L.row_off[L.rep_off[r]]));
         }
-        // called by every lane (warp-cooperative potentials need all 32)
-        pot.eval(valid, valid ? i : 0, j, t, o, sh_stats);
-        if (Pot::kCountActive) {
-            // stats[0] listed pairs, stats[1] pairs inside the range
-            const unsigned va = __ballot_sync(0xffffffffu, valid), ac = __ballot_sync(0xffffffffu, o.act != 0);
-            if (lane == 0) {
-                atomicAdd(&sh_stats[0], (unsigned long long)__popc(va));
-                if (ac) atomicAdd(&sh_stats[1], (unsigned long long)__popc(ac));
+        if constexpr (!FILTER) {
+            pair_process<Pot, Pot::kCountActive>(L, pot, t, valid, pe, vir, sh_stats);
+        } else {
+            bool keep = false;
+            if (valid) keep = pot.in_range(L.pair_i[t], L.pair_j[t]);
+            const unsigned vm = __ballot_sync(0xffffffffu, valid), km = __ballot_sync(0xffffffffu, keep);
+            if (Pot::kCountActive && lane == 0) {
+                atomicAdd(&sh_stats[0], (unsigned long long)__popc(vm));
+                if (km) atomicAdd(&sh_stats[1], (unsigned long long)__popc(km));
+            }
+            if (keep) q[qn + __popc(km & ((1u << lane) - 1u))] = t;
+            qn += __popc(km);
+            __syncwarp();
+            if (qn >= 32) {
+                const int tq = q[lane];
+                __syncwarp();
+                if (lane < qn - 32) q[lane] = q[32 + lane];
+                __syncwarp();
+                qn -= 32;
+                pair_process<Pot, false>(L, pot, tq, true, pe, vir, sh_stats);
             }
         }
-        if (valid && (!Pot::kCountActive || o.act)) {   // out-of-range pairs add nothing
-            atomic_add_f3(&L.force[j], make_float3(-o.f.x, -o.f.y, -o.f.z));
-            if (Pot::kTorque) atomic_add_f3(&L.torque[j], o.tj);
-        }
-        pe += o.pe;
-        vir += o.vir;
-        segmented_scatter_i<Pot::kTorque>(L, i, o.f, o.ti);
+    }
+    if (FILTER && qn > 0) {   // qn is warp-uniform
+        const int tq = lane < qn ? q[lane] : 0;
+        pair_process<Pot, false>(L, pot, tq, lane < qn, pe, vir, sh_stats);
     }
     if (kSh) {
         __syncthreads();
@@ -131,20 +187,46 @@ __global__ void __launch_bounds__(256) k_pair(PairLaunch L, Pot pot) {
     block_reduce_finish<2>(e, L.partials, L.done, L.acc, L.acc_total);
 }
 
+// Launch shape of the pair kernels: block size and the range filter. The
+// autotuner (sg_pair_autotune) times the variants on the live list and
+// stores the fastest per (kind, size bucket); untuned kinds use defaults.
+PairTune sg_pair_tune_for(sg_ctx* ctx, int kind, bool filterable);
+
+template <class Pot, bool FILTER>
+int launch_pair_v(sg_ctx* ctx, PairLaunch L, Pot pot, int block) {
+    pot.prefiltered = FILTER ? 1 : 0;
+    const void* fn = (const void*)k_pair<Pot, FILTER>;
+    int grid = sg_grid_for(ctx, fn, block, 0);
+    int64_t max_useful = (ctx->nl.pair_capacity + block - 1) / block;
+    if (grid > max_useful) grid = (int)std::max<int64_t>(1, max_useful);
+    if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
+    L.partials = ctx->partials;
+    k_pair<Pot, FILTER><<<grid, block, 0, ctx->stream>>>(L, pot);
+    SG_LAUNCH_CHECK(ctx, "k_pair");
+    return SG_OK;
+}
+
 // Launch helper: persistent grid sized from occupancy.
 template <class Pot>
-int launch_pair(sg_ctx* ctx, const Pot& pot) {
+int launch_pair(sg_ctx* ctx, Pot pot, int kind) {
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "pair forces need sg_nlist_init first");
     PairLaunch L;
     L.pair_i = ctx->nl.pair_i;
     L.pair_j = ctx->nl.pair_j;
     L.npairs = ctx->nl.dev_flags + 2;
     L.begin = nullptr;
+    L.row_off = ctx->nl.row_off;
+    L.rep_off = ctx->rep.off;
+    L.sec = nullptr;
+    L.chunk_rep = nullptr;
+    L.nrep = ctx->nrep;
     if (ctx->nrep) {
-        // pairs of one potential family: rows of the family's particle range
+        // pairs of one potential family: rows of the family's replicas
         const int f = ctx->launch_family;
         L.begin = ctx->nl.row_off + ctx->fam_pstart[f];
         L.npairs = ctx->nl.row_off + ctx->fam_pstart[f + 1];
+        L.sec = ctx->nl.rep_pad_off;
+        L.chunk_rep = ctx->nl.chunk_rep;
     }
     L.force = ctx->force;
     L.torque = ctx->torque;
@@ -152,14 +234,9 @@ int launch_pair(sg_ctx* ctx, const Pot& pot) {
     L.acc = ctx->acc + 4;
     L.acc_total = ctx->acc;
     L.stats = ctx->stats;
-    int grid = sg_grid_for(ctx, (const void*)k_pair<Pot>, 256, 0);
-    int64_t max_useful = (ctx->nl.pair_capacity + 255) / 256;
-    if (grid > max_useful) grid = (int)std::max<int64_t>(1, max_useful);
-    if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
-    L.partials = ctx->partials;
-    k_pair<Pot><<<grid, 256, 0, ctx->stream>>>(L, pot);
-    SG_LAUNCH_CHECK(ctx, "k_pair");
-    return SG_OK;
+    const PairTune tune = sg_pair_tune_for(ctx, kind, Pot::kFilterable);
+    if (Pot::kFilterable && tune.filter) return launch_pair_v<Pot, Pot::kFilterable>(ctx, L, pot, tune.block);
+    return launch_pair_v<Pot, false>(ctx, L, pot, tune.block);
 }
 
 struct BoxF {

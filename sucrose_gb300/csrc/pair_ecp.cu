@@ -359,6 +359,9 @@ struct PotECP {
     static constexpr bool kTorque = true;
     static constexpr bool kStats = true;
     static constexpr bool kCountActive = false;
+    static constexpr bool kFilterable = false;
+    int prefiltered;
+    SG_DEV bool in_range(int, int) const { return true; }
     const float4* __restrict__ pos;
     const float4* __restrict__ quat;
     const float4* __restrict__ shape;
@@ -634,7 +637,7 @@ int launch_ecp(sg_ctx* ctx, const sg_pair_params* p, int mu, int nu) {
     pot.weld = (p->kind == SG_ECPW || p->kind == SG_ECPWC);
     pot.chiral = (p->kind == SG_ECPC || p->kind == SG_ECPWC);
     pot.rep = (p->kind == SG_ECPR);
-    return launch_pair(ctx, pot);
+    return launch_pair(ctx, pot, p->kind);
 }
 
 }  // namespace

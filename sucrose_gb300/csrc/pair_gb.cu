@@ -49,11 +49,27 @@ struct PotGB {
     static constexpr bool kWeld = (KIND == SG_GBW || KIND == SG_GBWC);
     static constexpr bool kTaper = (KIND != SG_GBR);
     static constexpr bool kChiral = (KIND == SG_GBC || KIND == SG_GBWC);
+    static constexpr bool kFilterable = true;
     const float4* __restrict__ pos;
     const float4* __restrict__ prep;
     BoxF b;
     float cutoff, wf, chirality;
     int mu, nu;
+    int prefiltered;   // eval only sees pairs that passed in_range
+
+    // The range test of eval, alone: r against the orientation-dependent
+    // contact distance sigma (shape anisotropy of I) plus the cut-off.
+    SG_DEV bool in_range(int i, int j) const {
+        const float3 r = pair_rij(pos, i, j, b);
+        const float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
+        const float rmag = sqrtf(rsq);
+        const float4 pi0 = prep[2 * i], pi1 = prep[2 * i + 1], pj0 = prep[2 * j];
+        const float3 U1 = make_float3(pi0.x, pi0.y, pi0.z), U2 = make_float3(pj0.x, pj0.y, pj0.z);
+        const GTerms gc = gterms(pi1.x, dot3(r, U1), dot3(r, U2), dot3(U1, U2), rsq);
+        const float sigma = pi0.w / sqrtf(gc.g);
+        const float reach = kWeld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
+        return (KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach);
+    }
 
     SG_DEV void eval(bool valid, int i, int j, int, PairOut& o, unsigned long long*) const {
         if (!valid) return;
@@ -73,7 +89,7 @@ struct PotGB {
         const float sigma = lprp / sqrtf(gc.g);   // correctly rounded: r - sigma sets the envelope
         const float ginv = sigma / gc.g;
         const float reach = kWeld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
-        const bool active = (KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach);
+        const bool active = prefiltered || ((KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach));
         if (!active) return;
         o.act = 1;
         float sr;
@@ -177,7 +193,7 @@ int launch_gb(sg_ctx* ctx, const sg_pair_params* p, float4* prep, int mu, int nu
     pot.chirality = (float)p->chirality;
     pot.mu = mu;
     pot.nu = nu;
-    return launch_pair(ctx, pot);
+    return launch_pair(ctx, pot, KIND);
 }
 
 }  // namespace

@@ -10,18 +10,29 @@ struct PotLJ {
     static constexpr bool kTorque = false;
     static constexpr bool kStats = false;
     static constexpr bool kCountActive = true;
+    static constexpr bool kFilterable = true;
     const float4* __restrict__ pos;
     BoxF b;
     int kind;
     float sigma, eps, rc, rc2, wf, sig2;
     float pot_cut;    // shift at the cutoff, from the FP64 host value
+    int prefiltered;  // eval only sees pairs that passed in_range
+
+    // The range test of eval, alone.
+    SG_DEV bool in_range(int i, int j) const {
+        const float3 r = pair_rij(pos, i, j, b);
+        const float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
+        if (kind == SG_LJ || kind == SG_LJ12) return rsq < rc2;
+        if (kind == SG_LJW) return sqrtf(rsq) < rc + wf;
+        return rsq <= sig2;
+    }
 
     SG_DEV void eval(bool valid, int i, int j, int, PairOut& o, unsigned long long*) const {
         if (!valid) return;
         float3 r = pair_rij(pos, i, j, b);
         float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
         if (kind == SG_LJ) {                         // force.f90:26-47
-            if (rsq < rc2) {
+            if (prefiltered || rsq < rc2) {
                 float inv = 1.f / rsq;
                 float sr2 = sig2 * inv, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
                 o.pe = 4.f * eps * (sr12 - sr6) - pot_cut;
@@ -31,7 +42,7 @@ struct PotLJ {
                 o.act = 1;
             }
         } else if (kind == SG_LJ12) {                // force.f90:72-91
-            if (rsq < rc2) {
+            if (prefiltered || rsq < rc2) {
                 float inv = 1.f / rsq;
                 float sr2 = sig2 * inv, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
                 o.pe = eps * (sr12 - 2.f * sr6) - pot_cut;
@@ -42,7 +53,7 @@ struct PotLJ {
             }
         } else if (kind == SG_LJW) {                 // force.f90:116-144
             float rmag = sqrtf(rsq);
-            if (rmag < rc + wf) {
+            if (prefiltered || rmag < rc + wf) {
                 float sr;
                 if (rmag < sigma) sr = sigma / rmag;
                 else if (rmag < sigma + wf) sr = 1.f;
@@ -55,7 +66,7 @@ struct PotLJ {
                 o.act = 1;
             }
         } else {                                      // SG_WCA, force.f90:175-188
-            if (rsq <= sig2) {
+            if (prefiltered || rsq <= sig2) {
                 float inv = 1.f / rsq;
                 float sr2 = sig2 * inv, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
                 o.pe = eps * (sr12 - 2.f * sr6) + eps;
@@ -94,5 +105,5 @@ int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p) {
         cut = e * (c6 * c6 - 2.0 * c6);
     }
     pot.pot_cut = (float)cut;
-    return launch_pair(ctx, pot);
+    return launch_pair(ctx, pot, p->kind);
 }

@@ -72,12 +72,17 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     ctx->h_rep_family.assign(family, family + R);
     for (int r = 0; r < R; ++r) ctx->h_rep_off[r + 1] = ctx->h_rep_off[r] + n_per_rep[r];
     for (int f = 0; f < 3; ++f) {
-        int first = n;
+        int first = n, first_r = R;
         for (int r = R - 1; r >= 0; --r)
-            if (family[r] >= f) first = ctx->h_rep_off[r];
+            if (family[r] >= f) {
+                first = ctx->h_rep_off[r];
+                first_r = r;
+            }
         ctx->fam_pstart[f] = first;
+        ctx->fam_rstart[f] = first_r;
     }
     ctx->fam_pstart[3] = n;
+    ctx->fam_rstart[3] = R;
     double bmax[3] = {0, 0, 0};
     for (int r = 0; r < R; ++r)
         for (int d = 0; d < 3; ++d) bmax[d] = std::max(bmax[d], boxes[3 * r + d]);

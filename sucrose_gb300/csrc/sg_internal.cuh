@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/sucrose_gpu.h"
@@ -61,7 +62,15 @@ struct sg_nlist_state {
     int* rep_need = nullptr;         // [R] longest row seen when a row overflowed
     int* rep_flag = nullptr;         // [R] rebuild requested for this replica
     int* cell_unsorted = nullptr;    // [n] cell members before ordering
+    int* chunk_rep = nullptr;        // [capacity / 32 + 2] replica of each 32-pair chunk
     std::vector<int> h_rep_max_nb;
+    std::vector<long long> h_rep_pad_off;
+};
+
+// Launch shape of a pair kernel (chosen by the autotuner).
+struct PairTune {
+    int block = 256;   // threads per block (128 or 256)
+    int filter = 0;    // range filter + per-warp queue of in-range pairs
 };
 
 struct sg_ctx {
@@ -136,7 +145,9 @@ struct sg_ctx {
     RepDev rep;
     int nrep = 0;
     int fam_pstart[4] = {0, 0, 0, 0};  // particle ranges of the LJ / GB / ECP families
+    int fam_rstart[4] = {0, 0, 0, 0};  // replica ranges of the families
     int launch_family = 0;             // family of the pair launch being enqueued
+    std::map<long long, PairTune> tune;   // autotuned pair launch shapes by (kind, size bucket)
     void* rep_alloc = nullptr;         // one device allocation backing the tables
     std::vector<int> h_rep_off;        // host copies
     std::vector<double> h_rep_box;
@@ -182,8 +193,9 @@ SG_DEV float3 min_image(float3 d, float3 box, float3 inv_box, int periodic) {
 // Shared block reduction of K doubles; the last block to finish adds the
 // per-block partials, in block order, into acc[k] (deterministic). Must be
 // called by every thread of the block. partials holds gridDim.x * K slots.
+// Returns true in the block that finished the sum (block-uniform).
 template <int K>
-__device__ void block_reduce_finish(double (&v)[K], double* partials, unsigned int* done, double* acc,
+__device__ bool block_reduce_finish(double (&v)[K], double* partials, unsigned int* done, double* acc,
                                     double* acc_also = nullptr) {
     __shared__ double sh[32][K];
     __shared__ bool last;
@@ -208,20 +220,43 @@ __device__ void block_reduce_finish(double (&v)[K], double* partials, unsigned i
         last = (t == gridDim.x - 1);
     }
     __syncthreads();
-    if (last) {
+    if (last) {   // block-uniform
         __threadfence();
+        // every thread sums a fixed strided subset of the block partials, then
+        // a fixed tree: the order of additions does not depend on timing
+        double s[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) s[k] = 0.0;
+        for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) s[k] += ((volatile double*)partials)[(size_t)b * K + k];
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double x = s[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) sh[warp][k] = x;
+        }
+        __syncthreads();
         if (threadIdx.x < K) {
-            double s = 0.0;
-            for (unsigned int b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[(size_t)b * K + threadIdx.x];
-            acc[threadIdx.x] += s;
-            if (acc_also) acc_also[threadIdx.x] += s;
+            double t = 0.0;
+            for (int w = 0; w < nw; ++w) t += sh[w][threadIdx.x];
+            acc[threadIdx.x] += t;
+            if (acc_also) acc_also[threadIdx.x] += t;
         }
         if (threadIdx.x == 0) *done = 0u;
     }
+    return last;
 }
 
 // --------------------------------------------------- internal entry points --
 int sg_ecp_prepare(sg_ctx* ctx, const sg_pair_params* p, int need64);
+int sg_gather_pair_floats(sg_ctx* ctx, const float* dev, int64_t k, float* out);
+int sg_nhc_step_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t rot_chain,
+                        int32_t rotations);
+int sg_nhc_step_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t rot_chain,
+                      int32_t rotations);
 int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p);

@@ -66,10 +66,11 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c) {
         case SG_INT_LANGEVIN:
             rc = sg_lgv_initial(ctx, dt, 0, c.damping, c.target_temp, c.has_key ? c.key : nullptr);
             break;
-        case SG_INT_NH:
+        case SG_INT_NH:   // standard chain: fused kernels, same arithmetic as nht + qq
+            rc = sg_nhc_step_initial(ctx, dt, c.target_temp, c.coupling, c.rot_chain, c.rotations);
+            break;
         case SG_INT_NH_REF:
-            rc = sg_nht_initial(ctx, dt, c.target_temp, c.coupling, c.integrator == SG_INT_NH ? 1 : 0,
-                                c.integrator == SG_INT_NH ? c.rot_chain : 0);
+            rc = sg_nht_initial(ctx, dt, c.target_temp, c.coupling, 0, 0);
             if (!rc && c.rotations) rc = sg_qq_initial(ctx, dt);
             break;
         default: rc = sg_fail(ctx, SG_EINVAL, "unknown integrator %d", c.integrator);
@@ -81,9 +82,9 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c) {
         switch (c.integrator) {
             case SG_INT_NVE: rc = sg_vv_final(ctx, dt, nullptr); if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr); break;
             case SG_INT_LANGEVIN: rc = sg_lgv_final(ctx, dt, c.damping, nullptr, nullptr); break;
+            case SG_INT_NH: rc = sg_nhc_step_final(ctx, dt, c.target_temp, c.coupling, c.rot_chain, c.rotations); break;
             default:
-                rc = sg_nht_final(ctx, dt, c.target_temp, c.coupling, c.integrator == SG_INT_NH ? 1 : 0,
-                                  c.integrator == SG_INT_NH ? c.rot_chain : 0, nullptr);
+                rc = sg_nht_final(ctx, dt, c.target_temp, c.coupling, 0, 0, nullptr);
                 if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr);
         }
     }

@@ -1,0 +1,108 @@
+// Autotuner of the pair kernels' launch shape (no counterpart in the
+// reference). The variants are the block size (128 or 256 threads) and, for
+// potentials with a cheap range test (LJ family, Gay-Berne family), whether
+// the kernel filters the list first and evaluates only the in-range pairs,
+// 32 per warp. The best variant depends on the potential, the share of
+// listed pairs that are in range and the system size, so it is measured on
+// the live list and cached per (kind, particle-count bucket, density bucket).
+#include <cmath>
+#include <vector>
+
+#include "sg_internal.cuh"
+
+namespace {
+
+long long tune_key(const sg_ctx* ctx, int kind) {
+    const double vol = ctx->box[0] * ctx->box[1] * ctx->box[2];
+    const int nb = (int)std::floor(std::log2((double)std::max(ctx->n, 1)));
+    const int db = vol > 0 ? (int)std::floor(4.0 * std::log2(std::max(ctx->n / vol, 1e-6))) : 0;
+    return ((long long)kind << 32) | ((long long)(nb & 0xffff) << 16) | (long long)(db & 0xffff);
+}
+
+}  // namespace
+
+PairTune sg_pair_tune_for(sg_ctx* ctx, int kind, bool filterable) {
+    auto it = ctx->tune.find(tune_key(ctx, kind));
+    if (it != ctx->tune.end()) return it->second;
+    PairTune t;
+    t.block = 256;
+    // default before tuning: filter the Gay-Berne kinds, whose range test is
+    // a small part of the pair's work and often fails
+    t.filter = filterable && kind >= SG_GB && kind < SG_ECP;
+    return t;
+}
+
+extern "C" {
+
+int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune_result* out) {
+    if (!ctx || !p) return SG_EINVAL;
+    if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_pair_autotune");
+    if (reps < 1) reps = 5;
+    const int n = ctx->n;
+    const bool filterable = p->kind < SG_ECP;
+    // keep the caller's forces, torques and accumulators
+    float4* save = nullptr;
+    double acc[8];
+    SG_CUDA(ctx, cudaMalloc(&save, sizeof(float4) * 2 * (size_t)n));
+    SG_CUDA(ctx, cudaMemcpyAsync(save, ctx->force, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(save + n, ctx->torque, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(acc, ctx->acc, sizeof(acc), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const long long key = tune_key(ctx, p->kind);
+    const PairTune cand[4] = {{256, 0}, {128, 0}, {256, 1}, {128, 1}};
+    const int ncand = filterable ? 4 : 2;
+    float best = 1e30f;
+    PairTune pick = cand[0];
+    int rc = SG_OK;
+    sg_tune_result res{};
+    for (int c = 0; c < ncand && !rc; ++c) {
+        ctx->tune[key] = cand[c];
+        rc = sg_pair_forces_async(ctx, p);   // warm-up (allocations, caches)
+        float tot = 0.f;
+        for (int k = 0; k < reps && !rc; ++k) {
+            cudaEventRecord(e0, ctx->stream);
+            rc = sg_pair_forces_async(ctx, p);
+            cudaEventRecord(e1, ctx->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            tot += ms;
+        }
+        const float ms = tot / reps;
+        res.ms[c] = ms;
+        if (!rc && ms < best) {
+            best = ms;
+            pick = cand[c];
+        }
+    }
+    ctx->tune[key] = pick;
+    ctx->graph_epoch++;   // captured steps hold the old launch shape
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaMemcpyAsync(ctx->force, save, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(ctx->torque, save + n, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(ctx->acc, acc, sizeof(acc), cudaMemcpyHostToDevice, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(save);
+    if (rc) return rc;
+    res.block = pick.block;
+    res.filter = pick.filter;
+    res.candidates = ncand;
+    if (out) *out = res;
+    return SG_OK;
+}
+
+int sg_pair_set_launch(sg_ctx* ctx, int32_t kind, int32_t block, int32_t filter) {
+    if (!ctx || (block != 128 && block != 256)) return SG_EINVAL;
+    PairTune t;
+    t.block = block;
+    t.filter = (filter && kind < SG_ECP) ? 1 : 0;
+    ctx->tune[tune_key(ctx, kind)] = t;
+    ctx->graph_epoch++;
+    return SG_OK;
+}
+
+}  // extern "C"

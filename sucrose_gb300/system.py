@@ -224,6 +224,16 @@ class GpuSystem:
             return pe.value, vir.value, st
         return pe.value, vir.value
 
+    def autotune(self, params, reps=5):
+        """Time the pair kernel's launch variants on the current list and keep
+        the fastest (sg_pair_autotune). Returns the capi.TuneResult."""
+        res = capi.TuneResult()
+        self._c(self.L.sg_pair_autotune(self.ctx, C.byref(params), int(reps), C.byref(res)))
+        return res
+
+    def set_launch(self, kind, block=256, filter=0):
+        self._c(self.L.sg_pair_set_launch(self.ctx, int(kind), int(block), int(filter)))
+
     def pair_forces_async(self, params):
         self._c(self.L.sg_pair_forces_async(self.ctx, C.byref(params)))
 

@@ -1,0 +1,96 @@
+"""Launch variants of the pair kernels and the autotuner.
+
+Every variant (block 128 / 256, with or without the range filter) must give
+the same forces, torques and energies (only the order of float atomics
+differs), the same listed / in-range counts, and the autotuner must leave the
+caller's forces and accumulators as they were."""
+import numpy as np
+import pytest
+
+from helpers import ellipsoids, f32, jittered_fcc, rel
+from sucrose_gb300 import GpuSystem, capi, configs
+
+pytestmark = pytest.mark.gpu
+VARIANTS = [(256, 0), (128, 0), (256, 1), (128, 1)]
+
+
+def lj_system():
+    r, q, box = jittered_fcc(8, 0.8442, seed=4)
+    g = GpuSystem(len(r), box)
+    g.upload(r=f32(r))
+    g.init_nlist(0.3, 2.5)
+    return g, GpuSystem.params(capi.LJ, cutoff=2.5)
+
+
+def gb_system(kind=capi.GB):
+    sig = (1.0, 1.0, 3.0)
+    r, q, box = ellipsoids((16, 16, 8), sig, 0.3, seed=6, tilt=0.6)
+    g = GpuSystem(len(r), box)
+    g.set_particles(sig=sig, eps=(1.0, 1.0, 0.2))
+    g.upload(r=f32(r), q=f32(q))
+    g.init_nlist(0.4, 6.0)
+    return g, GpuSystem.params(kind, cutoff=4.0, mu=2, nu=1)
+
+
+def forces_with(g, p, block, filt):
+    g.set_launch(p.kind, block, filt)
+    g.zero_forces()
+    pe, vir, st = g.pair_forces(p, want_stats=True)
+    F, T = g.forces()
+    return pe, vir, F, T, (st.pairs, st.solver_evals)
+
+
+@pytest.mark.parametrize("make", [lj_system, gb_system, lambda: gb_system(capi.GBR), lambda: gb_system(capi.GBW)],
+                         ids=["lj", "gb", "gbr", "gbw"])
+def test_variants_agree(lib, make):
+    g, p = make()
+    ref = forces_with(g, p, *VARIANTS[0])
+    assert ref[4][0] == g.npairs() and 0 < ref[4][1] <= ref[4][0]
+    for v in VARIANTS[1:]:
+        pe, vir, F, T, counts = forces_with(g, p, *v)
+        # the filter's range test and eval's may round differently on the boundary
+        assert counts[0] == ref[4][0] and abs(counts[1] - ref[4][1]) <= 2, v
+        assert abs(pe - ref[0]) <= 1e-6 * max(1.0, abs(ref[0])), v
+        assert abs(vir - ref[1]) <= 1e-6 * max(1.0, abs(ref[1])), v
+        assert rel(F, ref[2]) < 1e-6, v
+        if p.kind != capi.LJ:
+            assert rel(T, ref[3]) < 1e-6, v
+    g.close()
+
+
+def test_autotune_restores_state(lib):
+    g, p = gb_system()
+    g.zero_forces()
+    g.pair_forces(p)
+    F0, T0 = g.forces()
+    e0 = g.energies()
+    res = g.autotune(p, reps=3)
+    assert res.candidates == 4 and res.block in (128, 256) and res.filter in (0, 1)
+    assert all(res.ms[k] > 0 for k in range(4))
+    F1, T1 = g.forces()
+    assert np.array_equal(F0, F1) and np.array_equal(T0, T1)
+    assert np.array_equal(e0, g.energies())
+    # the tuned shape is used and agrees with the default one
+    g.zero_forces()
+    pe = g.pair_forces(p)[0]
+    F2, _ = g.forces()
+    assert rel(F2, F0) < 1e-6
+    g.close()
+
+
+def test_autotuned_captured_step(lib):
+    """A tuned launch shape invalidates the captured step, which re-captures."""
+    sig = (1.0, 1.0, 3.0)
+    r, q, box = ellipsoids((16, 16, 8), sig, 0.3, seed=6, tilt=0.05)
+    g = GpuSystem(len(r), box)
+    g.set_particles(sig=sig, eps=(1.0, 1.0, 0.2), inertia=configs.default_inertia(sig))
+    g.upload(r=f32(r), q=f32(q))
+    g.init_nlist(0.4, 6.0)
+    p = GpuSystem.params(capi.GB, cutoff=4.0, mu=2, nu=1)
+    g.configure_step(p, integrator=capi.INT_LANGEVIN, dt=0.0005, rotations=1)
+    g.step(2)
+    g.step_check()
+    g.autotune(p, reps=2)
+    g.step(3)
+    g.step_check()
+    g.close()
