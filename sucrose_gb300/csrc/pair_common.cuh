@@ -8,9 +8,9 @@
 //   * the I-side terms are summed across lanes with a segmented shuffle scan
 //     (segments = runs of equal i), and the last lane of each run issues one
 //     float4 atomic,
-//   * PE and the pair virial r_ij . F_ij are summed per thread in FP32, then
-//     reduced per block in FP64 and finished deterministically by the last
-//     block (block_reduce_finish).
+//   * PE and the pair virial r_ij . F_ij are summed per thread in FP32, per
+//     warp in double-float, then per block in FP64, and finished
+//     deterministically by the last block (block_reduce_finish_f).
 // The grid is persistent (a multiple of the SM count); the pair count is read
 // from device memory so the launch needs no host synchronisation.
 #pragma once
@@ -85,11 +85,11 @@ SG_DEV void segmented_scatter_i(const PairLaunch& L, int i, float3 f, float3 t) 
 #define SG_PAIR_MAX_BLOCK 256
 
 // One pair per lane, evaluated and scattered (all 32 lanes call it).
+// i, j: the pair's particles (loaded by the caller; ignored when !valid).
 template <class Pot, bool COUNT>
-SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, bool valid, float& pe, float& vir,
+SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int j, bool valid, float& pe, float& vir,
                          unsigned long long* sh_stats) {
     const int lane = threadIdx.x & 31;
-    int i = -1, j = 0;
     PairOut o;
     o.f = make_float3(0.f, 0.f, 0.f);
     o.ti = o.f;
@@ -97,9 +97,9 @@ SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, bool valid,
     o.pe = 0.f;
     o.vir = 0.f;
     o.act = 0;
-    if (valid) {
-        i = L.pair_i[t];
-        j = L.pair_j[t];
+    if (!valid) {
+        i = -1;
+        j = 0;
     }
     // called by every lane (warp-cooperative potentials need all 32)
     pot.eval(valid, valid ? i : 0, j, t, o, sh_stats);
@@ -124,9 +124,10 @@ SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, bool valid,
 // range queue up per warp (in list order, so rows stay contiguous) and are
 // evaluated 32 at a time, so no lane idles on an out-of-range pair.
 template <class Pot, bool FILTER>
-__global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK) k_pair(PairLaunch L, Pot pot) {
+__global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? 4 : 1) k_pair(PairLaunch L, Pot pot) {
     __shared__ unsigned long long sh_stats[SG_NSTATS];
-    __shared__ int sh_queue[FILTER ? SG_PAIR_MAX_BLOCK * 2 : 1];
+    // per-warp queue of in-range pairs: storage index, i, j (64 slots each)
+    __shared__ int sh_queue[FILTER ? SG_PAIR_MAX_BLOCK * 2 * 3 : 1];
     constexpr bool kSh = Pot::kStats || Pot::kCountActive;
     if (kSh) {
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x) sh_stats[k] = 0ull;
@@ -138,53 +139,80 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK) k_pair(PairLaunch L, Pot po
     const int np = *L.npairs;
     const int b0 = L.begin ? *L.begin : 0;
     float pe = 0.f, vir = 0.f;
-    int* q = sh_queue + (FILTER ? (threadIdx.x >> 5) * 64 : 0);
+    int* qt = sh_queue + (FILTER ? (threadIdx.x >> 5) * 192 : 0);
+    int* qi = qt + 64;
+    int* qj = qt + 128;
     int qn = 0;
     // replica sections: warps walk whole 32-pair chunks, whose first replica is tabulated
     const int bstart = L.sec ? (b0 & ~31) : b0;
-    for (int base = bstart + gwarp * 32; base < np; base += nwarps * 32) {
+    const int stride = nwarps * 32;
+    // storage index and particles of this lane's pair in the chunk at `base`
+    auto fetch = [&](int base, int& t, int& i, int& j, bool& valid) {
         const int v = base + lane;
-        const bool valid = v < np && v >= b0;
-        int t = v;
-        if (L.sec && valid) {
-            int r = L.chunk_rep[base >> 5];
-            while (r + 1 < L.nrep && L.row_off[L.rep_off[r + 1]] <= v) ++r;
-            t = (int)(L.sec[r] + (long long)(v - L.row_off[L.rep_off[r]]));
+        valid = v < np && v >= b0;
+        t = v;
+        i = -1;
+        j = 0;
+        if (valid) {
+            if (L.sec) {
+                int r = L.chunk_rep[base >> 5];
+                while (r + 1 < L.nrep && L.row_off[L.rep_off[r + 1]] <= v) ++r;
+                t = (int)(L.sec[r] + (long long)(v - L.row_off[L.rep_off[r]]));
+            }
+            i = L.pair_i[t];
+            j = L.pair_j[t];
         }
+    };
+    int tn, in_, jn;
+    bool vn;
+    fetch(bstart + gwarp * 32, tn, in_, jn, vn);
+    for (int base = bstart + gwarp * 32; base < np; base += stride) {
+        const int t = tn, i = in_, j = jn;
+        const bool valid = vn;
+        if (base + stride < np) fetch(base + stride, tn, in_, jn, vn);   // next chunk's indices in flight
         if constexpr (!FILTER) {
-            pair_process<Pot, Pot::kCountActive>(L, pot, t, valid, pe, vir, sh_stats);
+            pair_process<Pot, Pot::kCountActive>(L, pot, t, i, j, valid, pe, vir, sh_stats);
         } else {
-            bool keep = false;
-            if (valid) keep = pot.in_range(L.pair_i[t], L.pair_j[t]);
+            const bool keep = valid && pot.in_range(i, j);
             const unsigned vm = __ballot_sync(0xffffffffu, valid), km = __ballot_sync(0xffffffffu, keep);
             if (Pot::kCountActive && lane == 0) {
                 atomicAdd(&sh_stats[0], (unsigned long long)__popc(vm));
                 if (km) atomicAdd(&sh_stats[1], (unsigned long long)__popc(km));
             }
-            if (keep) q[qn + __popc(km & ((1u << lane) - 1u))] = t;
+            if (keep) {
+                const int slot = qn + __popc(km & ((1u << lane) - 1u));
+                qt[slot] = t;
+                qi[slot] = i;
+                qj[slot] = j;
+            }
             qn += __popc(km);
             __syncwarp();
             if (qn >= 32) {
-                const int tq = q[lane];
+                const int tq = qt[lane], iq = qi[lane], jq = qj[lane];
                 __syncwarp();
-                if (lane < qn - 32) q[lane] = q[32 + lane];
+                if (lane < qn - 32) {
+                    qt[lane] = qt[32 + lane];
+                    qi[lane] = qi[32 + lane];
+                    qj[lane] = qj[32 + lane];
+                }
                 __syncwarp();
                 qn -= 32;
-                pair_process<Pot, false>(L, pot, tq, true, pe, vir, sh_stats);
+                pair_process<Pot, false>(L, pot, tq, iq, jq, true, pe, vir, sh_stats);
             }
         }
     }
     if (FILTER && qn > 0) {   // qn is warp-uniform
-        const int tq = lane < qn ? q[lane] : 0;
-        pair_process<Pot, false>(L, pot, tq, lane < qn, pe, vir, sh_stats);
+        const bool ok = lane < qn;
+        pair_process<Pot, false>(L, pot, ok ? qt[lane] : 0, ok ? qi[lane] : 0, ok ? qj[lane] : 0, ok, pe, vir,
+                                 sh_stats);
     }
     if (kSh) {
         __syncthreads();
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x)
             if (sh_stats[k]) atomicAdd(&L.stats[k], sh_stats[k]);
     }
-    double e[2] = {(double)pe, (double)vir};
-    block_reduce_finish<2>(e, L.partials, L.done, L.acc, L.acc_total);
+    const float e[2] = {pe, vir};
+    block_reduce_finish_f<2>(e, L.partials, L.done, L.acc, L.acc_total);
 }
 
 // Launch shape of the pair kernels: block size and the range filter. The

@@ -193,19 +193,17 @@ SG_DEV float3 min_image(float3 d, float3 box, float3 inv_box, int periodic) {
 // Shared block reduction of K doubles; the last block to finish adds the
 // per-block partials, in block order, into acc[k] (deterministic). Must be
 // called by every thread of the block. partials holds gridDim.x * K slots.
-// Returns true in the block that finished the sum (block-uniform).
+// Block sums from one value per warp (held by lane 0), then the grid sum in
+// the block that arrives last. Returns true in that block (block-uniform).
 template <int K>
-__device__ bool block_reduce_finish(double (&v)[K], double* partials, unsigned int* done, double* acc,
-                                    double* acc_also = nullptr) {
+__device__ bool block_finish_from_warps(const double (&wv)[K], double* partials, unsigned int* done, double* acc,
+                                        double* acc_also) {
     __shared__ double sh[32][K];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        double x = v[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[warp][k] = x;
+        for (int k = 0; k < K; ++k) sh[warp][k] = wv[k];
     }
     __syncthreads();
     if (threadIdx.x < K) {
@@ -248,6 +246,48 @@ __device__ bool block_reduce_finish(double (&v)[K], double* partials, unsigned i
         if (threadIdx.x == 0) *done = 0u;
     }
     return last;
+}
+
+// Per-thread FP64 values: warp sums by shuffles, then block_finish_from_warps.
+template <int K>
+__device__ bool block_reduce_finish(double (&v)[K], double* partials, unsigned int* done, double* acc,
+                                    double* acc_also = nullptr) {
+    double wv[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        wv[k] = x;
+    }
+    return block_finish_from_warps<K>(wv, partials, done, acc, acc_also);
+}
+
+// The same for per-thread FP32 sums (pair energies and virials): the warp
+// level adds in double-float (error-free FP32 two-sums, ~48-bit significand)
+// on the FP32 pipe, and FP64 takes over from one value per warp, so the
+// result matches an FP64 sum of the FP32 terms to ~1e-14 relative while the
+// FP64 pipe sees 1/32 of the additions.
+template <int K>
+__device__ bool block_reduce_finish_f(const float (&v)[K], double* partials, unsigned int* done, double* acc,
+                                      double* acc_also = nullptr) {
+    double w[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        float hi = v[k], lo = 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ho = __shfl_down_sync(0xffffffffu, hi, o);
+            const float lo2 = __shfl_down_sync(0xffffffffu, lo, o);
+            const float s = hi + ho;
+            const float bb = s - hi;
+            const float err = (hi - (s - bb)) + (ho - bb);
+            hi = s;
+            lo = lo + lo2 + err;
+        }
+        w[k] = (double)hi + (double)lo;   // used from lane 0
+    }
+    return block_finish_from_warps<K>(w, partials, done, acc, acc_also);
 }
 
 // --------------------------------------------------- internal entry points --
