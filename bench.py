@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--config", default="ecp", choices=sorted(WORKLOADS) + ["replicas"])
     ap.add_argument("--nrep", type=int, default=4096, help="replicas (config replicas)")
     ap.add_argument("--rep-equil", type=int, default=300, help="untimed equilibration steps (config replicas)")
+    ap.add_argument("--flat-graph", action="store_true",
+                    help="list build as flag-gated kernels instead of a conditional graph node (for ncu launch lists)")
     ap.add_argument("--solver", default="newton", choices=["newton", "brent", "mlp"])
     ap.add_argument("--equil", type=int, default=1500, help="untimed Langevin equilibration steps")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU-baseline sample")
@@ -134,13 +136,17 @@ def pair_params(g, w, solver):
     return g.params(kind, cutoff=w["cutoff"], mu=w.get("mu", 0), nu=w.get("nu", 0), solver=s)
 
 
+FLAGS = 0   # step-graph flags (capi.STEP_FLAT under --flat-graph)
+
+
 def configure(g, w, pp, langevin=False, first_step=1):
     from sucrose_gb300 import capi
     if langevin or w["integrator"] == "LANGEVIN":
         g.configure_step(pp, integrator=capi.INT_LANGEVIN, dt=w["dt"], target_temp=w["T"], damping=1.0,
-                         rotations=1, first_step=first_step)
+                         rotations=1, first_step=first_step, flags=FLAGS)
     else:
-        g.configure_step(pp, integrator=capi.INT_NH, dt=w["dt"], target_temp=w["T"], rotations=1, rot_chain=1)
+        g.configure_step(pp, integrator=capi.INT_NH, dt=w["dt"], target_temp=w["T"], rotations=1, rot_chain=1,
+                         flags=FLAGS)
 
 
 def pair_flops(kind, listed, in_range, mean_evals=0.0):
@@ -495,7 +501,7 @@ def run_replicas(a):
 
     def configure(step_dt, first):
         g.configure_step_pairs(pairs, integrator=capi.INT_LANGEVIN, dt=step_dt, damping=W["damping"], rotations=1,
-                               first_step=first)
+                               first_step=first, flags=FLAGS)
 
     # untimed equilibration from the lattice: short steps first
     configure(dt / 4, 1)
@@ -790,6 +796,8 @@ def run_reference(a):
 
 if __name__ == "__main__":
     args = parse()
+    if args.flat_graph:
+        FLAGS = 1
     if args.impl == "reference":
         run_reference(args)
     elif args.config == "replicas":

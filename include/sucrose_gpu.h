@@ -233,9 +233,12 @@ typedef struct {
     double dt, target_temp, damping, coupling;
     uint32_t key[2];       /* Langevin Philox key (has_key = 1), else the reference key */
     int32_t has_key;
-    int32_t reserved;
+    int32_t flags;         /* SG_STEP_FLAT: list build as flag-gated kernels in the
+                              graph instead of a conditional node (same results; for
+                              profilers that do not follow conditional nodes)      */
     sg_pair_params pair;   /* the pair potential evaluated every step              */
 } sg_step_config;
+#define SG_STEP_FLAT 1
 
 /* Set the step program. The first sg_step call runs one step eagerly (which
  * allocates every buffer), then captures one step as a CUDA graph; later

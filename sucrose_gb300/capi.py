@@ -31,10 +31,11 @@ class StepConfig(C.Structure):
     _fields_ = [("integrator", C.c_int32), ("rotations", C.c_int32), ("rot_chain", C.c_int32),
                 ("first_step", C.c_int32), ("dt", C.c_double), ("target_temp", C.c_double),
                 ("damping", C.c_double), ("coupling", C.c_double), ("key", C.c_uint32 * 2),
-                ("has_key", C.c_int32), ("reserved", C.c_int32), ("pair", PairParams)]
+                ("has_key", C.c_int32), ("flags", C.c_int32), ("pair", PairParams)]
 
 
 INT_NVE, INT_LANGEVIN, INT_NH, INT_NH_REF = 0, 1, 2, 3
+STEP_FLAT = 1
 
 
 class TuneResult(C.Structure):

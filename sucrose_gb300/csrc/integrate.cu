@@ -250,16 +250,12 @@ struct NhConst {
     double HB[3], HBr[3];
 };
 
-__device__ double exprel_d(double x) {
-    if (fabs(x) > 0.01) return (exp(x) - 1.0) / x;
-    const double g[5] = {1.0 / 1, 1.0 / 6, 1.0 / 120, 1.0 / 5040, 1.0 / 362880};
-    double y = (x / 2) * (x / 2);
-    double f = g[4];
-    for (int k = 3; k >= 0; --k) f = f * y + g[k];
-    return exp(x / 2) * f;
-}
 
-// u4_propagator: G1 from the supplied sum (m v^2 or L_b^2/I)
+// u4_propagator: G1 from the supplied sum (m v^2 or L_b^2/I), with
+// exprel(y) = (e^y - 1)/y (integrators.f90:233-301). One FP64 exponential per
+// chain element: with h = exp(-x/2), exp(-x) = h^2 and exprel(-x) is
+// (h^2 - 1)/(-x), or for |x| <= 0.01 h times the even series
+// sinh(x/2)/(x/2) = sum (x/2)^2k / (2k+1)!, so the two share it.
 __device__ void u4(double t, int j_start, int j_stop, int stride, double* p, const double* HB, double sum, double ndof,
                    double T) {
     for (int j = j_start; stride > 0 ? j <= j_stop : j >= j_stop; j += stride) {
@@ -267,9 +263,20 @@ __device__ void u4(double t, int j_start, int j_stop, int stride, double* p, con
         if (j == 3) {
             p[2] = p[2] + t * gj;
         } else {
-            double x = t * p[j] / HB[j];
-            double c = exprel_d(-x);
-            p[j - 1] = p[j - 1] * exp(-x) + t * gj * c;
+            const double x = t * p[j] / HB[j];
+            const double h = exp(-0.5 * x);
+            const double ex = h * h;
+            double c;
+            if (fabs(x) > 0.01) {
+                c = (ex - 1.0) / (-x);
+            } else {
+                const double g[5] = {1.0 / 1, 1.0 / 6, 1.0 / 120, 1.0 / 5040, 1.0 / 362880};
+                const double y = (0.5 * x) * (0.5 * x);
+                double f = g[4];
+                for (int k = 3; k >= 0; --k) f = f * y + g[k];
+                c = h * f;
+            }
+            p[j - 1] = p[j - 1] * ex + t * gj * c;
         }
     }
 }
@@ -292,33 +299,33 @@ __global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* _
 
 // Standard NHC half step on the chain(s): nh[14], nh[15] hold the sums on
 // entry (zeroed by the host before the reduction). Writes the scale factors.
-__device__ void nhc_chain(const NhConst& c, double* nh, int rot) {
-    double* eta = nh;
-    double* p = nh + 3;
-    double K = nh[14];
-    u4(c.dt / 4.0, 3, 1, -1, p, c.HB, K, c.ndof, c.T);
-    double sc = exp(-0.5 * c.dt * p[0] / c.HB[0]);
-    for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] / c.HB[k];
-    u4(c.dt / 4.0, 1, 3, 1, p, c.HB, K * sc * sc, c.ndof, c.T);
-    nh[12] = sc;
-    nh[16] = K * sc * sc;
-    if (rot) {
-        double* er = nh + 6;
-        double* pr = nh + 9;
-        double Kr = nh[15];
-        u4(c.dt / 4.0, 3, 1, -1, pr, c.HBr, Kr, c.nrot, c.T);
-        double scr = exp(-0.5 * c.dt * pr[0] / c.HBr[0]);
-        for (int k = 0; k < 3; ++k) er[k] = er[k] + 0.5 * c.dt * pr[k] / c.HBr[k];
-        u4(c.dt / 4.0, 1, 3, 1, pr, c.HBr, Kr * scr * scr, c.nrot, c.T);
-        nh[13] = scr;
-    } else {
-        nh[13] = 1.0;
+// The translational chain (which = 0) and the rotational chain (which = 1)
+// are independent, and the caller runs them in two different warps.
+__device__ void nhc_chain_one(const NhConst& c, double* nh, int which) {
+    double* eta = nh + 6 * which;
+    double* p = eta + 3;
+    const double* HB = which ? c.HBr : c.HB;
+    const double K = nh[14 + which];
+    u4(c.dt / 4.0, 3, 1, -1, p, HB, K, which ? c.nrot : c.ndof, c.T);
+    const double sc = exp(-0.5 * c.dt * p[0] / HB[0]);
+    for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] / HB[k];
+    u4(c.dt / 4.0, 1, 3, 1, p, HB, K * sc * sc, which ? c.nrot : c.ndof, c.T);
+    nh[12 + which] = sc;
+    if (!which) nh[16] = K * sc * sc;
+}
+
+// threads 0 (translation) and 32 (rotation, or the unit scale without it)
+__device__ void nhc_chain_threads(const NhConst& c, double* nh, int rot) {
+    if (threadIdx.x == 0) nhc_chain_one(c, nh, 0);
+    if (threadIdx.x == 32) {
+        if (rot) nhc_chain_one(c, nh, 1);
+        else nh[13] = 1.0;
     }
 }
 
 __global__ void k_nhc_chain(NhConst c, double* nh, int rot) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    nhc_chain(c, nh, rot);
+    if (blockIdx.x != 0) return;
+    nhc_chain_threads(c, nh, rot);
 }
 
 // ---- fused Nose-Hoover step (the captured step's form) -----------------------
@@ -351,7 +358,7 @@ __global__ void k_nhc_sum_chain(int n, float dt, int kick, float4* __restrict__ 
     if (block_reduce_finish<2>(e, partials, done, nh + 14)) {
         __syncthreads();
         __threadfence_block();
-        if (threadIdx.x == 0) nhc_chain(c, nh, rot);
+        nhc_chain_threads(c, nh, rot);
     }
 }
 
@@ -645,7 +652,7 @@ int sg_nht_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, 
         return SG_OK;
     }
     if (int rc = sum_mv2(ctx, rot_chain)) return rc;
-    k_nhc_chain<<<1, 32, 0, ctx->stream>>>(c, ctx->nh, rot_chain);
+    k_nhc_chain<<<1, 64, 0, ctx->stream>>>(c, ctx->nh, rot_chain);
     k_nhc_apply<<<nb, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, 1, (float)dt, make_geo(ctx), ctx->pos, ctx->vel,
                                              ctx->force, ctx->angm, rot_chain);
     SG_LAUNCH_CHECK(ctx, "k_nhc_apply");
@@ -670,7 +677,7 @@ int sg_nht_final(sg_ctx* ctx, double dt, double target_temp, double coupling, in
     }
     k_kick<<<nb, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->vel, ctx->force);
     if (int rc = sum_mv2(ctx, rot_chain)) return rc;
-    k_nhc_chain<<<1, 32, 0, ctx->stream>>>(c, ctx->nh, rot_chain);
+    k_nhc_chain<<<1, 64, 0, ctx->stream>>>(c, ctx->nh, rot_chain);
     k_nhc_apply<<<nb, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, 0, (float)dt, make_geo(ctx), ctx->pos, ctx->vel,
                                              ctx->force, ctx->angm, rot_chain);
     SG_LAUNCH_CHECK(ctx, "k_nhc_apply");

@@ -18,14 +18,14 @@ __global__ void k_set_rebuild_condition(cudaGraphConditionalHandle h, const int*
 // step; the build kernels sit in the body of a conditional graph node that
 // executes only when a rebuild was requested, so a step without a rebuild
 // launches none of them. Outside capture the flag-gated kernels are enqueued.
-int enqueue_list_update(sg_ctx* ctx) {
+int enqueue_list_update(sg_ctx* ctx, bool flat) {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
     cudaGraph_t cg = nullptr;
     const cudaGraphNode_t* deps = nullptr;
     const cudaGraphEdgeData* edges = nullptr;
     size_t nd = 0;
     SG_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &edges, &nd));
-    if (st != cudaStreamCaptureStatusActive) return sg_nlist_update(ctx);
+    if (flat || st != cudaStreamCaptureStatusActive) return sg_nlist_update(ctx);
     if (int rc = sg_nlist_enqueue_check(ctx)) return rc;
     cudaGraphConditionalHandle h;
     SG_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &edges, &nd));
@@ -75,7 +75,7 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c) {
             break;
         default: rc = sg_fail(ctx, SG_EINVAL, "unknown integrator %d", c.integrator);
     }
-    if (!rc) rc = enqueue_list_update(ctx);
+    if (!rc) rc = enqueue_list_update(ctx, (c.flags & SG_STEP_FLAT) != 0);
     if (!rc) rc = sg_zero_forces(ctx);
     for (int k = 0; !rc && k < ctx->step_npairs; ++k) rc = sg_pair_forces_async(ctx, &ctx->step_pairs[k]);
     if (!rc) {

@@ -15,7 +15,9 @@ filter (for example ncu -k regex:k_pair -c 2). Cases:
   langevin  Langevin step (initial + final) with rotations, N = 32 768
   nhc       Nose-Hoover chain step with rotations, N = 65 536
   mlp_train one MLP training step on 65 536 samples
-  replicas  one captured step of 1 024 replicas (LJ + GB)
+  ecp_step  captured Nose-Hoover steps of the ECP system (list build as
+            flag-gated kernels, so that a profiler sees every kernel)
+  replicas  captured steps of 1 024 replicas (LJ + GB), same flag
 """
 import argparse
 import os
@@ -63,7 +65,7 @@ def main():
     ap.add_argument("case")
     ap.add_argument("--reps", type=int, default=3)
     a = ap.parse_args()
-    if a.case in ("ecp", "ecp_mlp", "list", "nhc"):
+    if a.case in ("ecp", "ecp_mlp", "list", "nhc", "ecp_step"):
         g, p = ecp_system()
     elif a.case in ("gb", "langevin"):
         g, p = gb_system()
@@ -111,6 +113,10 @@ def main():
             g.qq_initial(0.001)
             g.nht_final(0.001, 1.2, 0.0, mode=1, rot_chain=1)
             g.qq_final(0.001)
+    elif a.case == "ecp_step":
+        g.configure_step(p, integrator=capi.INT_NH, dt=0.001, target_temp=1.2, rotations=1, rot_chain=1,
+                         flags=capi.STEP_FLAT)
+        g.step(1 + a.reps)
     elif a.case == "mlp_train":
         from sucrose_gb300 import mlp
 
@@ -129,7 +135,8 @@ def main():
         LJ, GB = configs.LJ_REPLICA, configs.GB_REPLICA
         g.init_rep_nlist([LJ["skin"], GB["skin"], 0.3], [LJ["list_cutoff"], GB["list_cutoff"], 3.0], trigger_mode=1)
         pairs = bench.replica_pair_params()
-        g.configure_step_pairs(pairs, integrator=capi.INT_LANGEVIN, dt=0.0005, damping=1.0, rotations=1)
+        g.configure_step_pairs(pairs, integrator=capi.INT_LANGEVIN, dt=0.0005, damping=1.0, rotations=1,
+                               flags=capi.STEP_FLAT)
         g.step(1 + a.reps)
     g.synchronize()
     print("profile case", a.case, "done")

@@ -300,8 +300,9 @@ class GpuSystem:
 
     # ---- captured timestep -------------------------------------------------------------
     def configure_step(self, pair, integrator=capi.INT_NVE, dt=0.001, target_temp=1.0, damping=1.0, coupling=0.0,
-                       rotations=0, rot_chain=0, first_step=1, key=None):
+                       rotations=0, rot_chain=0, first_step=1, key=None, flags=0):
         cfg = capi.StepConfig()
+        cfg.flags = flags
         cfg.integrator, cfg.rotations, cfg.rot_chain, cfg.first_step = integrator, rotations, rot_chain, first_step
         cfg.dt, cfg.target_temp, cfg.damping, cfg.coupling = dt, target_temp, damping, coupling
         if key is not None:
@@ -312,10 +313,11 @@ class GpuSystem:
         self._c(self.L.sg_step_configure(self.ctx, C.byref(cfg)))
 
     def configure_step_pairs(self, pairs, integrator=capi.INT_NVE, dt=0.001, target_temp=1.0, damping=1.0,
-                             coupling=0.0, rotations=0, rot_chain=0, first_step=1, key=None):
+                             coupling=0.0, rotations=0, rot_chain=0, first_step=1, key=None, flags=0):
         """Step whose pair stage runs several parameter sets in order, one per
         potential family (replica contexts)."""
         cfg = capi.StepConfig()
+        cfg.flags = flags
         cfg.integrator, cfg.rotations, cfg.rot_chain, cfg.first_step = integrator, rotations, rot_chain, first_step
         cfg.dt, cfg.target_temp, cfg.damping, cfg.coupling = dt, target_temp, damping, coupling
         if key is not None:
