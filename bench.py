@@ -412,8 +412,10 @@ def run_ours(a):
     cpu = None
     if rank == 0:
         cpu_rate, m = cpu_baseline(g, w, a.cpu_seconds, nthreads=1)
+        routine = ("the reference's ecpr_ with its Brent solve and per-pair setup" if w["kind"].startswith("ECP")
+                   else "the reference's gb_ (mu 2, nu 1)")
         cpu = {"value": cpu_rate, "unit": "pair-evals/s", "cores": 1, "kind": "port",
-               "sample": f"{m} listed pairs of this workload's list, reference Brent + per-pair setup, FP64, "
+               "sample": f"{m} listed pairs of this workload's list, {routine}, FP64, "
                          f"oracle restatement built -O3 -ffast-math, 1 thread"}
     if rank == 0:
         line = {
@@ -789,7 +791,8 @@ def run_reference(a):
             "config": {"workload": w["workload"], "n": n, "listed_pairs": int(len(pi)), "per_step_pairs": per_step},
             "cpu_baseline": {"value": value, "unit": "pair-evals/s", "cores": nth, "kind": "port",
                              "sample": f"{per_step} pairs per step of the {len(pi)}-pair list; the reference pair "
-                                       "routine (Brent, per-pair setup, FP64) restated in C++, OpenMP"},
+                                       "routine (" + ("ecpr_: Brent, per-pair setup" if a.config == "ecp" else "gb_")
+                                       + ", FP64) restated in C++, OpenMP"},
             "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
