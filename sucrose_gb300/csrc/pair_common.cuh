@@ -269,10 +269,12 @@ int launch_pair(sg_ctx* ctx, Pot pot, int kind) {
 
 struct BoxF {
     float3 box, inv_box;
+    float3 box_lo;              // box - (float)box: with box, the FP64 box to ~1e-15
     int periodic;
     const int* rep_of;          // batched replicas: per-particle replica, else nullptr
     const float4* rbox;
     const float4* rinv;
+    const float4* rbox_lo;
 };
 
 inline BoxF make_boxf(const sg_ctx* ctx) {
@@ -280,6 +282,10 @@ inline BoxF make_boxf(const sg_ctx* ctx) {
     b.rep_of = ctx->rep.rep_of;
     b.rbox = ctx->rep.box;
     b.rinv = ctx->rep.inv_box;
+    b.rbox_lo = ctx->rep.box_lo;
+    b.box_lo = make_float3((float)(ctx->box[0] - (double)(float)ctx->box[0]),
+                           (float)(ctx->box[1] - (double)(float)ctx->box[1]),
+                           (float)(ctx->box[2] - (double)(float)ctx->box[2]));
     b.box = make_float3((float)ctx->box[0], (float)ctx->box[1], (float)ctx->box[2]);
     b.inv_box = make_float3((float)(1.0 / ctx->box[0]), (float)(1.0 / ctx->box[1]), (float)(1.0 / ctx->box[2]));
     b.periodic = ctx->periodic;
@@ -296,6 +302,39 @@ SG_DEV float3 pair_rij(const float4* __restrict__ pos, int i, int j, const BoxF&
                          make_float3(ib.x, ib.y, ib.z), 1);
     }
     return min_image(make_float3(a.x - c.x, a.y - c.y, a.z - c.z), b.box, b.inv_box, b.periodic);
+}
+
+// One component of the minimum image, to about 1e-12 absolute: the FP32
+// difference a - c with its exact rounding error (two-sum), the image shift
+// n * (box_hi + box_lo) applied to each part (for n = +-1 the difference is
+// within a factor two of box_hi, so d - n box_hi is exact). Without it, pairs
+// across the boundary carry the rounding of a - c (~ulp(box)/2) and of the
+// FP32 box.
+SG_DEV float min_image_precise(float a, float c, float L, float iL, float Llo, int periodic) {
+    const float d = a - c;
+    const float bb = d - a;
+    const float e = (a - (d - bb)) + (-c - bb);
+    if (!periodic) return d + e;
+    const float n = roundf(d * iL);
+    return __fsub_rn(d, n * L) + (e - n * Llo);
+}
+
+// pair_rij for the contact-distance potentials (ECP): see min_image_precise.
+SG_DEV float3 pair_rij_precise(const float4* __restrict__ pos, int i, int j, const BoxF& b) {
+    const float4 a = pos[i], c = pos[j];
+    float3 L = b.box, iL = b.inv_box, lo = b.box_lo;
+    int per = b.periodic;
+    if (b.rep_of) {
+        const int r = b.rep_of[i];
+        const float4 bx = b.rbox[r], ib = b.rinv[r], bl = b.rbox_lo[r];
+        L = make_float3(bx.x, bx.y, bx.z);
+        iL = make_float3(ib.x, ib.y, ib.z);
+        lo = make_float3(bl.x, bl.y, bl.z);
+        per = 1;
+    }
+    return make_float3(min_image_precise(a.x, c.x, L.x, iL.x, lo.x, per),
+                       min_image_precise(a.y, c.y, L.y, iL.y, lo.y, per),
+                       min_image_precise(a.z, c.z, L.z, iL.z, lo.z, per));
 }
 
 SG_DEV float ipowf(float x, int n) {

@@ -340,11 +340,19 @@ SG_DEV float3 lin_residual_df(const float* A, const float* D, float3 r, float la
     return make_float3(out[0], out[1], out[2]);
 }
 
+// K + dk as a float pair: hi = fl(K + dk) and the exact rounding error.
+SG_DEV void add_refinement(float3 K, float3 dk, float3& hi, float3& lo) {
+    float s, e;
+    two_sum(K.x, dk.x, s, e); hi.x = s; lo.x = e;
+    two_sum(K.y, dk.y, s, e); hi.y = s; lo.y = e;
+    two_sum(K.z, dk.z, s, e); hi.z = s; lo.z = e;
+}
+
 SG_DEV float residual_check(int mode, const float* A, const float* D, float3 r, float lam, const Chol& c, float3 K,
-                            float& rK_out, float& s2, float3& Kr) {
+                            float& rK_out, float& s2, float3& Kr, float3& Krlo) {
     const float3 e = mode == 2 ? lin_residual_df(A, D, r, lam, K) : lin_residual_fp64(A, D, r, lam, K);
     const float3 dk = chol_solve(c, e);
-    Kr = make_float3(K.x + dk.x, K.y + dk.y, K.z + dk.z);
+    add_refinement(K, dk, Kr, Krlo);
     const float3 DK = symv(D, Kr);
     const float rK = dot3(r, Kr), KDK = dot3(Kr, DK);
     const float3 Z = chol_solve(c, DK);
@@ -377,13 +385,14 @@ struct PotECP {
 
     SG_DEV void eval(bool valid, int i, int j, int t, PairOut& o, unsigned long long* sh) const;
     SG_DEV float solve_lambda(int i, int j, float3 r, const float* A, const float* Bm, float lam0, Chol& cR,
-                              float3& KR, unsigned& evals, unsigned& iters, bool& nonconv, bool& fallback,
+                              float3& KR, float3& KRlo, unsigned& evals, unsigned& iters, bool& nonconv, bool& fallback,
                               bool& refined) const;
 };
 
 template <int SOLVER>
 SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A, const float* Bm, float lam0,
-                                          Chol& cR, float3& KR, unsigned& evals, unsigned& iters, bool& nonconv,
+                                          Chol& cR, float3& KR, float3& KRlo, unsigned& evals, unsigned& iters,
+                                          bool& nonconv,
                                           bool& fallback, bool& refined) const {
     float D[6];
 #pragma unroll
@@ -411,11 +420,12 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
         for (int m = 0; m < 6; ++m) g[m] = fmaf(lam, D[m], A[m]);
         cR = chol(g);
         KR = chol_solve(cR, r);
+        KRlo = make_float3(0.f, 0.f, 0.f);
         if (fp64_check) {
             // refine K_R against the exact G(lambda): it sets the contact distance
             const float3 e = fp64_check == 2 ? lin_residual_df(A, D, r, lam, KR) : lin_residual_fp64(A, D, r, lam, KR);
             const float3 dk = chol_solve(cR, e);
-            KR = make_float3(KR.x + dk.x, KR.y + dk.y, KR.z + dk.z);
+            add_refinement(KR, dk, KR, KRlo);
         }
         return lam;
     }
@@ -430,10 +440,11 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
     iters = nr.iters;
     lam = nr.lam;
     nonconv = !nr.converged;
+    KRlo = make_float3(0.f, 0.f, 0.f);
     if (fp64_check) {
         float s2, rK;
         float3 Kr;
-        const float s1 = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2, Kr);
+        const float s1 = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2, Kr, KRlo);
         if (!(fabsf(s1) <= tol * rK)) {
             // one Newton step driven by the extended-precision residual
             refined = true;
@@ -449,7 +460,7 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
                     nr.K = chol_solve(nr.c, r);
                 }
             }
-            const float s1b = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2, Kr);
+            const float s1b = residual_check(fp64_check, A, D, r, lam, nr.c, nr.K, rK, s2, Kr, KRlo);
             if (!(fabsf(s1b) <= tol * rK)) nonconv = true;
         }
         nr.K = Kr;   // the refined K feeds the force terms
@@ -461,7 +472,7 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
 
 template <int SOLVER>
 SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, unsigned long long* sh) const {
-    const float3 r = pair_rij(pos, i, j, b);     // invalid lanes evaluate (0,0): never used
+    const float3 r = pair_rij_precise(pos, i, j, b);   // invalid lanes evaluate (0,0): never used
     float lam0 = 0.5f;
     if (SOLVER == SG_SOLVER_MLP_NEWTON) {
         float f[16];
@@ -482,10 +493,10 @@ SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, un
     unsigned evals = 0, iters = 0;
     bool nonconv = false, fallback = false, refined = false;
     Chol cR;
-    float3 KR = make_float3(0.f, 0.f, 0.f);
+    float3 KR = make_float3(0.f, 0.f, 0.f), KRlo = KR;
     float lam = 0.5f;
     if (valid) {
-        lam = solve_lambda(i, j, r, A, Bm, lam0, cR, KR, evals, iters, nonconv, fallback, refined);
+        lam = solve_lambda(i, j, r, A, Bm, lam0, cR, KR, KRlo, evals, iters, nonconv, fallback, refined);
         if (lam_out) lam_out[t] = lam;
     }
     {
@@ -530,11 +541,28 @@ SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, un
     const float inv_rsq = 1.f / rsq;
     const float eps2 = l1 * rKE * inv_rsq;
     // contact distance sigma = r / sqrt(S), S = l(1-l) r.K_R (force.f90:1316-1317); the
-    // envelope needs r - sigma, formed without cancellation as r (S-1) / (sqrt S (sqrt S + 1))
+    // envelope needs r - sigma, formed without cancellation as r (S-1) / (sqrt S (sqrt S + 1)).
+    // S - 1 is what sets the repulsion near contact, so it is formed in double-float:
+    // r.K_R from the refined K_R (hi + lo) with exact products, l(1-l) exactly.
     const float Sc = l1 * rKR;
+    float Sm1;
+    {
+        float omh, oml_e;
+        two_sum(1.f, -lam, omh, oml_e);                     // 1 - lambda = omh + oml_e
+        const float l1h = lam * omh, l1e = fmaf(lam, omh, -l1h) + lam * oml_e;
+        float rkh = r.x * KR.x, rke = fmaf(r.x, KR.x, -rkh);
+        float p = r.y * KR.y, pe = fmaf(r.y, KR.y, -p), s, e;
+        two_sum(rkh, p, s, e); rkh = s; rke += e + pe;
+        p = r.z * KR.z; pe = fmaf(r.z, KR.z, -p);
+        two_sum(rkh, p, s, e); rkh = s; rke += e + pe;
+        rke += r.x * KRlo.x + r.y * KRlo.y + r.z * KRlo.z;
+        const float Sh = l1h * rkh, Se = fmaf(l1h, rkh, -Sh) + l1h * rke + l1e * rkh;
+        two_sum(Sh, -1.f, s, e);
+        Sm1 = s + (e + Se);
+    }
     const float sqS = sqrtf(Sc);
     const float rexact = sqrtf(rsq);
-    const float rms = rexact * (Sc - 1.f) / (sqS * (sqS + 1.f));   // r - sigma
+    const float rms = rexact * Sm1 / (sqS * (sqS + 1.f));   // r - sigma
     const float sigma = rexact / sqS;
     const float fac = 2.f * l1 * inv_rsq;   // efac = rfac (lambda_E = lambda_R, force.f90:1308)
     const float pi32 = sigma * sigma * sigma;

@@ -93,7 +93,7 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     const size_t s_boxd = al(sizeof(double) * 3 * R), s_d = al(sizeof(double) * R), s_f4 = al(sizeof(float4) * R),
                  s_i4 = al(sizeof(int4) * R), s_u2 = al(sizeof(uint2) * R),
                  s_i = al(sizeof(int) * R), s_off = al(sizeof(int) * (R + 1)), s_of = al(sizeof(int) * (size_t)n);
-    const size_t bytes = s_boxd + 3 * s_d + 2 * s_f4 + s_i4 + s_u2 + s_i + s_off + s_of;
+    const size_t bytes = s_boxd + 3 * s_d + 3 * s_f4 + s_i4 + s_u2 + s_i + s_off + s_of;
     char* base = nullptr;
     SG_CUDA(ctx, cudaMalloc(&base, bytes));
     ctx->rep_alloc = base;
@@ -103,19 +103,22 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     double* trig = (double*)p; p += s_d;
     float4* box = (float4*)p; p += s_f4;
     float4* inv = (float4*)p; p += s_f4;
+    float4* blo = (float4*)p; p += s_f4;
     int4* grid = (int4*)p; p += s_i4;
     uint2* key = (uint2*)p; p += s_u2;
     double* temp = (double*)p; p += s_d;
     int* tint = (int*)p; p += s_i;
     int* off = (int*)p; p += s_off;
     int* rep_of = (int*)p;
-    std::vector<float4> hb(R), hi(R);
+    std::vector<float4> hb(R), hi(R), hl(R);
     std::vector<uint2> hk(R);
     std::vector<double> ht(R);
     std::vector<int> hti(R);
     for (int r = 0; r < R; ++r) {
         hb[r] = make_float4((float)boxes[3 * r], (float)boxes[3 * r + 1], (float)boxes[3 * r + 2], 0.f);
         hi[r] = make_float4((float)(1.0 / boxes[3 * r]), (float)(1.0 / boxes[3 * r + 1]), (float)(1.0 / boxes[3 * r + 2]), 0.f);
+        hl[r] = make_float4((float)(boxes[3 * r] - (double)hb[r].x), (float)(boxes[3 * r + 1] - (double)hb[r].y),
+                            (float)(boxes[3 * r + 2] - (double)hb[r].z), 0.f);
         hk[r] = keys ? make_uint2(keys[2 * r], keys[2 * r + 1]) : make_uint2(0x6D2B79F5u, 0x1B873593u);
         const double T = temps ? temps[r] : 1.0;
         ht[r] = T;
@@ -124,6 +127,7 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     SG_CUDA(ctx, cudaMemcpy(boxd, boxes, sizeof(double) * 3 * R, cudaMemcpyHostToDevice));
     SG_CUDA(ctx, cudaMemcpy(box, hb.data(), sizeof(float4) * R, cudaMemcpyHostToDevice));
     SG_CUDA(ctx, cudaMemcpy(inv, hi.data(), sizeof(float4) * R, cudaMemcpyHostToDevice));
+    SG_CUDA(ctx, cudaMemcpy(blo, hl.data(), sizeof(float4) * R, cudaMemcpyHostToDevice));
     SG_CUDA(ctx, cudaMemcpy(key, hk.data(), sizeof(uint2) * R, cudaMemcpyHostToDevice));
     SG_CUDA(ctx, cudaMemcpy(temp, ht.data(), sizeof(double) * R, cudaMemcpyHostToDevice));
     SG_CUDA(ctx, cudaMemcpy(tint, hti.data(), sizeof(int) * R, cudaMemcpyHostToDevice));
@@ -135,6 +139,7 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     ctx->rep.off = off;
     ctx->rep.box = box;
     ctx->rep.inv_box = inv;
+    ctx->rep.box_lo = blo;
     ctx->rep.boxd = boxd;
     ctx->rep.rl2 = rl2;
     ctx->rep.trig = trig;

@@ -22,6 +22,7 @@ struct RepDev {
     const int* off = nullptr;         // [R+1] first particle of each replica
     const float4* box = nullptr;      // [R] box lengths (x, y, z, 0)
     const float4* inv_box = nullptr;  // [R] 1 / box
+    const float4* box_lo = nullptr;   // [R] box - (float)box: the FP64 box as float hi + lo
     const double* boxd = nullptr;     // [3R] box lengths in FP64
     const double* rl2 = nullptr;      // [R] (rc + skin)^2 of the replica's list
     const double* trig = nullptr;     // [R] rebuild bound on 4 |dr|^2

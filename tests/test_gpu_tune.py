@@ -22,9 +22,10 @@ def lj_system():
     return g, GpuSystem.params(capi.LJ, cutoff=2.5)
 
 
-def gb_system(kind=capi.GB):
-    sig = (1.0, 1.0, 3.0)
-    r, q, box = ellipsoids((16, 16, 8), sig, 0.3, seed=6, tilt=0.6)
+def gb_system(kind=capi.GB, sig=(1.0, 1.0, 3.0)):
+    prolate = sig[2] > sig[0]
+    counts = (16, 16, 8) if prolate else (8, 8, 24)
+    r, q, box = ellipsoids(counts, sig, 0.3 if prolate else 0.1, seed=6, tilt=0.6 if prolate else 0.05)
     g = GpuSystem(len(r), box)
     g.set_particles(sig=sig, eps=(1.0, 1.0, 0.2))
     g.upload(r=f32(r), q=f32(q))
@@ -40,8 +41,9 @@ def forces_with(g, p, block, filt):
     return pe, vir, F, T, (st.pairs, st.solver_evals)
 
 
-@pytest.mark.parametrize("make", [lj_system, gb_system, lambda: gb_system(capi.GBR), lambda: gb_system(capi.GBW)],
-                         ids=["lj", "gb", "gbr", "gbw"])
+@pytest.mark.parametrize("make", [lj_system, gb_system, lambda: gb_system(capi.GBR), lambda: gb_system(capi.GBW),
+                                  lambda: gb_system(capi.GB, (3.0, 3.0, 1.0))],
+                         ids=["lj", "gb", "gbr", "gbw", "gb_oblate"])
 def test_variants_agree(lib, make):
     g, p = make()
     ref = forces_with(g, p, *VARIANTS[0])
