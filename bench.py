@@ -252,6 +252,7 @@ def force_error_vs_fp64(g, w, pp, nthreads=None):
 def mlp_leg(a, g, w, torch, stream, flush, npairs):
     """Train the learned guess on plain-Newton samples at T* 0.8, 1.2, 1.6 and
     time the MLP-guess path against the plain path on the same state."""
+    import ctypes
     from sucrose_gb300 import capi, mlp
     r, q, v, l = g.download()          # restore the timed state afterwards
     newton = pair_params(g, w, "newton")
@@ -274,12 +275,31 @@ def mlp_leg(a, g, w, torch, stream, flush, npairs):
     _, _, sp = g.pair_forces(newton, want_stats=True)
     tm = statistics.median(timed_forces(g, torch, stream, pm, 10, flush))
     tp = statistics.median(timed_forces(g, torch, stream, newton, 10, flush))
+    # the tensor-core guess pass alone (part of tm)
+    guess_buf = torch.empty(max(npairs_int := g.npairs(), 1), dtype=torch.float32, device="cuda")
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tg = []
+    with torch.cuda.stream(stream):
+        for _ in range(10):
+            ev0.record(stream)
+            capi.check(g.ctx, g.L.sg_mlp_guess_tc(g.ctx, ctypes.c_void_p(guess_buf.data_ptr()), guess_buf.numel()))
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            tg.append(ev0.elapsed_time(ev1) / 1e3)
+    t_guess = statistics.median(tg)
+    # the same network in the ECP kernel itself (warp mma.sync, one kernel)
+    capi.check(g.ctx, g.L.sg_mlp_set_inline(g.ctx, 1))
+    ti = statistics.median(timed_forces(g, torch, stream, pm, 10, flush))
+    capi.check(g.ctx, g.L.sg_mlp_set_inline(g.ctx, 0))
     configure(g, w, pm)
     g.step(5)
     g.step_check()
     t_step = timed_steps(g, torch, stream, 50, flush)
     return {"samples": a.mlp_samples, "epochs": a.mlp_epochs, "train_mse": hist, "gen_s": t_gen, "train_s": t_train,
             "force_kernel_ms": 1e3 * tm, "pair_evals_per_s_force_kernel": npairs / tm,
+            "guess_pass_ms_tcgen05": 1e3 * t_guess,
+            "guess_tensor_tflops": 18560.0 * npairs_int / t_guess / 1e12,
+            "inline_mma_sync_force_kernel_ms": 1e3 * ti,
             "plain_force_kernel_ms_same_state": 1e3 * tp, "speedup_vs_plain_force_kernel": tp / tm,
             "full_step_pair_evals_per_s": npairs * 50 / t_step,
             "mean_evals_per_pair": sm.solver_evals / max(sm.pairs, 1),
@@ -388,6 +408,7 @@ def run_ours(a):
         extras["nonconverged"] = int(st.nonconverged)
         extras["fp64_peak_tflops_measured"] = g.peak_fma(True)
         extras["list_rebuilds_in_timed_region"] = int(builds)
+        extras["stage_ms_eager"] = g.step_stage_times(20)
         extras["autotune"] = {"block": tune.block, "filter": tune.filter,
                               "variant_ms": {f"b{b}_f{f}": float(tune.ms[k]) for k, (b, f) in
                                              enumerate(((256, 0), (128, 0), (256, 1), (128, 1))[:tune.candidates])}}

@@ -252,8 +252,20 @@ int sg_step_configure_pairs(sg_ctx* ctx, const sg_step_config* cfg, const sg_pai
 int sg_step(sg_ctx* ctx, int32_t nsteps);
 /* Wait, then report list overflow (SG_ECAPACITY) or a non-finite energy (SG_ENAN). */
 int sg_step_check(sg_ctx* ctx);
+/* Run nsteps steps eagerly (not from the graph) with CUDA events between the
+ * stages and return the mean milliseconds of: initial half step, list check
+ * and rebuild, force zeroing, pair forces, final half step. */
+int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[5]);
 /* Kernel launches in one captured step (after the first sg_step call). */
 int sg_step_kernel_count(sg_ctx* ctx, int64_t* count);
+
+/* The learned guess for every listed pair on the tensor cores (tcgen05.mma,
+ * accumulators in tensor memory), into out_dev (device, >= pair count): the
+ * pass that SG_SOLVER_MLP_NEWTON runs before the Newton kernel. */
+int sg_mlp_guess_tc(sg_ctx* ctx, float* out_dev, int64_t capacity);
+/* inline_guess = 1: the ECP kernel evaluates the guess itself with warp-level
+ * mma.sync instead (one kernel, more registers); 0 (default): separate pass. */
+int sg_mlp_set_inline(sg_ctx* ctx, int32_t inline_guess);
 
 /* ---- autotuner of the pair kernels (no counterpart in the reference) ------- */
 typedef struct {

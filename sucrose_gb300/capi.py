@@ -94,10 +94,13 @@ SIGNATURES = [
     ("sg_create_replicas", C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _I32, _D, _U32, C.c_int32]),
     ("sg_rep_nlist_init", C.c_int, [_P, _D, _D, C.c_int32]),
     ("sg_rep_kinetic", C.c_int, [_P, _D]),
+    ("sg_mlp_guess_tc", C.c_int, [_P, C.c_void_p, C.c_int64]),
+    ("sg_mlp_set_inline", C.c_int, [_P, C.c_int32]),
     ("sg_pair_autotune", C.c_int, [_P, C.POINTER(PairParams), C.c_int32, C.POINTER(TuneResult)]),
     ("sg_pair_set_launch", C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     ("sg_step_configure", C.c_int, [_P, C.POINTER(StepConfig)]),
     ("sg_step_configure_pairs", C.c_int, [_P, C.POINTER(StepConfig), C.POINTER(PairParams), C.c_int32]),
+    ("sg_step_stage_times", C.c_int, [_P, C.c_int32, _D]),
     ("sg_step", C.c_int, [_P, C.c_int32]),
     ("sg_step_check", C.c_int, [_P]),
     ("sg_step_kernel_count", C.c_int, [_P, _I64]),

@@ -248,23 +248,42 @@ __global__ void k_lgv_final(int n, float dt, float4* __restrict__ vel, const flo
 struct NhConst {
     double dt, T, ndof, nrot;
     double HB[3], HBr[3];
+    double iHB[3], iHBr[3];   // 1 / HB: the chains multiply (an FP64 division is a long serial sequence)
 };
 
+
+// exp(x) in FP64. The chain's arguments are dt/4 p/Q-sized, |x| << 0.03, where
+// the Taylor polynomial of degree 9 is below half an ulp (x^10/10! < 2e-22 at
+// |x| = 0.03); a short dependent chain of FMAs instead of the library's range
+// reduction, which matters because the chains run in one thread each.
+__device__ __forceinline__ double exp_chain(double x) {
+    if (fabs(x) >= 0.03) return exp(x);
+    double f = 1.0 / 362880.0;
+    f = fma(f, x, 1.0 / 40320.0);
+    f = fma(f, x, 1.0 / 5040.0);
+    f = fma(f, x, 1.0 / 720.0);
+    f = fma(f, x, 1.0 / 120.0);
+    f = fma(f, x, 1.0 / 24.0);
+    f = fma(f, x, 1.0 / 6.0);
+    f = fma(f, x, 0.5);
+    f = fma(f, x, 1.0);
+    return fma(f, x, 1.0);
+}
 
 // u4_propagator: G1 from the supplied sum (m v^2 or L_b^2/I), with
 // exprel(y) = (e^y - 1)/y (integrators.f90:233-301). One FP64 exponential per
 // chain element: with h = exp(-x/2), exp(-x) = h^2 and exprel(-x) is
 // (h^2 - 1)/(-x), or for |x| <= 0.01 h times the even series
 // sinh(x/2)/(x/2) = sum (x/2)^2k / (2k+1)!, so the two share it.
-__device__ void u4(double t, int j_start, int j_stop, int stride, double* p, const double* HB, double sum, double ndof,
-                   double T) {
+__device__ void u4(double t, int j_start, int j_stop, int stride, double* p, const double* iHB, double sum,
+                   double ndof, double T) {
     for (int j = j_start; stride > 0 ? j <= j_stop : j >= j_stop; j += stride) {
-        double gj = (j == 1) ? (sum - ndof * T) : ((p[j - 2] * p[j - 2] / HB[j - 2]) - T);
+        double gj = (j == 1) ? (sum - ndof * T) : ((p[j - 2] * p[j - 2] * iHB[j - 2]) - T);
         if (j == 3) {
             p[2] = p[2] + t * gj;
         } else {
-            const double x = t * p[j] / HB[j];
-            const double h = exp(-0.5 * x);
+            const double x = t * p[j] * iHB[j];
+            const double h = exp_chain(-0.5 * x);
             const double ex = h * h;
             double c;
             if (fabs(x) > 0.01) {
@@ -304,12 +323,12 @@ __global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* _
 __device__ void nhc_chain_one(const NhConst& c, double* nh, int which) {
     double* eta = nh + 6 * which;
     double* p = eta + 3;
-    const double* HB = which ? c.HBr : c.HB;
+    const double* iHB = which ? c.iHBr : c.iHB;
     const double K = nh[14 + which];
-    u4(c.dt / 4.0, 3, 1, -1, p, HB, K, which ? c.nrot : c.ndof, c.T);
-    const double sc = exp(-0.5 * c.dt * p[0] / HB[0]);
-    for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] / HB[k];
-    u4(c.dt / 4.0, 1, 3, 1, p, HB, K * sc * sc, which ? c.nrot : c.ndof, c.T);
+    u4(c.dt / 4.0, 3, 1, -1, p, iHB, K, which ? c.nrot : c.ndof, c.T);
+    const double sc = exp_chain(-0.5 * c.dt * p[0] * iHB[0]);
+    for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] * iHB[k];
+    u4(c.dt / 4.0, 1, 3, 1, p, iHB, K * sc * sc, which ? c.nrot : c.ndof, c.T);
     nh[12 + which] = sc;
     if (!which) nh[16] = K * sc * sc;
 }
@@ -489,7 +508,7 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
             vx = (float)vx; vy = (float)vy; vz = (float)vz;
             K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
         }
-        u4(c.dt / 4.0, 3, 1, -1, p, c.HB, K, c.ndof, c.T);
+        u4(c.dt / 4.0, 3, 1, -1, p, c.iHB, K, c.ndof, c.T);
         const double sc = exp(-0.5 * c.dt * p[0] / c.HB[0]);
         {
             const double ox = vx, oy = vy, oz = vz;
@@ -497,7 +516,7 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
             K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
         }
         for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] / c.HB[k];
-        u4(c.dt / 4.0, 1, 3, 1, p, c.HB, K, c.ndof, c.T);
+        u4(c.dt / 4.0, 1, 3, 1, p, c.iHB, K, c.ndof, c.T);
         if (initial) {
             const double ox = vx, oy = vy, oz = vz;
             vx = (float)(vx + h * (f.x * im)); vy = (float)(vy + h * (f.y * im)); vz = (float)(vz + h * (f.z * im));
@@ -533,6 +552,10 @@ NhConst nh_const(const sg_ctx* ctx, double dt, double T, double coupling) {
     if (!(coupling > 0.0)) {
         c.HB[0] = c.ndof * T * tau * tau;
         c.HBr[0] = c.nrot * T * tau * tau;
+    }
+    for (int k = 0; k < 3; ++k) {
+        c.iHB[k] = 1.0 / c.HB[k];
+        c.iHBr[k] = 1.0 / c.HBr[k];
     }
     return c;
 }

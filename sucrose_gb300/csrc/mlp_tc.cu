@@ -1,0 +1,295 @@
+// Learned λ guess for every listed pair on the 5th-generation tensor cores
+// (no counterpart in the reference). One CTA of 128 threads takes 128 pairs at
+// a time: each thread forms its pair's 16 features (ecp_mlp.cuh) into shared
+// memory, one elected thread issues tcgen05.mma (BF16 operands from shared
+// memory, FP32 accumulator in tensor memory) for the 128×64 products of each
+// layer, and the four warps read their 32 accumulator rows back with
+// tcgen05.ld for bias, ReLU and the BF16 operand of the next layer. The last
+// layer (64 → 1) and the sigmoid run in registers. The guess goes to out[t]
+// for pair t, where the ECP kernel reads it as its starting λ.
+//
+// Operand layout in shared memory: K-major, no swizzle; 8×8 BF16 core matrices
+// (128 contiguous bytes, 16 bytes per row), K-adjacent cores 128 B apart,
+// 8-row groups (K/8)·128 B apart (the descriptor's leading and stride byte
+// offsets).
+//
+// Every wait is bounded: a wait that runs out sets *err and the CTA stops
+// after releasing its tensor memory.
+#include <cuda_bf16.h>
+
+#include "sg_internal.cuh"
+#include "ecp_mlp.cuh"
+
+namespace {
+
+constexpr int TM = 128;   // pairs per tile: the MMA's M
+constexpr int HN = 64;    // hidden width: the MMA's N
+constexpr uint32_t TMEM_COLS = 64;
+constexpr long long WAIT_LIMIT = 1ll << 24;
+
+struct __align__(128) TcSmem {
+    __nv_bfloat16 a1[TM * 16];   // layer-1 operand (features), 4 KB
+    __nv_bfloat16 h[TM * HN];    // hidden activations, 16 KB
+    __nv_bfloat16 w1[HN * 16];   // W1 [out][in], 2 KB
+    __nv_bfloat16 w2[HN * HN];   // 8 KB
+    __nv_bfloat16 w3[HN * HN];   // 8 KB
+    float b1[HN], b2[HN], b3[HN], w4[HN];
+    unsigned long long mbar;
+    uint32_t tmem_base;
+};
+
+// element offset of (row, k) in a K-major operand with K columns
+__device__ __forceinline__ int kmaj(int row, int k, int K) {
+    return (((row >> 3) * (K >> 3) + (k >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, leading / stride byte offsets, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;   // descriptor version field (bits 46-48 = 0b001)
+    return d;
+}
+
+// instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major, N = 64, M = 128
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(HN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_issue(uint32_t d_tmem, uint64_t a, uint64_t b, int accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+        :
+        : "r"(d_tmem), "l"(a), "l"(b), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    for (long long it = 0; it < WAIT_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Bias, ReLU and BF16 of one accumulator row (64 columns of TMEM lane `row`)
+// into the K-major operand h.
+__device__ __forceinline__ void hidden_row(uint32_t taddr, const float* bias, __nv_bfloat16* h, int row) {
+#pragma unroll
+    for (int c0 = 0; c0 < HN; c0 += 16) {
+        float v[16];
+        tmem_ld16(taddr + c0, v);
+        tmem_wait_ld();
+        uint32_t packed[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float lo = fmaxf(v[2 * k] + bias[c0 + 2 * k], 0.f);
+            const float hi = fmaxf(v[2 * k + 1] + bias[c0 + 2 * k + 1], 0.f);
+            __nv_bfloat162 p2 = __floats2bfloat162_rn(lo, hi);
+            packed[k] = *reinterpret_cast<uint32_t*>(&p2);
+        }
+        // columns c0..c0+15 are two core-matrix rows of 16 bytes
+        *reinterpret_cast<uint4*>(h + kmaj(row, c0, HN)) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        *reinterpret_cast<uint4*>(h + kmaj(row, c0 + 8, HN)) = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    }
+}
+
+__global__ void __launch_bounds__(TM) k_mlp_guess_tc(const int* __restrict__ pair_i, const int* __restrict__ pair_j,
+                                                     const int* npairs, const float4* __restrict__ pos,
+                                                     const float4* __restrict__ quat, const float4* __restrict__ shape,
+                                                     float3 box, float3 inv_box, int periodic, MlpDev m,
+                                                     float* __restrict__ out, int* err) {
+    __shared__ TcSmem s;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int np = *npairs;
+
+    // weights into the K-major layout, biases as FP32
+    for (int e = tid; e < HN * 16; e += TM) s.w1[kmaj(e >> 4, e & 15, 16)] = m.W1[e];
+    for (int e = tid; e < HN * HN; e += TM) {
+        s.w2[kmaj(e >> 6, e & 63, HN)] = m.W2[e];
+        s.w3[kmaj(e >> 6, e & 63, HN)] = m.W3[e];
+    }
+    for (int e = tid; e < HN; e += TM) {
+        s.b1[e] = m.b1[e];
+        s.b2[e] = m.b2[e];
+        s.b3[e] = m.b3[e];
+        s.w4[e] = m.w4[e];
+    }
+    const uint32_t mbar = smem_u32(&s.mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s.tmem_base)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = s.tmem_base;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
+    uint32_t phase = 0;
+    bool stopped = false;   // block-uniform: a completion wait ran out
+
+    const uint32_t a1 = smem_u32(s.a1), hh = smem_u32(s.h), w1 = smem_u32(s.w1), w2 = smem_u32(s.w2),
+                   w3 = smem_u32(s.w3);
+    for (int tile = blockIdx.x; tile * TM < np; tile += gridDim.x) {
+        const int t = tile * TM + tid;
+        const bool valid = t < np;
+        {
+            const int i = valid ? pair_i[t] : 0, j = valid ? pair_j[t] : 0;
+            const float4 a = pos[i], b = pos[j];
+            float3 r = min_image(make_float3(a.x - b.x, a.y - b.y, a.z - b.z), box, inv_box, periodic);
+            if (!valid) r = make_float3(1.f, 0.f, 0.f);
+            float f[16];
+            mlp_features(r, quat[i], quat[j], shape[i], shape[j], f);
+            uint32_t pk[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                __nv_bfloat162 p2 = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+                pk[k] = *reinterpret_cast<uint32_t*>(&p2);
+            }
+            *reinterpret_cast<uint4*>(s.a1 + kmaj(tid, 0, 16)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4*>(s.a1 + kmaj(tid, 8, 16)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
+        // three layers: (operand, K, weights, bias)
+#pragma unroll 1
+        for (int layer = 0; layer < 3; ++layer) {
+            fence_async_smem();
+            fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                fence_after_sync();
+                if (layer == 0) {
+                    mma_issue(tmem, smem_desc(a1, 128, 256), smem_desc(w1, 128, 256), 0);
+                } else {
+                    const uint32_t wb = layer == 1 ? w2 : w3;
+#pragma unroll
+                    for (int kk = 0; kk < HN / 16; ++kk)
+                        mma_issue(tmem, smem_desc(hh + 256 * kk, 128, 1024), smem_desc(wb + 256 * kk, 128, 1024), kk);
+                }
+                mma_commit(mbar);
+            }
+            // every thread waits, then the block agrees, so that all leave together
+            const bool ok = __syncthreads_and(mbar_wait(mbar, phase));
+            if (!ok) {
+                if (tid == 0) atomicExch(err, 1);
+                stopped = true;
+                break;
+            }
+            phase ^= 1u;
+            fence_after_sync();
+            if (layer < 2) {
+                hidden_row(trow, layer == 0 ? s.b1 : s.b2, s.h, tid);
+            } else {
+                float z = m.b4;
+#pragma unroll
+                for (int c0 = 0; c0 < HN; c0 += 16) {
+                    float v[16];
+                    tmem_ld16(trow + c0, v);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) z += fmaxf(v[k] + s.b3[c0 + k], 0.f) * s.w4[c0 + k];
+                }
+                const float lam = 1.f / (1.f + __expf(-z));
+                if (valid) out[t] = fminf(fmaxf(lam, 0.02f), 0.98f);
+            }
+        }
+        __syncthreads();
+        if (stopped) break;
+    }
+    // an MMA still in flight after a wait ran out: wait once more (bounded)
+    // before the tensor memory is released
+    if (stopped) mbar_wait(mbar, phase);
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after_sync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+}  // namespace
+
+// Guesses for the current list into out (device, capacity >= pair count).
+int sg_mlp_guess_tc_launch(sg_ctx* ctx, float* out) {
+    if (!ctx->mlp_ready) return sg_fail(ctx, SG_ENOTREADY, "MLP weights are not set");
+    if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "the learned guess runs on single-system contexts");
+    if (!ctx->mlp_tc_err) {
+        SG_CUDA(ctx, cudaMalloc(&ctx->mlp_tc_err, sizeof(int)));
+        SG_CUDA(ctx, cudaMemsetAsync(ctx->mlp_tc_err, 0, sizeof(int), ctx->stream));
+    }
+    MlpDev m;
+    memcpy(&m, ctx->mlp_host_desc, sizeof(m));
+    const float3 box = make_float3((float)ctx->box[0], (float)ctx->box[1], (float)ctx->box[2]);
+    const float3 ib = make_float3((float)(1.0 / ctx->box[0]), (float)(1.0 / ctx->box[1]), (float)(1.0 / ctx->box[2]));
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_mlp_guess_tc, TM, 0);
+    per_sm = std::max(1, per_sm);
+    const int64_t tiles = (ctx->nl.pair_capacity + TM - 1) / TM;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)per_sm * ctx->num_sms));
+    k_mlp_guess_tc<<<grid, TM, 0, ctx->stream>>>(ctx->nl.pair_i, ctx->nl.pair_j, ctx->nl.dev_flags + 2, ctx->pos,
+                                                 ctx->quat, ctx->shape, box, ib, ctx->periodic, m, out,
+                                                 ctx->mlp_tc_err);
+    SG_LAUNCH_CHECK(ctx, "k_mlp_guess_tc");
+    return SG_OK;
+}
+
+extern "C" {
+
+int sg_mlp_guess_tc(sg_ctx* ctx, float* out_dev, int64_t capacity) {
+    if (!ctx || !out_dev) return SG_EINVAL;
+    int64_t k = 0;
+    if (int rc = sg_nlist_count(ctx, &k)) return rc;
+    if (capacity < k) return sg_fail(ctx, SG_ECAPACITY, "guess capacity too small");
+    if (int rc = sg_mlp_guess_tc_launch(ctx, out_dev)) return rc;
+    int e = 0;
+    SG_CUDA(ctx, cudaMemcpyAsync(&e, ctx->mlp_tc_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (e) return sg_fail(ctx, SG_ECUDA, "tensor-core guess: a completion wait ran out");
+    return SG_OK;
+}
+
+int sg_mlp_set_inline(sg_ctx* ctx, int32_t inline_guess) {
+    if (!ctx) return SG_EINVAL;
+    ctx->mlp_inline = inline_guess ? 1 : 0;
+    ctx->graph_epoch++;
+    return SG_OK;
+}
+
+}  // extern "C"

@@ -26,6 +26,10 @@
 #include "pair_common.cuh"
 #include "ecp_mlp.cuh"
 
+// Internal solver id: Newton from a guess already stored in the per-pair
+// lambda array (the tensor-core guess pass of mlp_tc.cu).
+#define SOLVER_MLP_PRE 3
+
 namespace {
 
 // ------------------------------------------------------------------ prep ---
@@ -429,10 +433,11 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
         }
         return lam;
     }
-    const int budget = (SOLVER == SG_SOLVER_MLP_NEWTON) ? 3 : max_iter;
+    constexpr bool kGuess = (SOLVER == SG_SOLVER_MLP_NEWTON || SOLVER == SOLVER_MLP_PRE);
+    const int budget = kGuess ? 3 : max_iter;
     NewtonResult nr = newton_solve(A, D, r, lam0, budget, step_tol);
     evals = nr.iters;
-    if (SOLVER == SG_SOLVER_MLP_NEWTON && !nr.converged) {
+    if (kGuess && !nr.converged) {
         fallback = true;
         nr = newton_solve(A, D, r, 0.5f, max_iter, step_tol);
         evals += nr.iters;
@@ -474,6 +479,10 @@ template <int SOLVER>
 SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, unsigned long long* sh) const {
     const float3 r = pair_rij_precise(pos, i, j, b);   // invalid lanes evaluate (0,0): never used
     float lam0 = 0.5f;
+    if (SOLVER == SOLVER_MLP_PRE) {
+        // the guess of the tensor-core pass, stored where this pair's lambda goes
+        lam0 = valid ? lam_out[t] : 0.5f;
+    }
     if (SOLVER == SG_SOLVER_MLP_NEWTON) {
         float f[16];
         mlp_features(valid ? r : make_float3(1.f, 0.f, 0.f), quat[i], quat[j], shape[i], shape[j], f);
@@ -699,7 +708,11 @@ int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p) {
     switch (p->solver) {
         case SG_SOLVER_BRENT_COMPAT: return launch_ecp<SG_SOLVER_BRENT_COMPAT>(ctx, p, mu, nu);
         case SG_SOLVER_NEWTON: return launch_ecp<SG_SOLVER_NEWTON>(ctx, p, mu, nu);
-        case SG_SOLVER_MLP_NEWTON: return launch_ecp<SG_SOLVER_MLP_NEWTON>(ctx, p, mu, nu);
+        case SG_SOLVER_MLP_NEWTON:
+            if (ctx->mlp_inline) return launch_ecp<SG_SOLVER_MLP_NEWTON>(ctx, p, mu, nu);
+            // tensor-core guess pass, then Newton from it
+            if (int rc = sg_mlp_guess_tc_launch(ctx, ctx->ecp_lambda)) return rc;
+            return launch_ecp<SOLVER_MLP_PRE>(ctx, p, mu, nu);
         default: return sg_fail(ctx, SG_EINVAL, "unknown ECP solver %d", p->solver);
     }
 }

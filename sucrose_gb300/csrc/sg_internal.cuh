@@ -117,6 +117,8 @@ struct sg_ctx {
     void* mlp_wbf16 = nullptr;       // device: bf16 W1 W2 W3 then f32 b1 b2 b3 w4
     unsigned char mlp_host_desc[128];  // host copy of the MlpDev descriptor (device pointers)
     int mlp_ready = 0;
+    int* mlp_tc_err = nullptr;       // device flag: a tensor-core completion wait ran out
+    int mlp_inline = 0;              // 1: the ECP kernel evaluates the guess itself (mma.sync)
     void* mlp_work = nullptr;        // training workspace (mlp_train.cu)
     int mlp_adam_t = 0;
 
@@ -294,6 +296,7 @@ __device__ bool block_reduce_finish_f(const float (&v)[K], double* partials, uns
 // --------------------------------------------------- internal entry points --
 int sg_ecp_prepare(sg_ctx* ctx, const sg_pair_params* p, int need64);
 int sg_gather_pair_floats(sg_ctx* ctx, const float* dev, int64_t k, float* out);
+int sg_mlp_guess_tc_launch(sg_ctx* ctx, float* out);
 int sg_nhc_step_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t rot_chain,
                         int32_t rotations);
 int sg_nhc_step_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t rot_chain,

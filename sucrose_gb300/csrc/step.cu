@@ -56,11 +56,15 @@ int enqueue_list_update(sg_ctx* ctx, bool flat) {
     return SG_OK;
 }
 
-int enqueue_step(sg_ctx* ctx, const sg_step_config& c) {
+// ev (optional): 6 events recorded before the initial half step, the list
+// update, the force zeroing, the pair stage, the final half step and the
+// step counter (eager steps only; sg_step_stage_times).
+int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr) {
     const double dt = c.dt;
     ctx->lgv_step_dev = ctx->step_dev;
     ctx->lgv_rotations = c.rotations;
     int rc = SG_OK;
+    if (ev) cudaEventRecord(ev[0], ctx->stream);
     switch (c.integrator) {
         case SG_INT_NVE: rc = sg_vv_initial(ctx, dt); if (!rc && c.rotations) rc = sg_qq_initial(ctx, dt); break;
         case SG_INT_LANGEVIN:
@@ -75,9 +79,13 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c) {
             break;
         default: rc = sg_fail(ctx, SG_EINVAL, "unknown integrator %d", c.integrator);
     }
+    if (ev) cudaEventRecord(ev[1], ctx->stream);
     if (!rc) rc = enqueue_list_update(ctx, (c.flags & SG_STEP_FLAT) != 0);
+    if (ev) cudaEventRecord(ev[2], ctx->stream);
     if (!rc) rc = sg_zero_forces(ctx);
+    if (ev) cudaEventRecord(ev[3], ctx->stream);
     for (int k = 0; !rc && k < ctx->step_npairs; ++k) rc = sg_pair_forces_async(ctx, &ctx->step_pairs[k]);
+    if (ev) cudaEventRecord(ev[4], ctx->stream);
     if (!rc) {
         switch (c.integrator) {
             case SG_INT_NVE: rc = sg_vv_final(ctx, dt, nullptr); if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr); break;
@@ -88,6 +96,7 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c) {
                 if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr);
         }
     }
+    if (ev) cudaEventRecord(ev[5], ctx->stream);
     if (!rc) {
         k_step_incr<<<1, 1, 0, ctx->stream>>>(ctx->step_dev);
         cudaError_t e = cudaGetLastError();
@@ -179,6 +188,30 @@ int sg_step(sg_ctx* ctx, int32_t nsteps) {
         ctx->graph_epoch_captured = epoch;
     }
     for (int s = done; s < nsteps; ++s) SG_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    return SG_OK;
+}
+
+int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[5]) {
+    if (!ctx || !out_ms || nsteps < 1) return SG_EINVAL;
+    if (!ctx->step_ready) return sg_fail(ctx, SG_ENOTREADY, "sg_step_configure must precede sg_step_stage_times");
+    const sg_step_config& c = *reinterpret_cast<const sg_step_config*>(ctx->step_cfg);
+    std::vector<cudaEvent_t> ev(6 * (size_t)nsteps);
+    for (auto& e : ev) SG_CUDA(ctx, cudaEventCreate(&e));
+    int rc = SG_OK;
+    for (int s = 0; s < nsteps && !rc; ++s) rc = enqueue_step(ctx, c, ev.data() + 6 * s);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    for (int k = 0; k < 5; ++k) out_ms[k] = 0.0;
+    if (!rc && e == cudaSuccess) {
+        for (int s = 0; s < nsteps; ++s)
+            for (int k = 0; k < 5; ++k) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[6 * s + k], ev[6 * s + k + 1]);
+                out_ms[k] += ms / nsteps;
+            }
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (rc) return rc;
+    if (e != cudaSuccess) return sg_cuda_check(ctx, e, "sg_step_stage_times");
     return SG_OK;
 }
 

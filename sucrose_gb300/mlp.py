@@ -93,6 +93,16 @@ def predict(g, X):
     return out
 
 
+def guess_tc(g):
+    """The tensor-core guess pass (tcgen05) for the current list, same order as guess()."""
+    import torch
+    k = g.npairs()
+    out = torch.empty(max(k, 1), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    capi.check(g.ctx, g.L.sg_mlp_guess_tc(g.ctx, _ptr(out), out.numel()))
+    return out[:k]
+
+
 def guess(g):
     """The ECP kernel's in-kernel guesses for the current list (sg_nlist_pairs order)."""
     import torch

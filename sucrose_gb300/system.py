@@ -330,6 +330,13 @@ class GpuSystem:
     def step(self, nsteps=1):
         self._c(self.L.sg_step(self.ctx, int(nsteps)))
 
+    def step_stage_times(self, nsteps=10):
+        """Mean ms per stage of nsteps eager steps: initial half step, list,
+        zero forces, pairs, final half step."""
+        out = np.zeros(5)
+        self._c(self.L.sg_step_stage_times(self.ctx, int(nsteps), _dp(out)))
+        return dict(zip(("initial", "list", "zero_forces", "pairs", "final"), out.tolist()))
+
     def step_check(self):
         self._c(self.L.sg_step_check(self.ctx))
 

@@ -63,6 +63,43 @@ def test_inference_kernel_matches_training_forward(lib):
     assert np.max(np.abs(pred - inf)) < 2e-3
 
 
+def test_tensor_core_guess_matches_warp_mma_guess(lib):
+    """tcgen05 pass (TMEM accumulators) against the warp-level mma.sync path and
+    the training forward: the same BF16 operands and FP32 accumulation, so the
+    guesses agree to BF16 rounding of the hidden layers."""
+    import torch
+    P = small_ecp(seed=6)
+    g = P.g
+    capi.check(g.ctx, g.L.sg_mlp_init(g.ctx, 13))
+    g.zero_forces()
+    g.pair_forces(g.params(capi.ECPR, solver=capi.SOLVER_NEWTON))
+    warp = mlp.guess(g).cpu().numpy()
+    tc = mlp.guess_tc(g).cpu().numpy()
+    assert tc.shape == warp.shape and np.all(np.isfinite(tc))
+    assert np.max(np.abs(tc - warp)) < 2e-3
+
+
+@pytest.mark.parametrize("inline", [0, 1])
+def test_learned_guess_forces_match_fp64(lib, inline):
+    """Forces of the learned-guess path (either inference path) against the
+    FP64 oracle with the tightly converged contact parameter."""
+    import oracle as O
+    from helpers import rel
+    P = small_ecp(seed=7)
+    g = P.g
+    capi.check(g.ctx, g.L.sg_mlp_init(g.ctx, 17))
+    capi.check(g.ctx, g.L.sg_mlp_set_inline(g.ctx, inline))
+    g.zero_forces()
+    _, _, st = g.pair_forces(g.params(capi.ECPR, cutoff=3.0, solver=capi.SOLVER_MLP_NEWTON), want_stats=True)
+    F, T = g.forces()
+    assert st.nonconverged == 0
+    pi, pj = P.o.pairs(3.0, 0.3)
+    P.o.zero_forces()
+    P.o.forces(O.pair_params(O.ECPR, cutoff=3.0, solver=O.SOLVER_TIGHT), pi, pj)
+    Fo, To = P.oracle_forces()
+    assert rel(F, Fo) < 1e-5 and rel(T, To) < 1e-5
+
+
 def test_trained_guess_cuts_newton_iterations(lib):
     P = small_ecp(counts=(12, 16, 24), seed=5)
     g = P.g
