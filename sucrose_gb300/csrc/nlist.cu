@@ -300,6 +300,68 @@ __global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g0,
     row_done(i, cnt, cap, nb_count, flags, rp, pr);
 }
 
+// The same rows with one warp per particle, for dense cells: the lanes test
+// 32 members of a cell at once and the accepted ones are appended in member
+// order (ballot, then each accepting lane's rank among them), so each row is
+// exactly the one the thread-per-particle kernel writes.
+__global__ void __launch_bounds__(256) k_rows_cells_warp(int n, const float4* __restrict__ pos, ListGeom g0,
+                                                         const int* __restrict__ cell_start,
+                                                         const int* __restrict__ cell_particles, int max_nb,
+                                                         int* nb_pad, int* nb_count, int* flags, RepDev rp, PadRep pr,
+                                                         const int* rep_flag) {
+    if (!flags[F_REBUILD]) return;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    // persistent: each warp takes rows gwarp, gwarp + nwarps, ... (rows of
+    // replicas that keep their list are skipped at once)
+    for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n; i += nwarps) {   // warp-uniform
+        if (rp.rep_of && !rep_flag[rp.rep_of[i]]) continue;
+        const float4 pi = pos[i];
+        ListGeom g = g0;
+        int first_cell = 0;
+        size_t base, stride;
+        int cap;
+        pad_slot(n, i, max_nb, rp, pr, base, stride, cap);
+        if (rp.rep_of) {
+            const int r = rp.rep_of[i];
+            const int4 gr = rp.grid[r];
+            if (!gr.x) continue;   // all-pairs replicas: k_rows_cells
+            g = geom_for(g0, rp, r);
+            first_cell = gr.w;
+        }
+        int cnt = 0;
+        int cx, cy, cz;
+        cell_of(pi, g, cx, cy, cz);
+        for (int dz = -1; dz <= 1; ++dz) {
+            const int zz = wrapc(cz + dz, g.nc[2]);
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int yy = wrapc(cy + dy, g.nc[1]);
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int xx = wrapc(cx + dx, g.nc[0]);
+                    const int c = first_cell + (zz * g.nc[1] + yy) * g.nc[0] + xx;
+                    const int b = cell_start[c], e = cell_start[c + 1];
+                    for (int k0 = b; k0 < e; k0 += 32) {
+                        const int k = k0 + lane;
+                        int j = 0;
+                        bool acc = false;
+                        if (k < e) {
+                            j = cell_particles[k];
+                            acc = j > i && accept_pair(pi, pos[j], g);
+                        }
+                        const unsigned m = __ballot_sync(0xffffffffu, acc);
+                        if (acc) {
+                            const int slot = cnt + __popc(m & ((1u << lane) - 1u));
+                            if (slot < cap) nb_pad[base + (size_t)slot * stride] = j;
+                        }
+                        cnt += __popc(m);
+                    }
+                }
+            }
+        }
+        if (lane == 0) row_done(i, cnt, cap, nb_count, flags, rp, pr);
+    }
+}
+
 // All-pairs variant for boxes with fewer than three cells per side and for
 // open boundaries: every j > i is tested.
 __global__ void k_rows_all(int n, const float4* __restrict__ pos, ListGeom g, int max_nb, int* nb_pad, int* nb_count,
@@ -542,8 +604,16 @@ int enqueue_build(sg_ctx* ctx) {
                                             nl.dev_flags);
         k_sort_cells<<<(nl.ncells + 7) / 8, 256, 0, ctx->stream>>>(nl.ncells, nl.cell_start, nl.cell_unsorted,
                                                                     nl.cell_particles, nl.dev_flags);
-        k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
-                                                  nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag);
+        // one large system with dense cells: a warp per row; sparse cells or many
+    // small replicas rebuilding at once: a thread per row
+        if (nl.dense_cells)
+            k_rows_cells_warp<<<(int)std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 8 * ctx->num_sms), 256, 0,
+                                ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb, nl.nb_pad,
+                                               nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag);
+        else
+            k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
+                                                      nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag);
+
     } else {
         k_begin<<<1, 32, 0, ctx->stream>>>(nl.dev_flags, nl.cell_count, nl.cell_fill, 0);
         k_rows_all<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
@@ -639,6 +709,7 @@ int sg_nlist_init(sg_ctx* ctx, double skin, double cutoff, int32_t trigger_mode)
     }
     if (!nl.use_cells) nl.ncell[0] = nl.ncell[1] = nl.ncell[2] = 1;
     nl.ncells = nl.ncell[0] * nl.ncell[1] * nl.ncell[2];
+    nl.dense_cells = nl.use_cells && n >= 12 * nl.ncells;
     double vol = ctx->box[0] * ctx->box[1] * ctx->box[2];
     double rho = n / vol;
     // rows hold the j > i neighbours in index order, so a particle of low
@@ -703,6 +774,7 @@ int sg_rep_nlist_init(sg_ctx* ctx, const double* skin, const double* cutoff, int
         grid[r] = cells ? make_int4(nc[0], nc[1], nc[2], total_cells) : make_int4(0, 0, 0, total_cells);
         total_cells += cells ? nc[0] * nc[1] * nc[2] : 1;
         const int nr = ctx->h_rep_off[r + 1] - ctx->h_rep_off[r];
+
         const double rho = nr / (b[0] * b[1] * b[2]);
         // full neighbour count: index-ordered half rows of low index reach it
         const double expect = (4.0 / 3.0) * M_PI * rs * rs * rs * rho;
@@ -720,6 +792,8 @@ int sg_rep_nlist_init(sg_ctx* ctx, const double* skin, const double* cutoff, int
     nl.use_cells = 1;
     nl.ncell[0] = nl.ncell[1] = nl.ncell[2] = 1;
     nl.ncells = total_cells;
+    // many small lists rebuild at once here: a thread per row keeps every lane busy
+    nl.dense_cells = 0;
     nl.h_rep_max_nb = max_nb_r;
     SG_CUDA(ctx, cudaMalloc(&nl.rep_max_nb, sizeof(int) * R));
     SG_CUDA(ctx, cudaMalloc(&nl.rep_pad_off, sizeof(long long) * R));

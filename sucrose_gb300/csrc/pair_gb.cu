@@ -31,13 +31,14 @@ struct GTerms {
     float a, b, g;   // (ru1+ru2)/(1+c uu), (ru1-ru2)/(1-c uu), g_func
 };
 
-SG_DEV GTerms gterms(float c, float ru1, float ru2, float uu, float rsq) {
+// inv_rsq = 1 / r^2: the divisions by r^2 of the reference become products
+SG_DEV GTerms gterms(float c, float ru1, float ru2, float uu, float inv_rsq) {
     GTerms t;
     float sp = ru1 + ru2, sm = ru1 - ru2;
     float dp = 1.f / (1.f + c * uu), dm = 1.f / (1.f - c * uu);
     t.a = sp * dp;
     t.b = sm * dm;
-    t.g = 1.f - (c * 0.5f / rsq) * (sp * t.a + sm * t.b);
+    t.g = 1.f - (c * 0.5f * inv_rsq) * (sp * t.a + sm * t.b);
     return t;
 }
 
@@ -65,7 +66,7 @@ struct PotGB {
         const float rmag = sqrtf(rsq);
         const float4 pi0 = prep[2 * i], pi1 = prep[2 * i + 1], pj0 = prep[2 * j];
         const float3 U1 = make_float3(pi0.x, pi0.y, pi0.z), U2 = make_float3(pj0.x, pj0.y, pj0.z);
-        const GTerms gc = gterms(pi1.x, dot3(r, U1), dot3(r, U2), dot3(U1, U2), rsq);
+        const GTerms gc = gterms(pi1.x, dot3(r, U1), dot3(r, U2), dot3(U1, U2), 1.f / rsq);
         const float sigma = pi0.w / sqrtf(gc.g);
         const float reach = kWeld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
         return (KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach);
@@ -77,17 +78,18 @@ struct PotGB {
         const float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
         const float rmag = sqrtf(rsq);
         const float rinv = 1.f / rmag;
+        const float inv_rsq = 1.f / rsq;
         const float3 rhat = rinv * r;
         const float4 pi0 = prep[2 * i], pi1 = prep[2 * i + 1], pj0 = prep[2 * j];
         const float3 U1 = make_float3(pi0.x, pi0.y, pi0.z), U2 = make_float3(pj0.x, pj0.y, pj0.z);
         const float lprp = pi0.w, chi = pi1.x, xhi = pi1.y, inv_ez = pi1.z;
         const float ru1 = dot3(r, U1), ru2 = dot3(r, U2), uu = dot3(U1, U2);
-        const GTerms gc = gterms(chi, ru1, ru2, uu, rsq);
-        const GTerms gx = gterms(xhi, ru1, ru2, uu, rsq);
+        const GTerms gc = gterms(chi, ru1, ru2, uu, inv_rsq);
+        const GTerms gx = gterms(xhi, ru1, ru2, uu, inv_rsq);
         const float eps1 = rsqrtf(1.f - (chi * uu) * (chi * uu));
         const float eps2 = gx.g * inv_ez;
         const float sigma = lprp / sqrtf(gc.g);   // correctly rounded: r - sigma sets the envelope
-        const float ginv = sigma / gc.g;
+        const float ginv = sigma * (1.f / gc.g);
         const float reach = kWeld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
         const bool active = prefiltered || ((KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach));
         if (!active) return;
@@ -109,12 +111,12 @@ struct PotGB {
         const float pe_fac = e1n * ((float)mu * ipowf(eps2, mu - 1));
         const float e1_fac = e2m * ((float)nu * ipowf(eps1, nu + 2));
         // dG/dr, dG/du1, dG/du2 for chi (shape) and chi' (energy), force.f90:266-306
-        const float cr = chi / rsq, xr = xhi / rsq;
+        const float cr = chi * inv_rsq, xr = xhi * inv_rsq;
         const float3 Up = U1 + U2, Um = U1 - U2;
-        const float3 dGr_c = (-cr) * (gc.a * Up + gc.b * Um) + ((2.f / rsq) * (1.f - gc.g)) * r;
-        const float3 dGr_x = (-xr) * (gx.a * Up + gx.b * Um) + ((2.f / rsq) * (1.f - gx.g)) * r;
-        const float qc = chi * chi * 0.5f / rsq * (gc.a * gc.a - gc.b * gc.b);
-        const float qx = xhi * xhi * 0.5f / rsq * (gx.a * gx.a - gx.b * gx.b);
+        const float3 dGr_c = (-cr) * (gc.a * Up + gc.b * Um) + ((2.f * inv_rsq) * (1.f - gc.g)) * r;
+        const float3 dGr_x = (-xr) * (gx.a * Up + gx.b * Um) + ((2.f * inv_rsq) * (1.f - gx.g)) * r;
+        const float qc = chi * chi * 0.5f * inv_rsq * (gc.a * gc.a - gc.b * gc.b);
+        const float qx = xhi * xhi * 0.5f * inv_rsq * (gx.a * gx.a - gx.b * gx.b);
         const float3 dGu1_c = (-cr * (gc.a + gc.b)) * r + qc * U2;
         const float3 dGu1_x = (-xr * (gx.a + gx.b)) * r + qx * U2;
         const float3 dGu2_c = (-cr * (gc.a - gc.b)) * r + qc * U1;

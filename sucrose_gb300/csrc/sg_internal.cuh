@@ -39,6 +39,7 @@ struct sg_nlist_state {
     double rl2 = 0.0;                // (rc+skin)^2 in FP64, the reference's r_skin_sq after a build
     double trigger_sq = 0.0;         // compared with 4 * max displacement^2
     int use_cells = 0;
+    int dense_cells = 0;             // >= 12 particles per cell: one warp per row in the search
     int ncell[3] = {0, 0, 0};
     int ncells = 0;
     int max_nb = 0;                  // capacity per particle (half list)

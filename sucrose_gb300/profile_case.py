@@ -12,6 +12,7 @@ filter (for example ncu -k regex:k_pair -c 2). Cases:
   gb        Gay-Berne (3,5,2,1), N = 32 768, filtered launch
   lj        Lennard-Jones fcc, N = 32 000
   list      neighbour-list rebuild of the ECP system (forced, every launch)
+  gb_list   neighbour-list rebuild of the Gay-Berne system (list radius 6.4)
   langevin  Langevin step (initial + final) with rotations, N = 32 768
   nhc       Nose-Hoover chain step with rotations, N = 65 536
   mlp_train one MLP training step on 65 536 samples
@@ -67,7 +68,7 @@ def main():
     a = ap.parse_args()
     if a.case in ("ecp", "ecp_mlp", "list", "nhc", "ecp_step"):
         g, p = ecp_system()
-    elif a.case in ("gb", "langevin"):
+    elif a.case in ("gb", "langevin", "gb_list"):
         g, p = gb_system()
     elif a.case == "lj":
         g, p = lj_system()
@@ -96,7 +97,7 @@ def main():
         for _ in range(1 + a.reps):
             g.zero_forces()
             g.pair_forces(pm)
-    elif a.case == "list":
+    elif a.case in ("list", "gb_list"):
         for _ in range(1 + a.reps):
             g.build_nlist()
     elif a.case == "langevin":

@@ -55,6 +55,17 @@ def test_nlist_cells_jittered(lib, cells, density):
     assert _pairs_equal(P, 2.5, 0.3) > 0
 
 
+def test_nlist_dense_cells_long_range(lib):
+    # ~150 particles per cell (list radius 6.4 at density 0.3): rows built by
+    # one warp per particle
+    rng = np.random.default_rng(11)
+    box = (4096 / 0.3) ** (1 / 3)
+    r = rng.uniform(-box / 2, box / 2, size=(4096, 3))
+    P = Pair(r, None, box)
+    P.g.init_nlist(0.4, 6.0)
+    assert _pairs_equal(P, 6.0, 0.4) > 100000
+
+
 def test_nlist_threshold_pairs(lib):
     # pairs placed within a few ulps of (rc+skin) on both sides, across the
     # periodic boundary: the FP64 re-test must decide them like the reference
