@@ -263,6 +263,12 @@ int sg_step_kernel_count(sg_ctx* ctx, int64_t* count);
  * accumulators in tensor memory), into out_dev (device, >= pair count): the
  * pass that SG_SOLVER_MLP_NEWTON runs before the Newton kernel. */
 int sg_mlp_guess_tc(sg_ctx* ctx, float* out_dev, int64_t capacity);
+/* Failure-path test hook: the next tensor-core guess pass issues no MMA, so
+ * its completion waits run out after a short bound; the pass stops, releases
+ * its tensor memory and the call reports SG_ECUDA. No fault, no hang. */
+int sg_mlp_test_wait_timeout(sg_ctx* ctx);
+/* Clear the tensor-core pass's error flag (after a reported timeout). */
+int sg_mlp_clear_error(sg_ctx* ctx);
 /* inline_guess = 1: the ECP kernel evaluates the guess itself with warp-level
  * mma.sync instead (one kernel, more registers); 0 (default): separate pass. */
 int sg_mlp_set_inline(sg_ctx* ctx, int32_t inline_guess);

@@ -96,6 +96,8 @@ SIGNATURES = [
     ("sg_rep_kinetic", C.c_int, [_P, _D]),
     ("sg_mlp_guess_tc", C.c_int, [_P, C.c_void_p, C.c_int64]),
     ("sg_mlp_set_inline", C.c_int, [_P, C.c_int32]),
+    ("sg_mlp_test_wait_timeout", C.c_int, [_P]),
+    ("sg_mlp_clear_error", C.c_int, [_P]),
     ("sg_pair_autotune", C.c_int, [_P, C.POINTER(PairParams), C.c_int32, C.POINTER(TuneResult)]),
     ("sg_pair_set_launch", C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     ("sg_step_configure", C.c_int, [_P, C.POINTER(StepConfig)]),

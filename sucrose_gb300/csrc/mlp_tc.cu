@@ -25,7 +25,8 @@ namespace {
 constexpr int TM = 128;   // pairs per tile: the MMA's M
 constexpr int HN = 64;    // hidden width: the MMA's N
 constexpr uint32_t TMEM_COLS = 64;
-constexpr long long WAIT_LIMIT = 1ll << 24;
+constexpr long long WAIT_LIMIT = 1ll << 24;        // about a second of polling
+constexpr long long WAIT_LIMIT_TEST = 1ll << 12;   // the failure-path test's short bound
 
 struct __align__(128) TcSmem {
     __nv_bfloat16 a1[TM * 16];   // layer-1 operand (features), 4 KB
@@ -72,8 +73,8 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
                  : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
-    for (long long it = 0; it < WAIT_LIMIT; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, long long limit) {
+    for (long long it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(TM) k_mlp_guess_tc(const int* __restrict__ pai
                                                      const int* npairs, const float4* __restrict__ pos,
                                                      const float4* __restrict__ quat, const float4* __restrict__ shape,
                                                      float3 box, float3 inv_box, int periodic, MlpDev m,
-                                                     float* __restrict__ out, int* err) {
+                                                     float* __restrict__ out, int* err, int test_no_mma) {
     __shared__ TcSmem s;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int np = *npairs;
@@ -165,6 +166,8 @@ __global__ void __launch_bounds__(TM) k_mlp_guess_tc(const int* __restrict__ pai
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
     uint32_t phase = 0;
     bool stopped = false;   // block-uniform: a completion wait ran out
+    // test_no_mma: the failure-path test issues nothing, so the waits run out
+    const long long limit = test_no_mma ? WAIT_LIMIT_TEST : WAIT_LIMIT;
 
     const uint32_t a1 = smem_u32(s.a1), hh = smem_u32(s.h), w1 = smem_u32(s.w1), w2 = smem_u32(s.w2),
                    w3 = smem_u32(s.w3);
@@ -193,7 +196,7 @@ __global__ void __launch_bounds__(TM) k_mlp_guess_tc(const int* __restrict__ pai
             fence_async_smem();
             fence_before_sync();
             __syncthreads();
-            if (tid == 0) {
+            if (tid == 0 && !test_no_mma) {
                 fence_after_sync();
                 if (layer == 0) {
                     mma_issue(tmem, smem_desc(a1, 128, 256), smem_desc(w1, 128, 256), 0);
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(TM) k_mlp_guess_tc(const int* __restrict__ pai
                 mma_commit(mbar);
             }
             // every thread waits, then the block agrees, so that all leave together
-            const bool ok = __syncthreads_and(mbar_wait(mbar, phase));
+            const bool ok = __syncthreads_and(mbar_wait(mbar, phase, limit));
             if (!ok) {
                 if (tid == 0) atomicExch(err, 1);
                 stopped = true;
@@ -235,7 +238,7 @@ __global__ void __launch_bounds__(TM) k_mlp_guess_tc(const int* __restrict__ pai
     }
     // an MMA still in flight after a wait ran out: wait once more (bounded)
     // before the tensor memory is released
-    if (stopped) mbar_wait(mbar, phase);
+    if (stopped) mbar_wait(mbar, phase, limit);
     fence_before_sync();
     __syncthreads();
     if (warp == 0) {
@@ -265,7 +268,8 @@ int sg_mlp_guess_tc_launch(sg_ctx* ctx, float* out) {
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)per_sm * ctx->num_sms));
     k_mlp_guess_tc<<<grid, TM, 0, ctx->stream>>>(ctx->nl.pair_i, ctx->nl.pair_j, ctx->nl.dev_flags + 2, ctx->pos,
                                                  ctx->quat, ctx->shape, box, ib, ctx->periodic, m, out,
-                                                 ctx->mlp_tc_err);
+                                                 ctx->mlp_tc_err, ctx->mlp_tc_test_no_mma);
+    ctx->mlp_tc_test_no_mma = 0;   // the test hook acts once
     SG_LAUNCH_CHECK(ctx, "k_mlp_guess_tc");
     return SG_OK;
 }
@@ -282,6 +286,18 @@ int sg_mlp_guess_tc(sg_ctx* ctx, float* out_dev, int64_t capacity) {
     SG_CUDA(ctx, cudaMemcpyAsync(&e, ctx->mlp_tc_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (e) return sg_fail(ctx, SG_ECUDA, "tensor-core guess: a completion wait ran out");
+    return SG_OK;
+}
+
+int sg_mlp_test_wait_timeout(sg_ctx* ctx) {
+    if (!ctx) return SG_EINVAL;
+    ctx->mlp_tc_test_no_mma = 1;
+    return SG_OK;
+}
+
+int sg_mlp_clear_error(sg_ctx* ctx) {
+    if (!ctx) return SG_EINVAL;
+    if (ctx->mlp_tc_err) SG_CUDA(ctx, cudaMemsetAsync(ctx->mlp_tc_err, 0, sizeof(int), ctx->stream));
     return SG_OK;
 }
 

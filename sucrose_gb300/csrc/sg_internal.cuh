@@ -120,6 +120,7 @@ struct sg_ctx {
     int mlp_ready = 0;
     int* mlp_tc_err = nullptr;       // device flag: a tensor-core completion wait ran out
     int mlp_inline = 0;              // 1: the ECP kernel evaluates the guess itself (mma.sync)
+    int mlp_tc_test_no_mma = 0;      // failure-path test: the next guess pass issues no MMA
     void* mlp_work = nullptr;        // training workspace (mlp_train.cu)
     int mlp_adam_t = 0;
 

@@ -79,6 +79,23 @@ def test_tensor_core_guess_matches_warp_mma_guess(lib):
     assert np.max(np.abs(tc - warp)) < 2e-3
 
 
+def test_tensor_core_wait_timeout_is_reported(lib):
+    """A completion wait that runs out (the test hook issues no MMA) stops the
+    pass with a status the host reads; the context stays usable."""
+    P = small_ecp(seed=8)
+    g = P.g
+    capi.check(g.ctx, g.L.sg_mlp_init(g.ctx, 19))
+    g.zero_forces()
+    g.pair_forces(g.params(capi.ECPR, solver=capi.SOLVER_NEWTON))
+    capi.check(g.ctx, g.L.sg_mlp_test_wait_timeout(g.ctx))
+    with pytest.raises(capi.SgError) as e:
+        mlp.guess_tc(g)
+    assert e.value.code == capi.SG_ECUDA
+    capi.check(g.ctx, g.L.sg_mlp_clear_error(g.ctx))
+    ok = mlp.guess_tc(g).cpu().numpy()          # next pass runs normally
+    assert np.all(np.isfinite(ok)) and np.max(np.abs(ok - mlp.guess(g).cpu().numpy())) < 2e-3
+
+
 @pytest.mark.parametrize("inline", [0, 1])
 def test_learned_guess_forces_match_fp64(lib, inline):
     """Forces of the learned-guess path (either inference path) against the
