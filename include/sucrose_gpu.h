@@ -47,6 +47,10 @@ typedef enum {
     SG_LJ12 = 1,   /* lj12_calculate_forces   fortran/force.f90:51-93    */
     SG_LJW = 2,    /* ljw_calculate_forces    fortran/force.f90:95-146   */
     SG_WCA = 3,    /* wca_calculate_forces    fortran/force.f90:155-190  */
+    SG_MORSE = 4,  /* morse_calculate_forces  fortran/force.f90:199-233  */
+    SG_DH = 5,     /* dh_calculate_forces     fortran/force.f90:2589-2617 (charges) */
+    SG_COULOMB = 6,/* coulombic_calculate_forces fortran/force.f90:2627-2665 (charges) */
+    SG_DIPOLE = 7, /* dipole_calculate_forces fortran/force.f90:2687-2751 (charge x body z axis) */
     SG_GB = 10,    /* gb_calculate_forces     fortran/force.f90:308-428  */
     SG_GBR = 11,   /* gbr_calculate_forces    fortran/force.f90:430-533  */
     SG_GBW = 12,   /* gbw_calculate_forces    fortran/force.f90:535-663  */
@@ -80,6 +84,11 @@ typedef struct {
     int32_t newton_max_iter;  /* 0 selects 20                                       */
     int32_t fp64_check; /* Newton residual check: 1 = FP64 (default), 2 = double-float on the FP32 pipe,
                            0 = none (FP32 step-size test only) */
+    double dissoc;      /* Morse well depth D (dissoc)                              */
+    double width;       /* Morse width alpha (width)                                */
+    double rmin;        /* Morse equilibrium distance r0 (rmin)                     */
+    double db_len;      /* Debye length (dh)                                        */
+    double dielectric;  /* relative permittivity (dh, coulombic, dipole)            */
 } sg_pair_params;
 
 /* Per-call statistics of a pair-force evaluation. ECP kinds fill every field;
@@ -112,6 +121,26 @@ int sg_set_box(sg_ctx* ctx, const double box[3], int32_t periodic);
 int sg_set_particles(sg_ctx* ctx, const double* mass, const double* sig_x, const double* sig_y,
                      const double* sig_z, const double* eps_x, const double* eps_y, const double* eps_z,
                      const double* ixx, const double* iyy, const double* izz);
+
+/* set_atom_charge (fortran/system.f90:148-165) for every particle; NULL sets
+ * all charges to 0. reference_defaults = 1 also applies initialize_system's
+ * rule (fortran/system.f90:595-598): a negative charge becomes 0. The charges
+ * feed SG_DH, SG_COULOMB and SG_DIPOLE. */
+int sg_set_charges(sg_ctx* ctx, const double* charge, int32_t reference_defaults);
+
+/* Reaction field of the dipole potential (module dipole, fortran/force.f90:2669-2767).
+ * init_reaction_field (:2677-2685): zero DIP (per particle) and RFL. Every
+ * SG_DIPOLE call then sets DIP(I) for the I side of each pair in range and adds
+ * U2 * dip_coeff to RFL, which the reference adds to every element of its RFL
+ * arrays (:2743-2745), so RFL is one vector shared by all particles; it keeps
+ * growing across calls until the next init, as in the reference.
+ * eval_reaction_field (:2753-2766): for every particle with charge != 0 adds
+ * 0.5 DIP.RFL to the potential energy and subtracts DIP x RFL from its torque;
+ * *pot_eng (may be NULL) gets the energy added. Single-system contexts only. */
+int sg_reaction_field_init(sg_ctx* ctx);
+int sg_reaction_field_eval(sg_ctx* ctx, double* pot_eng);
+/* RFL (3 doubles) and DIP (NULL arrays skip). */
+int sg_reaction_field_read(sg_ctx* ctx, double rfl[3], double* dipx, double* dipy, double* dipz);
 
 /* Copy state in / out. Any array may be NULL to skip it. Quaternions are (w,x,y,z). */
 int sg_upload_state(sg_ctx* ctx, const double* rx, const double* ry, const double* rz, const double* qw,
@@ -239,14 +268,18 @@ typedef struct {
     sg_pair_params pair;   /* the pair potential evaluated every step              */
 } sg_step_config;
 #define SG_STEP_FLAT 1
+#define SG_STEP_REACTION_FIELD 2   /* eval_reaction_field after the pair stage (SG_DIPOLE) */
 
 /* Set the step program. The first sg_step call runs one step eagerly (which
  * allocates every buffer), then captures one step as a CUDA graph; later
  * steps launch the graph. Reallocation (list regrowth) forces a re-capture. */
 int sg_step_configure(sg_ctx* ctx, const sg_step_config* cfg);
 /* Same, with the step's pair stage given as npairs (1..3) parameter sets run in
- * order, at most one per potential family: a replica context holding LJ and
- * GB replicas passes one LJ and one GB set. cfg->pair is ignored. */
+ * order, their forces and energies summed as the reference's user loop sums
+ * several calculate_forces calls (e.g. WCA plus Coulomb). In a replica context
+ * each set acts on the replicas of its potential family (LJ-like kinds < 10,
+ * GB, ECP): one replica context holding LJ and GB replicas passes one LJ and
+ * one GB set. cfg->pair is ignored. */
 int sg_step_configure_pairs(sg_ctx* ctx, const sg_step_config* cfg, const sg_pair_params* pairs, int32_t npairs);
 /* Enqueue nsteps timesteps on the context stream; returns without waiting. */
 int sg_step(sg_ctx* ctx, int32_t nsteps);

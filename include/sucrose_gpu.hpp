@@ -14,6 +14,7 @@
 // Header-only; link with -lsucrose_gb300.
 #pragma once
 
+#include <cmath>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -56,6 +57,12 @@ class Context {
                        const double* eps_x, const double* eps_y, const double* eps_z, const double* ixx,
                        const double* iyy, const double* izz) {
         check(ctx_, sg_set_particles(ctx_, mass, sig_x, sig_y, sig_z, eps_x, eps_y, eps_z, ixx, iyy, izz));
+    }
+
+    // set_atom_charge for every particle (fortran/system.f90:148); reference_defaults
+    // applies initialize_system's negative-to-zero rule (:595-598)
+    void set_charges(const double* charge, bool reference_defaults = false) {
+        check(ctx_, sg_set_charges(ctx_, charge, reference_defaults ? 1 : 0));
     }
 
     // init_nlist (fortran/system.f90:895); trigger 0 = the reference's (rc+skin)^2 bound
@@ -149,6 +156,40 @@ class LennardJones_WCA : public Force {   // LennardJones_WCA (src/force.cpp:71)
   public:
     LennardJones_WCA(Context& c, double epsilon, double sigma) : Force(c) {
         p_.kind = SG_WCA; p_.epsilon = epsilon; p_.sigma = sigma; p_.cutoff = sigma;
+    }
+};
+class MorsePotential : public Force {     // MorsePotential (src/force.cpp:113): no cutoff, no shift
+  public:
+    MorsePotential(Context& c, double dissociation_energy, double equilibrium_distance, double width,
+                   double cutoff = HUGE_VAL)   // a finite cutoff gives morse_ (force.f90:199-233)
+        : Force(c) {
+        p_.kind = SG_MORSE; p_.dissoc = dissociation_energy; p_.rmin = equilibrium_distance; p_.width = width;
+        p_.cutoff = cutoff;
+    }
+};
+class DebyeHuckel : public Force {        // dh_calculate_forces (force.f90:2589-2617)
+  public:
+    DebyeHuckel(Context& c, double cutoff, double db_len, double dielectric) : Force(c) {
+        p_.kind = SG_DH; p_.cutoff = cutoff; p_.db_len = db_len; p_.dielectric = dielectric;
+    }
+};
+class Coulombic : public Force {          // coulombic_calculate_forces (force.f90:2627-2665)
+  public:
+    Coulombic(Context& c, double cutoff, double dielectric) : Force(c) {
+        p_.kind = SG_COULOMB; p_.cutoff = cutoff; p_.dielectric = dielectric;
+    }
+};
+class Dipole : public Force {             // module dipole (force.f90:2669-2767)
+  public:
+    Dipole(Context& c, double cutoff, double dielectric) : Force(c) {
+        p_.kind = SG_DIPOLE; p_.cutoff = cutoff; p_.dielectric = dielectric;
+    }
+    void init_reaction_field() { check(ctx_.get(), sg_reaction_field_init(ctx_.get())); }
+    // adds 0.5 DIP.RFL over charged particles to the returned energy and DIP x RFL to the torques
+    double eval_reaction_field() {
+        double e = 0.0;
+        check(ctx_.get(), sg_reaction_field_eval(ctx_.get(), &e));
+        return e;
     }
 };
 class GayBerne : public Force {           // gb_ family (force.f90:308-1030); kind SG_GB .. SG_GBWC

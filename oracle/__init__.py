@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 # Pair kinds (shared numbering with the product's C-ABI)
 LJ, LJ12, LJW, WCA = 0, 1, 2, 3
+MORSE, DH, COULOMB, DIPOLE = 4, 5, 6, 7
 GB, GBR, GBW, GBC, GBWC = 10, 11, 12, 13, 14
 ECP, ECPR, ECPW, ECPC, ECPWC = 20, 21, 22, 23, 24
 SOLVER_BRENT, SOLVER_TIGHT, SOLVER_GIVEN = 0, 1, 2
@@ -35,13 +36,15 @@ class OrSys(C.Structure):
                [(k, C.c_double) for k in ("pot_eng", "kin_eng", "kin_rot", "temp", "pressure", "density", "virial",
                                           "target_temp")] + \
                [("eta", C.c_double * 3), ("p_eta", C.c_double * 3), ("eta_r", C.c_double * 3),
-                ("p_eta_r", C.c_double * 3)]
+                ("p_eta_r", C.c_double * 3)] + \
+               [(k, _D) for k in ("charge", "dipx", "dipy", "dipz")] + [("rfl", C.c_double * 3)]
 
 
 class OrPairParams(C.Structure):
     _fields_ = [("kind", C.c_int), ("mu", C.c_int), ("nu", C.c_int), ("solver", C.c_int),
                 ("sigma", C.c_double), ("epsilon", C.c_double), ("cutoff", C.c_double), ("wf", C.c_double),
-                ("chirality", C.c_double), ("lam_in", C.c_double)]
+                ("chirality", C.c_double), ("lam_in", C.c_double), ("dissoc", C.c_double), ("width", C.c_double),
+                ("rmin", C.c_double), ("db_len", C.c_double), ("dielectric", C.c_double)]
 
 
 _libs = {}
@@ -70,6 +73,8 @@ def lib(fast=False):
         L.or_nht_final.argtypes = [P, C.c_double, C.c_double, C.c_int, C.c_int]
         L.or_nhr_half.argtypes = [P, C.c_double, C.c_double, C.c_int]
         L.or_calculate_thermo.argtypes = [P]
+        L.or_reaction_field_init.argtypes = [P]
+        L.or_reaction_field_eval.argtypes = [P]
         L.or_set_velocity_to_temperature.argtypes = [P, C.c_double, C.c_int, C.c_int]
         L.or_generate_fcc.argtypes = [C.c_int, C.c_double] + [_D] * 7
         _libs[key] = L
@@ -87,6 +92,8 @@ def ref_lib():
             L = C.CDLL(path)
             L.ref_lj_forces.argtypes = [C.c_int, C.c_double, C.c_int, _D, _D, _D, C.c_double, C.c_double, C.c_int,
                                         _I, _I, _D, _D, _D, _D]
+            L.ref_morse_forces.argtypes = [C.c_int, C.c_double, C.c_int, _D, _D, _D, C.c_double, C.c_double,
+                                           C.c_double, C.c_int, _I, _I, _D, _D, _D, _D]
             L.ref_vv_step.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double] + [_D] * 9 + [C.c_int]
             L.ref_det3.argtypes = [_D]
             L.ref_det3.restype = C.c_double
@@ -108,7 +115,8 @@ def uptr(a):
 
 PARTICLE_FIELDS = ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "qw", "qx", "qy", "qz",
                    "lx", "ly", "lz", "tx", "ty", "tz", "mass", "inv_mass", "sig_x", "sig_y", "sig_z",
-                   "eps_x", "eps_y", "eps_z", "ixx", "iyy", "izz", "ixx_inv", "iyy_inv", "izz_inv")
+                   "eps_x", "eps_y", "eps_z", "ixx", "iyy", "izz", "ixx_inv", "iyy_inv", "izz_inv",
+                   "charge", "dipx", "dipy", "dipz")
 
 
 class System:
@@ -229,6 +237,16 @@ class System:
     def nhr_half(self, dt, coupling=None):
         self.L.or_nhr_half(self.ptr(), dt, 0.0 if coupling is None else coupling, 0 if coupling is None else 1)
 
+    def reaction_field_init(self):
+        self.L.or_reaction_field_init(self.ptr())
+
+    def reaction_field_eval(self):
+        self.L.or_reaction_field_eval(self.ptr())
+
+    @property
+    def rfl(self):
+        return np.array([self.s.rfl[0], self.s.rfl[1], self.s.rfl[2]])
+
     def thermo(self):
         self.L.or_calculate_thermo(self.ptr())
 
@@ -237,10 +255,11 @@ class System:
 
 
 def pair_params(kind, sigma=1.0, epsilon=1.0, cutoff=2.5, wf=0.0, chirality=0.0, mu=None, nu=None,
-                solver=SOLVER_BRENT, lam_in=0.0):
+                solver=SOLVER_BRENT, lam_in=0.0, dissoc=1.0, width=1.0, rmin=1.0, db_len=1.0, dielectric=1.0):
     if mu is None:
         mu, nu = (1, 2) if 10 <= kind < 20 else (2, 1)
-    return OrPairParams(kind, mu, nu, solver, sigma, epsilon, cutoff, wf, chirality, lam_in)
+    return OrPairParams(kind, mu, nu, solver, sigma, epsilon, cutoff, wf, chirality, lam_in, dissoc, width, rmin,
+                        db_len, dielectric)
 
 
 def philox4x32(ctr, key=(0x6D2B79F5, 0x1B873593)):

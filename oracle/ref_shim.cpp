@@ -6,6 +6,7 @@
 // oracle/_ref/. It lets the tests pin the FP64 restatement in
 // sucrose_oracle.cpp against code the reference itself ships:
 //   LennardJones::calculate_forces   src/force.cpp:6-37 (untruncated 12-6, rint image)
+//   MorsePotential::calculate_forces src/force.cpp:113-140 (no cutoff, no shift)
 //   VerletIntegrator                  src/integrators.cpp:7-38 (unit mass)
 //   Matrix3::determinant              src/xmath.cpp:55
 #include <vector>
@@ -38,6 +39,19 @@ void ref_lj_forces(int n, double box_len, int periodic, const double* rx, const 
     load(s, n, box_len, periodic, rx, ry, rz);
     LennardJones lj(s, epsilon, sigma);
     for (int k = 0; k < npairs; ++k) lj.calculate_forces(pi[k], pj[k]);
+    for (int i = 0; i < n; ++i) { fx[i] = s.atom.fx[i]; fy[i] = s.atom.fy[i]; fz[i] = s.atom.fz[i]; }
+    *pot = s.potential_energy;
+}
+
+// Calls MorsePotential::calculate_forces(i, j) (src/force.cpp:113-140: no
+// cutoff, no shift) for each listed pair (0-based).
+void ref_morse_forces(int n, double box_len, int periodic, const double* rx, const double* ry, const double* rz,
+                      double dissoc, double rmin, double width, int npairs, const int* pi, const int* pj, double* fx,
+                      double* fy, double* fz, double* pot) {
+    System s;
+    load(s, n, box_len, periodic, rx, ry, rz);
+    MorsePotential m(s, dissoc, rmin, width);
+    for (int k = 0; k < npairs; ++k) m.calculate_forces(pi[k], pj[k]);
     for (int i = 0; i < n; ++i) { fx[i] = s.atom.fx[i]; fy[i] = s.atom.fy[i]; fz[i] = s.atom.fz[i]; }
     *pot = s.potential_energy;
 }

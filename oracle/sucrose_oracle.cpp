@@ -202,6 +202,9 @@ typedef struct OrSys {
     double pot_eng, kin_eng, kin_rot, temp, pressure, density, virial, target_temp;
     double eta[3], p_eta[3];       // Nose-Hoover chain (integrators.f90:230)
     double eta_r[3], p_eta_r[3];   // rotational chain of the standard NHC mode
+    double* charge;                // system.f90:7 (NULL: all zero)
+    double *dipx, *dipy, *dipz;    // module dipole DIP arrays (force.f90:2671)
+    double rfl[3];                 // RFL: every element of the reference's RFL arrays holds this vector
 } OrSys;
 
 // Pair-potential parameters shared by every family.
@@ -211,10 +214,12 @@ typedef struct OrPairParams {
     int solver;      // ECP: 0 = reference Brent, 1 = tightly converged FP64, 2 = use lam_in
     double sigma, epsilon, cutoff, wf, chirality;
     double lam_in;   // ECP with solver 2
+    double dissoc, width, rmin;   // morse
+    double db_len, dielectric;    // dh, coulombic, dipole
 } OrPairParams;
 
 enum {
-    OR_LJ = 0, OR_LJ12 = 1, OR_LJW = 2, OR_WCA = 3,
+    OR_LJ = 0, OR_LJ12 = 1, OR_LJW = 2, OR_WCA = 3, OR_MORSE = 4, OR_DH = 5, OR_COULOMB = 6, OR_DIPOLE = 7,
     OR_GB = 10, OR_GBR = 11, OR_GBW = 12, OR_GBC = 13, OR_GBWC = 14,
     OR_ECP = 20, OR_ECPR = 21, OR_ECPW = 22, OR_ECPC = 23, OR_ECPWC = 24,
 };
@@ -241,6 +246,7 @@ template <class T> struct PairIn {
     T rij[3];                 // minimum image r_i - r_j
     T qi[4], qj[4];           // (w,x,y,z)
     T si[3], sj[3], ei[3], ej[3];
+    T ci, cj;                 // charges
 };
 
 template <class T> inline void min_image(T r[3], const double box[3], int periodic) {
@@ -265,6 +271,8 @@ template <class T> PairIn<T> load_pair(const OrSys* s, int i, int j) {
         p.si[0] = T(s->sig_x[i]); p.si[1] = T(s->sig_y[i]); p.si[2] = T(s->sig_z[i]);
         p.sj[0] = T(s->sig_x[j]); p.sj[1] = T(s->sig_y[j]); p.sj[2] = T(s->sig_z[j]);
     }
+    p.ci = s->charge ? T(s->charge[i]) : T(0.0);
+    p.cj = s->charge ? T(s->charge[j]) : T(0.0);
     if (s->eps_x) {
         p.ei[0] = T(s->eps_x[i]); p.ei[1] = T(s->eps_y[i]); p.ei[2] = T(s->eps_z[i]);
         p.ej[0] = T(s->eps_x[j]); p.ej[1] = T(s->eps_y[j]); p.ej[2] = T(s->eps_z[j]);
@@ -272,7 +280,12 @@ template <class T> PairIn<T> load_pair(const OrSys* s, int i, int j) {
     return p;
 }
 
-struct PairOut { double pe, f[3], ti[3], tj[3], lam; int nevals; };
+struct PairOut {
+    double pe, f[3], ti[3], tj[3], lam;
+    int nevals;
+    int rf;                  // dipole pair in range: DIP(I) = u1, RFL += u2 dip_coeff
+    double u1[3], u2[3];
+};
 
 // ----------------------------------------------------------- LJ family -----
 template <class T> void lj_pair(const PairIn<T>& in, const OrPairParams& pp, PairOut& o) { // force.f90:6-49
@@ -336,6 +349,94 @@ template <class T> void wca_pair(const PairIn<T>& in, const OrPairParams& pp, Pa
         o.pe = double(eps * (sr12 - T(2.0) * sr6) + eps);
         T coeff = T(12.0) * eps * (sr12 - sr6);
         for (int d = 0; d < 3; ++d) o.f[d] = double(coeff * r[d] / rsq);
+    }
+}
+
+// ------------------------------------------------ Morse and charges -----
+template <class T> void morse_pair(const PairIn<T>& in, const OrPairParams& pp, PairOut& o) { // force.f90:199-233
+    const T* r = in.rij;
+    T D = T(pp.dissoc), w = T(pp.width), r0 = T(pp.rmin), rc = T(pp.cutoff);
+    T rmag = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    if (rmag < rc) {
+        T e = std::exp(-w * (rmag - r0));
+        T ec = std::exp(-w * (rc - r0));
+        T pot = D * ((T(1.0) - e) * (T(1.0) - e) - T(1.0));
+        T potc = D * ((T(1.0) - ec) * (T(1.0) - ec) - T(1.0));
+        o.pe = double(pot - potc);
+        for (int d = 0; d < 3; ++d) o.f[d] = double(T(-2.0) * w * D * (T(1.0) - e) * e * r[d] / rmag);
+    }
+}
+
+template <class T> void dh_pair(const PairIn<T>& in, const OrPairParams& pp, PairOut& o) { // force.f90:2589-2617
+    const T* r = in.rij;
+    T rc = T(pp.cutoff), db = T(pp.db_len), diel = T(pp.dielectric);
+    T rsq = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    T rmag = std::sqrt(rsq);
+    if (rmag < rc) {
+        T pe = (in.ci * in.cj * std::exp(-rmag / db)) / (T(4.0) * T(M_PI) * diel * rmag);
+        o.pe = double(pe);
+        for (int d = 0; d < 3; ++d) o.f[d] = double(pe * (T(1.0) + rmag / db) * r[d] / rsq);
+    }
+}
+
+template <class T> void coulomb_pair(const PairIn<T>& in, const OrPairParams& pp, PairOut& o) { // force.f90:2627-2665
+    const T* r = in.rij;
+    T rc = T(pp.cutoff), diel = T(pp.dielectric);
+    T rsq = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    T rmag = std::sqrt(rsq);
+    T sw = rc - T(2.0);
+    T factor = T(1.0) / (rc - sw);
+    T x = (rmag - sw) * factor;
+    T sx = T(1.0) - T(6.0) * x * x * x * x * x + T(15.0) * x * x * x * x - T(10.0) * x * x * x;
+    T sdx = T(-30.0) * x * x * x * x + T(60.0) * x * x * x - T(30.0) * x * x;
+    if (rmag < rc) {
+        T pe = in.ci * in.cj / (T(4.0) * T(M_PI) * diel * rmag);
+        T f[3];
+        for (int d = 0; d < 3; ++d) f[d] = pe * r[d] / rsq;
+        if (rmag >= sw) {
+            pe = sx * pe;
+            // the scaled PE, subtracted from every component (:2660-2661)
+            for (int d = 0; d < 3; ++d) f[d] = sx * f[d] - sdx * pe * factor;
+        }
+        o.pe = double(pe);
+        for (int d = 0; d < 3; ++d) o.f[d] = double(f[d]);
+    }
+}
+
+template <class T> void dipole_pair(const PairIn<T>& in, const OrPairParams& pp, PairOut& o) { // force.f90:2687-2751
+    const T* r = in.rij;
+    T rc = T(pp.cutoff);
+    T rsq = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    T rmag = std::sqrt(rsq);
+    const T* a = in.qi;
+    const T* b = in.qj;   // (w, x, y, z)
+    T U1[3] = {T(2.0) * (a[1] * a[3] + a[0] * a[2]), T(2.0) * (a[2] * a[3] - a[0] * a[1]),
+               a[0] * a[0] - a[1] * a[1] - a[2] * a[2] + a[3] * a[3]};
+    T U2[3] = {T(2.0) * (b[1] * b[3] + b[0] * b[2]), T(2.0) * (b[2] * b[3] - b[0] * b[1]),
+               b[0] * b[0] - b[1] * b[1] - b[2] * b[2] + b[3] * b[3]};
+    for (int d = 0; d < 3; ++d) { U1[d] = U1[d] * in.ci; U2[d] = U2[d] * in.cj; }
+    if (rmag < rc) {
+        T ci = U1[0] * r[0] + U1[1] * r[1] + U1[2] * r[2];
+        T cj = U2[0] * r[0] + U2[1] * r[1] + U2[2] * r[2];
+        T cij = U1[0] * U2[0] + U1[1] * U2[1] + U1[2] * U2[2];
+        T t1[3], t2[3], t3[3], c1[3], c2[3];
+        for (int d = 0; d < 3; ++d) {
+            t1[d] = (cij - (T(5.0) * ci * cj / rsq)) * r[d] + cj * U1[d] + ci * U2[d];
+            t2[d] = T(3.0) * cj * (r[d] / rsq) - U2[d];
+            t3[d] = T(3.0) * ci * (r[d] / rsq) - U1[d];
+        }
+        T r3 = rsq * rmag, r5 = r3 * rsq;
+        cross(U1, t2, c1);
+        cross(U2, t3, c2);
+        o.pe = double((cij / r3) - ((T(3.0) * ci * cj) / r5));
+        for (int d = 0; d < 3; ++d) {
+            o.f[d] = double((T(3.0) / r5) * t1[d]);
+            o.ti[d] = double((T(1.0) / r3) * c1[d]);
+            o.tj[d] = double((T(1.0) / r3) * c2[d]);
+            o.u1[d] = double(U1[d]);
+            o.u2[d] = double(U2[d]);
+        }
+        o.rf = 1;
     }
 }
 
@@ -853,6 +954,10 @@ template <class T> void eval_pair(const OrSys* s, int i, int j, const OrPairPara
         case OR_LJ12: lj12_pair(in, pp, o); break;
         case OR_LJW: ljw_pair(in, pp, o); break;
         case OR_WCA: wca_pair(in, pp, o); break;
+        case OR_MORSE: morse_pair(in, pp, o); break;
+        case OR_DH: dh_pair(in, pp, o); break;
+        case OR_COULOMB: coulomb_pair(in, pp, o); break;
+        case OR_DIPOLE: dipole_pair(in, pp, o); break;
         case OR_GB: case OR_GBR: case OR_GBW: case OR_GBC: case OR_GBWC: gb_pair(in, pp, o); break;
         default: ecp_pair(in, pp, o); break;
     }
@@ -915,6 +1020,31 @@ void or_forces(OrSys* s, const OrPairParams* pp, int npairs, const int* pi, cons
         }
         if (lam_out) lam_out[k] = o.lam;
         if (nevals_out) nevals_out[k] = o.nevals;
+        if (o.rf && s->dipx) {   // force.f90:2739-2745
+            const double rc = pp->cutoff, eps = pp->dielectric;
+            const double dip_coeff = ((2.0 * (eps - 1.0)) / (2.0 * eps + 1.0)) / (rc * rc * rc);
+            s->dipx[i] = o.u1[0]; s->dipy[i] = o.u1[1]; s->dipz[i] = o.u1[2];
+            for (int d = 0; d < 3; ++d) s->rfl[d] = s->rfl[d] + o.u2[d] * dip_coeff;
+        }
+    }
+}
+
+// init_reaction_field (force.f90:2677-2685): DIP and RFL to zero.
+void or_reaction_field_init(OrSys* s) {
+    for (int i = 0; i < s->n; ++i) s->dipx[i] = s->dipy[i] = s->dipz[i] = 0.0;
+    s->rfl[0] = s->rfl[1] = s->rfl[2] = 0.0;
+}
+
+// eval_reaction_field (force.f90:2753-2766)
+void or_reaction_field_eval(OrSys* s) {
+    const double* R = s->rfl;
+    for (int i = 0; i < s->n; ++i) {
+        if (s->charge[i] != 0.0) {
+            s->pot_eng = s->pot_eng + 0.5 * (s->dipx[i] * R[0] + s->dipy[i] * R[1] + s->dipz[i] * R[2]);
+            s->tx[i] = s->tx[i] - (s->dipy[i] * R[2] - s->dipz[i] * R[1]);
+            s->ty[i] = s->ty[i] - (s->dipz[i] * R[0] - s->dipx[i] * R[2]);
+            s->tz[i] = s->tz[i] - (s->dipx[i] * R[1] - s->dipy[i] * R[0]);
+        }
     }
 }
 

@@ -15,6 +15,7 @@ STATUS_NAMES = {0: "SG_OK", 1: "SG_EINVAL", 2: "SG_ECUTOFF_GT_HALFBOX", 3: "SG_E
                 5: "SG_ECAPACITY", 6: "SG_ECUDA", 7: "SG_ENOTREADY"}
 
 LJ, LJ12, LJW, WCA = 0, 1, 2, 3
+MORSE, DH, COULOMB, DIPOLE = 4, 5, 6, 7
 GB, GBR, GBW, GBC, GBWC = 10, 11, 12, 13, 14
 ECP, ECPR, ECPW, ECPC, ECPWC = 20, 21, 22, 23, 24
 SOLVER_BRENT_COMPAT, SOLVER_NEWTON, SOLVER_MLP_NEWTON = 0, 1, 2
@@ -24,7 +25,8 @@ class PairParams(C.Structure):
     _fields_ = [("kind", C.c_int32), ("mu", C.c_int32), ("nu", C.c_int32), ("solver", C.c_int32),
                 ("sigma", C.c_double), ("epsilon", C.c_double), ("cutoff", C.c_double), ("wf", C.c_double),
                 ("chirality", C.c_double), ("newton_tol", C.c_double), ("newton_max_iter", C.c_int32),
-                ("fp64_check", C.c_int32)]
+                ("fp64_check", C.c_int32), ("dissoc", C.c_double), ("width", C.c_double), ("rmin", C.c_double),
+                ("db_len", C.c_double), ("dielectric", C.c_double)]
 
 
 class StepConfig(C.Structure):
@@ -36,6 +38,7 @@ class StepConfig(C.Structure):
 
 INT_NVE, INT_LANGEVIN, INT_NH, INT_NH_REF = 0, 1, 2, 3
 STEP_FLAT = 1
+STEP_REACTION_FIELD = 2
 
 
 class TuneResult(C.Structure):
@@ -64,6 +67,10 @@ SIGNATURES = [
     ("sg_synchronize", C.c_int, [_P]),
     ("sg_set_box", C.c_int, [_P, _D, C.c_int32]),
     ("sg_set_particles", C.c_int, [_P] + [_D] * 10),
+    ("sg_set_charges", C.c_int, [_P, _D, C.c_int32]),
+    ("sg_reaction_field_init", C.c_int, [_P]),
+    ("sg_reaction_field_eval", C.c_int, [_P, _D]),
+    ("sg_reaction_field_read", C.c_int, [_P, _D, _D, _D, _D]),
     ("sg_upload_state", C.c_int, [_P] + [_D] * 13),
     ("sg_download_state", C.c_int, [_P] + [_D] * 13),
     ("sg_download_forces", C.c_int, [_P] + [_D] * 6),

@@ -106,7 +106,8 @@ int sg_destroy(sg_ctx* ctx) {
     sg_mlp_free(ctx);
     void* bufs[] = {ctx->pos, ctx->quat, ctx->vel, ctx->angm, ctx->force, ctx->torque, ctx->shape, ctx->eshape,
                     ctx->inert, ctx->inert_inv, ctx->acc, ctx->partials, ctx->done_counter, ctx->stats, ctx->nh,
-                    ctx->ecp_prep, ctx->ecp_prep64, ctx->ecp_lambda, ctx->mlp_w, ctx->mlp_wbf16, ctx->mlp_tc_err};
+                    ctx->ecp_prep, ctx->ecp_prep64, ctx->ecp_lambda, ctx->mlp_w, ctx->mlp_wbf16, ctx->mlp_tc_err,
+                    ctx->rf_dip, ctx->rf_mark, ctx->rf_cnt, ctx->rf_field};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
@@ -248,6 +249,21 @@ int sg_set_particles(sg_ctx* ctx, const double* mass, const double* sig_x, const
     // inverse mass lives in vel.w
     if (int rc = upload4(ctx, ctx->vel, nullptr, nullptr, nullptr, im.data(), nullptr, 0)) return rc;
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // the host vectors above go out of scope
+    return SG_OK;
+}
+
+int sg_set_charges(sg_ctx* ctx, const double* charge, int32_t reference_defaults) {
+    if (!ctx) return SG_EINVAL;
+    std::vector<double> q(ctx->n, 0.0);
+    for (int i = 0; i < ctx->n && charge; ++i) {
+        q[i] = charge[i];
+        // initialize_system (fortran/system.f90:595-598): negative charges become 0
+        if (reference_defaults && q[i] < 0.0) q[i] = 0.0;
+        if (!std::isfinite(q[i])) return sg_fail(ctx, SG_EINVAL, "non-finite charge at particle %d", i);
+    }
+    // the charge rides in the position's w lane
+    if (int rc = upload4(ctx, ctx->pos, nullptr, nullptr, nullptr, q.data(), nullptr, 0)) return rc;
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // q goes out of scope
     return SG_OK;
 }
 

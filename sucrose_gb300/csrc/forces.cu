@@ -19,6 +19,7 @@ int launch_forces(sg_ctx* ctx, const sg_pair_params* p) {
         return SG_OK;   // no replica of this family
     switch (p->kind) {
         case SG_LJ: case SG_LJ12: case SG_LJW: case SG_WCA: return sg_launch_pair_simple(ctx, p);
+        case SG_MORSE: case SG_DH: case SG_COULOMB: case SG_DIPOLE: return sg_launch_pair_elec(ctx, p);
         case SG_GB: case SG_GBR: case SG_GBW: case SG_GBC: case SG_GBWC: return sg_launch_pair_gb(ctx, p);
         case SG_ECP: case SG_ECPR: case SG_ECPW: case SG_ECPC: case SG_ECPWC: return sg_launch_pair_ecp(ctx, p);
         default: return sg_fail(ctx, SG_EINVAL, "unknown pair kind %d", p->kind);

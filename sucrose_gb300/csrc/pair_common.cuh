@@ -304,6 +304,19 @@ SG_DEV float3 pair_rij(const float4* __restrict__ pos, int i, int j, const BoxF&
     return min_image(make_float3(a.x - c.x, a.y - c.y, a.z - c.z), b.box, b.inv_box, b.periodic);
 }
 
+// pair_rij that also returns the product of the two charges (pos.w).
+SG_DEV float3 pair_rij_q(const float4* __restrict__ pos, int i, int j, const BoxF& b, float& qq) {
+    const float4 a = pos[i], c = pos[j];
+    qq = a.w * c.w;
+    const float3 d = make_float3(a.x - c.x, a.y - c.y, a.z - c.z);
+    if (b.rep_of) {
+        const int r = b.rep_of[i];
+        const float4 bx = b.rbox[r], ib = b.rinv[r];
+        return min_image(d, make_float3(bx.x, bx.y, bx.z), make_float3(ib.x, ib.y, ib.z), 1);
+    }
+    return min_image(d, b.box, b.inv_box, b.periodic);
+}
+
 // One component of the minimum image, to about 1e-12 absolute: the FP32
 // difference a - c with its exact rounding error (two-sum), the image shift
 // n * (box_hi + box_lo) applied to each part (for n = +-1 the difference is

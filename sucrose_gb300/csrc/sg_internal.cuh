@@ -124,6 +124,13 @@ struct sg_ctx {
     void* mlp_work = nullptr;        // training workspace (mlp_train.cu)
     int mlp_adam_t = 0;
 
+    // dipole reaction field (sg_reaction_field_init): DIP per particle, the
+    // pair kernel's marks (I side in range) and counts (J side in range), RFL
+    float4* rf_dip = nullptr;
+    int* rf_mark = nullptr;
+    int* rf_cnt = nullptr;
+    double* rf_field = nullptr;      // RFL x, y, z (+ one spare)
+
     // staging (pinned host) for uploads / downloads
     float4* h_stage = nullptr;
     size_t h_stage_bytes = 0;
@@ -304,6 +311,8 @@ int sg_nhc_step_initial(sg_ctx* ctx, double dt, double target_temp, double coupl
 int sg_nhc_step_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t rot_chain,
                       int32_t rotations);
 int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p);
+int sg_launch_pair_elec(sg_ctx* ctx, const sg_pair_params* p);
+int sg_reaction_field_eval_async(sg_ctx* ctx);
 int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p);
 int sg_nlist_free(sg_ctx* ctx);

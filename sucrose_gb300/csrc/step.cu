@@ -85,6 +85,7 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
     if (!rc) rc = sg_zero_forces(ctx);
     if (ev) cudaEventRecord(ev[3], ctx->stream);
     for (int k = 0; !rc && k < ctx->step_npairs; ++k) rc = sg_pair_forces_async(ctx, &ctx->step_pairs[k]);
+    if (!rc && (c.flags & SG_STEP_REACTION_FIELD)) rc = sg_reaction_field_eval_async(ctx);
     if (ev) cudaEventRecord(ev[4], ctx->stream);
     if (!rc) {
         switch (c.integrator) {
@@ -131,13 +132,6 @@ int sg_step_configure(sg_ctx* ctx, const sg_step_config* cfg) {
 
 int sg_step_configure_pairs(sg_ctx* ctx, const sg_step_config* cfg, const sg_pair_params* pairs, int32_t npairs) {
     if (!ctx || !cfg || !pairs || npairs < 1 || npairs > 3) return SG_EINVAL;
-    int seen = 0;
-    for (int k = 0; k < npairs; ++k) {
-        const int f = pairs[k].kind < 10 ? 0 : (pairs[k].kind < 20 ? 1 : 2);
-        if (seen & (1 << f)) return sg_fail(ctx, SG_EINVAL, "two pair sets of the same potential family");
-        seen |= 1 << f;
-    }
-    if (npairs > 1 && !ctx->nrep) return sg_fail(ctx, SG_EINVAL, "several pair sets need a replica context");
     if (int rc = sg_step_configure(ctx, cfg)) return rc;
     for (int k = 0; k < npairs; ++k) ctx->step_pairs[k] = pairs[k];
     ctx->step_npairs = npairs;

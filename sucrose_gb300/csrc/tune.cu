@@ -47,6 +47,15 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
     SG_CUDA(ctx, cudaMemcpyAsync(save, ctx->force, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     SG_CUDA(ctx, cudaMemcpyAsync(save + n, ctx->torque, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     SG_CUDA(ctx, cudaMemcpyAsync(acc, ctx->acc, sizeof(acc), cudaMemcpyDeviceToHost, ctx->stream));
+    // the dipole kind also moves the reaction field (DIP, RFL): keep those too
+    const bool rf = p->kind == SG_DIPOLE && ctx->rf_field;
+    double rfl[4];
+    std::vector<float4> dip;
+    if (rf) {
+        dip.resize(n);
+        SG_CUDA(ctx, cudaMemcpyAsync(rfl, ctx->rf_field, sizeof(rfl), cudaMemcpyDeviceToHost, ctx->stream));
+        SG_CUDA(ctx, cudaMemcpyAsync(dip.data(), ctx->rf_dip, sizeof(float4) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -85,6 +94,10 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
     cudaMemcpyAsync(ctx->force, save, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream);
     cudaMemcpyAsync(ctx->torque, save + n, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream);
     cudaMemcpyAsync(ctx->acc, acc, sizeof(acc), cudaMemcpyHostToDevice, ctx->stream);
+    if (rf) {
+        cudaMemcpyAsync(ctx->rf_field, rfl, sizeof(rfl), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(ctx->rf_dip, dip.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream);
+    }
     cudaStreamSynchronize(ctx->stream);
     cudaFree(save);
     if (rc) return rc;

@@ -118,6 +118,29 @@ class GpuSystem:
         self._c(self.L.sg_set_particles(self.ctx, _dp(m), *[_dp(a) for a in s], *[_dp(a) for a in e],
                                         *[_dp(a) for a in I]))
 
+    def set_charges(self, charge, reference_defaults=False):
+        """Per-particle charges (set_atom_charge); reference_defaults applies
+        initialize_system's rule that a negative charge becomes 0."""
+        q = _f64(charge, self.n) if charge is not None else None
+        self._keep_q = q
+        self._c(self.L.sg_set_charges(self.ctx, _dp(q), 1 if reference_defaults else 0))
+
+    def reaction_field_init(self):
+        self._c(self.L.sg_reaction_field_init(self.ctx))
+
+    def reaction_field_eval(self):
+        """eval_reaction_field: returns the energy it added."""
+        e = C.c_double(0.0)
+        self._c(self.L.sg_reaction_field_eval(self.ctx, C.byref(e)))
+        return e.value
+
+    def reaction_field(self):
+        """(RFL (3,), DIP (n, 3))."""
+        rfl = np.zeros(3)
+        d = [np.zeros(self.n) for _ in range(3)]
+        self._c(self.L.sg_reaction_field_read(self.ctx, _dp(rfl), *[_dp(a) for a in d]))
+        return rfl, np.stack(d, 1)
+
     # ---- state transfer -------------------------------------------------------
     def upload(self, r=None, q=None, v=None, l=None):
         """r, v, l: (n,3) FP64; q: (n,4) (w,x,y,z)."""
@@ -209,9 +232,10 @@ class GpuSystem:
     # ---- pair forces ------------------------------------------------------------
     @staticmethod
     def params(kind, sigma=1.0, epsilon=1.0, cutoff=2.5, wf=0.0, chirality=0.0, mu=0, nu=0,
-               solver=capi.SOLVER_NEWTON, newton_tol=1e-6, newton_max_iter=20, fp64_check=1):
+               solver=capi.SOLVER_NEWTON, newton_tol=1e-6, newton_max_iter=20, fp64_check=1, dissoc=1.0, width=1.0,
+               rmin=1.0, db_len=1.0, dielectric=1.0):
         return PairParams(kind, mu, nu, solver, sigma, epsilon, cutoff, wf, chirality, newton_tol, newton_max_iter,
-                          fp64_check)
+                          fp64_check, dissoc, width, rmin, db_len, dielectric)
 
     def pair_forces(self, params, want_stats=False, allow=()):
         pe = C.c_double(0.0)
@@ -314,8 +338,8 @@ class GpuSystem:
 
     def configure_step_pairs(self, pairs, integrator=capi.INT_NVE, dt=0.001, target_temp=1.0, damping=1.0,
                              coupling=0.0, rotations=0, rot_chain=0, first_step=1, key=None, flags=0):
-        """Step whose pair stage runs several parameter sets in order, one per
-        potential family (replica contexts)."""
+        """Step whose pair stage runs several parameter sets in order (summed
+        potentials; in replica contexts each set acts on its family's replicas)."""
         cfg = capi.StepConfig()
         cfg.flags = flags
         cfg.integrator, cfg.rotations, cfg.rot_chain, cfg.first_step = integrator, rotations, rot_chain, first_step

@@ -7,6 +7,10 @@ the reference tree is present):
                           over all pairs of a jittered 108-particle FCC box.
   ref_vv_step.npz         one VerletIntegrator initial_step / final_step of the
                           same C++ port (src/integrators.cpp:7-38), unit mass.
+  ref_morse.npz           forces and energy of the reference's C++
+                          MorsePotential::calculate_forces (src/force.cpp:113-140,
+                          no cutoff, no shift), all pairs of the same box,
+                          D = 1.3, r0 = 1.1, alpha = 1.7.
   philox_words.npz        Philox4x32-10 words of the reference key for fixed
                           counters, from the oracle restatement (xmath.f90:42-76),
                           as a regression anchor for the device and host copies.
@@ -67,6 +71,12 @@ def main():
     s = O.System(108, L)
     s.set_velocity_to_temperature(0.722, 15)
     np.savez(os.path.join(HERE, "readme_velocities.npz"), v=np.stack([s.vx, s.vy, s.vz], 1))
+
+    fx, fy, fz, pot = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(1)
+    R.ref_morse_forces(n, L, 1, O.dptr(rx), O.dptr(ry), O.dptr(rz), 1.3, 1.1, 1.7, len(pi), O.iptr(pi), O.iptr(pj),
+                       O.dptr(fx), O.dptr(fy), O.dptr(fz), O.dptr(pot))
+    np.savez(os.path.join(HERE, "ref_morse.npz"), r=r, box=L, D=1.3, r0=1.1, alpha=1.7, fx=fx, fy=fy, fz=fz,
+             pot=pot[0])
 
 
 if __name__ == "__main__":
