@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="ecp", choices=sorted(WORKLOADS) + ["replicas"])
+    ap.add_argument("--config", default="ecp", choices=sorted(WORKLOADS) + ["replicas", "charged"])
     ap.add_argument("--nrep", type=int, default=4096, help="replicas (config replicas)")
     ap.add_argument("--rep-equil", type=int, default=300, help="untimed equilibration steps (config replicas)")
     ap.add_argument("--flat-graph", action="store_true",
@@ -465,6 +465,229 @@ def run_ours(a):
         dist.destroy_process_group()
 
 
+# ----------------------------------------------------------------- charged ---
+CHARGED = dict(workload="charged_wca_coulomb_langevin_N131072_rho0.5", cells=32, density=0.5, cutoff=3.5, skin=0.3,
+               dielectric=1.0, T=1.0, dt=0.002, damping=1.0, seed=1007)
+
+# FP32 flops per pair, counted from pair_elec.cu (FMA = 2, sqrt / div / exp = 1):
+# every listed pair pays the minimum image and the range test; pairs in range
+# pay the potential's terms
+ELEC_FLOPS = {"COULOMB": (20.0, 40.0), "DH": (20.0, 45.0), "MORSE": (20.0, 45.0), "DIPOLE": (20.0, 130.0)}
+
+
+def charged_state(seed):
+    from sucrose_gb300 import configs
+    w = CHARGED
+    r, q, box = configs.fcc_lattice(w["cells"], w["density"])
+    n = len(r)
+    rng = np.random.default_rng(seed)
+    charge = rng.permutation(np.repeat([1.0, -1.0], n // 2))
+    v = configs.velocities_to_temperature(n, w["T"], seed)
+    return r, q, box, v, charge
+
+
+def charged_params(g):
+    from sucrose_gb300 import capi
+    w = CHARGED
+    return [g.params(capi.WCA, sigma=1.0), g.params(capi.COULOMB, cutoff=w["cutoff"], dielectric=w["dielectric"])]
+
+
+def run_charged(a):
+    """Charged spheres: WCA plus the switched Coulomb of coulombic_ summed in
+    one captured Langevin step; the other charge and Morse kinds timed alone
+    on the same list."""
+    import ctypes as C
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from sucrose_gb300 import GpuSystem, capi, ranks
+    rank, world, local = ranks.rank_info()
+    torch.cuda.set_device(local)
+    w = CHARGED
+    r, q, box, v, charge = charged_state(ranks.replica_seed(w["seed"], rank))
+    n = len(r)
+    g = GpuSystem(n, box)
+    g.upload(r=r, q=q, v=v)
+    g.set_charges(charge)
+    g.init_nlist(w["skin"], w["cutoff"], trigger_mode=1)
+    stream = torch.cuda.ExternalStream(g.stream_ptr())
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    sets = charged_params(g)
+    g.configure_step_pairs(sets, integrator=capi.INT_LANGEVIN, dt=w["dt"], target_temp=w["T"],
+                           damping=w["damping"], rotations=0, flags=FLAGS)
+    g.step(a.equil)
+    g.step_check()
+    tunes = [g.autotune(p, reps=5) for p in sets]
+    g.configure_step_pairs(sets, integrator=capi.INT_LANGEVIN, dt=w["dt"], target_temp=w["T"],
+                           damping=w["damping"], rotations=0, first_step=a.equil + 1, flags=FLAGS)
+    g.step(max(a.warmup, 3))
+    g.step_check()
+    kernels_per_step = g.step_kernel_count()
+    p_before = g.npairs()
+    builds0 = g.nlist_builds()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_dev = timed_steps(g, torch, stream, a.steps, flush)
+    g.step_check()
+    builds = g.nlist_builds() - builds0
+    npairs = 0.5 * (p_before + g.npairs())
+    if dist is not None:
+        t_dev = ranks.max_over_ranks(t_dev, device="cuda")
+    # pair-evals of one step: each listed pair is evaluated by both sets
+    evals_per_step = 2.0 * npairs
+    value = evals_per_step * a.steps * world / t_dev
+    steps_per_s = a.steps / t_dev
+
+    # the Coulomb kernel alone (dominant), then the other kinds on the same list
+    peak32 = g.peak_fma(False)
+    hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs") \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    kinds = {}
+    extra_params = {
+        "COULOMB": sets[1],
+        "DH": g.params(capi.DH, cutoff=w["cutoff"], db_len=1.0, dielectric=w["dielectric"]),
+        "MORSE": g.params(capi.MORSE, cutoff=w["cutoff"], dissoc=1.0, width=2.0, rmin=1.1),
+        "DIPOLE": g.params(capi.DIPOLE, cutoff=w["cutoff"], dielectric=4.0),
+    }
+    g.reaction_field_init()
+    for name, p in extra_params.items():
+        if name != "COULOMB":
+            g.autotune(p, reps=3)
+        _, _, st = g.pair_forces(p, want_stats=True)
+        t = statistics.median(timed_forces(g, torch, stream, p, 20, flush))
+        fl = ELEC_FLOPS[name][0] * st.pairs + ELEC_FLOPS[name][1] * st.solver_evals
+        # minimum DRAM bytes of one launch: the list (i, j int32 per pair), the
+        # positions read once and the forces read and written once
+        by = 8.0 * st.pairs + 48.0 * n + (48.0 * n if name == "DIPOLE" else 0.0)
+        kinds[name] = {"kernel_ms": 1e3 * t, "pair_evals_per_s": st.pairs / t,
+                       "in_range_frac": st.solver_evals / max(st.pairs, 1),
+                       "fp32_tflops": fl / t / 1e12, "fp32_frac": fl / t / 1e12 / peak32,
+                       "min_dram_gbs": by / t / 1e9, "min_dram_frac": (by / t / 1e9 / hbm) if hbm else None}
+    c = kinds["COULOMB"]
+
+    # e2e: FP64 host arrays in and out through the C ABI every step
+    pin = lambda: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    host = [pin() for _ in range(13)]
+    rr, qq, vv, ll = g.download()
+    for k in range(3):
+        host[k][:] = rr[:, k]
+        host[7 + k][:] = vv[:, k]
+        host[10 + k][:] = ll[:, k]
+    for k in range(4):
+        host[3 + k][:] = qq[:, k]
+    D = C.POINTER(C.c_double)
+    ptrs = [h.ctypes.data_as(D) for h in host]
+    energies = np.zeros(4)
+    e_steps = max(10, a.steps // 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e_steps):
+        capi.check(g.ctx, g.L.sg_upload_state(g.ctx, *ptrs))
+        g.step(1)
+        capi.check(g.ctx, g.L.sg_download_state(g.ctx, *ptrs))
+        capi.check(g.ctx, g.L.sg_read_energies(g.ctx, energies.ctypes.data_as(D)))
+    t_e2e = time.perf_counter() - t0
+
+    cpu = None
+    if rank == 0:
+        rate, m = charged_cpu_sample(g, charge, a.cpu_seconds, 1)
+        cpu = {"value": rate, "unit": "pair-evals/s", "cores": 1, "kind": "port",
+               "sample": f"{m} listed pairs of this workload's list through the reference's coulombic_ "
+                         "(FP64, oracle restatement built -O3 -ffast-math), 1 thread"}
+        line = {
+            "metric": "charged pair-evals/s (WCA + switched Coulomb, full MD step)",
+            "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (fp64 sums)", "data": "synthetic (seeded FCC lattice, +-1 charges, device-equilibrated)",
+            "config": {"workload": w["workload"], "n": n, "listed_pairs": npairs, "pair_sets": ["WCA", "COULOMB"],
+                       "dt": w["dt"], "T": w["T"], "cutoff": w["cutoff"], "skin": w["skin"],
+                       "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": "replicas only" if world > 1 else "single GPU"},
+            "ns_per_day": steps_per_s * w["dt"] * TAU_PS * 1e-3 * 86400.0,
+            "tau_per_day": steps_per_s * w["dt"] * 86400.0,
+            "e2e": {"value": evals_per_step * e_steps / t_e2e, "unit": "pair-evals/s",
+                    "h2d_bytes_per_step": 13 * 8 * n, "d2h_bytes_per_step": 13 * 8 * n + 32},
+            "gpu_launches": int(kernels_per_step * a.steps),
+            "roofline": {"bound": "hbm", "kernel": "k_pair<PotElec> (COULOMB)", "achieved": c["min_dram_gbs"],
+                         "peak": hbm, "unit": "GB/s", "frac": c["min_dram_frac"],
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)",
+                         "bytes_per_launch": "8 per listed pair + 48 per particle", "traffic": None,
+                         "fp32_tflops": c["fp32_tflops"], "fp32_frac_of_measured": c["fp32_frac"]},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "kinds_alone": kinds,
+            "list_rebuilds_in_timed_region": int(builds),
+            "autotune": [{"block": t.block, "filter": t.filter} for t in tunes],
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def charged_cpu_sample(g, charge, seconds, nthreads):
+    """The oracle's coulombic_ over a bounded sample of the device's list."""
+    import oracle as O
+    r, q, v, l = g.download()
+    pi, pj = g.pairs()
+    s = O.System(g.n, g.box, fast=True)
+    s.rx[:], s.ry[:], s.rz[:] = r.T
+    s.charge[:] = charge
+    pp = O.pair_params(O.COULOMB, cutoff=CHARGED["cutoff"], dielectric=CHARGED["dielectric"])
+    m0 = min(len(pi), 20000 * nthreads)
+    t = time.perf_counter()
+    s.pair_batch(pp, pi[:m0], pj[:m0], nthreads)
+    per = (time.perf_counter() - t) / max(m0, 1)
+    m = int(min(len(pi), max(m0, seconds / max(per, 1e-9))))
+    t = time.perf_counter()
+    s.pair_batch(pp, pi[:m], pj[:m], nthreads)
+    return m / (time.perf_counter() - t), m
+
+
+def run_reference_charged(a):
+    """Reference arm for the charged workload: the restated coulombic_ on all
+    host cores over the lattice's list, a fixed slice per step."""
+    import oracle as O
+    from scipy.spatial import cKDTree
+    w = CHARGED
+    r, q, box, v, charge = charged_state(w["seed"])
+    n = len(r)
+    b = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,))
+    tree = cKDTree((r + b / 2.0) % b, boxsize=b)
+    pairs = tree.query_pairs(w["cutoff"] + w["skin"], output_type="ndarray")
+    pairs.sort(axis=1)
+    pairs = pairs[np.lexsort((pairs[:, 1], pairs[:, 0]))]
+    pi, pj = pairs[:, 0].astype(np.int32), pairs[:, 1].astype(np.int32)
+    s = O.System(n, box, fast=True)
+    s.rx[:], s.ry[:], s.rz[:] = r.T
+    s.charge[:] = charge
+    pp = O.pair_params(O.COULOMB, cutoff=w["cutoff"], dielectric=w["dielectric"])
+    nth = os.cpu_count() or 1
+    per_step = min(len(pi), 2000000)
+    for _ in range(a.warmup):
+        s.pair_batch(pp, pi[:per_step // 10], pj[:per_step // 10], nth)
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        off = (k * per_step) % max(1, len(pi) - per_step + 1)
+        s.pair_batch(pp, pi[off:off + per_step], pj[off:off + per_step], nth)
+    dt = time.perf_counter() - t0
+    value = per_step * a.steps / dt
+    line = {"impl": "reference", "metric": "charged pair-evals/s (WCA + switched Coulomb, full MD step)",
+            "value": value, "unit": "pair-evals/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * dt / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64", "data": "synthetic (seeded FCC lattice, +-1 charges)",
+            "config": {"workload": w["workload"], "n": n, "listed_pairs": int(len(pi)), "per_step_pairs": per_step},
+            "cpu_baseline": {"value": value, "unit": "pair-evals/s", "cores": nth, "kind": "port",
+                             "sample": f"{per_step} pairs per step of the {len(pi)}-pair list; the reference "
+                                       "coulombic_ (FP64) restated in C++, OpenMP"},
+            "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- replicas ---
 REPLICAS = dict(workload="replicas_4096_lj_gb_langevin_n64to2048", nrep=4096, seed=1005, dt=0.002, damping=1.0)
 
@@ -777,6 +1000,8 @@ def run_reference(a):
         return
     if a.config == "replicas":
         return run_reference_replicas(a)
+    if a.config == "charged":
+        return run_reference_charged(a)
     import oracle as O
     from scipy.spatial import cKDTree
     from sucrose_gb300 import configs
@@ -826,5 +1051,7 @@ if __name__ == "__main__":
         run_reference(args)
     elif args.config == "replicas":
         run_replicas(args)
+    elif args.config == "charged":
+        run_charged(args)
     else:
         run_ours(args)

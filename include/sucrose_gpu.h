@@ -219,8 +219,43 @@ int sg_nht_final(sg_ctx* ctx, double dt, double target_temp, double coupling, in
 /* Chain state (eta[3], p_eta[3], eta_rot[3], p_eta_rot[3]) in / out. */
 int sg_nht_state(sg_ctx* ctx, double* get12, const double* set12);
 /* calculate_thermo (fortran/system.f90:725-741): out = {temp, virial, pressure};
- * dof and density as in initialize_system; kin_eng/kin_rot from the last integrator call. */
+ * dof and density as in initialize_system; kin_eng/kin_rot from the last integrator call.
+ * With constraints set, virial_bonded (reset by sg_zero_forces, like initialize_forces)
+ * joins the virial when it is not negative (:732-736). */
 int sg_thermo(sg_ctx* ctx, int32_t dof, double density, int32_t nrigid, double* out3);
+
+/* ---- bond constraints (module constraints, fortran/system.f90:1055-1210) ------ */
+/* set_num_constraints + add_constraint for every bond (fortran/system.f90:97-108,
+ * 345-360): atoms I, J (one_based selects 1-based indices) at fixed distance
+ * length. The list is split into molecules (connected components); each is
+ * solved by one device thread in the list's order. Single-system contexts only. */
+int sg_set_constraints(sg_ctx* ctx, int32_t nc, const int32_t* bbi, const int32_t* bbj, const double* length,
+                       int32_t one_based);
+/* RX_old = RX: the start-of-step positions apply_constraints_a measures against. */
+int sg_constraints_save(sg_ctx* ctx);
+/* apply_constraints_a(DT) :1060-1142 and apply_constraints_b(DT) :1144-1208, enqueued
+ * without waiting; both add to virial_bonded. Where the reference stops on a
+ * constraint failure (:1102-1106) the kernel records it and leaves that molecule;
+ * sg_constraints_check (and sg_step_check) then returns SG_ENOCONV. */
+int sg_constraints_a(sg_ctx* ctx, double dt);
+int sg_constraints_b(sg_ctx* ctx, double dt);
+int sg_constraints_check(sg_ctx* ctx);
+int sg_constraints_clear_error(sg_ctx* ctx);
+/* Counters since the last reset: {max sweeps a, molecules still moving after 100
+ * sweeps a, corrections a, the same three for b}. */
+int sg_constraint_stats(sg_ctx* ctx, int64_t out[6], int32_t reset);
+/* Constrained integrators (fortran/integrators.f90): vvc_ :55-106, nhtc_ :394-490,
+ * lgvc_ :678-855. Each is the plain half step of this header with RX_old saved
+ * before it and apply_constraints_a / _b after it; the initial steps wait and
+ * report a constraint failure. */
+int sg_vvc_initial(sg_ctx* ctx, double dt);
+int sg_vvc_final(sg_ctx* ctx, double dt, double* kin_eng);
+int sg_nhtc_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain);
+int sg_nhtc_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain,
+                  double* kin_eng);
+int sg_lgvc_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double target_temp,
+                    const uint32_t* key);
+int sg_lgvc_final(sg_ctx* ctx, double dt, double damping, double* kin_eng, double* kin_rot);
 
 /* ---- batched replicas (no counterpart in the reference: its state is one
  * global system, fortran/system.f90:7-39) ------------------------------------ */
@@ -269,6 +304,9 @@ typedef struct {
 } sg_step_config;
 #define SG_STEP_FLAT 1
 #define SG_STEP_REACTION_FIELD 2   /* eval_reaction_field after the pair stage (SG_DIPOLE) */
+#define SG_STEP_CONSTRAINTS 4      /* RATTLE around the integrator: RX_old saved before the initial half
+                                      step, apply_constraints_a after it, apply_constraints_b after the
+                                      final half step (vvc_, nhtc_, lgvc_ with the chosen integrator) */
 
 /* Set the step program. The first sg_step call runs one step eagerly (which
  * allocates every buffer), then captures one step as a CUDA graph; later

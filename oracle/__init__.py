@@ -37,7 +37,10 @@ class OrSys(C.Structure):
                                           "target_temp")] + \
                [("eta", C.c_double * 3), ("p_eta", C.c_double * 3), ("eta_r", C.c_double * 3),
                 ("p_eta_r", C.c_double * 3)] + \
-               [(k, _D) for k in ("charge", "dipx", "dipy", "dipz")] + [("rfl", C.c_double * 3)]
+               [(k, _D) for k in ("charge", "dipx", "dipy", "dipz")] + [("rfl", C.c_double * 3)] + \
+               [(k, _D) for k in ("rx_old", "ry_old", "rz_old")] + [("bbi", _I), ("bbj", _I), ("bb_len", _D),
+                                                                    ("virial_bonded", C.c_double),
+                                                                    ("rattle_sweeps", C.c_int)]
 
 
 class OrPairParams(C.Structure):
@@ -74,6 +77,10 @@ def lib(fast=False):
         L.or_nhr_half.argtypes = [P, C.c_double, C.c_double, C.c_int]
         L.or_calculate_thermo.argtypes = [P]
         L.or_reaction_field_init.argtypes = [P]
+        L.or_constraints_a.argtypes = [P, C.c_double]
+        L.or_constraints_a.restype = C.c_int
+        L.or_constraints_b.argtypes = [P, C.c_double]
+        L.or_constraints_save.argtypes = [P]
         L.or_reaction_field_eval.argtypes = [P]
         L.or_set_velocity_to_temperature.argtypes = [P, C.c_double, C.c_int, C.c_int]
         L.or_generate_fcc.argtypes = [C.c_int, C.c_double] + [_D] * 7
@@ -116,7 +123,7 @@ def uptr(a):
 PARTICLE_FIELDS = ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "qw", "qx", "qy", "qz",
                    "lx", "ly", "lz", "tx", "ty", "tz", "mass", "inv_mass", "sig_x", "sig_y", "sig_z",
                    "eps_x", "eps_y", "eps_z", "ixx", "iyy", "izz", "ixx_inv", "iyy_inv", "izz_inv",
-                   "charge", "dipx", "dipy", "dipz")
+                   "charge", "dipx", "dipy", "dipz", "rx_old", "ry_old", "rz_old")
 
 
 class System:
@@ -162,9 +169,11 @@ class System:
         return C.byref(self.s)
 
     def zero_forces(self):
+        """initialize_forces (system.f90:423-436)."""
         for f in ("fx", "fy", "fz", "tx", "ty", "tz"):
             getattr(self, f)[:] = 0.0
         self.s.pot_eng = 0.0
+        self.s.virial_bonded = 0.0
 
     # --- pair potentials -------------------------------------------------
     def pair(self, i, j, params, prec=64):
@@ -236,6 +245,27 @@ class System:
 
     def nhr_half(self, dt, coupling=None):
         self.L.or_nhr_half(self.ptr(), dt, 0.0 if coupling is None else coupling, 0 if coupling is None else 1)
+
+    # --- bond constraints (module constraints, system.f90:1055-1210) ----------
+    def set_constraints(self, bbi, bbj, length):
+        """set_num_constraints + add_constraint, 0-based atom indices."""
+        self.bbi = np.ascontiguousarray(bbi, dtype=np.int32)
+        self.bbj = np.ascontiguousarray(bbj, dtype=np.int32)
+        self.bb_len = np.ascontiguousarray(np.broadcast_to(np.asarray(length, dtype=np.float64), self.bbi.shape))
+        self.s.nc = len(self.bbi)
+        self.s.bbi = iptr(self.bbi)
+        self.s.bbj = iptr(self.bbj)
+        self.s.bb_len = dptr(self.bb_len)
+
+    def constraints_save(self):
+        self.L.or_constraints_save(self.ptr())
+
+    def constraints_a(self, dt):
+        """0, or 1 + the index of the failing constraint."""
+        return self.L.or_constraints_a(self.ptr(), dt)
+
+    def constraints_b(self, dt):
+        self.L.or_constraints_b(self.ptr(), dt)
 
     def reaction_field_init(self):
         self.L.or_reaction_field_init(self.ptr())

@@ -25,6 +25,7 @@
 #include <cstring>
 #include <cstdlib>
 #include <algorithm>
+#include <vector>
 
 namespace {
 
@@ -205,6 +206,11 @@ typedef struct OrSys {
     double* charge;                // system.f90:7 (NULL: all zero)
     double *dipx, *dipy, *dipz;    // module dipole DIP arrays (force.f90:2671)
     double rfl[3];                 // RFL: every element of the reference's RFL arrays holds this vector
+    double *rx_old, *ry_old, *rz_old;   // system.f90:22
+    int *bbi, *bbj;                // constraint atoms, 0-based, nc of them (system.f90:32-33)
+    double* bb_len;
+    double virial_bonded;          // system.f90:29
+    int rattle_sweeps;             // sweeps of the last apply_constraints_a / _b call
 } OrSys;
 
 // Pair-potential parameters shared by every family.
@@ -1381,8 +1387,111 @@ void or_calculate_thermo(OrSys* s) {                             // system.f90:7
     double vir = 0.0;
     for (int i = 0; i < s->n; ++i) vir += s->rx[i] * s->fx[i] + s->ry[i] * s->fy[i] + s->rz[i] * s->fz[i];
     s->virial = vir;
+    if (s->nc > 0 && s->virial_bonded >= 0.0) s->virial = vir + s->virial_bonded;   // :732-736
     double volume = s->box[0] * s->box[1] * s->box[2];
     s->pressure = (s->density * s->nrigid * s->temp) + (s->virial / (3.0 * volume));
+}
+
+// ------------------------------------------------------------- RATTLE -----
+// apply_constraints_a (system.f90:1060-1142): one global Gauss-Seidel loop over
+// the constraint list in order, moved flags per atom, at most 100 sweeps.
+// Returns 0, or 1 + the index of the constraint whose vdot test failed (the
+// reference prints and stops there).
+int or_constraints_a(OrSys* s, double dt) {
+    const double r_tol = 1.0e-5;
+    const int max_rattle = 100;
+    std::vector<char> moved(s->n, 1);
+    int rattle = 0;
+    auto any = [&]() {
+        for (char m : moved)
+            if (m) return true;
+        return false;
+    };
+    while (any() && rattle < max_rattle) {
+        for (int ix = 0; ix < s->nc; ++ix) {
+            const int i = s->bbi[ix], j = s->bbj[ix];
+            const double len = s->bb_len[ix];
+            if (moved[i] || moved[j]) {
+                double r[3] = {s->rx[i] - s->rx[j], s->ry[i] - s->ry[j], s->rz[i] - s->rz[j]};
+                min_image(r, s->box, s->periodic);
+                const double chi = len * len - (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+                if (std::fabs(chi) > 2 * r_tol * len * len) {
+                    double ro[3] = {s->rx_old[i] - s->rx_old[j], s->ry_old[i] - s->ry_old[j],
+                                    s->rz_old[i] - s->rz_old[j]};
+                    min_image(ro, s->box, s->periodic);
+                    const double vdot = r[0] * ro[0] + r[1] * ro[1] + r[2] * ro[2];
+                    if (vdot < r_tol * len * len) {
+                        s->rattle_sweeps = rattle;
+                        return ix + 1;
+                    }
+                    const double L = chi / (2.0 * vdot * (s->inv_mass[i] + s->inv_mass[j]));
+                    s->virial_bonded = s->virial_bonded + (L * len * len) / (dt * dt);
+                    const double ai = L * s->inv_mass[i], aj = L * s->inv_mass[j];
+                    s->rx[i] += ai * ro[0]; s->ry[i] += ai * ro[1]; s->rz[i] += ai * ro[2];
+                    s->rx[j] -= aj * ro[0]; s->ry[j] -= aj * ro[1]; s->rz[j] -= aj * ro[2];
+                    s->vx[i] += ai * ro[0] / dt; s->vy[i] += ai * ro[1] / dt; s->vz[i] += ai * ro[2] / dt;
+                    s->vx[j] -= aj * ro[0] / dt; s->vy[j] -= aj * ro[1] / dt; s->vz[j] -= aj * ro[2] / dt;
+                    moved[i] = 1;
+                    moved[j] = 1;
+                } else {
+                    moved[i] = 0;
+                    moved[j] = 0;
+                }
+            }
+        }
+        rattle = rattle + 1;
+    }
+    s->rattle_sweeps = rattle;
+    return 0;
+}
+
+// apply_constraints_b (system.f90:1144-1208)
+void or_constraints_b(OrSys* s, double dt) {
+    const double r_tol = 1.0e-5;
+    const int max_rattle = 100;
+    std::vector<char> moved(s->n, 1);
+    int rattle = 0;
+    auto any = [&]() {
+        for (char m : moved)
+            if (m) return true;
+        return false;
+    };
+    while (any() && rattle < max_rattle) {
+        for (int ix = 0; ix < s->nc; ++ix) {
+            const int i = s->bbi[ix], j = s->bbj[ix];
+            const double len = s->bb_len[ix];
+            if (moved[i] || moved[j]) {
+                double r[3] = {s->rx[i] - s->rx[j], s->ry[i] - s->ry[j], s->rz[i] - s->rz[j]};
+                min_image(r, s->box, s->periodic);
+                const double v[3] = {s->vx[i] - s->vx[j], s->vy[i] - s->vy[j], s->vz[i] - s->vz[j]};
+                const double vdot = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+                const double L = -vdot / ((s->inv_mass[i] + s->inv_mass[j]) * len * len);
+                if (std::fabs(L) > r_tol) {
+                    s->virial_bonded = s->virial_bonded + (L * len * len) / dt;
+                    const double ai = L * s->inv_mass[i], aj = L * s->inv_mass[j];
+                    s->vx[i] += ai * r[0]; s->vy[i] += ai * r[1]; s->vz[i] += ai * r[2];
+                    s->vx[j] -= aj * r[0]; s->vy[j] -= aj * r[1]; s->vz[j] -= aj * r[2];
+                    moved[i] = 1;
+                    moved[j] = 1;
+                } else {
+                    moved[i] = 0;
+                    moved[j] = 0;
+                }
+            }
+        }
+        rattle = rattle + 1;
+    }
+    s->rattle_sweeps = rattle;
+}
+
+// RX_old(I) = RX(I), taken by vvc_ / nhtc_ / lgvc_ before the drift
+// (integrators.f90:67-69, 432-434, 714-716).
+void or_constraints_save(OrSys* s) {
+    for (int i = 0; i < s->n; ++i) {
+        s->rx_old[i] = s->rx[i];
+        s->ry_old[i] = s->ry[i];
+        s->rz_old[i] = s->rz[i];
+    }
 }
 
 // set_velocity_to_temperature (system.f90:362-421), quirk: scales sum v^2 to

@@ -39,6 +39,7 @@ class StepConfig(C.Structure):
 INT_NVE, INT_LANGEVIN, INT_NH, INT_NH_REF = 0, 1, 2, 3
 STEP_FLAT = 1
 STEP_REACTION_FIELD = 2
+STEP_CONSTRAINTS = 4
 
 
 class TuneResult(C.Structure):
@@ -98,6 +99,19 @@ SIGNATURES = [
     ("sg_nht_final", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, _D]),
     ("sg_nht_state", C.c_int, [_P, _D, _D]),
     ("sg_thermo", C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
+    ("sg_set_constraints", C.c_int, [_P, C.c_int32, _I32, _I32, _D, C.c_int32]),
+    ("sg_constraints_save", C.c_int, [_P]),
+    ("sg_constraints_a", C.c_int, [_P, C.c_double]),
+    ("sg_constraints_b", C.c_int, [_P, C.c_double]),
+    ("sg_constraints_check", C.c_int, [_P]),
+    ("sg_constraints_clear_error", C.c_int, [_P]),
+    ("sg_constraint_stats", C.c_int, [_P, _I64, C.c_int32]),
+    ("sg_vvc_initial", C.c_int, [_P, C.c_double]),
+    ("sg_vvc_final", C.c_int, [_P, C.c_double, _D]),
+    ("sg_nhtc_initial", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32]),
+    ("sg_nhtc_final", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, _D]),
+    ("sg_lgvc_initial", C.c_int, [_P, C.c_double, C.c_int32, C.c_double, C.c_double, _U32]),
+    ("sg_lgvc_final", C.c_int, [_P, C.c_double, C.c_double, _D, _D]),
     ("sg_create_replicas", C.c_int, [C.POINTER(_P), C.c_int32, _I32, _D, _I32, _D, _U32, C.c_int32]),
     ("sg_rep_nlist_init", C.c_int, [_P, _D, _D, C.c_int32]),
     ("sg_rep_kinetic", C.c_int, [_P, _D]),

@@ -104,6 +104,7 @@ int sg_destroy(sg_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     sg_nlist_free(ctx);
     sg_mlp_free(ctx);
+    sg_constraints_free(ctx);
     void* bufs[] = {ctx->pos, ctx->quat, ctx->vel, ctx->angm, ctx->force, ctx->torque, ctx->shape, ctx->eshape,
                     ctx->inert, ctx->inert_inv, ctx->acc, ctx->partials, ctx->done_counter, ctx->stats, ctx->nh,
                     ctx->ecp_prep, ctx->ecp_prep64, ctx->ecp_lambda, ctx->mlp_w, ctx->mlp_wbf16, ctx->mlp_tc_err,
@@ -314,6 +315,7 @@ int sg_zero_forces(sg_ctx* ctx) {
     SG_CUDA(ctx, cudaMemsetAsync(ctx->force, 0, sizeof(float4) * (size_t)ctx->n, ctx->stream));
     SG_CUDA(ctx, cudaMemsetAsync(ctx->torque, 0, sizeof(float4) * (size_t)ctx->n, ctx->stream));
     SG_CUDA(ctx, cudaMemsetAsync(ctx->acc, 0, sizeof(double) * 4, ctx->stream));
+    SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 6, 0, sizeof(double), ctx->stream));   // virial_bonded
     return SG_OK;
 }
 
@@ -345,14 +347,16 @@ extern "C" int sg_thermo(sg_ctx* ctx, int32_t dof, double density, int32_t nrigi
     k_virial<<<grid, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->force, ctx->partials, ctx->done_counter,
                                             ctx->acc + 4);
     SG_LAUNCH_CHECK(ctx, "k_virial");
-    double a[5];
-    SG_CUDA(ctx, cudaMemcpyAsync(a, ctx->acc, sizeof(double) * 5, cudaMemcpyDeviceToHost, ctx->stream));
+    double a[7];
+    SG_CUDA(ctx, cudaMemcpyAsync(a, ctx->acc, sizeof(double) * 7, cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     double kin_tot = a[2] + a[3];
     double temp = 2.0 * kin_tot / (double)dof;
     double volume = ctx->box[0] * ctx->box[1] * ctx->box[2];
+    // the bonded virial joins when NC > 0 and it is not negative (system.f90:732-736)
+    const double virial = (ctx->con_n > 0 && a[6] >= 0.0) ? a[4] + a[6] : a[4];
     out3[0] = temp;
-    out3[1] = a[4];
-    out3[2] = (density * nrigid * temp) + (a[4] / (3.0 * volume));
+    out3[1] = virial;
+    out3[2] = (density * nrigid * temp) + (virial / (3.0 * volume));
     return SG_OK;
 }

@@ -131,6 +131,19 @@ struct sg_ctx {
     int* rf_cnt = nullptr;
     double* rf_field = nullptr;      // RFL x, y, z (+ one spare)
 
+    // bond constraints (sg_set_constraints): constraints grouped by molecule
+    // (connected component), each group in the reference's list order
+    int con_n = 0;                   // NC
+    int con_nmol = 0;
+    int con_max_len = 0;             // constraints in the largest molecule
+    int2* con_ij = nullptr;          // (I, J) 0-based
+    float* con_len = nullptr;
+    int* con_mol = nullptr;          // nmol + 1 offsets into con_ij
+    unsigned char* con_moved = nullptr;   // per particle
+    float4* pos_old = nullptr;       // RX_old .. RZ_old
+    int* con_err = nullptr;          // [0] 1 + first failing constraint, [1] I, [2] J
+    unsigned long long* con_stats = nullptr;   // see sg_constraint_stats
+
     // staging (pinned host) for uploads / downloads
     float4* h_stage = nullptr;
     size_t h_stage_bytes = 0;
@@ -313,6 +326,7 @@ int sg_nhc_step_final(sg_ctx* ctx, double dt, double target_temp, double couplin
 int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_elec(sg_ctx* ctx, const sg_pair_params* p);
 int sg_reaction_field_eval_async(sg_ctx* ctx);
+int sg_constraints_free(sg_ctx* ctx);
 int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p);
 int sg_nlist_free(sg_ctx* ctx);

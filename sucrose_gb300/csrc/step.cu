@@ -65,7 +65,9 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
     ctx->lgv_rotations = c.rotations;
     int rc = SG_OK;
     if (ev) cudaEventRecord(ev[0], ctx->stream);
-    switch (c.integrator) {
+    const bool con = (c.flags & SG_STEP_CONSTRAINTS) != 0;
+    if (con) rc = sg_constraints_save(ctx);
+    if (!rc) switch (c.integrator) {
         case SG_INT_NVE: rc = sg_vv_initial(ctx, dt); if (!rc && c.rotations) rc = sg_qq_initial(ctx, dt); break;
         case SG_INT_LANGEVIN:
             rc = sg_lgv_initial(ctx, dt, 0, c.damping, c.target_temp, c.has_key ? c.key : nullptr);
@@ -79,6 +81,7 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
             break;
         default: rc = sg_fail(ctx, SG_EINVAL, "unknown integrator %d", c.integrator);
     }
+    if (!rc && con) rc = sg_constraints_a(ctx, dt);
     if (ev) cudaEventRecord(ev[1], ctx->stream);
     if (!rc) rc = enqueue_list_update(ctx, (c.flags & SG_STEP_FLAT) != 0);
     if (ev) cudaEventRecord(ev[2], ctx->stream);
@@ -97,6 +100,7 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
                 if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr);
         }
     }
+    if (!rc && con) rc = sg_constraints_b(ctx, dt);
     if (ev) cudaEventRecord(ev[5], ctx->stream);
     if (!rc) {
         k_step_incr<<<1, 1, 0, ctx->stream>>>(ctx->step_dev);
@@ -224,6 +228,7 @@ int sg_step_check(sg_ctx* ctx) {
     if (int rc = sg_read_energies(ctx, e)) return rc;
     for (int i = 0; i < 4; ++i)
         if (!std::isfinite(e[i])) return sg_fail(ctx, SG_ENAN, "non-finite energy accumulator %d", i);
+    if (ctx->con_n) return sg_constraints_check(ctx);
     return SG_OK;
 }
 

@@ -314,6 +314,64 @@ class GpuSystem:
         self._c(self.L.sg_nht_state(self.ctx, _dp(out), _dp(s)))
         return out
 
+    # ---- bond constraints -------------------------------------------------------------
+    def set_constraints(self, bbi, bbj, length, one_based=False):
+        """set_num_constraints + add_constraint for every bond."""
+        i = np.ascontiguousarray(bbi, dtype=np.int32)
+        j = np.ascontiguousarray(bbj, dtype=np.int32)
+        ln = np.ascontiguousarray(np.broadcast_to(np.asarray(length, dtype=np.float64), i.shape))
+        P = C.POINTER(C.c_int32)
+        self._c(self.L.sg_set_constraints(self.ctx, len(i), i.ctypes.data_as(P), j.ctypes.data_as(P), _dp(ln),
+                                          1 if one_based else 0))
+
+    def constraints_save(self):
+        self._c(self.L.sg_constraints_save(self.ctx))
+
+    def constraints_a(self, dt):
+        self._c(self.L.sg_constraints_a(self.ctx, dt))
+
+    def constraints_b(self, dt):
+        self._c(self.L.sg_constraints_b(self.ctx, dt))
+
+    def constraints_check(self):
+        self._c(self.L.sg_constraints_check(self.ctx))
+
+    def constraints_clear_error(self):
+        self._c(self.L.sg_constraints_clear_error(self.ctx))
+
+    def constraint_stats(self, reset=False):
+        out = np.zeros(6, dtype=np.int64)
+        self._c(self.L.sg_constraint_stats(self.ctx, out.ctypes.data_as(C.POINTER(C.c_int64)), 1 if reset else 0))
+        return dict(zip(("sweeps_a", "unconverged_a", "corrections_a", "sweeps_b", "unconverged_b",
+                         "corrections_b"), out.tolist()))
+
+    def vvc_initial(self, dt):
+        self._c(self.L.sg_vvc_initial(self.ctx, dt))
+
+    def vvc_final(self, dt):
+        ke = C.c_double(0.0)
+        self._c(self.L.sg_vvc_final(self.ctx, dt, C.byref(ke)))
+        return ke.value
+
+    def nhtc_initial(self, dt, target_temp, coupling=0.0, mode=0, rot_chain=0):
+        self._c(self.L.sg_nhtc_initial(self.ctx, dt, target_temp, coupling, mode, rot_chain))
+
+    def nhtc_final(self, dt, target_temp, coupling=0.0, mode=0, rot_chain=0):
+        ke = C.c_double(0.0)
+        self._c(self.L.sg_nhtc_final(self.ctx, dt, target_temp, coupling, mode, rot_chain, C.byref(ke)))
+        return ke.value
+
+    def lgvc_initial(self, dt, step, damping=1.0, target_temp=1.0, key=None):
+        k = None if key is None else np.asarray(key, dtype=np.uint32)
+        self._c(self.L.sg_lgvc_initial(self.ctx, dt, int(step), damping, target_temp,
+                                       None if k is None else k.ctypes.data_as(C.POINTER(C.c_uint32))))
+
+    def lgvc_final(self, dt, damping=1.0):
+        ke = C.c_double(0.0)
+        kr = C.c_double(0.0)
+        self._c(self.L.sg_lgvc_final(self.ctx, dt, damping, C.byref(ke), C.byref(kr)))
+        return ke.value, kr.value
+
     def thermo(self, dof, density, nrigid=1):
         out = np.zeros(3)
         self._c(self.L.sg_thermo(self.ctx, int(dof), float(density), int(nrigid), _dp(out)))
