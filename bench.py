@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="ecp", choices=sorted(WORKLOADS) + ["replicas", "charged"])
+    ap.add_argument("--config", default="ecp", choices=sorted(WORKLOADS) + ["replicas", "charged", "constrained", "polymer"])
     ap.add_argument("--nrep", type=int, default=4096, help="replicas (config replicas)")
     ap.add_argument("--rep-equil", type=int, default=300, help="untimed equilibration steps (config replicas)")
     ap.add_argument("--flat-graph", action="store_true",
@@ -570,28 +570,7 @@ def run_charged(a):
                        "min_dram_gbs": by / t / 1e9, "min_dram_frac": (by / t / 1e9 / hbm) if hbm else None}
     c = kinds["COULOMB"]
 
-    # e2e: FP64 host arrays in and out through the C ABI every step
-    pin = lambda: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
-    host = [pin() for _ in range(13)]
-    rr, qq, vv, ll = g.download()
-    for k in range(3):
-        host[k][:] = rr[:, k]
-        host[7 + k][:] = vv[:, k]
-        host[10 + k][:] = ll[:, k]
-    for k in range(4):
-        host[3 + k][:] = qq[:, k]
-    D = C.POINTER(C.c_double)
-    ptrs = [h.ctypes.data_as(D) for h in host]
-    energies = np.zeros(4)
-    e_steps = max(10, a.steps // 4)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(e_steps):
-        capi.check(g.ctx, g.L.sg_upload_state(g.ctx, *ptrs))
-        g.step(1)
-        capi.check(g.ctx, g.L.sg_download_state(g.ctx, *ptrs))
-        capi.check(g.ctx, g.L.sg_read_energies(g.ctx, energies.ctypes.data_as(D)))
-    t_e2e = time.perf_counter() - t0
+    e2e_value, h2d, d2h = e2e_rate(g, torch, max(10, a.steps // 4), evals_per_step)
 
     cpu = None
     if rank == 0:
@@ -610,8 +589,8 @@ def run_charged(a):
                        "parallelism": "replicas only" if world > 1 else "single GPU"},
             "ns_per_day": steps_per_s * w["dt"] * TAU_PS * 1e-3 * 86400.0,
             "tau_per_day": steps_per_s * w["dt"] * 86400.0,
-            "e2e": {"value": evals_per_step * e_steps / t_e2e, "unit": "pair-evals/s",
-                    "h2d_bytes_per_step": 13 * 8 * n, "d2h_bytes_per_step": 13 * 8 * n + 32},
+            "e2e": {"value": e2e_value, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
             "gpu_launches": int(kernels_per_step * a.steps),
             "roofline": {"bound": "hbm", "kernel": "k_pair<PotElec> (COULOMB)", "achieved": c["min_dram_gbs"],
                          "peak": hbm, "unit": "GB/s", "frac": c["min_dram_frac"],
@@ -627,6 +606,201 @@ def run_charged(a):
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------- constrained ---
+MOLECULAR = {
+    # rigid dimers: RATTLE bonds and WCA between all atoms
+    "constrained": dict(workload="constrained_dimers_wca_langevin_N128000", cells=40, spacing=1.6, sigma=0.9,
+                        bond=1.0, skin=0.3, T=1.0, dt=0.002, damping=1.0, seed=1009,
+                        metric="constraint-solves/s (rigid WCA dimers, RATTLE a + b, full MD step)"),
+    # bead chains of 10: RATTLE bonds, harmonic bends (angle_bend_, 4, 120 deg), dihedrals (dih_, 0.5), WCA
+    "polymer": dict(workload="polymer_chains10_wca_bend_dih_rattle_langevin_N96000", counts=(6, 40, 40), length=10,
+                    sigma=0.9, bond=1.0, skin=0.3, T=1.0, dt=0.002, damping=1.0, seed=1011,
+                    metric="constraint-solves/s (WCA bead chains, bends, dihedrals, RATTLE, full MD step)"),
+}
+CONSTRAINED = MOLECULAR["constrained"]
+
+
+def molecular_state(name, seed):
+    """Positions, box, bond constraints (bbi, bbj, length) and the bonded
+    term lists [(kind, atoms, coeff, angle)] of a molecular workload."""
+    from sucrose_gb300 import capi
+    from sucrose_gb300.molecules import molecular_mix, polymer_chains
+    w = MOLECULAR[name]
+    if name == "constrained":
+        r, box, bbi, bbj, ln, mol = molecular_mix(w["cells"], w["spacing"], seed, bond=w["bond"], kinds=("dimer",))
+        return r, box, bbi, bbj, ln, []
+    r, box, bonds, bends, dihs = polymer_chains(w["counts"], w["length"], seed, bond=w["bond"])
+    terms = [(capi.ANGLE_BEND, bends, 4.0, 120.0), (capi.DIH, dihs, 0.5, None)]
+    return r, box, bonds[:, 0].copy(), bonds[:, 1].copy(), np.full(len(bonds), w["bond"]), terms
+
+
+def run_constrained(a):
+    """Molecular workloads (config constrained: rigid dimers; polymer: bead
+    chains with bonded terms) with RATTLE bonds and WCA between all atoms:
+    one captured Langevin step with the constraint (and bonded) stages."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from sucrose_gb300 import GpuSystem, capi, configs, ranks
+    rank, world, local = ranks.rank_info()
+    torch.cuda.set_device(local)
+    w = MOLECULAR[a.config]
+    seed = ranks.replica_seed(w["seed"], rank)
+    r, box, bbi, bbj, ln, terms = molecular_state(a.config, seed)
+    n = len(r)
+    v = configs.velocities_to_temperature(n, w["T"], seed)
+    g = GpuSystem(n, box)
+    g.upload(r=r, v=v)
+    g.set_constraints(bbi, bbj, ln)
+    for kind, atoms, coeff, angle in terms:
+        g.bonded_set(kind, atoms, coeff, angle)
+    g.init_nlist(w["skin"], w["sigma"], trigger_mode=1)
+    stream = torch.cuda.ExternalStream(g.stream_ptr())
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    pp = g.params(capi.WCA, sigma=w["sigma"], cutoff=w["sigma"])
+    cfg = dict(integrator=capi.INT_LANGEVIN, dt=w["dt"], target_temp=w["T"], damping=w["damping"], rotations=0,
+               flags=FLAGS | capi.STEP_CONSTRAINTS | (capi.STEP_BONDED if terms else 0))
+    g.configure_step(pp, first_step=1, **cfg)
+    g.step(a.equil)
+    g.step_check()
+    tune = g.autotune(pp, reps=5)
+    g.configure_step(pp, first_step=a.equil + 1, **cfg)
+    g.step(max(a.warmup, 3))
+    g.step_check()
+    kernels_per_step = g.step_kernel_count()
+    p_before = g.npairs()
+    builds0 = g.nlist_builds()
+    g.constraint_stats(reset=True)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_dev = timed_steps(g, torch, stream, a.steps, flush)
+    g.step_check()
+    cst = g.constraint_stats(reset=True)
+    builds = g.nlist_builds() - builds0
+    npairs = 0.5 * (p_before + g.npairs())
+    if dist is not None:
+        t_dev = ranks.max_over_ranks(t_dev, device="cuda")
+    nc = len(bbi)
+    value = nc * a.steps * world / t_dev
+    steps_per_s = a.steps / t_dev
+    stages = g.step_stage_times(20)
+    # RATTLE pass a: per correction it reads and writes two positions and two
+    # velocities and reads two start-of-step positions (16 B each), plus the
+    # constraint record (12 B); HBM-bound at best, latency-bound per molecule
+    hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs") \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    ta = stages["constraints_a"] * 1e-3
+    bytes_a = nc * (2 * 16 * 2 + 2 * 16 * 2 + 2 * 16 + 12)
+    e2e_value, h2d, d2h = e2e_rate(g, torch, max(10, a.steps // 4), nc)
+    if rank == 0:
+        line = {
+            "metric": w["metric"],
+            "value": value, "unit": "constraint-solves/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (fp64 sums)", "data": "synthetic (seeded molecule lattice, device-equilibrated)",
+            "config": {"workload": w["workload"], "n": n, "constraints": nc,
+                       "bonded_terms": {int(k): int(len(at)) for k, at, _, _ in terms},
+                       "listed_pairs": npairs, "dt": w["dt"], "T": w["T"],
+                       "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": "replicas only" if world > 1 else "single GPU"},
+            "ns_per_day": steps_per_s * w["dt"] * TAU_PS * 1e-3 * 86400.0,
+            "tau_per_day": steps_per_s * w["dt"] * 86400.0,
+            "pair_evals_per_s": npairs * a.steps * world / t_dev,
+            "e2e": {"value": e2e_value, "unit": "constraint-solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(kernels_per_step * a.steps),
+            "roofline": {"bound": "hbm", "kernel": "k_rattle_a", "achieved": bytes_a / ta / 1e9 if ta > 0 else None,
+                         "peak": hbm, "unit": "GB/s", "frac": (bytes_a / ta / 1e9 / hbm) if (hbm and ta > 0) else None,
+                         "bytes_per_launch": "124 per constraint (one correction)", "traffic": None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"},
+            "cpu_baseline": None,
+            "clocks": clk.summary(),
+            "stage_ms_eager": stages,
+            "constraint_stats_timed": cst,
+            "list_rebuilds_in_timed_region": int(builds),
+            "autotune": {"block": tune.block, "filter": tune.filter},
+        }
+        if terms:
+            line["bonded_kernel_ms"] = bonded_kernel_ms(g, torch, stream, terms, flush)
+        line["cpu_baseline"] = constrained_cpu_sample(g, bbi, bbj, ln, w, a.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def bonded_kernel_ms(g, torch, stream, terms, flush, reps=20):
+    """Median CUDA-event time of each registered bonded list's kernel."""
+    out = {}
+    for kind, atoms, _, _ in terms:
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        with torch.cuda.stream(stream):
+            for s, e in ev:
+                s.record(stream)
+                g.L.sg_bonded_forces_async(g.ctx, int(kind))
+                e.record(stream)
+                flush.add_(1.0)
+        torch.cuda.synchronize()
+        out[str(int(kind))] = statistics.median(s.elapsed_time(e) for s, e in ev)
+    return out
+
+
+def constrained_cpu_sample(g, bbi, bbj, ln, w, seconds):
+    """The oracle's apply_constraints_a (the reference's global Gauss-Seidel
+    loop, FP64, one core) on the device's current state after one drift."""
+    import oracle as O
+    r, q, v, l = g.download()
+    s = O.System(g.n, g.box, fast=True)
+    s.rx[:], s.ry[:], s.rz[:] = r.T
+    s.vx[:], s.vy[:], s.vz[:] = v.T
+    s.set_constraints(bbi, bbj, ln)
+    calls, t = 0, 0.0
+    while t < seconds and calls < 50:
+        s.constraints_save()
+        s.vv_initial(w["dt"])
+        t0 = time.perf_counter()
+        s.constraints_a(w["dt"])
+        t += time.perf_counter() - t0
+        calls += 1
+    rate = len(bbi) * calls / t
+    return {"value": rate, "unit": "constraint-solves/s", "cores": 1, "kind": "port",
+            "sample": f"{calls} apply_constraints_a calls on this workload's state (oracle restatement, FP64, "
+                      "-O3 -ffast-math, 1 thread), the RATTLE pass alone"}
+
+
+def e2e_rate(g, torch, steps, units_per_step):
+    """The metric through the C ABI with FP64 host arrays (pinned) copied in
+    and out every step, and the energies read back. Returns (rate, h2d bytes
+    per step, d2h bytes per step)."""
+    import ctypes as C
+    from sucrose_gb300 import capi
+    n = g.n
+    pin = lambda: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    host = [pin() for _ in range(13)]
+    rr, qq, vv, ll = g.download()
+    for k in range(3):
+        host[k][:] = rr[:, k]
+        host[7 + k][:] = vv[:, k]
+        host[10 + k][:] = ll[:, k]
+    for k in range(4):
+        host[3 + k][:] = qq[:, k]
+    D = C.POINTER(C.c_double)
+    ptrs = [h.ctypes.data_as(D) for h in host]
+    energies = np.zeros(4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        capi.check(g.ctx, g.L.sg_upload_state(g.ctx, *ptrs))
+        g.step(1)
+        capi.check(g.ctx, g.L.sg_download_state(g.ctx, *ptrs))
+        capi.check(g.ctx, g.L.sg_read_energies(g.ctx, energies.ctypes.data_as(D)))
+    t = time.perf_counter() - t0
+    return units_per_step * steps / t, 13 * 8 * n, 13 * 8 * n + 32
 
 
 def charged_cpu_sample(g, charge, seconds, nthreads):
@@ -685,6 +859,44 @@ def run_reference_charged(a):
                              "sample": f"{per_step} pairs per step of the {len(pi)}-pair list; the reference "
                                        "coulombic_ (FP64) restated in C++, OpenMP"},
             "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_constrained(a):
+    """Reference arm for the molecular workloads: the restated
+    apply_constraints_a (one global Gauss-Seidel loop, FP64) on the lattice
+    state after one drift, each step one call."""
+    import oracle as O
+    from sucrose_gb300 import configs
+    w = MOLECULAR[a.config]
+    r, box, bbi, bbj, ln, terms = molecular_state(a.config, w["seed"])
+    n = len(r)
+    v = configs.velocities_to_temperature(n, w["T"], w["seed"])
+    s = O.System(n, box, fast=True)
+    s.set_constraints(bbi, bbj, ln)
+
+    def one():
+        s.rx[:], s.ry[:], s.rz[:] = r.T
+        s.vx[:], s.vy[:], s.vz[:] = v.T
+        s.constraints_save()
+        s.vv_initial(w["dt"])
+        t0 = time.perf_counter()
+        s.constraints_a(w["dt"])
+        return time.perf_counter() - t0
+
+    for _ in range(a.warmup):
+        one()
+    dt = sum(one() for _ in range(a.steps))
+    value = len(bbi) * a.steps / dt
+    line = {"impl": "reference", "metric": w["metric"],
+            "value": value, "unit": "constraint-solves/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * dt / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64", "data": "synthetic (seeded molecule lattice)",
+            "config": {"workload": w["workload"], "n": n, "constraints": int(len(bbi))},
+            "cpu_baseline": {"value": value, "unit": "constraint-solves/s", "cores": 1, "kind": "port",
+                             "sample": "apply_constraints_a alone per step (the reference's loop is serial), "
+                                       "FP64 restatement; favours the CPU (no forces, no pass b)"},
+            "e2e": {"value": value, "unit": "constraint-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -1002,6 +1214,8 @@ def run_reference(a):
         return run_reference_replicas(a)
     if a.config == "charged":
         return run_reference_charged(a)
+    if a.config in ("constrained", "polymer"):
+        return run_reference_constrained(a)
     import oracle as O
     from scipy.spatial import cKDTree
     from sucrose_gb300 import configs
@@ -1053,5 +1267,7 @@ if __name__ == "__main__":
         run_replicas(args)
     elif args.config == "charged":
         run_charged(args)
+    elif args.config in ("constrained", "polymer"):
+        run_constrained(args)
     else:
         run_ours(args)

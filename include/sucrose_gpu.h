@@ -224,6 +224,26 @@ int sg_nht_state(sg_ctx* ctx, double* get12, const double* set12);
  * joins the virial when it is not negative (:732-736). */
 int sg_thermo(sg_ctx* ctx, int32_t dof, double density, int32_t nrigid, double* out3);
 
+/* ---- bonded terms (module bonded, fortran/force.f90:2238-2581) ---------------- */
+typedef enum {
+    SG_BEND = 0,          /* bend_calculate_forces         fortran/force.f90:2244-2284 */
+    SG_DIH = 1,           /* dih_calculate_forces          fortran/force.f90:2286-2343 */
+    SG_COSINE_BEND = 2,   /* cosine_bend_calculate_forces  fortran/force.f90:2345-2390 */
+    SG_COSINE_DIH = 3,    /* cosine_dih_calculate_forces   fortran/force.f90:2392-2462 */
+    SG_ANGLE_BEND = 4,    /* angle_bend_calculate_forces   fortran/force.f90:2464-2506 */
+    SG_ANGLE_DIH = 5      /* angle_dih_calculate_forces    fortran/force.f90:2508-2579 */
+} sg_bonded_kind;
+/* Register the term list of one kind (replacing any earlier list of that kind):
+ * nterms terms of 3 (bends) or 4 (dihedrals) atoms, I J K [L] in the routine's
+ * argument order (one_based selects 1-based indices), coeff per term and, for
+ * the cosine_ and angle_ kinds, angle per term in degrees (NULL otherwise). */
+int sg_bonded_set(sg_ctx* ctx, int32_t kind, int32_t nterms, const int32_t* atoms, const double* coeff,
+                  const double* angle, int32_t one_based);
+/* The user's loop over that list: F(I) += FXI, F(J) += FXJ, F(K) += FXK
+ * [, F(L) += FXL], pot_eng += PE; *pot_eng (may be NULL) gets the energy. */
+int sg_bonded_forces(sg_ctx* ctx, int32_t kind, double* pot_eng);
+int sg_bonded_forces_async(sg_ctx* ctx, int32_t kind);
+
 /* ---- bond constraints (module constraints, fortran/system.f90:1055-1210) ------ */
 /* set_num_constraints + add_constraint for every bond (fortran/system.f90:97-108,
  * 345-360): atoms I, J (one_based selects 1-based indices) at fixed distance
@@ -304,6 +324,7 @@ typedef struct {
 } sg_step_config;
 #define SG_STEP_FLAT 1
 #define SG_STEP_REACTION_FIELD 2   /* eval_reaction_field after the pair stage (SG_DIPOLE) */
+#define SG_STEP_BONDED 8           /* every registered bonded list after the pair stage */
 #define SG_STEP_CONSTRAINTS 4      /* RATTLE around the integrator: RX_old saved before the initial half
                                       step, apply_constraints_a after it, apply_constraints_b after the
                                       final half step (vvc_, nhtc_, lgvc_ with the chosen integrator) */
@@ -324,9 +345,10 @@ int sg_step(sg_ctx* ctx, int32_t nsteps);
 /* Wait, then report list overflow (SG_ECAPACITY) or a non-finite energy (SG_ENAN). */
 int sg_step_check(sg_ctx* ctx);
 /* Run nsteps steps eagerly (not from the graph) with CUDA events between the
- * stages and return the mean milliseconds of: initial half step, list check
- * and rebuild, force zeroing, pair forces, final half step. */
-int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[5]);
+ * stages and return the mean milliseconds of: initial half step, constraints a,
+ * list check and rebuild, force zeroing, pair forces, final half step,
+ * constraints b (the constraint stages are 0 without SG_STEP_CONSTRAINTS). */
+int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[7]);
 /* Kernel launches in one captured step (after the first sg_step call). */
 int sg_step_kernel_count(sg_ctx* ctx, int64_t* count);
 

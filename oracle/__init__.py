@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # Pair kinds (shared numbering with the product's C-ABI)
 LJ, LJ12, LJW, WCA = 0, 1, 2, 3
 MORSE, DH, COULOMB, DIPOLE = 4, 5, 6, 7
+BEND, DIH, COSINE_BEND, COSINE_DIH, ANGLE_BEND, ANGLE_DIH = range(6)
 GB, GBR, GBW, GBC, GBWC = 10, 11, 12, 13, 14
 ECP, ECPR, ECPW, ECPC, ECPWC = 20, 21, 22, 23, 24
 SOLVER_BRENT, SOLVER_TIGHT, SOLVER_GIVEN = 0, 1, 2
@@ -81,6 +82,8 @@ def lib(fast=False):
         L.or_constraints_a.restype = C.c_int
         L.or_constraints_b.argtypes = [P, C.c_double]
         L.or_constraints_save.argtypes = [P]
+        L.or_bonded.argtypes = [P, C.c_int, _I, C.c_double, C.c_double, _D]
+        L.or_bonded_forces.argtypes = [P, C.c_int, C.c_int, _I, _D, _D]
         L.or_reaction_field_eval.argtypes = [P]
         L.or_set_velocity_to_temperature.argtypes = [P, C.c_double, C.c_int, C.c_int]
         L.or_generate_fcc.argtypes = [C.c_int, C.c_double] + [_D] * 7
@@ -266,6 +269,23 @@ class System:
 
     def constraints_b(self, dt):
         self.L.or_constraints_b(self.ptr(), dt)
+
+    # --- bonded terms (module bonded, force.f90:2238-2581) -------------------
+    def bonded(self, kind, atoms, coeff, angle=0.0):
+        """One term: (PE, F on each of its 3 or 4 atoms as an (4, 3) array)."""
+        at = np.ascontiguousarray(atoms, dtype=np.int32)
+        out = np.zeros(13)
+        self.L.or_bonded(self.ptr(), int(kind), iptr(at), float(coeff), float(angle), dptr(out))
+        return out[0], out[1:].reshape(4, 3)
+
+    def bonded_forces(self, kind, atoms, coeff, angle=None):
+        """The user's loop over a term list, accumulating into F and pot_eng."""
+        at = np.ascontiguousarray(atoms, dtype=np.int32)
+        nt = len(at)
+        c = np.ascontiguousarray(np.broadcast_to(np.asarray(coeff, dtype=np.float64), (nt,)))
+        a = None if angle is None else np.ascontiguousarray(np.broadcast_to(np.asarray(angle, dtype=np.float64),
+                                                                             (nt,)))
+        self.L.or_bonded_forces(self.ptr(), int(kind), nt, iptr(at), dptr(c), None if a is None else dptr(a))
 
     def reaction_field_init(self):
         self.L.or_reaction_field_init(self.ptr())

@@ -1041,6 +1041,107 @@ void or_reaction_field_init(OrSys* s) {
     s->rfl[0] = s->rfl[1] = s->rfl[2] = 0.0;
 }
 
+// ---------------------------------------------------------------- bonded -----
+// module bonded (force.f90:2238-2581). kind: 0 bend, 1 dih, 2 cosine_bend,
+// 3 cosine_dih, 4 angle_bend, 5 angle_dih. atoms: I J K [L] 0-based. out:
+// PE, FXI, FXJ, FXK, FXL (13 doubles; FXL zero for three-body kinds).
+void or_bonded(const OrSys* s, int kind, const int* at, double coeff, double angle, double* out) {
+    const double PI_ = 3.1415926535897932384626433832795;
+    auto vec = [&](int a, int b, double v[3]) {   // r_b - r_a, minimum image
+        v[0] = s->rx[b] - s->rx[a];
+        v[1] = s->ry[b] - s->ry[a];
+        v[2] = s->rz[b] - s->rz[a];
+        min_image(v, s->box, s->periodic);
+    };
+    auto dot = [](const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    for (int k = 0; k < 13; ++k) out[k] = 0.0;
+    double* FI = out + 1;
+    double* FJ = out + 4;
+    double* FK = out + 7;
+    double* FL = out + 10;
+    double VI[3], VJ[3], VK[3];
+    vec(at[0], at[1], VI);
+    vec(at[1], at[2], VJ);
+    if (kind == 0 || kind == 2 || kind == 4) {   // bend family (:2244-2284, :2345-2390, :2464-2506)
+        const double C11 = dot(VI, VI), C12 = dot(VI, VJ), C22 = dot(VJ, VJ);
+        const double prefac = 1.0 / std::sqrt(C11 * C22);
+        const double fac = C12, fac1 = fac / C22, fac2 = fac / C11;
+        double strength = coeff;
+        if (kind == 0) {
+            out[0] = coeff * (1.0 - prefac * fac);
+        } else if (kind == 2) {
+            const double th0 = PI_ - (PI_ / 180.0) * angle;
+            const double c0 = std::cos(th0), c = prefac * fac;
+            strength = coeff * (c - c0);
+            out[0] = (coeff / 2.0) * (c - c0) * (c - c0);
+        } else {
+            const double th0 = PI_ - (PI_ / 180.0) * angle;
+            const double th = std::acos(prefac * fac);
+            strength = coeff * (th - th0) / std::sin(th);
+            out[0] = (coeff / 2.0) * (th - th0) * (th - th0);
+        }
+        for (int d = 0; d < 3; ++d) {
+            FK[d] = -strength * prefac * (fac1 * VJ[d] - VI[d]);
+            FJ[d] = strength * prefac * (fac1 * VJ[d] - fac2 * VI[d] + VJ[d] - VI[d]);
+            FI[d] = strength * prefac * (fac2 * VI[d] - VJ[d]);
+        }
+        return;
+    }
+    // dihedral family (:2286-2343, :2392-2462, :2508-2579)
+    vec(at[2], at[3], VK);
+    const double C11 = dot(VI, VI), C12 = dot(VI, VJ), C13 = dot(VI, VK);
+    const double C22 = dot(VJ, VJ), C23 = dot(VJ, VK), C33 = dot(VK, VK);
+    const double D12 = C11 * C22 - C12 * C12, D23 = C22 * C33 - C23 * C23;
+    const double prefac = 1.0 / std::sqrt(D23 * D12);
+    const double fac = C23 * C12 - C13 * C22, fac1 = fac / D23, fac2 = fac / D12;
+    double strength = coeff;
+    if (kind == 1) {
+        out[0] = coeff * (1.0 + prefac * fac);
+    } else {
+        const double x[3] = {VI[1] * VJ[2] - VI[2] * VJ[1], VI[2] * VJ[0] - VI[0] * VJ[2],
+                             VI[0] * VJ[1] - VI[1] * VJ[0]};
+        const double fac_sin = dot(x, VK);
+        const double ph0 = PI_ - (PI_ / 180.0) * angle;
+        const double cph = -prefac * fac;
+        const double sph = prefac * fac_sin * std::sqrt(dot(VJ, VJ));
+        if (kind == 3) {
+            const double c0 = std::cos(ph0), cs = std::cos(std::atan2(sph, cph));
+            strength = coeff * (cs - c0);
+            out[0] = (coeff / 2.0) * (cs - c0) * (cs - c0);
+        } else {
+            const double c0 = std::cos(ph0), s0 = std::sin(ph0);
+            strength = coeff * (c0 - s0 * (cph / sph));
+            out[0] = coeff * (1.0 - cph * c0 - sph * s0);
+        }
+    }
+    const double a = -strength * prefac;
+    for (int d = 0; d < 3; ++d) {
+        FL[d] = a * (C12 * VJ[d] - C22 * VI[d] - fac1 * (C22 * VK[d] - C23 * VJ[d]));
+        FK[d] = a * (C12 * VK[d] - C12 * VJ[d] + C23 * VI[d] + C22 * VI[d] - 2.0 * C13 * VJ[d] -
+                     fac2 * (C11 * VJ[d] - C12 * VI[d]) - fac1 * (C33 * VJ[d] - C22 * VK[d] - C23 * VK[d] + C23 * VJ[d]));
+        FJ[d] = a * (-C12 * VK[d] + C23 * VJ[d] - C23 * VI[d] - C22 * VK[d] + 2.0 * C13 * VJ[d] -
+                     fac2 * (C22 * VI[d] - C11 * VJ[d] - C12 * VJ[d] + C12 * VI[d]) - fac1 * (-C33 * VJ[d] + C23 * VK[d]));
+        FI[d] = a * (-C23 * VJ[d] + C22 * VK[d] - fac2 * (-C22 * VI[d] + C12 * VJ[d]));
+    }
+}
+
+// The user's loop over a bonded term list: F(I) += FXI, F(J) += FXJ,
+// F(K) += FXK [, F(L) += FXL], pot_eng += PE. nat = 3 or 4 atoms per term.
+void or_bonded_forces(OrSys* s, int kind, int nterms, const int* atoms, const double* coeff, const double* angle) {
+    const int nat = (kind == 1 || kind == 3 || kind == 5) ? 4 : 3;
+    double out[13];
+    for (int t = 0; t < nterms; ++t) {
+        const int* at = atoms + (size_t)nat * t;
+        or_bonded(s, kind, at, coeff[t], angle ? angle[t] : 0.0, out);
+        s->pot_eng += out[0];
+        for (int a = 0; a < nat; ++a) {
+            s->fx[at[a]] += out[1 + 3 * a];
+            s->fy[at[a]] += out[2 + 3 * a];
+            s->fz[at[a]] += out[3 + 3 * a];
+        }
+    }
+}
+
 // eval_reaction_field (force.f90:2753-2766)
 void or_reaction_field_eval(OrSys* s) {
     const double* R = s->rfl;

@@ -40,6 +40,8 @@ INT_NVE, INT_LANGEVIN, INT_NH, INT_NH_REF = 0, 1, 2, 3
 STEP_FLAT = 1
 STEP_REACTION_FIELD = 2
 STEP_CONSTRAINTS = 4
+STEP_BONDED = 8
+BEND, DIH, COSINE_BEND, COSINE_DIH, ANGLE_BEND, ANGLE_DIH = range(6)
 
 
 class TuneResult(C.Structure):
@@ -99,6 +101,9 @@ SIGNATURES = [
     ("sg_nht_final", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, _D]),
     ("sg_nht_state", C.c_int, [_P, _D, _D]),
     ("sg_thermo", C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
+    ("sg_bonded_set", C.c_int, [_P, C.c_int32, C.c_int32, _I32, _D, _D, C.c_int32]),
+    ("sg_bonded_forces", C.c_int, [_P, C.c_int32, _D]),
+    ("sg_bonded_forces_async", C.c_int, [_P, C.c_int32]),
     ("sg_set_constraints", C.c_int, [_P, C.c_int32, _I32, _I32, _D, C.c_int32]),
     ("sg_constraints_save", C.c_int, [_P]),
     ("sg_constraints_a", C.c_int, [_P, C.c_double]),

@@ -38,14 +38,35 @@ ConGeo con_geo(const sg_ctx* ctx) {
 }
 
 struct ConArgs {
-    int nmol;
+    int nmol;                    // molecules this launch walks: ids list[0 .. nmol)
+    const int* __restrict__ list;
     const int2* __restrict__ ij;
     const float* __restrict__ len;
     const int* __restrict__ mol;
+    const int* __restrict__ atom_off;
+    const int* __restrict__ atoms;
+    const int2* __restrict__ loc;
     unsigned char* moved;
     int* err;
     unsigned long long* stats;   // [0] max sweeps a, [1] unconverged a, [2] corrections a, [3..5] the same for b
 };
+
+constexpr int kSmallAtoms = 16;   // molecules up to this size sweep in shared memory
+constexpr int kSmallBlock = 64;
+constexpr size_t kSmallSmem = (size_t)kSmallBlock * kSmallAtoms * (3 * sizeof(float4) + 1);
+
+// Per-thread counters summed over the warp, then one atomic per warp and
+// counter: tens of thousands of same-address atomics would serialise.
+SG_DEV void flush_stats(unsigned long long* st, unsigned sweeps, unsigned unconverged, unsigned corrections) {
+    const unsigned mx = __reduce_max_sync(0xffffffffu, sweeps);
+    const unsigned un = __reduce_add_sync(0xffffffffu, unconverged);
+    const unsigned co = __reduce_add_sync(0xffffffffu, corrections);
+    if ((threadIdx.x & 31) == 0) {
+        if (mx) atomicMax(&st[0], (unsigned long long)mx);
+        if (un) atomicAdd(&st[1], (unsigned long long)un);
+        if (co) atomicAdd(&st[2], (unsigned long long)co);
+    }
+}
 
 SG_DEV void add3(float4& a, float s, float3 d) {
     a.x += s * d.x;
@@ -60,7 +81,9 @@ __global__ void k_rattle_a(ConArgs c, ConGeo g, float dt, float4* pos, float4* v
     double vir[1] = {0.0};
     const float inv_dt = 1.f / dt;
     const double inv_dt2 = 1.0 / ((double)dt * (double)dt);
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < c.nmol; m += gridDim.x * blockDim.x) {
+    unsigned t_sweeps = 0, t_unconverged = 0, t_corrections = 0;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < c.nmol; q += gridDim.x * blockDim.x) {
+        const int m = c.list[q];
         const int b = c.mol[m], e = c.mol[m + 1];
         for (int k = b; k < e; ++k) {
             c.moved[c.ij[k].x] = 1;
@@ -68,7 +91,6 @@ __global__ void k_rattle_a(ConArgs c, ConGeo g, float dt, float4* pos, float4* v
         }
         int sweep = 0;
         bool any = true, failed = false;
-        unsigned long long corrections = 0;
         while (any && sweep < kMaxRattle && !failed) {
             for (int k = b; k < e; ++k) {
                 const int i = c.ij[k].x, j = c.ij[k].y;
@@ -107,7 +129,7 @@ __global__ void k_rattle_a(ConArgs c, ConGeo g, float dt, float4* pos, float4* v
                     vel[j] = wj;
                     c.moved[i] = 1;
                     c.moved[j] = 1;
-                    ++corrections;
+                    ++t_corrections;
                 } else {
                     c.moved[i] = 0;
                     c.moved[j] = 0;
@@ -117,10 +139,10 @@ __global__ void k_rattle_a(ConArgs c, ConGeo g, float dt, float4* pos, float4* v
             any = false;
             for (int k = b; k < e && !any; ++k) any = c.moved[c.ij[k].x] || c.moved[c.ij[k].y];
         }
-        atomicMax(&c.stats[0], (unsigned long long)sweep);
-        if (any && !failed) atomicAdd(&c.stats[1], 1ull);
-        if (corrections) atomicAdd(&c.stats[2], corrections);
+        t_sweeps = max(t_sweeps, (unsigned)sweep);
+        if (any && !failed) ++t_unconverged;
     }
+    flush_stats(c.stats, t_sweeps, t_unconverged, t_corrections);
     block_reduce_finish<1>(vir, partials, done, vir_out);
 }
 
@@ -129,7 +151,9 @@ __global__ void k_rattle_b(ConArgs c, ConGeo g, float dt, const float4* __restri
                            double* partials, unsigned int* done, double* vir_out) {
     double vir[1] = {0.0};
     const double inv_dt = 1.0 / (double)dt;
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < c.nmol; m += gridDim.x * blockDim.x) {
+    unsigned t_sweeps = 0, t_unconverged = 0, t_corrections = 0;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < c.nmol; q += gridDim.x * blockDim.x) {
+        const int m = c.list[q];
         const int b = c.mol[m], e = c.mol[m + 1];
         for (int k = b; k < e; ++k) {
             c.moved[c.ij[k].x] = 1;
@@ -137,7 +161,6 @@ __global__ void k_rattle_b(ConArgs c, ConGeo g, float dt, const float4* __restri
         }
         int sweep = 0;
         bool any = true;
-        unsigned long long corrections = 0;
         while (any && sweep < kMaxRattle) {
             for (int k = b; k < e; ++k) {
                 const int i = c.ij[k].x, j = c.ij[k].y;
@@ -159,7 +182,7 @@ __global__ void k_rattle_b(ConArgs c, ConGeo g, float dt, const float4* __restri
                     vel[j] = wj;
                     c.moved[i] = 1;
                     c.moved[j] = 1;
-                    ++corrections;
+                    ++t_corrections;
                 } else {
                     c.moved[i] = 0;
                     c.moved[j] = 0;
@@ -169,16 +192,176 @@ __global__ void k_rattle_b(ConArgs c, ConGeo g, float dt, const float4* __restri
             any = false;
             for (int k = b; k < e && !any; ++k) any = c.moved[c.ij[k].x] || c.moved[c.ij[k].y];
         }
-        atomicMax(&c.stats[3], (unsigned long long)sweep);
-        if (any) atomicAdd(&c.stats[4], 1ull);
-        if (corrections) atomicAdd(&c.stats[5], corrections);
+        t_sweeps = max(t_sweeps, (unsigned)sweep);
+        if (any) ++t_unconverged;
     }
+    flush_stats(c.stats + 3, t_sweeps, t_unconverged, t_corrections);
     block_reduce_finish<1>(vir, partials, done, vir_out);
 }
 
-ConArgs con_args(sg_ctx* ctx) {
+// The same two passes for molecules of at most kSmallAtoms atoms: the
+// molecule's positions, start-of-step positions, velocities and moved flags
+// are staged in shared memory ([atom][thread], conflict-free), swept there with
+// the same visits and tests, and written back once. The sweeps' dependent
+// loads become shared-memory latencies instead of L2 round trips.
+__global__ void __launch_bounds__(kSmallBlock) k_rattle_a_small(ConArgs c, ConGeo g, float dt, float4* pos,
+                                                                 float4* vel, const float4* __restrict__ pos_old,
+                                                                 double* partials, unsigned int* done,
+                                                                 double* vir_out) {
+    extern __shared__ float4 sh[];
+    const int T = kSmallBlock, tid = threadIdx.x;
+    float4* P = sh;
+    float4* O = sh + kSmallAtoms * T;
+    float4* V = sh + 2 * kSmallAtoms * T;
+    unsigned char* M = reinterpret_cast<unsigned char*>(sh + 3 * kSmallAtoms * T);
+    double vir[1] = {0.0};
+    const float inv_dt = 1.f / dt;
+    const double inv_dt2 = 1.0 / ((double)dt * (double)dt);
+    unsigned t_sweeps = 0, t_unconverged = 0, t_corrections = 0;
+    for (int q = blockIdx.x * T + tid; q < c.nmol; q += gridDim.x * T) {
+        const int m = c.list[q];
+        const int a0 = c.atom_off[m], na = c.atom_off[m + 1] - a0;
+        for (int a = 0; a < na; ++a) {
+            const int id = c.atoms[a0 + a];
+            P[a * T + tid] = pos[id];
+            O[a * T + tid] = pos_old[id];
+            V[a * T + tid] = vel[id];
+            M[a * T + tid] = 1;
+        }
+        const int b = c.mol[m], e = c.mol[m + 1];
+        int sweep = 0;
+        bool any = true, failed = false;
+        while (any && sweep < kMaxRattle && !failed) {
+            for (int k = b; k < e; ++k) {
+                const int2 l = c.loc[k];
+                const int i = l.x * T + tid, j = l.y * T + tid;
+                if (!(M[i] || M[j])) continue;
+                const float len2 = c.len[k] * c.len[k];
+                const float4 pi = P[i], pj = P[j];
+                const float3 r = min_image(make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z), g.box, g.inv_box,
+                                           g.periodic);
+                const float chi = len2 - dot3(r, r);
+                if (fabsf(chi) > 2.f * kRtol * len2) {
+                    const float4 oi = O[i], oj = O[j];
+                    const float3 ro = min_image(make_float3(oi.x - oj.x, oi.y - oj.y, oi.z - oj.z), g.box,
+                                                g.inv_box, g.periodic);
+                    const float vdot = dot3(r, ro);
+                    if (vdot < kRtol * len2) {
+                        if (atomicCAS(&c.err[0], 0, k + 1) == 0) {
+                            c.err[1] = c.ij[k].x;
+                            c.err[2] = c.ij[k].y;
+                        }
+                        failed = true;
+                        break;
+                    }
+                    float4 wi = V[i], wj = V[j];
+                    const float imi = wi.w, imj = wj.w;
+                    const float L = chi / (2.f * vdot * (imi + imj));
+                    vir[0] += (double)L * (double)len2 * inv_dt2;
+                    float4 qi = pi, qj = pj;
+                    add3(qi, L * imi, ro);
+                    add3(qj, -(L * imj), ro);
+                    add3(wi, L * imi * inv_dt, ro);
+                    add3(wj, -(L * imj * inv_dt), ro);
+                    P[i] = qi;
+                    P[j] = qj;
+                    V[i] = wi;
+                    V[j] = wj;
+                    M[i] = 1;
+                    M[j] = 1;
+                    ++t_corrections;
+                } else {
+                    M[i] = 0;
+                    M[j] = 0;
+                }
+            }
+            ++sweep;
+            any = false;
+            for (int a = 0; a < na && !any; ++a) any = M[a * T + tid] != 0;
+        }
+        for (int a = 0; a < na; ++a) {
+            const int id = c.atoms[a0 + a];
+            pos[id] = P[a * T + tid];
+            vel[id] = V[a * T + tid];
+        }
+        t_sweeps = max(t_sweeps, (unsigned)sweep);
+        if (any && !failed) ++t_unconverged;
+    }
+    flush_stats(c.stats, t_sweeps, t_unconverged, t_corrections);
+    block_reduce_finish<1>(vir, partials, done, vir_out);
+}
+
+__global__ void __launch_bounds__(kSmallBlock) k_rattle_b_small(ConArgs c, ConGeo g, float dt,
+                                                                 const float4* __restrict__ pos, float4* vel,
+                                                                 double* partials, unsigned int* done,
+                                                                 double* vir_out) {
+    extern __shared__ float4 sh[];
+    const int T = kSmallBlock, tid = threadIdx.x;
+    float4* P = sh;
+    float4* V = sh + 2 * kSmallAtoms * T;
+    unsigned char* M = reinterpret_cast<unsigned char*>(sh + 3 * kSmallAtoms * T);
+    double vir[1] = {0.0};
+    const double inv_dt = 1.0 / (double)dt;
+    unsigned t_sweeps = 0, t_unconverged = 0, t_corrections = 0;
+    for (int q = blockIdx.x * T + tid; q < c.nmol; q += gridDim.x * T) {
+        const int m = c.list[q];
+        const int a0 = c.atom_off[m], na = c.atom_off[m + 1] - a0;
+        for (int a = 0; a < na; ++a) {
+            const int id = c.atoms[a0 + a];
+            P[a * T + tid] = pos[id];
+            V[a * T + tid] = vel[id];
+            M[a * T + tid] = 1;
+        }
+        const int b = c.mol[m], e = c.mol[m + 1];
+        int sweep = 0;
+        bool any = true;
+        while (any && sweep < kMaxRattle) {
+            for (int k = b; k < e; ++k) {
+                const int2 l = c.loc[k];
+                const int i = l.x * T + tid, j = l.y * T + tid;
+                if (!(M[i] || M[j])) continue;
+                const float len2 = c.len[k] * c.len[k];
+                const float4 pi = P[i], pj = P[j];
+                const float3 r = min_image(make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z), g.box, g.inv_box,
+                                           g.periodic);
+                float4 wi = V[i], wj = V[j];
+                const float3 v = make_float3(wi.x - wj.x, wi.y - wj.y, wi.z - wj.z);
+                const float imi = wi.w, imj = wj.w;
+                const float L = -dot3(r, v) / ((imi + imj) * len2);
+                if (fabsf(L) > kRtol) {
+                    vir[0] += (double)L * (double)len2 * inv_dt;
+                    add3(wi, L * imi, r);
+                    add3(wj, -(L * imj), r);
+                    V[i] = wi;
+                    V[j] = wj;
+                    M[i] = 1;
+                    M[j] = 1;
+                    ++t_corrections;
+                } else {
+                    M[i] = 0;
+                    M[j] = 0;
+                }
+            }
+            ++sweep;
+            any = false;
+            for (int a = 0; a < na && !any; ++a) any = M[a * T + tid] != 0;
+        }
+        for (int a = 0; a < na; ++a) vel[c.atoms[a0 + a]] = V[a * T + tid];
+        t_sweeps = max(t_sweeps, (unsigned)sweep);
+        if (any) ++t_unconverged;
+    }
+    flush_stats(c.stats + 3, t_sweeps, t_unconverged, t_corrections);
+    block_reduce_finish<1>(vir, partials, done, vir_out);
+}
+
+// small = true: the shared-memory molecules, else the large ones
+ConArgs con_args(sg_ctx* ctx, bool small) {
     ConArgs c;
-    c.nmol = ctx->con_nmol;
+    c.nmol = small ? ctx->con_nsmall : ctx->con_nlarge;
+    c.list = ctx->con_small + (small ? 0 : ctx->con_nsmall);
+    c.atom_off = ctx->con_atom_off;
+    c.atoms = ctx->con_atoms;
+    c.loc = ctx->con_loc;
     c.ij = ctx->con_ij;
     c.len = ctx->con_len;
     c.mol = ctx->con_mol;
@@ -188,9 +371,9 @@ ConArgs con_args(sg_ctx* ctx) {
     return c;
 }
 
-int con_grid(sg_ctx* ctx) {
-    // one thread per molecule; small blocks spread short molecules over the SMs
-    return std::max(1, std::min((ctx->con_nmol + 127) / 128, 8 * ctx->num_sms));
+int con_grid(sg_ctx* ctx, int nmol, int block) {
+    // one thread per molecule
+    return std::max(1, std::min((nmol + block - 1) / block, 8 * ctx->num_sms));
 }
 
 int need(sg_ctx* ctx) {
@@ -213,9 +396,14 @@ int check_failure(sg_ctx* ctx) {
 
 int sg_constraints_free(sg_ctx* ctx) {
     void* bufs[] = {ctx->con_ij, ctx->con_len, ctx->con_mol, ctx->con_moved, ctx->pos_old, ctx->con_err,
-                    ctx->con_stats};
+                    ctx->con_stats, ctx->con_small, ctx->con_atom_off, ctx->con_atoms, ctx->con_loc};
     for (void* b : bufs)
         if (b) cudaFree(b);
+    ctx->con_small = nullptr;
+    ctx->con_atom_off = nullptr;
+    ctx->con_atoms = nullptr;
+    ctx->con_loc = nullptr;
+    ctx->con_nsmall = ctx->con_nlarge = 0;
     ctx->con_ij = nullptr;
     ctx->con_len = nullptr;
     ctx->con_mol = nullptr;
@@ -277,6 +465,28 @@ int sg_set_constraints(sg_ctx* ctx, int32_t nc, const int32_t* bbi, const int32_
         ij[slot] = make_int2(I[k], J[k]);
         len[slot] = (float)length[k];
     }
+    // each molecule's atoms in order of first appearance, the constraints'
+    // atoms as indices into that list, and the small / large split
+    std::vector<int> atom_off(nmol + 1, 0), atoms, small, large;
+    std::vector<int2> loc(nc);
+    std::vector<int> local(n, -1);
+    atoms.reserve(2 * (size_t)nc);
+    for (int m = 0; m < nmol; ++m) {
+        atom_off[m] = (int)atoms.size();
+        for (int k = start[m]; k < start[m + 1]; ++k) {
+            for (int a : {ij[k].x, ij[k].y})
+                if (local[a] < 0) {
+                    local[a] = (int)atoms.size() - atom_off[m];
+                    atoms.push_back(a);
+                }
+            loc[k] = make_int2(local[ij[k].x], local[ij[k].y]);
+        }
+        for (int t = atom_off[m]; t < (int)atoms.size(); ++t) local[atoms[t]] = -1;
+        ((int)atoms.size() - atom_off[m] <= kSmallAtoms ? small : large).push_back(m);
+    }
+    atom_off[nmol] = (int)atoms.size();
+    const int nsmall = (int)small.size(), nlarge = (int)large.size();
+    small.insert(small.end(), large.begin(), large.end());
     sg_constraints_free(ctx);
     ctx->graph_epoch++;
     if (nc == 0) return SG_OK;
@@ -296,7 +506,22 @@ int sg_set_constraints(sg_ctx* ctx, int32_t nc, const int32_t* bbi, const int32_
                                  ctx->stream));
     SG_CUDA(ctx, cudaMemsetAsync(ctx->con_err, 0, sizeof(int) * 4, ctx->stream));
     SG_CUDA(ctx, cudaMemsetAsync(ctx->con_stats, 0, sizeof(unsigned long long) * 8, ctx->stream));
+    SG_CUDA(ctx, cudaMalloc(&ctx->con_small, sizeof(int) * nmol));
+    SG_CUDA(ctx, cudaMalloc(&ctx->con_atom_off, sizeof(int) * (nmol + 1)));
+    SG_CUDA(ctx, cudaMalloc(&ctx->con_atoms, sizeof(int) * atoms.size()));
+    SG_CUDA(ctx, cudaMalloc(&ctx->con_loc, sizeof(int2) * nc));
+    SG_CUDA(ctx, cudaMemcpyAsync(ctx->con_small, small.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(ctx->con_atom_off, atom_off.data(), sizeof(int) * (nmol + 1),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(ctx->con_atoms, atoms.data(), sizeof(int) * atoms.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    SG_CUDA(ctx, cudaMemcpyAsync(ctx->con_loc, loc.data(), sizeof(int2) * nc, cudaMemcpyHostToDevice, ctx->stream));
+    SG_CUDA(ctx, cudaFuncSetAttribute(k_rattle_a_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem));
+    SG_CUDA(ctx, cudaFuncSetAttribute(k_rattle_b_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->con_nsmall = nsmall;
+    ctx->con_nlarge = nlarge;
     ctx->con_n = nc;
     ctx->con_nmol = nmol;
     ctx->con_max_len = *std::max_element(count.begin(), count.end());
@@ -312,21 +537,41 @@ int sg_constraints_save(sg_ctx* ctx) {
 
 int sg_constraints_a(sg_ctx* ctx, double dt) {
     if (int rc = need(ctx)) return rc;
-    const int grid = con_grid(ctx);
-    if (int rc = sg_ensure_partials(ctx, grid)) return rc;
-    k_rattle_a<<<grid, 128, 0, ctx->stream>>>(con_args(ctx), con_geo(ctx), (float)dt, ctx->pos, ctx->vel,
-                                              ctx->pos_old, ctx->partials, ctx->done_counter, ctx->acc + 6);
-    SG_LAUNCH_CHECK(ctx, "k_rattle_a");
+    if (ctx->con_nsmall) {
+        const int grid = con_grid(ctx, ctx->con_nsmall, kSmallBlock);
+        if (int rc = sg_ensure_partials(ctx, grid)) return rc;
+        k_rattle_a_small<<<grid, kSmallBlock, kSmallSmem, ctx->stream>>>(
+            con_args(ctx, true), con_geo(ctx), (float)dt, ctx->pos, ctx->vel, ctx->pos_old, ctx->partials,
+            ctx->done_counter, ctx->acc + 6);
+        SG_LAUNCH_CHECK(ctx, "k_rattle_a_small");
+    }
+    if (ctx->con_nlarge) {
+        const int grid = con_grid(ctx, ctx->con_nlarge, 128);
+        if (int rc = sg_ensure_partials(ctx, grid)) return rc;
+        k_rattle_a<<<grid, 128, 0, ctx->stream>>>(con_args(ctx, false), con_geo(ctx), (float)dt, ctx->pos, ctx->vel,
+                                                  ctx->pos_old, ctx->partials, ctx->done_counter, ctx->acc + 6);
+        SG_LAUNCH_CHECK(ctx, "k_rattle_a");
+    }
     return SG_OK;
 }
 
 int sg_constraints_b(sg_ctx* ctx, double dt) {
     if (int rc = need(ctx)) return rc;
-    const int grid = con_grid(ctx);
-    if (int rc = sg_ensure_partials(ctx, grid)) return rc;
-    k_rattle_b<<<grid, 128, 0, ctx->stream>>>(con_args(ctx), con_geo(ctx), (float)dt, ctx->pos, ctx->vel,
-                                              ctx->partials, ctx->done_counter, ctx->acc + 6);
-    SG_LAUNCH_CHECK(ctx, "k_rattle_b");
+    if (ctx->con_nsmall) {
+        const int grid = con_grid(ctx, ctx->con_nsmall, kSmallBlock);
+        if (int rc = sg_ensure_partials(ctx, grid)) return rc;
+        k_rattle_b_small<<<grid, kSmallBlock, kSmallSmem, ctx->stream>>>(con_args(ctx, true), con_geo(ctx),
+                                                                         (float)dt, ctx->pos, ctx->vel, ctx->partials,
+                                                                         ctx->done_counter, ctx->acc + 6);
+        SG_LAUNCH_CHECK(ctx, "k_rattle_b_small");
+    }
+    if (ctx->con_nlarge) {
+        const int grid = con_grid(ctx, ctx->con_nlarge, 128);
+        if (int rc = sg_ensure_partials(ctx, grid)) return rc;
+        k_rattle_b<<<grid, 128, 0, ctx->stream>>>(con_args(ctx, false), con_geo(ctx), (float)dt, ctx->pos, ctx->vel,
+                                                  ctx->partials, ctx->done_counter, ctx->acc + 6);
+        SG_LAUNCH_CHECK(ctx, "k_rattle_b");
+    }
     return SG_OK;
 }
 

@@ -105,6 +105,7 @@ int sg_destroy(sg_ctx* ctx) {
     sg_nlist_free(ctx);
     sg_mlp_free(ctx);
     sg_constraints_free(ctx);
+    sg_bonded_free(ctx);
     void* bufs[] = {ctx->pos, ctx->quat, ctx->vel, ctx->angm, ctx->force, ctx->torque, ctx->shape, ctx->eshape,
                     ctx->inert, ctx->inert_inv, ctx->acc, ctx->partials, ctx->done_counter, ctx->stats, ctx->nh,
                     ctx->ecp_prep, ctx->ecp_prep64, ctx->ecp_lambda, ctx->mlp_w, ctx->mlp_wbf16, ctx->mlp_tc_err,

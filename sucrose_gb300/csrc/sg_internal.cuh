@@ -131,6 +131,12 @@ struct sg_ctx {
     int* rf_cnt = nullptr;
     double* rf_field = nullptr;      // RFL x, y, z (+ one spare)
 
+    // bonded term lists (sg_bonded_set), one per sg_bonded_kind: atoms
+    // (I, J, K, L or -1) and (coeff, cos theta0, sin theta0, theta0)
+    int bonded_n[6] = {0, 0, 0, 0, 0, 0};
+    int4* bonded_atoms[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    float4* bonded_par[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+
     // bond constraints (sg_set_constraints): constraints grouped by molecule
     // (connected component), each group in the reference's list order
     int con_n = 0;                   // NC
@@ -140,6 +146,13 @@ struct sg_ctx {
     float* con_len = nullptr;
     int* con_mol = nullptr;          // nmol + 1 offsets into con_ij
     unsigned char* con_moved = nullptr;   // per particle
+    // molecules of at most 16 atoms run from shared memory: their atoms
+    // (atom_off / atoms) and each constraint's atoms as local indices
+    int con_nsmall = 0, con_nlarge = 0;
+    int* con_small = nullptr;        // molecule ids, then the large ones (nmol in all)
+    int* con_atom_off = nullptr;     // nmol + 1
+    int* con_atoms = nullptr;
+    int2* con_loc = nullptr;         // per constraint, local atom indices
     float4* pos_old = nullptr;       // RX_old .. RZ_old
     int* con_err = nullptr;          // [0] 1 + first failing constraint, [1] I, [2] J
     unsigned long long* con_stats = nullptr;   // see sg_constraint_stats
@@ -327,6 +340,7 @@ int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_elec(sg_ctx* ctx, const sg_pair_params* p);
 int sg_reaction_field_eval_async(sg_ctx* ctx);
 int sg_constraints_free(sg_ctx* ctx);
+void sg_bonded_free(sg_ctx* ctx);
 int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p);
 int sg_nlist_free(sg_ctx* ctx);

@@ -81,15 +81,18 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
             break;
         default: rc = sg_fail(ctx, SG_EINVAL, "unknown integrator %d", c.integrator);
     }
-    if (!rc && con) rc = sg_constraints_a(ctx, dt);
     if (ev) cudaEventRecord(ev[1], ctx->stream);
-    if (!rc) rc = enqueue_list_update(ctx, (c.flags & SG_STEP_FLAT) != 0);
+    if (!rc && con) rc = sg_constraints_a(ctx, dt);
     if (ev) cudaEventRecord(ev[2], ctx->stream);
-    if (!rc) rc = sg_zero_forces(ctx);
+    if (!rc) rc = enqueue_list_update(ctx, (c.flags & SG_STEP_FLAT) != 0);
     if (ev) cudaEventRecord(ev[3], ctx->stream);
+    if (!rc) rc = sg_zero_forces(ctx);
+    if (ev) cudaEventRecord(ev[4], ctx->stream);
     for (int k = 0; !rc && k < ctx->step_npairs; ++k) rc = sg_pair_forces_async(ctx, &ctx->step_pairs[k]);
     if (!rc && (c.flags & SG_STEP_REACTION_FIELD)) rc = sg_reaction_field_eval_async(ctx);
-    if (ev) cudaEventRecord(ev[4], ctx->stream);
+    for (int k = 0; !rc && (c.flags & SG_STEP_BONDED) && k < 6; ++k)
+        if (ctx->bonded_n[k]) rc = sg_bonded_forces_async(ctx, k);
+    if (ev) cudaEventRecord(ev[5], ctx->stream);
     if (!rc) {
         switch (c.integrator) {
             case SG_INT_NVE: rc = sg_vv_final(ctx, dt, nullptr); if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr); break;
@@ -100,8 +103,9 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
                 if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr);
         }
     }
+    if (ev) cudaEventRecord(ev[6], ctx->stream);
     if (!rc && con) rc = sg_constraints_b(ctx, dt);
-    if (ev) cudaEventRecord(ev[5], ctx->stream);
+    if (ev) cudaEventRecord(ev[7], ctx->stream);
     if (!rc) {
         k_step_incr<<<1, 1, 0, ctx->stream>>>(ctx->step_dev);
         cudaError_t e = cudaGetLastError();
@@ -189,21 +193,21 @@ int sg_step(sg_ctx* ctx, int32_t nsteps) {
     return SG_OK;
 }
 
-int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[5]) {
+int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[7]) {
     if (!ctx || !out_ms || nsteps < 1) return SG_EINVAL;
     if (!ctx->step_ready) return sg_fail(ctx, SG_ENOTREADY, "sg_step_configure must precede sg_step_stage_times");
     const sg_step_config& c = *reinterpret_cast<const sg_step_config*>(ctx->step_cfg);
-    std::vector<cudaEvent_t> ev(6 * (size_t)nsteps);
+    std::vector<cudaEvent_t> ev(8 * (size_t)nsteps);
     for (auto& e : ev) SG_CUDA(ctx, cudaEventCreate(&e));
     int rc = SG_OK;
-    for (int s = 0; s < nsteps && !rc; ++s) rc = enqueue_step(ctx, c, ev.data() + 6 * s);
+    for (int s = 0; s < nsteps && !rc; ++s) rc = enqueue_step(ctx, c, ev.data() + 8 * s);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    for (int k = 0; k < 5; ++k) out_ms[k] = 0.0;
+    for (int k = 0; k < 7; ++k) out_ms[k] = 0.0;
     if (!rc && e == cudaSuccess) {
         for (int s = 0; s < nsteps; ++s)
-            for (int k = 0; k < 5; ++k) {
+            for (int k = 0; k < 7; ++k) {
                 float ms = 0.f;
-                cudaEventElapsedTime(&ms, ev[6 * s + k], ev[6 * s + k + 1]);
+                cudaEventElapsedTime(&ms, ev[8 * s + k], ev[8 * s + k + 1]);
                 out_ms[k] += ms / nsteps;
             }
     }

@@ -50,3 +50,28 @@ def molecular_mix(cells, spacing, seed, bond=1.0, kinds=("dimer", "trimer", "tri
         mol += [m] * (len(r) - base)
     return (np.array(r), box, np.array(bbi, dtype=np.int32), np.array(bbj, dtype=np.int32), np.array(ln),
             np.array(mol))
+
+
+def polymer_chains(counts, length, seed, bond=1.0, spacing=1.6, jitter=0.05):
+    """Planar zig-zag chains (bond angle 120 degrees, all-trans) of `length`
+    beads running along x, on a counts[1] x counts[2] grid in (y, z) and
+    counts[0] chains end to end along x, with seeded jitter. Returns r (n,3),
+    box (3,), bonds (nb,2), bends (na,3), dihedrals (nd,4), all 0-based."""
+    rng = np.random.default_rng(seed)
+    step_x = bond * np.cos(np.radians(30.0))
+    chain_x = length * step_x + spacing
+    box = np.array([counts[0] * chain_x, counts[1] * spacing, counts[2] * spacing])
+    r, bonds, bends, dihs = [], [], [], []
+    for a in range(counts[0]):
+        for b in range(counts[1]):
+            for c in range(counts[2]):
+                base = len(r)
+                for k in range(length):
+                    r.append([a * chain_x + k * step_x, b * spacing + (k % 2) * 0.5 * bond, c * spacing])
+                bonds += [[base + k, base + k + 1] for k in range(length - 1)]
+                bends += [[base + k, base + k + 1, base + k + 2] for k in range(length - 2)]
+                dihs += [[base + k, base + k + 1, base + k + 2, base + k + 3] for k in range(length - 3)]
+    r = np.array(r) - box / 2.0 + 0.25
+    r += jitter * np.clip(rng.normal(size=r.shape), -3, 3)
+    return (r, box, np.array(bonds, dtype=np.int32), np.array(bends, dtype=np.int32),
+            np.array(dihs, dtype=np.int32))

@@ -314,6 +314,22 @@ class GpuSystem:
         self._c(self.L.sg_nht_state(self.ctx, _dp(out), _dp(s)))
         return out
 
+    # ---- bonded terms -----------------------------------------------------------------
+    def bonded_set(self, kind, atoms, coeff, angle=None, one_based=False):
+        """Register the term list of one bonded kind: atoms (nterms, 3|4)."""
+        at = np.ascontiguousarray(atoms, dtype=np.int32)
+        nt = len(at)
+        c = np.ascontiguousarray(np.broadcast_to(np.asarray(coeff, dtype=np.float64), (nt,)))
+        a = None if angle is None else np.ascontiguousarray(np.broadcast_to(np.asarray(angle, dtype=np.float64),
+                                                                             (nt,)))
+        self._c(self.L.sg_bonded_set(self.ctx, int(kind), nt, at.ctypes.data_as(C.POINTER(C.c_int32)), _dp(c),
+                                     _dp(a), 1 if one_based else 0))
+
+    def bonded_forces(self, kind):
+        e = C.c_double(0.0)
+        self._c(self.L.sg_bonded_forces(self.ctx, int(kind), C.byref(e)))
+        return e.value
+
     # ---- bond constraints -------------------------------------------------------------
     def set_constraints(self, bbi, bbj, length, one_based=False):
         """set_num_constraints + add_constraint for every bond."""
@@ -413,11 +429,12 @@ class GpuSystem:
         self._c(self.L.sg_step(self.ctx, int(nsteps)))
 
     def step_stage_times(self, nsteps=10):
-        """Mean ms per stage of nsteps eager steps: initial half step, list,
-        zero forces, pairs, final half step."""
-        out = np.zeros(5)
+        """Mean ms per stage of nsteps eager steps: initial half step,
+        constraints a, list, zero forces, pairs, final half step, constraints b."""
+        out = np.zeros(7)
         self._c(self.L.sg_step_stage_times(self.ctx, int(nsteps), _dp(out)))
-        return dict(zip(("initial", "list", "zero_forces", "pairs", "final"), out.tolist()))
+        return dict(zip(("initial", "constraints_a", "list", "zero_forces", "pairs", "final", "constraints_b"),
+                        out.tolist()))
 
     def step_check(self):
         self._c(self.L.sg_step_check(self.ctx))

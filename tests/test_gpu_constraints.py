@@ -173,3 +173,35 @@ def test_constraint_failure_is_reported(lib):
     assert e.value.code == capi.SG_ENOCONV
     g.constraints_clear_error()
     g.constraints_check()
+
+
+@pytest.mark.parametrize("length", [10, 24])
+def test_chains_small_and_large_paths(lib, length):
+    # chains of 10 atoms sweep in shared memory, chains of 24 in global memory
+    from sucrose_gb300.molecules import polymer_chains
+    r, box, bonds, bends, dihs = polymer_chains((1, 3, 3), length, 5, jitter=0.05)
+    n = len(r)
+    v = np.random.default_rng(length).normal(size=(n, 3))
+    P = Pair(r, None, box, v=v)
+    ln = np.ones(len(bonds))
+    P.g.set_constraints(bonds[:, 0], bonds[:, 1], ln)
+    P.o.set_constraints(bonds[:, 0], bonds[:, 1], ln)
+    dt = 0.004
+    for _ in range(3):
+        sync_oracle_to_gpu(P)
+        P.g.vvc_initial(dt)
+        P.o.constraints_save()
+        P.o.vv_initial(dt)
+        assert P.o.constraints_a(dt) == 0
+        r1, v1, ro, vo = pos_vel(P)
+        dr = r1 - ro
+        dr -= P.box * np.round(dr / P.box)
+        assert np.max(np.abs(dr)) < 3e-5
+        assert rel(v1, vo) < 2e-3
+        P.g.vvc_final(dt)
+        P.o.vv_final(dt)
+        P.o.constraints_b(dt)
+        r1, v1, ro, vo = pos_vel(P)
+        assert rel(v1, vo) < 2e-3
+    st = P.g.constraint_stats()
+    assert st["unconverged_a"] == 0 and st["corrections_a"] > 0
