@@ -570,6 +570,17 @@ def run_charged(a):
                        "min_dram_gbs": by / t / 1e9, "min_dram_frac": (by / t / 1e9 / hbm) if hbm else None}
     c = kinds["COULOMB"]
 
+    # Monte Carlo barostat (mc_barostat) with the step's two pair sets: one
+    # trial move = two energy evaluations + scaling + restore, host-driven
+    accepted = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nb = 10
+    for k in range(nb):
+        acc_k, _ = g.mc_barostat(sets, target_pressure=0.5, temperature=w["T"], max_dv=0.002, counter=k)
+        accepted += acc_k == 1
+    baro_ms = 1e3 * (time.perf_counter() - t0) / nb
+
     e2e_value, h2d, d2h = e2e_rate(g, torch, max(10, a.steps // 4), evals_per_step)
 
     cpu = None
@@ -600,6 +611,8 @@ def run_charged(a):
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "kinds_alone": kinds,
+            "mc_barostat": {"ms_per_trial_move": baro_ms, "accepted": int(accepted), "moves": nb,
+                            "note": "host wall time per call: two energy passes over both pair sets"},
             "list_rebuilds_in_timed_region": int(builds),
             "autotune": [{"block": t.block, "filter": t.filter} for t in tunes],
         }

@@ -111,7 +111,9 @@ const char* sg_last_error(const sg_ctx* ctx);
 void* sg_stream(sg_ctx* ctx);
 int sg_synchronize(sg_ctx* ctx);
 
-/* set_box / set_periodic_boundary (fortran/system.f90:185-213) */
+/* set_box / set_periodic_boundary (fortran/system.f90:185-213). On a context
+ * with a list, the cell grid follows the new box (the pair list itself waits
+ * for the next rebuild, as the reference's does); captured steps re-capture. */
 int sg_set_box(sg_ctx* ctx, const double box[3], int32_t periodic);
 
 /* Per-particle constants: mass, shape (sig_*), energy scales (eps_*) and
@@ -223,6 +225,21 @@ int sg_nht_state(sg_ctx* ctx, double* get12, const double* set12);
  * With constraints set, virial_bonded (reset by sg_zero_forces, like initialize_forces)
  * joins the virial when it is not negative (:732-736). */
 int sg_thermo(sg_ctx* ctx, int32_t dof, double density, int32_t nrigid, double* out3);
+
+/* ---- Monte Carlo barostat (fortran/integrators.f90:858-945) --------------------- */
+/* mc_barostat(compute_potential, accept, volume_change): one trial volume move.
+ * compute_potential is the sum of the npairs pair sets (plus every registered
+ * bonded list when include_bonded = 1) evaluated by this context's kernels;
+ * beta = 1 / temperature (the reference uses the last calculate_thermo's
+ * temperature); max_dv <= 0 selects 0.01. random_number is replaced by two
+ * Philox words of counter (counter lo, counter hi, 0x4D43, 0) under key (NULL:
+ * the reference key). Positions (atoms, not molecules) and the box are scaled
+ * by (V_new / V_old)^(1/3) and restored on rejection; forces, torques and the
+ * energy accumulators are left as they were. *accept = 1 accepted, 0 rejected,
+ * -1 no move (V_new <= 0, where the reference leaves accept unset). Waits. */
+int sg_mc_barostat(sg_ctx* ctx, const sg_pair_params* pairs, int32_t npairs, int32_t include_bonded,
+                   double target_pressure, double temperature, double max_dv, const uint32_t key[2],
+                   uint64_t counter, int32_t* accept, double* volume_out);
 
 /* ---- bonded terms (module bonded, fortran/force.f90:2238-2581) ---------------- */
 typedef enum {

@@ -83,6 +83,9 @@ def lib(fast=False):
         L.or_constraints_b.argtypes = [P, C.c_double]
         L.or_constraints_save.argtypes = [P]
         L.or_bonded.argtypes = [P, C.c_int, _I, C.c_double, C.c_double, _D]
+        L.or_mc_barostat.argtypes = [P, C.POINTER(OrPairParams), C.c_int, C.c_int, _I, _I, C.c_double, C.c_double,
+                                     C.c_double, _U, C.c_ulonglong, _D]
+        L.or_mc_barostat.restype = C.c_int
         L.or_bonded_forces.argtypes = [P, C.c_int, C.c_int, _I, _D, _D]
         L.or_reaction_field_eval.argtypes = [P]
         L.or_set_velocity_to_temperature.argtypes = [P, C.c_double, C.c_int, C.c_int]
@@ -269,6 +272,19 @@ class System:
 
     def constraints_b(self, dt):
         self.L.or_constraints_b(self.ptr(), dt)
+
+    # --- Monte Carlo barostat (integrators.f90:858-945) ---------------------
+    def mc_barostat(self, sets, pi, pj, target_pressure, temperature, max_dv=0.01, key=None, counter=0):
+        """One trial move; returns (accept, U_old, U_new, V_new)."""
+        arr = (OrPairParams * len(sets))(*sets)
+        pi = np.ascontiguousarray(pi, dtype=np.int32)
+        pj = np.ascontiguousarray(pj, dtype=np.int32)
+        k = None if key is None else np.ascontiguousarray(key, dtype=np.uint32)
+        u = np.zeros(3)
+        a = self.L.or_mc_barostat(self.ptr(), arr, len(sets), len(pi), iptr(pi), iptr(pj), float(target_pressure),
+                                  float(temperature), float(max_dv), None if k is None else uptr(k), int(counter),
+                                  dptr(u))
+        return a, u[0], u[1], u[2]
 
     # --- bonded terms (module bonded, force.f90:2238-2581) -------------------
     def bonded(self, kind, atoms, coeff, angle=0.0):

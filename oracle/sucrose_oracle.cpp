@@ -1035,6 +1035,75 @@ void or_forces(OrSys* s, const OrPairParams* pp, int npairs, const int* pi, cons
     }
 }
 
+// mc_barostat (integrators.f90:858-945) with compute_potential = the summed
+// energy of nsets pair parameter sets over the given pair list, and the two
+// random_number draws replaced by Philox words of counter (lo, hi, 0x4D43, 0)
+// under key. Forces and pot_eng are left as they were. Returns accept: 1, 0,
+// or -1 for no move (V_new <= 0).
+int or_mc_barostat(OrSys* s, const OrPairParams* sets, int nsets, int npairs, const int* pi, const int* pj,
+                   double target_pres, double temp, double max_dv, const uint32_t* key, unsigned long long counter,
+                   double* u_out) {
+    const int n = s->n;
+    std::vector<double> f(6 * (size_t)n), r(3 * (size_t)n);
+    double* F[6] = {s->fx, s->fy, s->fz, s->tx, s->ty, s->tz};
+    for (int k = 0; k < 6; ++k)
+        if (F[k]) std::memcpy(&f[(size_t)k * n], F[k], sizeof(double) * n);
+    const double pe_save = s->pot_eng;
+    auto potential = [&]() {
+        s->pot_eng = 0.0;
+        for (int k = 0; k < nsets; ++k) or_forces(s, &sets[k], npairs, pi, pj, 64, nullptr, nullptr, nullptr);
+        return s->pot_eng;
+    };
+    auto restore = [&]() {
+        for (int k = 0; k < 6; ++k)
+            if (F[k]) std::memcpy(F[k], &f[(size_t)k * n], sizeof(double) * n);
+        s->pot_eng = pe_save;
+    };
+    if (!(max_dv > 0.0)) max_dv = 0.01;
+    const double beta = 1.0 / temp;
+    const double L[3] = {s->box[0], s->box[1], s->box[2]};
+    const double V_old = L[0] * L[1] * L[2];
+    std::memcpy(&r[0], s->rx, sizeof(double) * n);
+    std::memcpy(&r[n], s->ry, sizeof(double) * n);
+    std::memcpy(&r[2 * (size_t)n], s->rz, sizeof(double) * n);
+    const double U_old = potential();
+    const uint32_t ctr[4] = {(uint32_t)counter, (uint32_t)(counter >> 32), 0x4D43u, 0u};
+    const uint32_t k0[2] = {PHILOX_KEY0, PHILOX_KEY1};
+    uint32_t w[4];
+    philox(ctr, key ? key : k0, w);
+    const double u1 = w[0] * (1.0 / 4294967296.0), u2 = w[1] * (1.0 / 4294967296.0);
+    const double V_new = V_old + max_dv * (2.0 * u1 - 1.0) * V_old;
+    if (u_out) { u_out[0] = U_old; u_out[1] = 0.0; u_out[2] = V_new; }
+    if (V_new <= 0.0) {
+        restore();
+        return -1;
+    }
+    const double scale = std::pow(V_new / V_old, 1.0 / 3.0);
+    for (int d = 0; d < 3; ++d) s->box[d] = L[d] * scale;
+    for (int i = 0; i < n; ++i) {
+        s->rx[i] = r[i] * scale;
+        s->ry[i] = r[n + i] * scale;
+        s->rz[i] = r[2 * (size_t)n + i] * scale;
+    }
+    const double U_new = potential();
+    if (u_out) u_out[1] = U_new;
+    const double dU = U_new - U_old;
+    const double exponent = -beta * dU - beta * target_pres * (V_new - V_old) + double(n) * std::log(V_new / V_old);
+    int accept;
+    if (std::log(u2) < exponent) {
+        accept = 1;
+        s->density = double(n) / (s->box[0] * s->box[1] * s->box[2]);
+    } else {
+        for (int d = 0; d < 3; ++d) s->box[d] = L[d];
+        std::memcpy(s->rx, &r[0], sizeof(double) * n);
+        std::memcpy(s->ry, &r[n], sizeof(double) * n);
+        std::memcpy(s->rz, &r[2 * (size_t)n], sizeof(double) * n);
+        accept = 0;
+    }
+    restore();
+    return accept;
+}
+
 // init_reaction_field (force.f90:2677-2685): DIP and RFL to zero.
 void or_reaction_field_init(OrSys* s) {
     for (int i = 0; i < s->n; ++i) s->dipx[i] = s->dipy[i] = s->dipz[i] = 0.0;

@@ -101,6 +101,8 @@ SIGNATURES = [
     ("sg_nht_final", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, _D]),
     ("sg_nht_state", C.c_int, [_P, _D, _D]),
     ("sg_thermo", C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
+    ("sg_mc_barostat", C.c_int, [_P, C.POINTER(PairParams), C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                 C.c_double, _U32, C.c_uint64, _I32, _D]),
     ("sg_bonded_set", C.c_int, [_P, C.c_int32, C.c_int32, _I32, _D, _D, C.c_int32]),
     ("sg_bonded_forces", C.c_int, [_P, C.c_int32, _D]),
     ("sg_bonded_forces_async", C.c_int, [_P, C.c_int32]),

@@ -199,7 +199,7 @@ __global__ void k_rattle_b(ConArgs c, ConGeo g, float dt, const float4* __restri
     block_reduce_finish<1>(vir, partials, done, vir_out);
 }
 
-// The same two passes for molecules of at most kSmallAtoms atoms: the
+// The same two passes for molecules of 3 to kSmallAtoms atoms: the
 // molecule's positions, start-of-step positions, velocities and moved flags
 // are staged in shared memory ([atom][thread], conflict-free), swept there with
 // the same visits and tests, and written back once. The sweeps' dependent
@@ -482,7 +482,10 @@ int sg_set_constraints(sg_ctx* ctx, int32_t nc, const int32_t* bbi, const int32_
             loc[k] = make_int2(local[ij[k].x], local[ij[k].y]);
         }
         for (int t = atom_off[m]; t < (int)atoms.size(); ++t) local[atoms[t]] = -1;
-        ((int)atoms.size() - atom_off[m] <= kSmallAtoms ? small : large).push_back(m);
+        // single bonds gain nothing from staging (two visits at most): they
+        // stay on the global-memory kernel with its larger blocks
+        const int na = (int)atoms.size() - atom_off[m];
+        (na >= 3 && na <= kSmallAtoms ? small : large).push_back(m);
     }
     atom_off[nmol] = (int)atoms.size();
     const int nsmall = (int)small.size(), nlarge = (int)large.size();

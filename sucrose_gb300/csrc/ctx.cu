@@ -140,7 +140,8 @@ int sg_set_box(sg_ctx* ctx, const double box[3], int32_t periodic) {
         if (!(box[d] > 0.0)) return sg_fail(ctx, SG_EINVAL, "box dimensions must be positive");
     for (int d = 0; d < 3; ++d) ctx->box[d] = box[d];
     ctx->periodic = periodic ? 1 : 0;
-    return SG_OK;
+    ctx->graph_epoch++;   // captured steps hold the box in their launch arguments
+    return sg_nlist_box_changed(ctx);
 }
 
 // FP64 SoA <-> float4 packing on the device. Host arrays are copied raw

@@ -678,6 +678,48 @@ int sg_nlist_free(sg_ctx* ctx) {
     return SG_OK;
 }
 
+// The box of a single-system context changed (sg_set_box, the barostat):
+// cells must stay at least one list radius wide. A shrinking box gets fewer
+// cells (within the allocated count); a growing one keeps its cells, which
+// are then wider than needed. Under three cells per side the build falls
+// back to the all-pairs rows. The current pair list is left as it is, as
+// the reference's list is: the next needs_rebuild decides.
+int sg_nlist_box_changed(sg_ctx* ctx) {
+    sg_nlist_state& nl = ctx->nl;
+    if (!nl.initialized || ctx->nrep) return SG_OK;
+    const double rskin = nl.cutoff + nl.skin;
+    int want[3];
+    bool cells = ctx->periodic != 0 && nl.ncells_cap > 1;
+    for (int d = 0; d < 3; ++d) {
+        want[d] = (int)std::floor(ctx->box[d] / (rskin * (1.0 + 1e-4)));
+        if (want[d] < 3) cells = false;
+    }
+    if (cells) {
+        const long long prod = (long long)want[0] * want[1] * want[2];
+        bool fits = prod <= nl.ncells_cap;
+        if (!fits) {   // grew: keep the current grid if its cells are still wide enough
+            fits = true;
+            for (int d = 0; d < 3; ++d) {
+                want[d] = nl.use_cells ? nl.ncell[d] : want[d];
+                if (ctx->box[d] / want[d] < rskin * (1.0 + 1e-4)) fits = false;
+            }
+            if (!nl.use_cells) fits = false;
+        }
+        cells = fits;
+    }
+    if (cells) {
+        for (int d = 0; d < 3; ++d) nl.ncell[d] = want[d];
+        nl.use_cells = 1;
+    } else {
+        nl.ncell[0] = nl.ncell[1] = nl.ncell[2] = 1;
+        nl.use_cells = 0;
+    }
+    nl.ncells = nl.ncell[0] * nl.ncell[1] * nl.ncell[2];
+    nl.dense_cells = nl.use_cells && ctx->n >= 12 * nl.ncells;
+    ctx->graph_epoch++;
+    return SG_OK;
+}
+
 extern "C" {
 
 static int alloc_list(sg_ctx* ctx, int max_nb);
@@ -726,6 +768,7 @@ static int alloc_list(sg_ctx* ctx, int max_nb) {
     sg_nlist_state& nl = ctx->nl;
     const int n = ctx->n;
     int ntiles = std::max((n + SCAN_TILE - 1) / SCAN_TILE, (nl.ncells + SCAN_TILE - 1) / SCAN_TILE) + 2;
+    nl.ncells_cap = nl.ncells;
     SG_CUDA(ctx, cudaMalloc(&nl.cell_count, sizeof(int) * (size_t)nl.ncells));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_start, sizeof(int) * ((size_t)nl.ncells + 1)));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_fill, sizeof(int) * (size_t)nl.ncells));

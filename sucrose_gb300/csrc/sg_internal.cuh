@@ -42,6 +42,7 @@ struct sg_nlist_state {
     int dense_cells = 0;             // >= 12 particles per cell: one warp per row in the search
     int ncell[3] = {0, 0, 0};
     int ncells = 0;
+    int ncells_cap = 0;              // cells the arrays were sized for
     int max_nb = 0;                  // capacity per particle (half list)
     int64_t pair_capacity = 0;       // capacity of the flattened list
     int* cell_count = nullptr;       // [ncells]
@@ -340,6 +341,7 @@ int sg_launch_pair_simple(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_elec(sg_ctx* ctx, const sg_pair_params* p);
 int sg_reaction_field_eval_async(sg_ctx* ctx);
 int sg_constraints_free(sg_ctx* ctx);
+int sg_nlist_box_changed(sg_ctx* ctx);   // cell grid for a new box (box scaling, barostat)
 void sg_bonded_free(sg_ctx* ctx);
 int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p);
 int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p);

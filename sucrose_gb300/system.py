@@ -314,6 +314,24 @@ class GpuSystem:
         self._c(self.L.sg_nht_state(self.ctx, _dp(out), _dp(s)))
         return out
 
+    # ---- Monte Carlo barostat -----------------------------------------------------------
+    def mc_barostat(self, pairs, target_pressure, temperature, max_dv=0.01, key=None, counter=0,
+                    include_bonded=False):
+        """One trial volume move; returns (accept: 1 / 0 / -1, volume)."""
+        arr = (PairParams * len(pairs))(*pairs)
+        k = None if key is None else np.asarray(key, dtype=np.uint32)
+        acc = C.c_int32(0)
+        vol = C.c_double(0.0)
+        self._c(self.L.sg_mc_barostat(self.ctx, arr, len(pairs), 1 if include_bonded else 0, float(target_pressure),
+                                      float(temperature), float(max_dv),
+                                      None if k is None else k.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                      int(counter), C.byref(acc), C.byref(vol)))
+        b = self.box
+        if acc.value == 1:
+            s = (vol.value / float(np.prod(b))) ** (1.0 / 3.0)
+            self.box = b * s
+        return acc.value, vol.value
+
     # ---- bonded terms -----------------------------------------------------------------
     def bonded_set(self, kind, atoms, coeff, angle=None, one_based=False):
         """Register the term list of one bonded kind: atoms (nterms, 3|4)."""
