@@ -226,6 +226,40 @@ int sg_nht_state(sg_ctx* ctx, double* get12, const double* set12);
  * joins the virial when it is not negative (:732-736). */
 int sg_thermo(sg_ctx* ctx, int32_t dof, double density, int32_t nrigid, double* out3);
 
+/* ---- reporters (fortran/reporters.f90) ------------------------------------------ */
+/* set_atom_type (fortran/system.f90:110-127) for every particle (NULL: all 0;
+ * negative types become 0 as initialize_system does). Used by the reporters. */
+int sg_set_types(sg_ctx* ctx, const int32_t* type);
+
+typedef struct sg_reporter sg_reporter;
+typedef enum {
+    SG_REPORT_STATE = 0,       /* state_data_reporter   reporters.f90:1-48    */
+    SG_REPORT_TRAJECTORY = 1,  /* trajectory_reporter   reporters.f90:50-101  */
+    SG_REPORT_CONFIG = 2,      /* config_reporter       reporters.f90:103-138 */
+    SG_REPORT_CHECKPOINT = 3   /* checkpoint_reporter   reporters.f90:140-231 */
+} sg_report_kind;
+/* open_*_file(unit, filename): the state-data kind writes its header line. */
+int sg_reporter_open(sg_ctx* ctx, int32_t kind, const char* path, sg_reporter** out);
+/* dof, density, Nrigid of calculate_thermo for the state-data kind. */
+int sg_reporter_set_thermo(sg_reporter* r, int32_t dof, double density, int32_t nrigid);
+/* report_*(unit, step): snapshots the device state at this point of the
+ * context stream and returns; a host thread formats and writes the record. */
+int sg_reporter_write(sg_reporter* r, int64_t step);
+/* Wait until every snapshot so far is written. */
+int sg_reporter_flush(sg_reporter* r);
+/* close_*_file: flush and close. */
+int sg_reporter_close(sg_reporter* r);
+/* load_checkpoint (reporters.f90:186-223): a new context from a checkpoint
+ * text file (atoms, masses, charges, shapes, energies, inertia, state, box,
+ * bonds as constraints); *out is set (and must be destroyed) whenever a
+ * context was created, also on a later error. */
+int sg_load_checkpoint(const char* path, int32_t device, sg_ctx** out, int64_t* config_index);
+/* Exact binary state (no counterpart in the reference): every particle array
+ * as stored on the device, box, thermostat chain, step counter, accumulators.
+ * Loading needs a context of the same particle count. */
+int sg_save_state(sg_ctx* ctx, const char* path);
+int sg_load_state(sg_ctx* ctx, const char* path);
+
 /* ---- Monte Carlo barostat (fortran/integrators.f90:858-945) --------------------- */
 /* mc_barostat(compute_potential, accept, volume_change): one trial volume move.
  * compute_potential is the sum of the npairs pair sets (plus every registered

@@ -41,6 +41,7 @@ STEP_FLAT = 1
 STEP_REACTION_FIELD = 2
 STEP_CONSTRAINTS = 4
 STEP_BONDED = 8
+REPORT_STATE, REPORT_TRAJECTORY, REPORT_CONFIG, REPORT_CHECKPOINT = range(4)
 BEND, DIH, COSINE_BEND, COSINE_DIH, ANGLE_BEND, ANGLE_DIH = range(6)
 
 
@@ -101,6 +102,15 @@ SIGNATURES = [
     ("sg_nht_final", C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32, _D]),
     ("sg_nht_state", C.c_int, [_P, _D, _D]),
     ("sg_thermo", C.c_int, [_P, C.c_int32, C.c_double, C.c_int32, _D]),
+    ("sg_set_types", C.c_int, [_P, _I32]),
+    ("sg_reporter_open", C.c_int, [_P, C.c_int32, C.c_char_p, C.POINTER(_P)]),
+    ("sg_reporter_set_thermo", C.c_int, [_P, C.c_int32, C.c_double, C.c_int32]),
+    ("sg_reporter_write", C.c_int, [_P, C.c_int64]),
+    ("sg_reporter_flush", C.c_int, [_P]),
+    ("sg_reporter_close", C.c_int, [_P]),
+    ("sg_load_checkpoint", C.c_int, [C.c_char_p, C.c_int32, C.POINTER(_P), _I64]),
+    ("sg_save_state", C.c_int, [_P, C.c_char_p]),
+    ("sg_load_state", C.c_int, [_P, C.c_char_p]),
     ("sg_mc_barostat", C.c_int, [_P, C.POINTER(PairParams), C.c_int32, C.c_int32, C.c_double, C.c_double,
                                  C.c_double, _U32, C.c_uint64, _I32, _D]),
     ("sg_bonded_set", C.c_int, [_P, C.c_int32, C.c_int32, _I32, _D, _D, C.c_int32]),

@@ -492,6 +492,9 @@ int sg_set_constraints(sg_ctx* ctx, int32_t nc, const int32_t* bbi, const int32_
     small.insert(small.end(), large.begin(), large.end());
     sg_constraints_free(ctx);
     ctx->graph_epoch++;
+    ctx->h_bbi = I;
+    ctx->h_bbj = J;
+    ctx->h_blen.assign(length, length + nc);
     if (nc == 0) return SG_OK;
     SG_CUDA(ctx, cudaMalloc(&ctx->con_ij, sizeof(int2) * nc));
     SG_CUDA(ctx, cudaMalloc(&ctx->con_len, sizeof(float) * nc));

@@ -138,6 +138,12 @@ struct sg_ctx {
     int4* bonded_atoms[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     float4* bonded_par[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 
+    // host copies for the reporters: atom types (set_atom_type) and the
+    // constraint list in its given order (0-based)
+    std::vector<int> h_types;
+    std::vector<int> h_bbi, h_bbj;
+    std::vector<double> h_blen;
+
     // bond constraints (sg_set_constraints): constraints grouped by molecule
     // (connected component), each group in the reference's list order
     int con_n = 0;                   // NC

@@ -314,6 +314,43 @@ class GpuSystem:
         self._c(self.L.sg_nht_state(self.ctx, _dp(out), _dp(s)))
         return out
 
+    # ---- reporters ---------------------------------------------------------------------
+    def set_types(self, types):
+        t = None if types is None else np.ascontiguousarray(np.broadcast_to(np.asarray(types, dtype=np.int32),
+                                                                             (self.n,)))
+        self._c(self.L.sg_set_types(self.ctx, None if t is None else t.ctypes.data_as(C.POINTER(C.c_int32))))
+
+    def reporter(self, kind, path, dof=None, density=None, nrigid=1):
+        """An asynchronous reporter (use as a context manager or close())."""
+        return Reporter(self, kind, path, dof, density, nrigid)
+
+    def save_state(self, path):
+        self._c(self.L.sg_save_state(self.ctx, str(path).encode()))
+
+    def load_state(self, path):
+        self._c(self.L.sg_load_state(self.ctx, str(path).encode()))
+
+    @classmethod
+    def load_checkpoint(cls, path, device=0):
+        """load_checkpoint: a new system from a checkpoint text file; returns
+        (system, config_index)."""
+        self = cls.__new__(cls)
+        self.L = capi.load()
+        ctx = C.c_void_p()
+        cfg = C.c_int64(0)
+        rc = self.L.sg_load_checkpoint(str(path).encode(), int(device), C.byref(ctx), C.byref(cfg))
+        self.ctx = ctx
+        if rc != 0 and not ctx.value:
+            raise capi.SgError(rc, f"cannot read checkpoint {path}")
+        check(ctx, rc)
+        with open(path) as f:
+            f.readline(); f.readline(); f.readline(); f.readline()
+            b = f.readline().split()[1:4]
+        self.n = int(open(path).readline().split()[1])
+        self.box = np.array([float(x) for x in b])
+        self.periodic = True
+        return self, cfg.value
+
     # ---- Monte Carlo barostat -----------------------------------------------------------
     def mc_barostat(self, pairs, target_pressure, temperature, max_dv=0.01, key=None, counter=0,
                     include_bonded=False):
@@ -496,3 +533,34 @@ class GpuSystem:
         w = np.zeros(n, dtype=np.float32)
         self._c(self.L.sg_mlp_get_weights(self.ctx, w.ctypes.data_as(C.POINTER(C.c_float)), n))
         return w
+
+
+class Reporter:
+    """sg_reporter: open_*_file / report_* / close_*_file of fortran/reporters.f90."""
+
+    def __init__(self, system, kind, path, dof=None, density=None, nrigid=1):
+        self.g = system
+        self.L = system.L
+        h = C.c_void_p()
+        system._c(self.L.sg_reporter_open(system.ctx, int(kind), str(path).encode(), C.byref(h)))
+        self.h = h
+        if dof is not None:
+            system._c(self.L.sg_reporter_set_thermo(h, int(dof), float(density or 0.0), int(nrigid)))
+
+    def write(self, step):
+        self.g._c(self.L.sg_reporter_write(self.h, int(step)))
+
+    def flush(self):
+        self.g._c(self.L.sg_reporter_flush(self.h))
+
+    def close(self):
+        if self.h:
+            rc = self.L.sg_reporter_close(self.h)
+            self.h = None
+            self.g._c(rc)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
