@@ -20,7 +20,10 @@ ROOT = os.path.dirname(HERE)
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no FMA contraction, so host arithmetic rounds as written (the
+# reporters' text must match other FP64 evaluations digit for digit)
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+         "-Xcompiler", "-ffp-contract=off",
          "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 

@@ -67,14 +67,15 @@ int sg_mc_barostat(sg_ctx* ctx, const sg_pair_params* pairs, int32_t npairs, int
     const int n = ctx->n;
     const size_t bytes = sizeof(float4) * (size_t)n;
     McScratch s;
-    SG_CUDA(ctx, cudaMalloc(&s.pos, 3 * bytes));
+    if (!ctx->mc_scratch) SG_CUDA(ctx, cudaMalloc(&ctx->mc_scratch, 3 * bytes));   // kept for later calls
+    s.pos = ctx->mc_scratch;
     s.force = s.pos + n;
     s.torque = s.pos + 2 * (size_t)n;
     double acc_save[8];
     auto copy = [&](float4* dst, const float4* src) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
     };
-    // restore forces, torques and the energy accumulators, wait, free the scratch
+    // restore forces, torques and the energy accumulators, then wait
     auto finish = [&](int rc) {
         cudaError_t e = copy(ctx->force, s.force);
         if (e == cudaSuccess) e = copy(ctx->torque, s.torque);
@@ -82,7 +83,6 @@ int sg_mc_barostat(sg_ctx* ctx, const sg_pair_params* pairs, int32_t npairs, int
             e = cudaMemcpyAsync(ctx->acc, acc_save, sizeof(acc_save), cudaMemcpyHostToDevice, ctx->stream);
         const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
         if (e == cudaSuccess) e = e2;
-        cudaFree(s.pos);
         if (rc == SG_OK && e != cudaSuccess) rc = sg_cuda_check(ctx, e, "sg_mc_barostat restore");
         return rc;
     };
@@ -91,10 +91,7 @@ int sg_mc_barostat(sg_ctx* ctx, const sg_pair_params* pairs, int32_t npairs, int
     if (e == cudaSuccess) e = copy(s.torque, ctx->torque);
     if (e == cudaSuccess) e = cudaMemcpyAsync(acc_save, ctx->acc, sizeof(acc_save), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) {
-        cudaFree(s.pos);
-        return sg_cuda_check(ctx, e, "sg_mc_barostat save");
-    }
+    if (e != cudaSuccess) return sg_cuda_check(ctx, e, "sg_mc_barostat save");
 
     const double beta = 1.0 / temperature;
     const double box_old[3] = {ctx->box[0], ctx->box[1], ctx->box[2]};

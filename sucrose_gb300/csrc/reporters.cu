@@ -12,6 +12,7 @@
 // form with d decimals (leading zero kept), I0 the shortest integer,
 // list-directed integers are right-justified in 12 columns, and nX spacing
 // after the last item of a record writes nothing.
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <condition_variable>
@@ -28,6 +29,36 @@ void put_f(std::string& s, double x, int d) {
     char b[64];
     std::snprintf(b, sizeof(b), "%.*f", d, x);
     s += b;
+}
+
+// F0.d of a value that came from FP32 (d <= 10): v * 10^d is exact in FP64
+// (24-bit mantissa times 5^d, at most 48 bits), so rounding it to the
+// nearest integer (ties to even, as printf does) gives printf's digits
+// without printf's cost. Anything outside the exact range goes to printf.
+void put_f32(std::string& s, float v, int d) {
+    static const double p10[11] = {1, 1e1, 1e2, 1e3, 1e4, 1e5, 1e6, 1e7, 1e8, 1e9, 1e10};
+    static const long long i10[11] = {1, 10, 100, 1000, 10000, 100000, 1000000, 10000000, 100000000,
+                                      1000000000, 10000000000LL};
+    const double q = (double)v * p10[d];
+    if (!(std::fabs(q) < 4.0e15)) {
+        put_f(s, v, d);
+        return;
+    }
+    const long long u = std::llabs((long long)std::nearbyint(q));
+    char b[48];
+    int k = 0;
+    long long ip = u / i10[d], fp = u % i10[d];
+    for (int j = 0; j < d; ++j) {   // fraction digits, low to high
+        b[k++] = (char)('0' + fp % 10);
+        fp /= 10;
+    }
+    if (d > 0) b[k++] = '.';
+    do {
+        b[k++] = (char)('0' + ip % 10);
+        ip /= 10;
+    } while (ip);
+    if (std::signbit(v)) b[k++] = '-';
+    while (k) s += b[--k];
 }
 void put_i(std::string& s, long long v) { s += std::to_string(v); }
 void put_list_int(std::string& s, long long v) {   // list-directed integer output
@@ -48,8 +79,30 @@ struct Rec {
     }
     Rec& i(long long v) { sep(); put_i(s, v); return *this; }
     Rec& f(double x, int d) { sep(); put_f(s, x, d); return *this; }
+    Rec& g(float x, int d) { sep(); put_f32(s, x, d); return *this; }
     void end() { s += '\n'; }
 };
+
+// Per-particle records formatted by up to 8 threads on contiguous ranges,
+// joined in order.
+template <class LineFn>
+void parallel_lines(int n, std::string& out, LineFn&& line) {
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int T = std::min(std::min(8, hw), std::max(1, n / 8192));
+    if (T <= 1) {
+        for (int i = 0; i < n; ++i) line(i, out);
+        return;
+    }
+    std::vector<std::string> parts(T);
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; ++t)
+        th.emplace_back([&, t] {
+            const int a = (int)((long long)n * t / T), b = (int)((long long)n * (t + 1) / T);
+            for (int i = a; i < b; ++i) line(i, parts[t]);
+        });
+    for (auto& x : th) x.join();
+    for (auto& p : parts) out += p;
+}
 
 // one snapshot of the device state, in pinned host memory
 enum { A_POS, A_VEL, A_QUAT, A_ANGM, A_FORCE, A_SHAPE, A_ESHAPE, A_INERT, A_N };
@@ -116,21 +169,21 @@ struct sg_reporter {
             out += "\nITEM: BOX BOUNDS pp pp pp\n";
             for (int d = 0; d < 3; ++d) Rec(out, true).f(-s.box[d] / 2.0, 3).f(s.box[d] / 2.0, 3).end();
             out += "ITEM: ATOMS id type shapex shapey shapez x y z vx vy vz fx fy fz quatw quati quatj quatk\n";
-            for (int i = 0; i < n; ++i) {
+            parallel_lines(n, out, [&](int i, std::string& o) {
                 const double w = Q[i].x, x = Q[i].y, y = Q[i].z, z = Q[i].w;
                 // the columns headed vx vy vz hold the body z axis (:82-84)
                 const double ux = 2.0 * (x * z + w * y), uy = 2.0 * (y * z - w * x), uz = w * w - x * x - y * y + z * z;
-                Rec r(out, true);
-                r.i(i + 1).i(types[i]).f(S[i].x, 3).f(S[i].y, 3).f(S[i].z, 3).f(P[i].x, 3).f(P[i].y, 3).f(P[i].z, 3);
-                r.f(ux, 3).f(uy, 3).f(uz, 3).f(F[i].x, 3).f(F[i].y, 3).f(F[i].z, 3);
-                r.f(w, 3).f(x, 3).f(y, 3).f(z, 3).end();
-            }
+                Rec r(o, true);
+                r.i(i + 1).i(types[i]).g(S[i].x, 3).g(S[i].y, 3).g(S[i].z, 3).g(P[i].x, 3).g(P[i].y, 3).g(P[i].z, 3);
+                r.f(ux, 3).f(uy, 3).f(uz, 3).g(F[i].x, 3).g(F[i].y, 3).g(F[i].z, 3);
+                r.g(Q[i].x, 3).g(Q[i].y, 3).g(Q[i].z, 3).g(Q[i].w, 3).end();
+            });
         } else if (kind == SG_REPORT_CONFIG) {   // report_confwriter (reporters.f90:120-129)
-            for (int i = 0; i < n; ++i) {
-                Rec r(out, false);
-                r.f(P[i].x, 3).f(P[i].y, 3).f(P[i].z, 3).f(V[i].x, 3).f(V[i].y, 3).f(V[i].z, 3);
-                r.f(L[i].x, 3).f(L[i].y, 3).f(L[i].z, 3).f(Q[i].x, 3).f(Q[i].y, 3).f(Q[i].z, 3).f(Q[i].w, 3).end();
-            }
+            parallel_lines(n, out, [&](int i, std::string& o) {
+                Rec r(o, false);
+                r.g(P[i].x, 3).g(P[i].y, 3).g(P[i].z, 3).g(V[i].x, 3).g(V[i].y, 3).g(V[i].z, 3);
+                r.g(L[i].x, 3).g(L[i].y, 3).g(L[i].z, 3).g(Q[i].x, 3).g(Q[i].y, 3).g(Q[i].z, 3).g(Q[i].w, 3).end();
+            });
         } else {   // report_checkpoint (reporters.f90:158-184)
             out += "ATOMS ";
             put_i(out, n);
@@ -140,19 +193,19 @@ struct sg_reporter {
             Rec(out, false).f(s.box[0], 10).f(s.box[1], 10).f(s.box[2], 10).end();
             out += "\nATOM: ID TYPE MASS CHARGE SHAPEX SHAPEY SHAPEZ ESHAPEX ESHAPEY ESHAPEZ IXX IYY IZZ RX RY RZ VX VY "
                    "VZ LX LY LZ QW QX QY QZ\n\n";
-            for (int i = 0; i < n; ++i) {
-                Rec r(out, true);
-                r.i(i + 1).i(types[i]).f(S[i].w, 10).f(P[i].w, 10).f(S[i].x, 10).f(S[i].y, 10).f(S[i].z, 10);
-                r.f(E[i].x, 10).f(E[i].y, 10).f(E[i].z, 10).f(I[i].x, 10).f(I[i].y, 10).f(I[i].z, 10);
-                r.f(P[i].x, 10).f(P[i].y, 10).f(P[i].z, 10).f(V[i].x, 10).f(V[i].y, 10).f(V[i].z, 10);
-                r.f(L[i].x, 10).f(L[i].y, 10).f(L[i].z, 10).f(Q[i].x, 10).f(Q[i].y, 10).f(Q[i].z, 10);
-                r.f(Q[i].w, 10).end();
-            }
+            parallel_lines(n, out, [&](int i, std::string& o) {
+                Rec r(o, true);
+                r.i(i + 1).i(types[i]).g(S[i].w, 10).g(P[i].w, 10).g(S[i].x, 10).g(S[i].y, 10).g(S[i].z, 10);
+                r.g(E[i].x, 10).g(E[i].y, 10).g(E[i].z, 10).g(I[i].x, 10).g(I[i].y, 10).g(I[i].z, 10);
+                r.g(P[i].x, 10).g(P[i].y, 10).g(P[i].z, 10).g(V[i].x, 10).g(V[i].y, 10).g(V[i].z, 10);
+                r.g(L[i].x, 10).g(L[i].y, 10).g(L[i].z, 10).g(Q[i].x, 10).g(Q[i].y, 10).g(Q[i].z, 10);
+                r.g(Q[i].w, 10).end();
+            });
             out += "\nBOND: ID I J LEN\n\n";
             for (size_t k = 0; k < bbi.size(); ++k)
                 Rec(out, true).i((long long)k + 1).i(bbi[k] + 1).i(bbj[k] + 1).f(blen[k], 10).end();
             out += "\n";
-            put_list_int(out, config_index);   // never advanced by the reference (:152, :182)
+            put_list_int(out, config_index);   // never advanced by the reference (:156, :184)
             out += "\n";
         }
     }

@@ -138,6 +138,8 @@ struct sg_ctx {
     int4* bonded_atoms[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     float4* bonded_par[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 
+    float4* mc_scratch = nullptr;    // barostat: saved positions, forces, torques (3 n)
+
     // host copies for the reporters: atom types (set_atom_type) and the
     // constraint list in its given order (0-based)
     std::vector<int> h_types;
