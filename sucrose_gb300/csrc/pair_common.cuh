@@ -350,6 +350,15 @@ SG_DEV float3 pair_rij_precise(const float4* __restrict__ pos, int i, int j, con
                        min_image_precise(a.z, c.z, L.z, iL.z, lo.z, per));
 }
 
+// Reciprocal by the approximate instruction (at most 1 ulp from 1/x for
+// normal x, PTX rcp.approx.ftz.f32): a division costs a dozen instructions,
+// this one. Used where a 1-ulp quotient is far inside the force tolerance.
+SG_DEV float fast_rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 SG_DEV float ipowf(float x, int n) {
     float r = 1.f;
     for (int k = 0; k < n; ++k) r *= x;

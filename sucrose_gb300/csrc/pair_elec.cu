@@ -52,18 +52,18 @@ struct PotElec {
             const float e = expf(-width * (rmag - rmin));
             const float om = 1.f - e;
             o.pe = dissoc * (om * om - 1.f) - pot_cut;
-            const float c = -2.f * width * dissoc * om * e / rmag;
+            const float c = -2.f * width * dissoc * om * e * fast_rcp(rmag);
             o.f = c * r;
             o.vir = c * rsq;
         } else if (kind == SG_DH) {                  // force.f90:2609-2615
-            const float pe = qq * kq * expf(-rmag * inv_db) / rmag;
-            const float c = pe * (1.f + rmag * inv_db) / rsq;
+            const float pe = qq * kq * expf(-rmag * inv_db) * fast_rcp(rmag);
+            const float c = pe * (1.f + rmag * inv_db) * fast_rcp(rsq);
             o.pe = pe;
             o.f = c * r;
             o.vir = c * rsq;
         } else {                                     // SG_COULOMB, force.f90:2643-2663
-            float pe = qq * kq / rmag;
-            float3 f = (pe / rsq) * r;
+            float pe = qq * kq * fast_rcp(rmag);
+            float3 f = (pe * fast_rcp(rsq)) * r;
             if (rmag >= sw) {
                 // the reference's quintic switch S(x) = 1 - 10x^3 + 15x^4 - 6x^5 and
                 // its derivative, in the factored forms (1-x)^3 (1 + 3x + 6x^2) and
@@ -115,8 +115,8 @@ struct PotDipole {
         const float3 u1 = a.w * body_z(quat[i]);
         const float3 u2 = c.w * body_z(quat[j]);
         const float ci = dot3(u1, r), cj = dot3(u2, r), cij = dot3(u1, u2);
-        const float inv2 = 1.f / rsq;
-        const float inv3 = inv2 / rmag;
+        const float inv2 = fast_rcp(rsq);
+        const float inv3 = inv2 * fast_rcp(rmag);
         const float inv5 = inv3 * inv2;
         const float3 term1 = (cij - 5.f * ci * cj * inv2) * r + cj * u1 + ci * u2;
         const float3 term2 = (3.f * cj * inv2) * r - u2;

@@ -35,7 +35,7 @@ struct GTerms {
 SG_DEV GTerms gterms(float c, float ru1, float ru2, float uu, float inv_rsq) {
     GTerms t;
     float sp = ru1 + ru2, sm = ru1 - ru2;
-    float dp = 1.f / (1.f + c * uu), dm = 1.f / (1.f - c * uu);
+    float dp = fast_rcp(1.f + c * uu), dm = fast_rcp(1.f - c * uu);
     t.a = sp * dp;
     t.b = sm * dm;
     t.g = 1.f - (c * 0.5f * inv_rsq) * (sp * t.a + sm * t.b);
@@ -66,7 +66,7 @@ struct PotGB {
         const float rmag = sqrtf(rsq);
         const float4 pi0 = prep[2 * i], pi1 = prep[2 * i + 1], pj0 = prep[2 * j];
         const float3 U1 = make_float3(pi0.x, pi0.y, pi0.z), U2 = make_float3(pj0.x, pj0.y, pj0.z);
-        const GTerms gc = gterms(pi1.x, dot3(r, U1), dot3(r, U2), dot3(U1, U2), 1.f / rsq);
+        const GTerms gc = gterms(pi1.x, dot3(r, U1), dot3(r, U2), dot3(U1, U2), fast_rcp(rsq));
         const float sigma = pi0.w / sqrtf(gc.g);
         const float reach = kWeld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
         return (KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach);
@@ -77,8 +77,8 @@ struct PotGB {
         const float3 r = pair_rij(pos, i, j, b);
         const float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
         const float rmag = sqrtf(rsq);
-        const float rinv = 1.f / rmag;
-        const float inv_rsq = 1.f / rsq;
+        const float rinv = fast_rcp(rmag);
+        const float inv_rsq = fast_rcp(rsq);
         const float3 rhat = rinv * r;
         const float4 pi0 = prep[2 * i], pi1 = prep[2 * i + 1], pj0 = prep[2 * j];
         const float3 U1 = make_float3(pi0.x, pi0.y, pi0.z), U2 = make_float3(pj0.x, pj0.y, pj0.z);
@@ -89,18 +89,18 @@ struct PotGB {
         const float eps1 = rsqrtf(1.f - (chi * uu) * (chi * uu));
         const float eps2 = gx.g * inv_ez;
         const float sigma = lprp / sqrtf(gc.g);   // correctly rounded: r - sigma sets the envelope
-        const float ginv = sigma * (1.f / gc.g);
+        const float ginv = sigma * fast_rcp(gc.g);
         const float reach = kWeld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
         const bool active = prefiltered || ((KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach));
         if (!active) return;
         o.act = 1;
         float sr;
         if (kWeld) {
-            if (rmag < sigma) sr = 1.f / (rmag - sigma + 1.f);
+            if (rmag < sigma) sr = fast_rcp(rmag - sigma + 1.f);
             else if (rmag <= sigma + wf) sr = 1.f;
-            else sr = 1.f / (rmag - sigma + 1.f - wf);
+            else sr = fast_rcp(rmag - sigma + 1.f - wf);
         } else {
-            sr = 1.f / (rmag - sigma + 1.f);
+            sr = fast_rcp(rmag - sigma + 1.f);
         }
         const float sr2 = sr * sr, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
         float srx = sr12 - 2.f * sr6;
@@ -164,7 +164,7 @@ struct PotGB {
         if (kTaper) {
             const float sw = 0.9f * reach;
             if (rmag >= sw && rmag <= reach) {
-                const float factor = 1.f / (reach - sw);
+                const float factor = fast_rcp(reach - sw);
                 const float xx = (rmag - sw) * factor;
                 const float x2 = xx * xx, x3 = x2 * xx;
                 const float sx = 1.f - 6.f * x3 * x2 + 15.f * x2 * x2 - 10.f * x3;

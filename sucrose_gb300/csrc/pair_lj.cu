@@ -33,7 +33,7 @@ struct PotLJ {
         float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
         if (kind == SG_LJ) {                         // force.f90:26-47
             if (prefiltered || rsq < rc2) {
-                float inv = 1.f / rsq;
+                float inv = fast_rcp(rsq);
                 float sr2 = sig2 * inv, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
                 o.pe = 4.f * eps * (sr12 - sr6) - pot_cut;
                 float coeff = 24.f * eps * (2.f * sr12 - sr6) * inv;
@@ -43,7 +43,7 @@ struct PotLJ {
             }
         } else if (kind == SG_LJ12) {                // force.f90:72-91
             if (prefiltered || rsq < rc2) {
-                float inv = 1.f / rsq;
+                float inv = fast_rcp(rsq);
                 float sr2 = sig2 * inv, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
                 o.pe = eps * (sr12 - 2.f * sr6) - pot_cut;
                 float coeff = 12.f * eps * (sr12 - sr6) * inv;
@@ -67,7 +67,7 @@ struct PotLJ {
             }
         } else {                                      // SG_WCA, force.f90:175-188
             if (prefiltered || rsq <= sig2) {
-                float inv = 1.f / rsq;
+                float inv = fast_rcp(rsq);
                 float sr2 = sig2 * inv, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
                 o.pe = eps * (sr12 - 2.f * sr6) + eps;
                 float coeff = 12.f * eps * (sr12 - sr6) * inv;
