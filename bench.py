@@ -138,6 +138,15 @@ def pair_params(g, w, solver):
 
 FLAGS = 0   # step-graph flags (capi.STEP_FLAT under --flat-graph)
 
+# DRAM bytes (read + write) of one launch of the dominant kernel, from the
+# committed ncu captures of these workloads (traffic is not measurable from
+# inside a timed run)
+NCU_TRAFFIC = {
+    "EC": {"bytes": 11.05e6, "source": "profiles/k_pair_ecp_newton_N65536.md: ncu, 0.46 M listed pairs (lattice state)"},
+    "GB": {"bytes": 45.31e6, "source": "profiles/k_pair_gb_filtered_N32768.md: ncu, 5.7 M listed pairs"},
+    "COULOMB": {"bytes": 65.06e6, "source": "profiles/k_pair_coulomb_charged_N131072.md: ncu, 7.57 M listed pairs"},
+}
+
 
 def configure(g, w, pp, langevin=False, first_step=1):
     from sucrose_gb300 import capi
@@ -455,7 +464,8 @@ def run_ours(a):
                          "achieved": achieved, "peak": peak32,
                          "unit": "TFLOP/s", "frac": achieved / peak32,
                          "peak_source": "measured FMA throughput (sg_peak_fma) on this GPU",
-                         "traffic": None},
+                         "traffic": NCU_TRAFFIC[w["kind"][:2]]["bytes"],
+                         "traffic_source": NCU_TRAFFIC[w["kind"][:2]]["source"]},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
@@ -628,7 +638,8 @@ def run_charged(a):
             "roofline": {"bound": "hbm", "kernel": "k_pair<PotElec> (COULOMB)", "achieved": c["min_dram_gbs"],
                          "peak": hbm, "unit": "GB/s", "frac": c["min_dram_frac"],
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)",
-                         "bytes_per_launch": "8 per listed pair + 48 per particle", "traffic": None,
+                         "bytes_per_launch": "8 per listed pair + 48 per particle",
+                         "traffic": NCU_TRAFFIC["COULOMB"]["bytes"], "traffic_source": NCU_TRAFFIC["COULOMB"]["source"],
                          "fp32_tflops": c["fp32_tflops"], "fp32_frac_of_measured": c["fp32_frac"]},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
