@@ -23,6 +23,15 @@
 //                 steps, else the plain Newton (counted as a fallback).
 #include <cmath>
 
+// Minimum resident blocks of 256 threads the Newton ECP pair kernels are
+// compiled for, which caps their registers: 4 -> 64 registers (~300 B
+// spilled to L1-resident local memory), 32 resident warps instead of 16. The
+// FP64 residual check's latency wants the extra warps: 79.8 -> 72.3 us on the
+// N = 65 536 benchmark (3 -> 80 registers: 75.6 us). The Brent and inline-MLP
+// kernels keep every register they use.
+#ifndef SG_ECP_MIN_BLOCKS
+#define SG_ECP_MIN_BLOCKS 4
+#endif
 #include "pair_common.cuh"
 #include "ecp_mlp.cuh"
 
@@ -372,6 +381,8 @@ struct PotECP {
     static constexpr bool kStats = true;
     static constexpr bool kCountActive = false;
     static constexpr bool kFilterable = false;
+    static constexpr int kMinBlocks =
+        (SOLVER == SG_SOLVER_NEWTON || SOLVER == SOLVER_MLP_PRE) ? SG_ECP_MIN_BLOCKS : 1;
     int prefiltered;
     SG_DEV bool in_range(int, int) const { return true; }
     const float4* __restrict__ pos;

@@ -25,6 +25,7 @@ struct PotElec {
     static constexpr bool kStats = false;
     static constexpr bool kCountActive = true;
     static constexpr bool kFilterable = true;
+    static constexpr int kMinBlocks = 1;
     const float4* __restrict__ pos;
     BoxF b;
     int kind;
@@ -90,6 +91,7 @@ struct PotDipole {
     static constexpr bool kStats = false;
     static constexpr bool kCountActive = true;
     static constexpr bool kFilterable = true;
+    static constexpr int kMinBlocks = 1;
     const float4* __restrict__ pos;
     const float4* __restrict__ quat;
     BoxF b;

@@ -51,6 +51,7 @@ struct PotGB {
     static constexpr bool kTaper = (KIND != SG_GBR);
     static constexpr bool kChiral = (KIND == SG_GBC || KIND == SG_GBWC);
     static constexpr bool kFilterable = true;
+    static constexpr int kMinBlocks = 1;
     const float4* __restrict__ pos;
     const float4* __restrict__ prep;
     BoxF b;

@@ -11,6 +11,7 @@ struct PotLJ {
     static constexpr bool kStats = false;
     static constexpr bool kCountActive = true;
     static constexpr bool kFilterable = true;
+    static constexpr int kMinBlocks = 1;
     const float4* __restrict__ pos;
     BoxF b;
     int kind;
