@@ -124,7 +124,8 @@ SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int 
 // range queue up per warp (in list order, so rows stay contiguous) and are
 // evaluated 32 at a time, so no lane idles on an out-of-range pair.
 template <class Pot, bool FILTER>
-__global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? 4 : Pot::kMinBlocks) k_pair(PairLaunch L, Pot pot) {
+__global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFiltered : Pot::kMinBlocks)
+    k_pair(PairLaunch L, Pot pot) {
     __shared__ unsigned long long sh_stats[SG_NSTATS];
     // per-warp queue of in-range pairs: storage index, i, j (64 slots each)
     __shared__ int sh_queue[FILTER ? SG_PAIR_MAX_BLOCK * 2 * 3 : 1];

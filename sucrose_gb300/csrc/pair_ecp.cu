@@ -383,6 +383,7 @@ struct PotECP {
     static constexpr bool kFilterable = false;
     static constexpr int kMinBlocks =
         (SOLVER == SG_SOLVER_NEWTON || SOLVER == SOLVER_MLP_PRE) ? SG_ECP_MIN_BLOCKS : 1;
+    static constexpr int kMinBlocksFiltered = 1;   // not filterable
     int prefiltered;
     SG_DEV bool in_range(int, int) const { return true; }
     const float4* __restrict__ pos;

@@ -26,6 +26,7 @@ struct PotElec {
     static constexpr bool kCountActive = true;
     static constexpr bool kFilterable = true;
     static constexpr int kMinBlocks = 1;
+    static constexpr int kMinBlocksFiltered = 4;
     const float4* __restrict__ pos;
     BoxF b;
     int kind;
@@ -92,6 +93,7 @@ struct PotDipole {
     static constexpr bool kCountActive = true;
     static constexpr bool kFilterable = true;
     static constexpr int kMinBlocks = 1;
+    static constexpr int kMinBlocksFiltered = 4;
     const float4* __restrict__ pos;
     const float4* __restrict__ quat;
     BoxF b;

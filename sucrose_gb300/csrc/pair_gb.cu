@@ -7,6 +7,9 @@
 // reference's U1 formula, :343-349), chi, chi' and 1/eps_z.
 #include <cmath>
 
+#ifndef SG_GB_FILTER_MIN_BLOCKS
+#define SG_GB_FILTER_MIN_BLOCKS 4
+#endif
 #include "pair_common.cuh"
 
 namespace {
@@ -52,6 +55,7 @@ struct PotGB {
     static constexpr bool kChiral = (KIND == SG_GBC || KIND == SG_GBWC);
     static constexpr bool kFilterable = true;
     static constexpr int kMinBlocks = 1;
+    static constexpr int kMinBlocksFiltered = SG_GB_FILTER_MIN_BLOCKS;
     const float4* __restrict__ pos;
     const float4* __restrict__ prep;
     BoxF b;

@@ -12,6 +12,7 @@ struct PotLJ {
     static constexpr bool kCountActive = true;
     static constexpr bool kFilterable = true;
     static constexpr int kMinBlocks = 1;
+    static constexpr int kMinBlocksFiltered = 4;
     const float4* __restrict__ pos;
     BoxF b;
     int kind;
