@@ -18,7 +18,7 @@ filter (for example ncu -k regex:k_pair -c 2). Cases:
   mlp_train one MLP training step on 65 536 samples
   ecp_step  captured Nose-Hoover steps of the ECP system (list build as
             flag-gated kernels, so that a profiler sees every kernel)
-  replicas  captured steps of 1 024 replicas (LJ + GB), same flag
+  replicas  captured steps of --nrep replicas (default 1 024, LJ + GB), same flag
 """
 import argparse
 import os
@@ -65,6 +65,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("case")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--nrep", type=int, default=1024, help="replicas (case replicas)")
     a = ap.parse_args()
     if a.case in ("ecp", "ecp_mlp", "list", "nhc", "ecp_step"):
         g, p = ecp_system()
@@ -127,7 +128,7 @@ def main():
         X, y = mlp.generate(g, p, langevin, samples=65536, every=2, equil=2)
         mlp.train(g, X, y, epochs=1 + a.reps, batch=65536, lr=2e-3, seed=1)
     elif a.case == "replicas":
-        e = configs.replica_ensemble(1024, seed=1005)
+        e = configs.replica_ensemble(a.nrep, seed=1005)
         import bench  # the benchmark's replica set-up, reused
         sig, eps, inert, v0, l0 = bench.replica_arrays(e)
         g = GpuSystem.replicas(e["n"], e["box"], e["family"], e["temp"], e["key"])
