@@ -50,21 +50,20 @@ __device__ __forceinline__ bool ref_accept(float4 pi, float4 pj, const ListGeom&
     return r2 < g.rl2;
 }
 
-__device__ __forceinline__ bool near_half(float d, float inv_b) {
-    float f = fabsf(d * inv_b);
-    f = f - floorf(f);
-    return fabsf(f - 0.5f) < 1e-4f;
-}
-
 // FP32 filter, exact FP64 decision inside the guard band.
 __device__ __forceinline__ bool accept_pair(float4 pi, float4 pj, const ListGeom& g) {
     float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     bool halfcase = false;
     if (g.periodic) {
-        halfcase = near_half(dx, g.inv_box.x) || near_half(dy, g.inv_box.y) || near_half(dz, g.inv_box.z);
-        dx -= roundf(dx * g.inv_box.x) * g.box.x;
-        dy -= roundf(dy * g.inv_box.y) * g.box.y;
-        dz -= roundf(dz * g.inv_box.z) * g.box.z;
+        // a component within 2e-4 of half a box may round the other way in
+        // FP64: such pairs take the exact test (the distance to the nearest
+        // integer of d / L is read off the rounding the image needs anyway)
+        const float tx = dx * g.inv_box.x, ty = dy * g.inv_box.y, tz = dz * g.inv_box.z;
+        const float nx = roundf(tx), ny = roundf(ty), nz = roundf(tz);
+        halfcase = fabsf(tx - nx) > 0.4998f || fabsf(ty - ny) > 0.4998f || fabsf(tz - nz) > 0.4998f;
+        dx -= nx * g.box.x;
+        dy -= ny * g.box.y;
+        dz -= nz * g.box.z;
     }
     float r2 = dx * dx + dy * dy + dz * dz;
     if (!halfcase) {
