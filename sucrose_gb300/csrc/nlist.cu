@@ -32,6 +32,7 @@ struct ListGeom {
     double bx, by, bz;
     double rl2;       // (rc+skin)^2
     float rl2_lo, rl2_hi;
+    float half_sq;    // (0.4998 min(box))^2, rounded down: a pair with a half-box component is at least this far
     int periodic;
     int nc[3];
 };
@@ -69,6 +70,8 @@ __device__ __forceinline__ bool accept_pair(float4 pi, float4 pj, const ListGeom
     if (!halfcase) {
         if (r2 < g.rl2_lo) return true;
         if (r2 > g.rl2_hi) return false;
+    } else if (g.half_sq > g.rl2_hi) {
+        return false;   // beyond the list radius whichever image FP64 picks
     }
     return ref_accept(pi, pj, g);
 }
@@ -85,6 +88,7 @@ __device__ __forceinline__ ListGeom geom_for(const ListGeom& base, const RepDev&
     g.rl2 = rp.rl2[r];
     g.rl2_lo = (float)(g.rl2 * (1.0 - 1e-4));
     g.rl2_hi = (float)(g.rl2 * (1.0 + 1e-4));
+    g.half_sq = rp.half_sq[r];
     const int4 gr = rp.grid[r];
     g.nc[0] = max(gr.x, 1);
     g.nc[1] = max(gr.y, 1);
@@ -527,6 +531,12 @@ __global__ void k_set_request(int* flags, int* rep_flag, int R) {
 
 int clear_grid(const sg_ctx* ctx) { return std::max(1, std::min(64, (ctx->nrep + 255) / 256)); }
 
+// (0.4998 min(box))^2 with a margin, as a float that never exceeds the true value
+float half_sq_of(const double* b) {
+    const double h = 0.4998 * std::min(b[0], std::min(b[1], b[2]));
+    return (float)(h * h * (1.0 - 1e-5));
+}
+
 ListGeom make_geom(const sg_ctx* ctx) {
     ListGeom g;
     g.box = make_float3((float)ctx->box[0], (float)ctx->box[1], (float)ctx->box[2]);
@@ -535,6 +545,7 @@ ListGeom make_geom(const sg_ctx* ctx) {
     g.rl2 = ctx->nl.rl2;
     g.rl2_lo = (float)(ctx->nl.rl2 * (1.0 - 1e-4));
     g.rl2_hi = (float)(ctx->nl.rl2 * (1.0 + 1e-4));
+    g.half_sq = half_sq_of(ctx->box);
     g.periodic = ctx->periodic;
     for (int d = 0; d < 3; ++d) g.nc[d] = ctx->nl.ncell[d] > 0 ? ctx->nl.ncell[d] : 1;
     return g;

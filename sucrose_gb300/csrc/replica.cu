@@ -93,7 +93,8 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     const size_t s_boxd = al(sizeof(double) * 3 * R), s_d = al(sizeof(double) * R), s_f4 = al(sizeof(float4) * R),
                  s_i4 = al(sizeof(int4) * R), s_u2 = al(sizeof(uint2) * R),
                  s_i = al(sizeof(int) * R), s_off = al(sizeof(int) * (R + 1)), s_of = al(sizeof(int) * (size_t)n);
-    const size_t bytes = s_boxd + 3 * s_d + 3 * s_f4 + s_i4 + s_u2 + s_i + s_off + s_of;
+    const size_t s_hs = al(sizeof(float) * R);
+    const size_t bytes = s_boxd + 3 * s_d + 3 * s_f4 + s_i4 + s_u2 + s_i + s_off + s_of + s_hs;
     char* base = nullptr;
     SG_CUDA(ctx, cudaMalloc(&base, bytes));
     ctx->rep_alloc = base;
@@ -109,12 +110,16 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     double* temp = (double*)p; p += s_d;
     int* tint = (int*)p; p += s_i;
     int* off = (int*)p; p += s_off;
+    float* half_sq = (float*)p; p += s_hs;
     int* rep_of = (int*)p;
     std::vector<float4> hb(R), hi(R), hl(R);
     std::vector<uint2> hk(R);
     std::vector<double> ht(R);
     std::vector<int> hti(R);
+    std::vector<float> hhs(R);
     for (int r = 0; r < R; ++r) {
+        const double hm = 0.4998 * std::min(boxes[3 * r], std::min(boxes[3 * r + 1], boxes[3 * r + 2]));
+        hhs[r] = (float)(hm * hm * (1.0 - 1e-5));
         hb[r] = make_float4((float)boxes[3 * r], (float)boxes[3 * r + 1], (float)boxes[3 * r + 2], 0.f);
         hi[r] = make_float4((float)(1.0 / boxes[3 * r]), (float)(1.0 / boxes[3 * r + 1]), (float)(1.0 / boxes[3 * r + 2]), 0.f);
         hl[r] = make_float4((float)(boxes[3 * r] - (double)hb[r].x), (float)(boxes[3 * r + 1] - (double)hb[r].y),
@@ -132,6 +137,7 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     SG_CUDA(ctx, cudaMemcpy(temp, ht.data(), sizeof(double) * R, cudaMemcpyHostToDevice));
     SG_CUDA(ctx, cudaMemcpy(tint, hti.data(), sizeof(int) * R, cudaMemcpyHostToDevice));
     SG_CUDA(ctx, cudaMemcpy(off, ctx->h_rep_off.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice));
+    SG_CUDA(ctx, cudaMemcpy(half_sq, hhs.data(), sizeof(float) * R, cudaMemcpyHostToDevice));
     k_rep_of<<<R, 128, 0, ctx->stream>>>(R, off, rep_of);
     SG_LAUNCH_CHECK(ctx, "k_rep_of");
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -147,6 +153,7 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
     ctx->rep.temp = temp;
     ctx->rep.temp_int = tint;
     ctx->rep.key = key;
+    ctx->rep.half_sq = half_sq;
     return SG_OK;
 }
 

@@ -30,6 +30,7 @@ struct RepDev {
     const double* temp = nullptr;     // [R] target temperature
     const int* temp_int = nullptr;    // [R] int(T * 1000) for the Philox counter
     const uint2* key = nullptr;       // [R] Philox key
+    const float* half_sq = nullptr;   // [R] (0.4998 min(box))^2, rounded down (list acceptance test)
 };
 
 struct sg_nlist_state {

@@ -66,6 +66,7 @@ def main():
     ap.add_argument("case")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--nrep", type=int, default=1024, help="replicas (case replicas)")
+    ap.add_argument("--equil", type=int, default=0, help="untimed steps before the profiled ones (case replicas)")
     a = ap.parse_args()
     if a.case in ("ecp", "ecp_mlp", "list", "nhc", "ecp_step"):
         g, p = ecp_system()
@@ -139,6 +140,8 @@ def main():
         pairs = bench.replica_pair_params()
         g.configure_step_pairs(pairs, integrator=capi.INT_LANGEVIN, dt=0.0005, damping=1.0, rotations=1,
                                flags=capi.STEP_FLAT)
+        if a.equil:   # untimed steps first, until replicas start to rebuild their lists
+            g.step(a.equil)
         g.step(1 + a.reps)
     g.synchronize()
     print("profile case", a.case, "done")
