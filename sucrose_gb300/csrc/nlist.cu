@@ -76,6 +76,14 @@ __device__ __forceinline__ bool accept_pair(float4 pi, float4 pj, const ListGeom
     return ref_accept(pi, pj, g);
 }
 
+// Relative half-width of the r^2 band where the FP32 test defers to the FP64
+// one. The FP32 r^2 of the same FP32 positions is within ~(1.1e-6 L / r_list
+// + 3e-7) of the FP64 value (the FP32 box in the image shift dominates), so
+// the band is 1e-4, widened for boxes over ~25 list radii.
+__host__ __device__ inline double guard_band(double box_max, double rl2) {
+    return fmax(1e-4, 4e-6 * box_max / sqrt(rl2));
+}
+
 // Geometry of replica r (batched contexts): its box, list radius and grid.
 __device__ __forceinline__ ListGeom geom_for(const ListGeom& base, const RepDev& rp, int r) {
     ListGeom g = base;
@@ -86,8 +94,9 @@ __device__ __forceinline__ ListGeom geom_for(const ListGeom& base, const RepDev&
     g.by = rp.boxd[3 * r + 1];
     g.bz = rp.boxd[3 * r + 2];
     g.rl2 = rp.rl2[r];
-    g.rl2_lo = (float)(g.rl2 * (1.0 - 1e-4));
-    g.rl2_hi = (float)(g.rl2 * (1.0 + 1e-4));
+    const double band = guard_band(fmax(g.bx, fmax(g.by, g.bz)), g.rl2);
+    g.rl2_lo = (float)(g.rl2 * (1.0 - band));
+    g.rl2_hi = (float)(g.rl2 * (1.0 + band));
     g.half_sq = rp.half_sq[r];
     const int4 gr = rp.grid[r];
     g.nc[0] = max(gr.x, 1);
@@ -543,8 +552,9 @@ ListGeom make_geom(const sg_ctx* ctx) {
     g.inv_box = make_float3((float)(1.0 / ctx->box[0]), (float)(1.0 / ctx->box[1]), (float)(1.0 / ctx->box[2]));
     g.bx = ctx->box[0]; g.by = ctx->box[1]; g.bz = ctx->box[2];
     g.rl2 = ctx->nl.rl2;
-    g.rl2_lo = (float)(ctx->nl.rl2 * (1.0 - 1e-4));
-    g.rl2_hi = (float)(ctx->nl.rl2 * (1.0 + 1e-4));
+    const double band = guard_band(std::max(ctx->box[0], std::max(ctx->box[1], ctx->box[2])), ctx->nl.rl2);
+    g.rl2_lo = (float)(ctx->nl.rl2 * (1.0 - band));
+    g.rl2_hi = (float)(ctx->nl.rl2 * (1.0 + band));
     g.half_sq = half_sq_of(ctx->box);
     g.periodic = ctx->periodic;
     for (int d = 0; d < 3; ++d) g.nc[d] = ctx->nl.ncell[d] > 0 ? ctx->nl.ncell[d] : 1;

@@ -84,6 +84,27 @@ def test_nlist_threshold_pairs(lib):
     _pairs_equal(P, 2.5, 0.3)
 
 
+@pytest.mark.parametrize("box", [60.0, 400.0])
+def test_nlist_threshold_pairs_large_box(lib, box):
+    # the same near-threshold pairs in boxes of 20 and 140 list radii, across
+    # the boundary: the FP32 image shift with an FP32 box is furthest from
+    # FP64 there, and the guard band widens with the box
+    rng = np.random.default_rng(int(box))
+    rl = 2.8
+    base = rng.uniform(-box / 2, box / 2, size=(300, 3))
+    base[:100, 0] = box / 2 - rng.uniform(0.0, 1.0, 100)   # partners wrap around in x
+    d = rng.normal(size=(300, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[:100, 0] = np.abs(d[:100, 0])
+    eps = rng.uniform(-3e-5, 3e-5, size=(300, 1))
+    partner = base + d * (rl + eps)
+    partner -= box * np.round(partner / box)
+    r = np.concatenate([base, partner])
+    P = Pair(r, None, box)
+    P.g.init_nlist(0.3, 2.5)
+    _pairs_equal(P, 2.5, 0.3)
+
+
 def test_nlist_ellipsoid_cells(lib):
     r, q, box = ellipsoids((12, 16, 24), (3.0, 2.0, 1.0), 0.1114, seed=5, tilt=0.4)
     P = Pair(r, q, box, sig=(3.0, 2.0, 1.0))
