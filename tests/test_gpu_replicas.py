@@ -121,6 +121,36 @@ def test_forces_match_single_runs(lib, ens):
     g.close()
 
 
+def test_charged_kinds_on_replicas(lib, ens):
+    # the charge and Morse kinds belong to the LJ-like family: on a replica
+    # context they act on the LJ replicas, charges riding in pos.w
+    g = batched(ens)
+    rng = np.random.default_rng(4)
+    q = f32(rng.choice([-1.0, 1.0], g.n))
+    g.set_charges(q)
+    kinds = [GpuSystem.params(capi.COULOMB, cutoff=LJ["cutoff"], dielectric=2.0),
+             GpuSystem.params(capi.MORSE, cutoff=LJ["cutoff"], dissoc=1.0, width=1.5, rmin=1.1)]
+    for p in kinds:
+        g.zero_forces()
+        pe, _ = g.pair_forces(p)
+        F, _ = g.forces()
+        pe_single = 0.0
+        for k in range(len(ens["n"])):
+            if ens["family"][k] != 0:
+                continue
+            a, b = ens["off"][k], ens["off"][k + 1]
+            s = single(ens, k)
+            s.set_charges(q[a:b])
+            s.zero_forces()
+            pk, _ = s.pair_forces(p)
+            pe_single += pk
+            Fs, _ = s.forces()
+            assert rel(F[a:b], Fs) < 1e-5, k
+            s.close()
+        assert abs(pe - pe_single) <= 1e-6 * max(1.0, abs(pe_single))
+    g.close()
+
+
 def test_langevin_streams_bit_exact(lib, ens):
     """Zero forces, one Langevin half step: every number in the update comes
     from the per-replica Philox stream, so the state must be bit-identical."""
