@@ -14,7 +14,23 @@
 // The grid is persistent (a multiple of the SM count); the pair count is read
 // from device memory so the launch needs no host synchronisation.
 #pragma once
+#include <type_traits>
+
 #include "sg_internal.cuh"
+
+// Optional traits of a potential, with their defaults:
+//   kQueueR (false): its range test hands r_ij to the in-range queue, and
+//     eval_r takes it from there instead of gathering the positions again;
+//   kExactFilter (true): in_range decides exactly as eval would. When false,
+//     in_range is a superset test and eval makes the decision (and counts it).
+template <class P, class = void>
+struct QueueR : std::false_type {};
+template <class P>
+struct QueueR<P, std::void_t<decltype(P::kQueueR)>> : std::integral_constant<bool, P::kQueueR> {};
+template <class P, class = void>
+struct ExactFilter : std::true_type {};
+template <class P>
+struct ExactFilter<P, std::void_t<decltype(P::kExactFilter)>> : std::integral_constant<bool, P::kExactFilter> {};
 
 struct PairOut {
     float3 f;    // force on I (FXIJ)
@@ -86,9 +102,11 @@ SG_DEV void segmented_scatter_i(const PairLaunch& L, int i, float3 f, float3 t) 
 
 // One pair per lane, evaluated and scattered (all 32 lanes call it).
 // i, j: the pair's particles (loaded by the caller; ignored when !valid).
-template <class Pot, bool COUNT>
+// COUNT: 0 nothing, 1 listed and in-range pairs, 2 in-range pairs only.
+// HAS_R: r_ij comes from the in-range queue (QueueR potentials).
+template <class Pot, int COUNT, bool HAS_R = false>
 SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int j, bool valid, float& pe, float& vir,
-                         unsigned long long* sh_stats) {
+                         unsigned long long* sh_stats, float3 rq = make_float3(0.f, 0.f, 0.f)) {
     const int lane = threadIdx.x & 31;
     PairOut o;
     o.f = make_float3(0.f, 0.f, 0.f);
@@ -102,12 +120,15 @@ SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int 
         j = 0;
     }
     // called by every lane (warp-cooperative potentials need all 32)
-    pot.eval(valid, valid ? i : 0, j, t, o, sh_stats);
+    if constexpr (HAS_R)
+        pot.eval_r(valid, valid ? i : 0, j, rq, o);
+    else
+        pot.eval(valid, valid ? i : 0, j, t, o, sh_stats);
     if (COUNT) {
         // stats[0] listed pairs, stats[1] pairs inside the range
         const unsigned va = __ballot_sync(0xffffffffu, valid), ac = __ballot_sync(0xffffffffu, o.act != 0);
         if (lane == 0) {
-            atomicAdd(&sh_stats[0], (unsigned long long)__popc(va));
+            if (COUNT == 1) atomicAdd(&sh_stats[0], (unsigned long long)__popc(va));
             if (ac) atomicAdd(&sh_stats[1], (unsigned long long)__popc(ac));
         }
     }
@@ -126,9 +147,12 @@ SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int 
 template <class Pot, bool FILTER>
 __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFiltered : Pot::kMinBlocks)
     k_pair(PairLaunch L, Pot pot) {
+    constexpr bool kQR = QueueR<Pot>::value;
+    constexpr bool kExact = ExactFilter<Pot>::value;
+    constexpr int kQW = kQR ? 6 : 3;   // queue words per slot
     __shared__ unsigned long long sh_stats[SG_NSTATS];
-    // per-warp queue of in-range pairs: storage index, i, j (64 slots each)
-    __shared__ int sh_queue[FILTER ? SG_PAIR_MAX_BLOCK * 2 * 3 : 1];
+    // per-warp queue of in-range pairs: storage index, i, j [, r_ij] (64 slots each)
+    __shared__ int sh_queue[FILTER ? SG_PAIR_MAX_BLOCK * 2 * kQW : 1];
     constexpr bool kSh = Pot::kStats || Pot::kCountActive;
     if (kSh) {
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x) sh_stats[k] = 0ull;
@@ -140,9 +164,10 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFil
     const int np = *L.npairs;
     const int b0 = L.begin ? *L.begin : 0;
     float pe = 0.f, vir = 0.f;
-    int* qt = sh_queue + (FILTER ? (threadIdx.x >> 5) * 192 : 0);
+    int* qt = sh_queue + (FILTER ? (threadIdx.x >> 5) * 64 * kQW : 0);
     int* qi = qt + 64;
     int* qj = qt + 128;
+    float* qr = reinterpret_cast<float*>(qt + 192);   // x, y, z at +0, +64, +128 (kQR only)
     int qn = 0;
     // replica sections: warps walk whole 32-pair chunks, whose first replica is tabulated
     const int bstart = L.sec ? (b0 & ~31) : b0;
@@ -172,40 +197,61 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFil
         const bool valid = vn;
         if (base + stride < np) fetch(base + stride, tn, in_, jn, vn);   // next chunk's indices in flight
         if constexpr (!FILTER) {
-            pair_process<Pot, Pot::kCountActive>(L, pot, t, i, j, valid, pe, vir, sh_stats);
+            pair_process<Pot, Pot::kCountActive ? 1 : 0>(L, pot, t, i, j, valid, pe, vir, sh_stats);
         } else {
-            const bool keep = valid && pot.in_range(i, j);
+            float3 rr = make_float3(0.f, 0.f, 0.f);
+            bool keep;
+            if constexpr (kQR)
+                keep = valid && pot.in_range_r(i, j, rr);
+            else
+                keep = valid && pot.in_range(i, j);
             const unsigned vm = __ballot_sync(0xffffffffu, valid), km = __ballot_sync(0xffffffffu, keep);
             if (Pot::kCountActive && lane == 0) {
                 atomicAdd(&sh_stats[0], (unsigned long long)__popc(vm));
-                if (km) atomicAdd(&sh_stats[1], (unsigned long long)__popc(km));
+                if (kExact && km) atomicAdd(&sh_stats[1], (unsigned long long)__popc(km));
             }
             if (keep) {
                 const int slot = qn + __popc(km & ((1u << lane) - 1u));
                 qt[slot] = t;
                 qi[slot] = i;
                 qj[slot] = j;
+                if constexpr (kQR) {
+                    qr[slot] = rr.x;
+                    qr[64 + slot] = rr.y;
+                    qr[128 + slot] = rr.z;
+                }
             }
             qn += __popc(km);
             __syncwarp();
             if (qn >= 32) {
                 const int tq = qt[lane], iq = qi[lane], jq = qj[lane];
+                float3 rq = make_float3(0.f, 0.f, 0.f);
+                if constexpr (kQR) rq = make_float3(qr[lane], qr[64 + lane], qr[128 + lane]);
                 __syncwarp();
                 if (lane < qn - 32) {
                     qt[lane] = qt[32 + lane];
                     qi[lane] = qi[32 + lane];
                     qj[lane] = qj[32 + lane];
+                    if constexpr (kQR) {
+                        qr[lane] = qr[32 + lane];
+                        qr[64 + lane] = qr[96 + lane];
+                        qr[128 + lane] = qr[160 + lane];
+                    }
                 }
                 __syncwarp();
                 qn -= 32;
-                pair_process<Pot, false>(L, pot, tq, iq, jq, true, pe, vir, sh_stats);
+                pair_process<Pot, (Pot::kCountActive && !kExact) ? 2 : 0, kQR>(L, pot, tq, iq, jq, true, pe, vir,
+                                                                                 sh_stats, rq);
             }
         }
     }
     if (FILTER && qn > 0) {   // qn is warp-uniform
         const bool ok = lane < qn;
-        pair_process<Pot, false>(L, pot, ok ? qt[lane] : 0, ok ? qi[lane] : 0, ok ? qj[lane] : 0, ok, pe, vir,
-                                 sh_stats);
+        float3 rq = make_float3(0.f, 0.f, 0.f);
+        if constexpr (kQR)
+            if (ok) rq = make_float3(qr[lane], qr[64 + lane], qr[128 + lane]);
+        pair_process<Pot, (Pot::kCountActive && !kExact) ? 2 : 0, kQR>(
+            L, pot, ok ? qt[lane] : 0, ok ? qi[lane] : 0, ok ? qj[lane] : 0, ok, pe, vir, sh_stats, rq);
     }
     if (kSh) {
         __syncthreads();
@@ -223,7 +269,7 @@ PairTune sg_pair_tune_for(sg_ctx* ctx, int kind, bool filterable);
 
 template <class Pot, bool FILTER>
 int launch_pair_v(sg_ctx* ctx, PairLaunch L, Pot pot, int block) {
-    pot.prefiltered = FILTER ? 1 : 0;
+    pot.prefiltered = (FILTER && ExactFilter<Pot>::value) ? 1 : 0;
     const void* fn = (const void*)k_pair<Pot, FILTER>;
     int grid = sg_grid_for(ctx, fn, block, 0);
     int64_t max_useful = (ctx->nl.pair_capacity + block - 1) / block;
@@ -360,8 +406,21 @@ SG_DEV float fast_rcp(float x) {
     return r;
 }
 
+// x^n by repeated multiplication, left to right (the rounding of a loop of
+// products); n is uniform across the warp. Up to n = 4 the products are
+// selected instead of looped.
 SG_DEV float ipowf(float x, int n) {
-    float r = 1.f;
-    for (int k = 0; k < n; ++k) r *= x;
+    const float x2 = x * x, x3 = x2 * x, x4 = x3 * x;
+    if (n <= 4) return n <= 0 ? 1.f : n == 1 ? x : n == 2 ? x2 : n == 3 ? x3 : x4;
+    float r = x4;
+    for (int k = 4; k < n; ++k) r *= x;
+    return r;
+}
+
+// 1/sqrt(x) by the approximate instruction (PTX rsqrt.approx.ftz.f32): for
+// superset range tests that carry a slack far above its error.
+SG_DEV float fast_rsqrt(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }

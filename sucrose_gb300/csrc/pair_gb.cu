@@ -54,6 +54,8 @@ struct PotGB {
     static constexpr bool kTaper = (KIND != SG_GBR);
     static constexpr bool kChiral = (KIND == SG_GBC || KIND == SG_GBWC);
     static constexpr bool kFilterable = true;
+    static constexpr bool kQueueR = true;        // the range test's r_ij is queued for eval_r
+    static constexpr bool kExactFilter = false;  // in_range_r is a superset; eval_r decides
     static constexpr int kMinBlocks = 1;
     static constexpr int kMinBlocksFiltered = SG_GB_FILTER_MIN_BLOCKS;
     const float4* __restrict__ pos;
@@ -61,25 +63,38 @@ struct PotGB {
     BoxF b;
     float cutoff, wf, chirality;
     int mu, nu;
-    int prefiltered;   // eval only sees pairs that passed in_range
+    int prefiltered;   // eval only sees pairs that passed an exact range test
 
-    // The range test of eval, alone: r against the orientation-dependent
-    // contact distance sigma (shape anisotropy of I) plus the cut-off.
-    SG_DEV bool in_range(int i, int j) const {
-        const float3 r = pair_rij(pos, i, j, b);
+    // A superset of eval's range test (r against the orientation-dependent
+    // contact distance sigma of I's shape plus the cut-off), without its
+    // correctly rounded square roots and division: approximate 1/sqrt for r
+    // and sigma (a few ulp each), and a slack of 1e-5 (r + sigma), some 80
+    // ulp of the larger, which also covers the rounding of sigma + shift. A
+    // NaN anywhere keeps the pair: eval_r decides. r_ij is handed on to
+    // eval_r.
+    SG_DEV bool in_range_r(int i, int j, float3& r) const {
+        r = pair_rij(pos, i, j, b);
         const float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
-        const float rmag = sqrtf(rsq);
         const float4 pi0 = prep[2 * i], pi1 = prep[2 * i + 1], pj0 = prep[2 * j];
         const float3 U1 = make_float3(pi0.x, pi0.y, pi0.z), U2 = make_float3(pj0.x, pj0.y, pj0.z);
         const GTerms gc = gterms(pi1.x, dot3(r, U1), dot3(r, U2), dot3(U1, U2), fast_rcp(rsq));
-        const float sigma = pi0.w / sqrtf(gc.g);
-        const float reach = kWeld ? (sigma + cutoff + wf - 1.f) : (sigma + cutoff - 1.f);
-        return (KIND == SG_GBR) ? (rmag <= sigma) : (rmag < reach);
+        const float sigma = pi0.w * fast_rsqrt(gc.g);
+        const float rmag = rsq * fast_rsqrt(rsq);
+        const float shift = (KIND == SG_GBR) ? 0.f : kWeld ? (cutoff + wf - 1.f) : (cutoff - 1.f);
+        return !(0.99999f * rmag >= 1.00001f * sigma + shift);
+    }
+    SG_DEV bool in_range(int i, int j) const {
+        float3 r;
+        return in_range_r(i, j, r);
     }
 
     SG_DEV void eval(bool valid, int i, int j, int, PairOut& o, unsigned long long*) const {
         if (!valid) return;
-        const float3 r = pair_rij(pos, i, j, b);
+        eval_r(valid, i, j, pair_rij(pos, i, j, b), o);
+    }
+
+    SG_DEV void eval_r(bool valid, int i, int j, float3 r, PairOut& o) const {
+        if (!valid) return;
         const float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
         const float rmag = sqrtf(rsq);
         const float rinv = fast_rcp(rmag);
