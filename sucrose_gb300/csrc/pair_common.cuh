@@ -339,6 +339,25 @@ inline BoxF make_boxf(const sg_ctx* ctx) {
     return b;
 }
 
+// r_ij = a - c by the minimum image of the box of i (BoxF).
+SG_DEV float3 pair_rij_of(float3 a, float3 c, int i, const BoxF& b) {
+    if (b.rep_of) {
+        const int r = b.rep_of[i];
+        const float4 bx = b.rbox[r], ib = b.rinv[r];
+        return min_image(make_float3(a.x - c.x, a.y - c.y, a.z - c.z), make_float3(bx.x, bx.y, bx.z),
+                         make_float3(ib.x, ib.y, ib.z), 1);
+    }
+    return min_image(make_float3(a.x - c.x, a.y - c.y, a.z - c.z), b.box, b.inv_box, b.periodic);
+}
+
+// Two float4 from one 32-byte aligned address in a single 256-bit load
+// (read-only path): a gather of 32 bytes per lane in one request.
+SG_DEV void ld_f4x2(const float4* __restrict__ p, float4& a, float4& c) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(c.x), "=f"(c.y), "=f"(c.z), "=f"(c.w)
+        : "l"(p));
+}
+
 SG_DEV float3 pair_rij(const float4* __restrict__ pos, int i, int j, const BoxF& b) {
     float4 a = pos[i], c = pos[j];
     if (b.rep_of) {

@@ -5,6 +5,13 @@
 // anisotropies are those of particle I. A per-particle prep pass hoists what
 // depends on one particle only: the body z axis u (first column of the
 // reference's U1 formula, :343-349), chi, chi' and 1/eps_z.
+//
+// Prep layout (one allocation of 4 float4 per particle):
+//   rec[2p]     = (x, y, z, sig_x)   the position, copied, and the width
+//   rec[2p + 1] = (u_x, u_y, u_z, chi)
+//   aux[p]      = (chi', 1/eps_z, 0, 0)   with aux = rec + 2n
+// so the range test reads each particle's position and axis in one 32-byte
+// load.
 #include <cmath>
 
 #ifndef SG_GB_FILTER_MIN_BLOCKS
@@ -14,10 +21,12 @@
 
 namespace {
 
-__global__ void k_gb_prep(int n, const float4* __restrict__ quat, const float4* __restrict__ shape,
-                          const float4* __restrict__ eshape, float muinv, float4* prep) {
+__global__ void k_gb_prep(int n, const float4* __restrict__ pos, const float4* __restrict__ quat,
+                          const float4* __restrict__ shape, const float4* __restrict__ eshape, float muinv,
+                          float4* prep) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
+    const float4 at = pos[p];
     float4 q = quat[p];  // w x y z
     float w = q.x, x = q.y, y = q.z, z = q.w;
     float3 u = make_float3(2.f * (x * z + w * y), 2.f * (y * z - w * x), w * w - x * x - y * y + z * z);
@@ -26,8 +35,9 @@ __global__ void k_gb_prep(int n, const float4* __restrict__ quat, const float4* 
     float chi = (lpar * lpar - lprp * lprp) / (lpar * lpar + lprp * lprp);
     float ep = powf(e.x, muinv), ez = powf(e.z, muinv);
     float xhi = (ep - ez) / (ep + ez);
-    prep[2 * p] = make_float4(u.x, u.y, u.z, lprp);
-    prep[2 * p + 1] = make_float4(chi, xhi, 1.f / e.z, 0.f);
+    prep[2 * p] = make_float4(at.x, at.y, at.z, lprp);
+    prep[2 * p + 1] = make_float4(u.x, u.y, u.z, chi);
+    prep[2 * (size_t)n + p] = make_float4(xhi, 1.f / e.z, 0.f, 0.f);
 }
 
 struct GTerms {
@@ -59,7 +69,8 @@ struct PotGB {
     static constexpr int kMinBlocks = 1;
     static constexpr int kMinBlocksFiltered = SG_GB_FILTER_MIN_BLOCKS;
     const float4* __restrict__ pos;
-    const float4* __restrict__ prep;
+    const float4* __restrict__ prep;   // rec: 2 per particle
+    const float4* __restrict__ aux;    // 1 per particle
     BoxF b;
     float cutoff, wf, chirality;
     int mu, nu;
@@ -73,11 +84,13 @@ struct PotGB {
     // NaN anywhere keeps the pair: eval_r decides. r_ij is handed on to
     // eval_r.
     SG_DEV bool in_range_r(int i, int j, float3& r) const {
-        r = pair_rij(pos, i, j, b);
+        float4 pi0, pi1, pj0, pj1;
+        ld_f4x2(prep + 2 * i, pi0, pi1);
+        ld_f4x2(prep + 2 * j, pj0, pj1);
+        r = pair_rij_of(make_float3(pi0.x, pi0.y, pi0.z), make_float3(pj0.x, pj0.y, pj0.z), i, b);
         const float rsq = r.x * r.x + r.y * r.y + r.z * r.z;
-        const float4 pi0 = prep[2 * i], pi1 = prep[2 * i + 1], pj0 = prep[2 * j];
-        const float3 U1 = make_float3(pi0.x, pi0.y, pi0.z), U2 = make_float3(pj0.x, pj0.y, pj0.z);
-        const GTerms gc = gterms(pi1.x, dot3(r, U1), dot3(r, U2), dot3(U1, U2), fast_rcp(rsq));
+        const float3 U1 = make_float3(pi1.x, pi1.y, pi1.z), U2 = make_float3(pj1.x, pj1.y, pj1.z);
+        const GTerms gc = gterms(pi1.w, dot3(r, U1), dot3(r, U2), dot3(U1, U2), fast_rcp(rsq));
         const float sigma = pi0.w * fast_rsqrt(gc.g);
         const float rmag = rsq * fast_rsqrt(rsq);
         const float shift = (KIND == SG_GBR) ? 0.f : kWeld ? (cutoff + wf - 1.f) : (cutoff - 1.f);
@@ -100,9 +113,9 @@ struct PotGB {
         const float rinv = fast_rcp(rmag);
         const float inv_rsq = fast_rcp(rsq);
         const float3 rhat = rinv * r;
-        const float4 pi0 = prep[2 * i], pi1 = prep[2 * i + 1], pj0 = prep[2 * j];
-        const float3 U1 = make_float3(pi0.x, pi0.y, pi0.z), U2 = make_float3(pj0.x, pj0.y, pj0.z);
-        const float lprp = pi0.w, chi = pi1.x, xhi = pi1.y, inv_ez = pi1.z;
+        const float4 pi1 = prep[2 * i + 1], pj1 = prep[2 * j + 1], ai = aux[i];
+        const float3 U1 = make_float3(pi1.x, pi1.y, pi1.z), U2 = make_float3(pj1.x, pj1.y, pj1.z);
+        const float lprp = prep[2 * i].w, chi = pi1.w, xhi = ai.x, inv_ez = ai.y;
         const float ru1 = dot3(r, U1), ru2 = dot3(r, U2), uu = dot3(U1, U2);
         const GTerms gc = gterms(chi, ru1, ru2, uu, inv_rsq);
         const GTerms gx = gterms(xhi, ru1, ru2, uu, inv_rsq);
@@ -209,6 +222,7 @@ int launch_gb(sg_ctx* ctx, const sg_pair_params* p, float4* prep, int mu, int nu
     PotGB<KIND> pot;
     pot.pos = ctx->pos;
     pot.prep = prep;
+    pot.aux = prep + 2 * (size_t)ctx->n;
     pot.b = make_boxf(ctx);
     pot.cutoff = (float)p->cutoff;
     pot.wf = (float)p->wf;
@@ -226,8 +240,8 @@ int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p) {
     if (mu < 1 || nu < 1 || mu > 8 || nu > 8) return sg_fail(ctx, SG_EINVAL, "GB exponents must be in 1..8");
     // prep buffer: reuse the ECP prep allocation (large enough: 4 float4 per particle)
     if (!ctx->ecp_prep) SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep, sizeof(float4) * 4 * (size_t)ctx->n));
-    k_gb_prep<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->quat, ctx->shape, ctx->eshape,
-                                                            1.f / (float)mu, ctx->ecp_prep);
+    k_gb_prep<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->quat, ctx->shape,
+                                                            ctx->eshape, 1.f / (float)mu, ctx->ecp_prep);
     SG_LAUNCH_CHECK(ctx, "k_gb_prep");
     switch (p->kind) {
         case SG_GB: return launch_gb<SG_GB>(ctx, p, ctx->ecp_prep, mu, nu);
