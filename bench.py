@@ -1026,12 +1026,16 @@ def run_replicas(a):
     kernels_per_step = g.step_kernel_count()
     p_before = g.npairs()
     builds0 = g.nlist_builds()
+    rep_builds0 = g.rep_nlist_builds()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t_dev = timed_steps(g, torch, stream, a.steps, flush)
     g.step_check()
     npairs = 0.5 * (p_before + g.npairs())
     builds = g.nlist_builds() - builds0
+    rep_builds = g.rep_nlist_builds() - rep_builds0
+    fam_of = np.asarray(e["family"])
+    rebuilt_per_step = {name: float(rep_builds[fam_of == f].sum()) / a.steps for f, name in ((0, "LJ"), (1, "GB"))}
     if world > 1:
         t_dev = ranks.max_over_ranks(t_dev, device="cuda")
     ms_per_step = 1e3 * t_dev / a.steps
@@ -1162,6 +1166,7 @@ def run_replicas(a):
             "autotune": tunes,
             "stage_ms_eager": breakdown,
             "list_rebuilds_in_timed_region": int(builds),
+            "replicas_rebuilt_per_step": rebuilt_per_step,
             "sequential_single_system": seq,
             "host_setup_s": t_setup_host,
         }

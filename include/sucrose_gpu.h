@@ -345,6 +345,9 @@ int sg_create_replicas(sg_ctx** out, int32_t nrep, const int32_t* n_per_rep, con
                        const int32_t* family, const double* temps, const uint32_t* keys, int32_t device);
 /* Verlet lists of every replica; skin[f], cutoff[f] per family f (3 each). */
 int sg_rep_nlist_init(sg_ctx* ctx, const double* skin, const double* cutoff, int32_t trigger_mode);
+/* Rebuilds of each replica's rows since sg_rep_nlist_init (counts[nrep]; the
+ * initial build counts one). */
+int sg_nlist_replica_builds(sg_ctx* ctx, int64_t* counts);
 /* Per-replica kinetic energies: ke2[2r] translational, ke2[2r+1] rotational (FP64). */
 int sg_rep_kinetic(sg_ctx* ctx, double* ke2);
 

@@ -87,6 +87,7 @@ SIGNATURES = [
     ("sg_nlist_count", C.c_int, [_P, _I64]),
     ("sg_nlist_export", C.c_int, [_P, _I32, C.c_int64, _I32, _I64, C.c_int32]),
     ("sg_nlist_builds", C.c_int, [_P, _I64]),
+    ("sg_nlist_replica_builds", C.c_int, [_P, _I64]),
     ("sg_nlist_pairs", C.c_int, [_P, _I32, _I32, C.c_int64, _I64]),
     ("sg_pair_forces", C.c_int, [_P, C.POINTER(PairParams), _D, _D, C.POINTER(EcpStats)]),
     ("sg_pair_forces_async", C.c_int, [_P, C.POINTER(PairParams)]),

@@ -529,9 +529,13 @@ __global__ void k_finish(int n, const float4* __restrict__ pos, float4* last, in
 }
 
 // Request flags: the global one and, in a replica context, one per replica.
-__global__ void k_clear_request(int* flags, int* rep_flag, int R) {
+// After a build (rep_builds given) each replica that rebuilt is counted.
+__global__ void k_clear_request(int* flags, int* rep_flag, int R, int* rep_builds) {
     if (blockIdx.x == 0 && threadIdx.x == 0) flags[F_REBUILD] = 0;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) rep_flag[r] = 0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) {
+        if (rep_builds && rep_flag[r]) rep_builds[r] += 1;
+        rep_flag[r] = 0;
+    }
 }
 __global__ void k_set_request(int* flags, int* rep_flag, int R) {
     if (blockIdx.x == 0 && threadIdx.x == 0) flags[F_REBUILD] = 1;
@@ -645,7 +649,7 @@ int enqueue_build(sg_ctx* ctx) {
         k_chunk_rep<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(nl.row_off, ctx->rep.off, ctx->nrep, nl.dev_flags,
                                                               nl.chunk_rep);
     k_finish<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, nl.pos_last, nl.dev_flags, ctx->rep.rep_of, nl.rep_flag);
-    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(nl.dev_flags, nl.rep_flag, ctx->nrep);
+    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(nl.dev_flags, nl.rep_flag, ctx->nrep, nl.rep_builds);
     SG_LAUNCH_CHECK(ctx, "nlist build");
     return SG_OK;
 }
@@ -691,7 +695,8 @@ int sg_nlist_free(sg_ctx* ctx) {
     sg_nlist_state& nl = ctx->nl;
     void* bufs[] = {nl.cell_count, nl.cell_start, nl.cell_fill, nl.cell_particles, nl.particle_cell, nl.nb_count,
                     nl.nb_pad, nl.row_off, nl.scan_tmp, nl.pair_i, nl.pair_j, nl.dev_flags, nl.pos_last,
-                    nl.rep_max_nb, nl.rep_pad_off, nl.rep_need, nl.rep_flag, nl.cell_unsorted, nl.chunk_rep};
+                    nl.rep_max_nb, nl.rep_pad_off, nl.rep_need, nl.rep_flag, nl.rep_builds, nl.cell_unsorted,
+                    nl.chunk_rep};
     for (void* b : bufs)
         if (b) cudaFree(b);
     nl = sg_nlist_state();
@@ -863,6 +868,8 @@ int sg_rep_nlist_init(sg_ctx* ctx, const double* skin, const double* cutoff, int
     SG_CUDA(ctx, cudaMalloc(&nl.rep_need, sizeof(int) * R));
     SG_CUDA(ctx, cudaMalloc(&nl.rep_flag, sizeof(int) * R));
     SG_CUDA(ctx, cudaMemset(nl.rep_flag, 0, sizeof(int) * R));
+    SG_CUDA(ctx, cudaMalloc(&nl.rep_builds, sizeof(int) * R));
+    SG_CUDA(ctx, cudaMemset(nl.rep_builds, 0, sizeof(int) * R));
     return alloc_list(ctx, *std::max_element(max_nb_r.begin(), max_nb_r.end()));
 }
 
@@ -876,14 +883,16 @@ int sg_nlist_needs_rebuild(sg_ctx* ctx, int32_t* flag) {
     if (!ctx || !flag) return SG_EINVAL;
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_nlist_needs_rebuild");
     ListGeom g = make_geom(ctx);
-    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(ctx->nl.dev_flags, ctx->nl.rep_flag, ctx->nrep);
+    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(ctx->nl.dev_flags, ctx->nl.rep_flag, ctx->nrep,
+                                                              nullptr);
     k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->nl.pos_last, g, ctx->nl.trigger_sq,
                                                            ctx->nl.dev_flags, ctx->rep, ctx->nl.rep_flag);
     SG_LAUNCH_CHECK(ctx, "k_check");
     int f = 0;
     SG_CUDA(ctx, cudaMemcpyAsync(&f, ctx->nl.dev_flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(ctx->nl.dev_flags, ctx->nl.rep_flag, ctx->nrep);
+    k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(ctx->nl.dev_flags, ctx->nl.rep_flag, ctx->nrep,
+                                                              nullptr);
     *flag = f;
     return SG_OK;
 }
@@ -906,6 +915,18 @@ int sg_nlist_count(sg_ctx* ctx, int64_t* npairs) {
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (flags[F_OVERFLOW]) return sg_fail(ctx, SG_ECAPACITY, "neighbour list overflowed (row of %d)", flags[F_OVERFLOW]);
     *npairs = flags[F_NPAIRS];
+    return SG_OK;
+}
+
+int sg_nlist_replica_builds(sg_ctx* ctx, int64_t* counts) {
+    if (!ctx || !counts) return SG_EINVAL;
+    if (!ctx->nl.initialized || !ctx->nl.rep_builds)
+        return sg_fail(ctx, SG_ENOTREADY, "no per-replica lists (sg_rep_nlist_init first)");
+    std::vector<int> c(ctx->nrep);
+    SG_CUDA(ctx, cudaMemcpyAsync(c.data(), ctx->nl.rep_builds, sizeof(int) * c.size(), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int r = 0; r < ctx->nrep; ++r) counts[r] = c[r];
     return SG_OK;
 }
 

@@ -72,6 +72,12 @@ class GpuSystem:
         c = np.ascontiguousarray(np.broadcast_to(np.asarray(cutoff, dtype=np.float64), (3,)))
         self._c(self.L.sg_rep_nlist_init(self.ctx, _dp(s), _dp(c), int(trigger_mode)))
 
+    def rep_nlist_builds(self):
+        """Rebuilds of each replica's list since init_rep_nlist, shape (nrep,)."""
+        out = np.zeros(self.nrep, dtype=np.int64)
+        self._c(self.L.sg_nlist_replica_builds(self.ctx, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out
+
     def rep_kinetic(self):
         """Per-replica (KE, KE_rot), FP64, shape (nrep, 2)."""
         out = np.zeros((self.nrep, 2))

@@ -230,8 +230,11 @@ def test_only_moved_replicas_rebuild(lib, ens):
     g.upload(r=r2)
     assert g.needs_rebuild()
     builds = g.nlist_builds()
+    assert np.array_equal(g.rep_nlist_builds(), np.ones(len(ens["n"]), dtype=np.int64))   # the initial build
     g.update_nlist()
     assert g.nlist_builds() == builds + 1
+    counts = g.rep_nlist_builds()
+    assert counts[k] == 2 and np.all(np.delete(counts, k) == 1)
     pi1, pj1 = g.raw_pairs()
     for kk in range(len(ens["n"])):
         lo, hi = ens["off"][kk], ens["off"][kk + 1]
