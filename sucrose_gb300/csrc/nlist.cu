@@ -472,20 +472,19 @@ __global__ void k_scan_add(int* out, int m, const int* __restrict__ tile_sums, i
 
 // Replica of the first pair of every 32-pair chunk of the row order: the
 // largest r with row_off[off[r]] <= 32 c (pair kernels start their search there).
+// With s_r = row_off[off[r]] the first pair of replica r, the chunks c with
+// s_r <= 32 c < s_(r+1) are replica r's: c in [ceil(s_r / 32), ceil(s_(r+1) / 32)).
+// A warp per replica writes its range (a replica without pairs has none, and
+// its chunk goes to the next replica with pairs, the largest r as required).
 __global__ void k_chunk_rep(const int* __restrict__ row_off, const int* __restrict__ rep_off, int R,
                             const int* flags, int* chunk_rep) {
     if (!flags[F_REBUILD]) return;
-    const int total = flags[F_NPAIRS];
-    const int nchunks = (total + 31) >> 5;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += gridDim.x * blockDim.x) {
-        const int v = c << 5;
-        int lo = 0, hi = R;   // row_off[off[lo]] <= v < row_off[off[hi]] (hi = R: past the end)
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (row_off[rep_off[mid]] <= v) lo = mid;
-            else hi = mid;
-        }
-        chunk_rep[c] = lo;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int r = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < R; r += nwarps) {
+        const int c0 = (row_off[rep_off[r]] + 31) >> 5;
+        const int c1 = (row_off[rep_off[r + 1]] + 31) >> 5;   // rep_off[R] = n: the total
+        for (int c = c0 + lane; c < c1; c += 32) chunk_rep[c] = r;
     }
 }
 
