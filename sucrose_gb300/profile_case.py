@@ -138,7 +138,7 @@ def main():
         LJ, GB = configs.LJ_REPLICA, configs.GB_REPLICA
         g.init_rep_nlist([LJ["skin"], GB["skin"], 0.3], [LJ["list_cutoff"], GB["list_cutoff"], 3.0], trigger_mode=1)
         pairs = bench.replica_pair_params()
-        g.configure_step_pairs(pairs, integrator=capi.INT_LANGEVIN, dt=0.0005, damping=1.0, rotations=1,
+        g.configure_step_pairs(pairs, integrator=capi.INT_LANGEVIN, dt=bench.REPLICAS["dt"], damping=1.0, rotations=1,
                                flags=capi.STEP_FLAT)
         if a.equil:   # untimed steps first, until replicas start to rebuild their lists
             g.step(a.equil)
