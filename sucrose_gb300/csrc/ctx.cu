@@ -170,6 +170,50 @@ __global__ void k_unpack4(int n, const float4* __restrict__ src, double* __restr
     dst[3 * (size_t)n + i] = v.w;
 }
 
+// The same conversions reading / writing the caller's host arrays in place.
+struct HostCols {
+    const double* in[4];
+    double* out[4];
+};
+
+__global__ void k_pack4_host(int n, float4* __restrict__ dst, HostCols c, int mask, const float* wfill) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = dst[i];
+    if (mask & 1) v.x = (float)c.in[0][i];
+    if (mask & 2) v.y = (float)c.in[1][i];
+    if (mask & 4) v.z = (float)c.in[2][i];
+    if (mask & 8) v.w = (float)c.in[3][i];
+    else if (wfill) v.w = wfill[i];
+    dst[i] = v;
+}
+
+__global__ void k_unpack4_host(int n, const float4* __restrict__ src, HostCols c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = src[i];
+    if (c.out[0]) c.out[0][i] = v.x;
+    if (c.out[1]) c.out[1][i] = v.y;
+    if (c.out[2]) c.out[2][i] = v.z;
+    if (c.out[3]) c.out[3][i] = v.w;
+}
+
+// Device address of a host array that kernels can read and write in place:
+// page-locked memory mapped into the device's address space (under unified
+// addressing every cudaHostAlloc allocation is), as the driver reports it for
+// this very pointer; nullptr otherwise (pageable memory: staged by copies).
+// Queried on every call: a cached answer could outlive the allocation.
+static void* host_view(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return a.devicePointer;
+}
+
 int sg_ensure_dstage(sg_ctx* ctx) {
     if (ctx->d_stage) return SG_OK;
     SG_CUDA(ctx, cudaMalloc(&ctx->d_stage, sizeof(double) * 16 * (size_t)ctx->n));
@@ -180,6 +224,24 @@ static int upload4(sg_ctx* ctx, float4* dst, const double* a, const double* b, c
                    const float* wfill_dev, int slot = 0) {
     const int n = ctx->n;
     if (!a && !b && !c && !d) return SG_OK;
+    {
+        // mapped page-locked arrays: one kernel reads them in place over the link
+        HostCols hc{};
+        const double* in[4] = {a, b, c, d};
+        int mask = 0;
+        bool mapped = true;
+        for (int k = 0; k < 4 && mapped; ++k)
+            if (in[k]) {
+                hc.in[k] = (const double*)host_view(in[k]);
+                mapped = hc.in[k] != nullptr;
+                mask |= 1 << k;
+            }
+        if (mapped) {
+            k_pack4_host<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, dst, hc, mask, wfill_dev);
+            SG_LAUNCH_CHECK(ctx, "k_pack4_host");
+            return SG_OK;
+        }
+    }
     if (int rc = sg_ensure_dstage(ctx)) return rc;
     double* st = ctx->d_stage + (size_t)slot * 4 * n;
     const double* src[4] = {a, b, c, d};
@@ -198,6 +260,21 @@ static int upload4(sg_ctx* ctx, float4* dst, const double* a, const double* b, c
 static int download4(sg_ctx* ctx, const float4* src, double* a, double* b, double* c, double* d, int slot = 0) {
     const int n = ctx->n;
     if (!a && !b && !c && !d) return SG_OK;
+    {
+        HostCols hc{};
+        double* out[4] = {a, b, c, d};
+        bool mapped = true;
+        for (int k = 0; k < 4 && mapped; ++k)
+            if (out[k]) {
+                hc.out[k] = (double*)host_view(out[k]);
+                mapped = hc.out[k] != nullptr;
+            }
+        if (mapped) {   // written in place; the caller's synchronisation makes them visible
+            k_unpack4_host<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, src, hc);
+            SG_LAUNCH_CHECK(ctx, "k_unpack4_host");
+            return SG_OK;
+        }
+    }
     if (int rc = sg_ensure_dstage(ctx)) return rc;
     double* st = ctx->d_stage + (size_t)slot * 4 * n;
     k_unpack4<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, src, st);
