@@ -214,6 +214,47 @@ static void* host_view(const void* p) {
     return a.devicePointer;
 }
 
+// The whole state (pos, quat, vel, angm: 13 columns, absent ones skipped) in
+// one pass over mapped host arrays, either way.
+struct StateCols {
+    double* c[13];
+};
+
+__global__ void k_state_from_host(int n, float4* __restrict__ pos, float4* __restrict__ quat,
+                                  float4* __restrict__ vel, float4* __restrict__ angm, StateCols s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4* dst[4] = {pos, quat, vel, angm};
+    const int first[4] = {0, 3, 7, 10}, width[4] = {3, 4, 3, 3};
+#pragma unroll
+    for (int gq = 0; gq < 4; ++gq) {
+        const int f = first[gq];
+        if (!s.c[f] && !s.c[f + 1] && !s.c[f + 2] && (width[gq] < 4 || !s.c[f + 3])) continue;
+        float4 v = dst[gq][i];
+        if (s.c[f]) v.x = (float)s.c[f][i];
+        if (s.c[f + 1]) v.y = (float)s.c[f + 1][i];
+        if (s.c[f + 2]) v.z = (float)s.c[f + 2][i];
+        if (width[gq] == 4 && s.c[f + 3]) v.w = (float)s.c[f + 3][i];
+        dst[gq][i] = v;
+    }
+}
+
+__global__ void k_state_to_host(int n, const float4* __restrict__ pos, const float4* __restrict__ quat,
+                                const float4* __restrict__ vel, const float4* __restrict__ angm, StateCols s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v[4] = {pos[i], quat[i], vel[i], angm[i]};
+    const int first[4] = {0, 3, 7, 10}, width[4] = {3, 4, 3, 3};
+#pragma unroll
+    for (int gq = 0; gq < 4; ++gq) {
+        const int f = first[gq];
+        if (s.c[f]) s.c[f][i] = v[gq].x;
+        if (s.c[f + 1]) s.c[f + 1][i] = v[gq].y;
+        if (s.c[f + 2]) s.c[f + 2][i] = v[gq].z;
+        if (width[gq] == 4 && s.c[f + 3]) s.c[f + 3][i] = v[gq].w;
+    }
+}
+
 int sg_ensure_dstage(sg_ctx* ctx) {
     if (ctx->d_stage) return SG_OK;
     SG_CUDA(ctx, cudaMalloc(&ctx->d_stage, sizeof(double) * 16 * (size_t)ctx->n));
@@ -351,6 +392,21 @@ int sg_upload_state(sg_ctx* ctx, const double* rx, const double* ry, const doubl
                     const double* qx, const double* qy, const double* qz, const double* vx, const double* vy,
                     const double* vz, const double* lx, const double* ly, const double* lz) {
     if (!ctx) return SG_EINVAL;
+    {
+        // every given column mapped page-locked memory: one kernel for the state
+        const double* in[13] = {rx, ry, rz, qw, qx, qy, qz, vx, vy, vz, lx, ly, lz};
+        StateCols sc{};
+        bool mapped = true;
+        for (int k = 0; k < 13 && mapped; ++k)
+            if (in[k]) mapped = (sc.c[k] = (double*)host_view(in[k])) != nullptr;
+        if (mapped) {
+            k_state_from_host<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->quat, ctx->vel,
+                                                                             ctx->angm, sc);
+            SG_LAUNCH_CHECK(ctx, "k_state_from_host");
+            if (ctx->sync_transfers) SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            return SG_OK;
+        }
+    }
     // separate staging slots so that the four copies can be in flight together;
     // quaternion (w x y z) occupies the four lanes in that order
     if (int rc = upload4(ctx, ctx->pos, rx, ry, rz, nullptr, nullptr, 0)) return rc;
@@ -364,6 +420,20 @@ int sg_upload_state(sg_ctx* ctx, const double* rx, const double* ry, const doubl
 int sg_download_state(sg_ctx* ctx, double* rx, double* ry, double* rz, double* qw, double* qx, double* qy,
                       double* qz, double* vx, double* vy, double* vz, double* lx, double* ly, double* lz) {
     if (!ctx) return SG_EINVAL;
+    {
+        double* out[13] = {rx, ry, rz, qw, qx, qy, qz, vx, vy, vz, lx, ly, lz};
+        StateCols sc{};
+        bool mapped = true;
+        for (int k = 0; k < 13 && mapped; ++k)
+            if (out[k]) mapped = (sc.c[k] = (double*)host_view(out[k])) != nullptr;
+        if (mapped) {
+            k_state_to_host<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->quat, ctx->vel,
+                                                                           ctx->angm, sc);
+            SG_LAUNCH_CHECK(ctx, "k_state_to_host");
+            SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            return SG_OK;
+        }
+    }
     if (int rc = download4(ctx, ctx->pos, rx, ry, rz, nullptr, 0)) return rc;
     if (int rc = download4(ctx, ctx->quat, qw, qx, qy, qz, 1)) return rc;
     if (int rc = download4(ctx, ctx->vel, vx, vy, vz, nullptr, 2)) return rc;
