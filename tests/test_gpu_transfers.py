@@ -15,8 +15,9 @@ pytestmark = pytest.mark.gpu
 D = C.POINTER(C.c_double)
 
 
-def _pinned(torch, n):
-    return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+def _pinned(torch, n, offset=0):
+    # offset 1: the column starts 8 bytes into the allocation (8-byte aligned only)
+    return torch.empty(n + offset, dtype=torch.float64, pin_memory=True).numpy()[offset:]
 
 
 def _state(n, seed):
@@ -28,8 +29,9 @@ def _state(n, seed):
     return cols
 
 
+@pytest.mark.parametrize("offset", [0, 1])
 @pytest.mark.parametrize("n", [1, 37, 4096])
-def test_pinned_state_round_trip_matches_pageable(lib, n):
+def test_pinned_state_round_trip_matches_pageable(lib, n, offset):
     torch = pytest.importorskip("torch")
     cols = _state(n, n)
     g = GpuSystem(n, 20.0)
@@ -39,11 +41,11 @@ def test_pinned_state_round_trip_matches_pageable(lib, n):
     assert g.L.sg_download_state(g.ctx, *[a.ctypes.data_as(D) for a in ref]) == 0
     # page-locked: in place
     g.L.sg_upload_state(g.ctx, *[np.zeros(n).ctypes.data_as(D) for _ in range(13)])
-    pin_in = [_pinned(torch, n) for _ in range(13)]
+    pin_in = [_pinned(torch, n, offset if k % 2 else 0) for k in range(13)]
     for p, c in zip(pin_in, cols):
         p[:] = c
     assert g.L.sg_upload_state(g.ctx, *[p.ctypes.data_as(D) for p in pin_in]) == 0
-    pin_out = [_pinned(torch, n) for _ in range(13)]
+    pin_out = [_pinned(torch, n, offset if k % 3 == 0 else 0) for k in range(13)]
     for p in pin_out:
         p[:] = np.nan
     assert g.L.sg_download_state(g.ctx, *[p.ctypes.data_as(D) for p in pin_out]) == 0
