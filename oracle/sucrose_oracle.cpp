@@ -713,7 +713,7 @@ template <class T> T brent(const EcpPair<T>& pair, int& nevals) {
 
 // Tightly converged maximiser of S(l) = l(1-l) r^T G(l)^-1 r on [0,1]:
 // bracketed Newton on S'(l) in the working precision, to |dl| < 1e-15.
-// Not in the reference; it is the FP64 judge of the Newton and MLP paths.
+// Not in the reference; it is the FP64 check of the Newton and MLP paths.
 template <class T> T tight_lambda(const EcpPair<T>& p, int& nevals) {
     T lo = 0, hi = 1, L = T(0.5);
     nevals = 0;
