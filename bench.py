@@ -142,8 +142,8 @@ FLAGS = 0   # step-graph flags (capi.STEP_FLAT under --flat-graph)
 # committed ncu captures of these workloads (traffic is not measurable from
 # inside a timed run)
 NCU_TRAFFIC = {
-    "EC": {"bytes": 11.05e6, "source": "profiles/k_pair_ecp_newton_N65536.md: ncu, 0.46 M listed pairs (lattice state)"},
-    "GB": {"bytes": 45.31e6, "source": "profiles/k_pair_gb_filtered_N32768.md: ncu, 5.7 M listed pairs"},
+    "EC": {"bytes": 12.60e6, "source": "profiles/k_pair_ecp_newton_N65536.md: ncu, 0.46 M listed pairs (lattice state)"},
+    "GB": {"bytes": 45.26e6, "source": "profiles/k_pair_gb_filtered_N32768.md: ncu, 5.32 M listed pairs (lattice state)"},
     "COULOMB": {"bytes": 65.06e6, "source": "profiles/k_pair_coulomb_charged_N131072.md: ncu, 7.57 M listed pairs"},
 }
 
