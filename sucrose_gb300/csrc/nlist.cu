@@ -256,11 +256,16 @@ __device__ __forceinline__ void row_done(int i, int cnt, int cap, int* nb_count,
     }
 }
 
+// block_order (replica contexts): the 256-row block each CTA takes, the
+// blocks with the longest rows first, so that no long block starts late and
+// leaves the other SMs idle at the end (rows and their contents unchanged)
 __global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g0, const int* __restrict__ cell_start,
                              const int* __restrict__ cell_particles, int max_nb, int* nb_pad, int* nb_count,
-                             int* flags, RepDev rp, PadRep pr, const int* rep_flag) {
+                             int* flags, RepDev rp, PadRep pr, const int* rep_flag,
+                             const int* __restrict__ block_order) {
     if (!flags[F_REBUILD]) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int bx = block_order ? block_order[blockIdx.x] : (int)blockIdx.x;
+    int i = bx * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (rp.rep_of && !rep_flag[rp.rep_of[i]]) return;   // this replica keeps its rows
     float4 pi = pos[i];
@@ -635,7 +640,8 @@ int enqueue_build(sg_ctx* ctx) {
                                                nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag);
         else
             k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
-                                                      nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag);
+                                                      nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag,
+                                                      nl.row_block_order);
 
     } else {
         k_begin<<<1, 32, 0, ctx->stream>>>(nl.dev_flags, nl.cell_count, nl.cell_fill, 0);
@@ -695,7 +701,7 @@ int sg_nlist_free(sg_ctx* ctx) {
     void* bufs[] = {nl.cell_count, nl.cell_start, nl.cell_fill, nl.cell_particles, nl.particle_cell, nl.nb_count,
                     nl.nb_pad, nl.row_off, nl.scan_tmp, nl.pair_i, nl.pair_j, nl.dev_flags, nl.pos_last,
                     nl.rep_max_nb, nl.rep_pad_off, nl.rep_need, nl.rep_flag, nl.rep_builds, nl.cell_unsorted,
-                    nl.chunk_rep};
+                    nl.chunk_rep, nl.row_block_order};
     for (void* b : bufs)
         if (b) cudaFree(b);
     nl = sg_nlist_state();
@@ -869,6 +875,28 @@ int sg_rep_nlist_init(sg_ctx* ctx, const double* skin, const double* cutoff, int
     SG_CUDA(ctx, cudaMemset(nl.rep_flag, 0, sizeof(int) * R));
     SG_CUDA(ctx, cudaMalloc(&nl.rep_builds, sizeof(int) * R));
     SG_CUDA(ctx, cudaMemset(nl.rep_builds, 0, sizeof(int) * R));
+    {
+        // blocks of the row kernel by their longest row: a one-cell replica's
+        // row i tests its N - 1 - i later particles, a row of a replica with
+        // cells visits 27 cells of about N / cells particles
+        const int n = ctx->n, nblk = (n + 255) / 256;
+        std::vector<double> work(nblk, 0.0);
+        for (int r = 0; r < R; ++r) {
+            const int o = ctx->h_rep_off[r], e = ctx->h_rep_off[r + 1], nr = e - o;
+            const int4 gr = grid[r];
+            const double cells = gr.x ? (double)gr.x * gr.y * gr.z : 1.0;
+            for (int i = o; i < e; ++i) {
+                const double w = gr.x ? 27.0 * nr / cells : (double)(e - 1 - i);
+                double& wb = work[i / 256];
+                wb = std::max(wb, w);
+            }
+        }
+        std::vector<int> order(nblk);
+        for (int b = 0; b < nblk; ++b) order[b] = b;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+        SG_CUDA(ctx, cudaMalloc(&nl.row_block_order, sizeof(int) * nblk));
+        SG_CUDA(ctx, cudaMemcpy(nl.row_block_order, order.data(), sizeof(int) * nblk, cudaMemcpyHostToDevice));
+    }
     return alloc_list(ctx, *std::max_element(max_nb_r.begin(), max_nb_r.end()));
 }
 

@@ -66,6 +66,7 @@ struct sg_nlist_state {
     int* rep_need = nullptr;         // [R] longest row seen when a row overflowed
     int* rep_flag = nullptr;         // [R] rebuild requested for this replica
     int* rep_builds = nullptr;       // [R] rebuilds of each replica's rows since sg_nlist_init
+    int* row_block_order = nullptr;  // replica contexts: 256-row blocks of the row kernel, longest rows first
     int* cell_unsorted = nullptr;    // [n] cell members before ordering
     int* chunk_rep = nullptr;        // [capacity / 32 + 2] replica of each 32-pair chunk
     std::vector<int> h_rep_max_nb;
