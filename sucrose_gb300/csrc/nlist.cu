@@ -498,25 +498,54 @@ __global__ void k_chunk_rep(const int* __restrict__ row_off, const int* __restri
 // in the replica's own section (it starts where the replica's padded rows
 // start), so only replicas that rebuilt are rewritten: the pair at row-order
 // index v of replica r sits at pad_off[r] + v - row_off[off[r]].
-__global__ void k_compact(int n, int max_nb, const int* __restrict__ nb_pad, const int* __restrict__ nb_count,
-                          const int* __restrict__ row_off, int* pair_i, int* pair_j, const int* flags, RepDev rp,
-                          PadRep pr, const int* rep_flag) {
+// A warp takes 32 consecutive rows and moves them 32 columns at a time
+// through shared memory: slot k of the 32 rows is one coalesced read of the
+// column-major padded rows, and each row's 32 entries one coalesced write of
+// the flat arrays.
+constexpr int COMPACT_BLOCK = 256;
+__global__ void __launch_bounds__(COMPACT_BLOCK) k_compact(int n, int max_nb, const int* __restrict__ nb_pad,
+                                                           const int* __restrict__ nb_count,
+                                                           const int* __restrict__ row_off, int* pair_i, int* pair_j,
+                                                           const int* flags, RepDev rp, PadRep pr,
+                                                           const int* rep_flag) {
     if (!flags[F_REBUILD]) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    size_t base, stride;
-    int cap;
-    pad_slot(n, i, max_nb, rp, pr, base, stride, cap);
-    size_t o = (size_t)row_off[i];
-    if (rp.rep_of) {
-        const int r = rp.rep_of[i];
-        if (!rep_flag[r]) return;
-        o = (size_t)pr.pad_off[r] + (size_t)(row_off[i] - row_off[rp.off[r]]);
+    __shared__ int tile[COMPACT_BLOCK / 32][32][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool on = i < n;
+    size_t base = 0, stride = 0, o = 0;
+    int c = 0;
+    if (on) {
+        int cap;
+        pad_slot(n, i, max_nb, rp, pr, base, stride, cap);
+        o = (size_t)row_off[i];
+        if (rp.rep_of) {
+            const int r = rp.rep_of[i];
+            on = rep_flag[r] != 0;
+            o = (size_t)pr.pad_off[r] + (size_t)(row_off[i] - row_off[rp.off[r]]);
+        }
+        c = on ? nb_count[i] : 0;
     }
-    const int c = nb_count[i];
-    for (int k = 0; k < c; ++k) {
-        pair_i[o + k] = i;
-        pair_j[o + k] = nb_pad[base + (size_t)k * stride];
+    int cmax = c;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) cmax = max(cmax, __shfl_xor_sync(0xffffffffu, cmax, s));
+    int (*t)[33] = tile[w];
+    for (int k0 = 0; k0 < cmax; k0 += 32) {
+        // read: lane = row, slots k0 .. k0 + 31
+        for (int kk = 0; kk < 32; ++kk)
+            if (k0 + kk < c) t[kk][lane] = nb_pad[base + (size_t)(k0 + kk) * stride];
+        __syncwarp();
+        // write: row by row, lane = slot
+        for (int rr = 0; rr < 32; ++rr) {
+            const int cr = __shfl_sync(0xffffffffu, c, rr);
+            const unsigned long long orr = __shfl_sync(0xffffffffu, (unsigned long long)o, rr);
+            const int k = k0 + lane;
+            if (k < cr) {
+                pair_i[orr + k] = blockIdx.x * blockDim.x + (w << 5) + rr;
+                pair_j[orr + k] = t[lane][rr];
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -648,8 +677,9 @@ int enqueue_build(sg_ctx* ctx) {
         k_rows_all<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
     }
     if (int rc = scan(ctx, nl.nb_count, n, nl.row_off, nl.dev_flags + F_NPAIRS, nl.dev_flags)) return rc;
-    k_compact<<<nb, 256, 0, ctx->stream>>>(n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off, nl.pair_i, nl.pair_j,
-                                           nl.dev_flags, ctx->rep, pad, nl.rep_flag);
+    k_compact<<<(n + COMPACT_BLOCK - 1) / COMPACT_BLOCK, COMPACT_BLOCK, 0, ctx->stream>>>(
+        n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off, nl.pair_i, nl.pair_j, nl.dev_flags, ctx->rep, pad,
+        nl.rep_flag);
     if (ctx->nrep)
         k_chunk_rep<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(nl.row_off, ctx->rep.off, ctx->nrep, nl.dev_flags,
                                                               nl.chunk_rep);
