@@ -77,8 +77,13 @@ __global__ void k_bonded(int n, const int4* __restrict__ atoms, const float4* __
                 strength = coeff * (c - p.y);
                 e[0] += 0.5f * coeff * (c - p.y) * (c - p.y);
             } else {
-                const float th = acosf(fminf(1.f, fmaxf(-1.f, prefac * C12)));
-                strength = coeff * (th - p.w) / sinf(th);
+                // theta and sin(theta) from the cross product: acos of the
+                // FP32 cosine is exactly 0 (and sin 0 divides) for bonds within
+                // ~3e-4 rad of parallel, where |VI x VJ| still resolves the angle
+                const float3 nb = cross3(VI, VJ);
+                const float sn = sqrtf(dot3(nb, nb));
+                const float th = atan2f(sn, C12);
+                strength = coeff * (th - p.w) / (sn * prefac);
                 e[0] += 0.5f * coeff * (th - p.w) * (th - p.w);
             }
             const float s = strength * prefac;
@@ -106,9 +111,16 @@ __global__ void k_bonded(int n, const int4* __restrict__ atoms, const float4* __
                 atomicAdd(&force[at.w], make_float4(F[3].x, F[3].y, F[3].z, 0.f));
                 continue;
             } else {
-                const float D12 = C11 * C22 - C12 * C12, D23 = C22 * C33 - C23 * C23;
+                // D12 = C11 C22 - C12^2 = |VI x VJ|^2, D23 = |VJ x VK|^2 and
+                // fac = C23 C12 - C13 C22 = (VI x VJ).(VJ x VK) (Lagrange and
+                // Binet-Cauchy identities), formed from the cross products: in
+                // FP32 the differences cancel to zero or below for bends within
+                // ~3e-4 rad of straight, which occur every few thousand steps in
+                // a chain melt, and the dihedral then turns NaN
+                const float3 n1 = cross3(VI, VJ), n2 = cross3(VJ, VK);
+                const float D12 = dot3(n1, n1), D23 = dot3(n2, n2);
                 prefac = rsqrtf(D23 * D12);
-                fac = C23 * C12 - C13 * C22;
+                fac = dot3(n1, n2);
                 fac1 = fac / D23;
                 fac2 = fac / D12;
                 if constexpr (KIND == SG_DIH) {

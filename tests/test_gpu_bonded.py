@@ -39,6 +39,67 @@ def test_bonded_parity(lib, kind):
     assert np.linalg.norm(F.sum(0)) < 1e-4 * np.linalg.norm(F)
 
 
+@pytest.mark.parametrize("kind", [capi.DIH, capi.COSINE_DIH])
+def test_dihedral_near_straight_bend(lib, kind):
+    # one bend of each dihedral straight to within 3e-5 to 3e-4 rad: the FP32
+    # dihedral stays finite and matches the FP64 oracle (forces of order
+    # 1 / angle there, and FP32 brackets with errors of order 1e-7 / angle,
+    # hence the looser bound)
+    rng = np.random.default_rng(21)
+    quads = []
+    for k, eps in enumerate(np.geomspace(3e-5, 3e-4, 12)):
+        o = np.array([8.0 * k - 40.0, 0.0, 0.0])
+        a = o + np.array([0.0, 0.0, 0.0])
+        b = a + np.array([1.0, 0.0, 0.0])
+        c = b + np.array([np.cos(eps), np.sin(eps), 0.0])          # bend a-b-c straight to within eps
+        ang = rng.uniform(0.5, 2.5)
+        d = c + np.array([0.3, np.cos(ang), np.sin(ang)])
+        quads.append([a, b, c, d])
+    r = np.concatenate(quads)
+    P = Pair(r, None, 100.0)
+    atoms = np.arange(len(r)).reshape(-1, 4)
+    angle = np.full(len(atoms), 150.0) if kind == capi.COSINE_DIH else None
+    P.g.zero_forces()
+    P.g.bonded_set(kind, atoms, 1.0, angle)
+    pe = P.g.bonded_forces(kind)
+    F, _ = P.g.forces()
+    assert np.isfinite(pe) and np.all(np.isfinite(F))
+    P.o.zero_forces()
+    P.o.bonded_forces(kind, atoms, np.ones(len(atoms)), angle)
+    Fo, _ = P.oracle_forces()
+    assert rel(F, Fo) < 2e-2
+    assert abs(pe - P.o.s.pot_eng) <= 1e-4 * max(1.0, abs(P.o.s.pot_eng))
+
+
+def test_angle_bend_near_parallel_bonds(lib):
+    # angle_bend_ with the two bond vectors parallel to within 3e-5 to 3e-4
+    # rad (a straight chain): finite, and the FP64 oracle's energy and forces
+    rng = np.random.default_rng(22)
+    tri = []
+    for k, eps in enumerate(np.geomspace(3e-5, 3e-4, 12)):
+        a = np.array([8.0 * k - 40.0, 0.0, 0.0])
+        b = a + np.array([1.0, 0.0, 0.0])
+        ax = rng.normal(size=3)
+        ax -= ax[0] * np.array([1.0, 0.0, 0.0])
+        ax /= np.linalg.norm(ax)
+        c = b + np.cos(eps) * np.array([1.0, 0.0, 0.0]) + np.sin(eps) * ax
+        tri.append([a, b, c])
+    r = np.concatenate(tri)
+    P = Pair(r, None, 100.0)
+    atoms = np.arange(len(r)).reshape(-1, 3)
+    angle = np.full(len(atoms), 60.0)
+    P.g.zero_forces()
+    P.g.bonded_set(capi.ANGLE_BEND, atoms, 2.0, angle)
+    pe = P.g.bonded_forces(capi.ANGLE_BEND)
+    F, _ = P.g.forces()
+    assert np.isfinite(pe) and np.all(np.isfinite(F))
+    P.o.zero_forces()
+    P.o.bonded_forces(capi.ANGLE_BEND, atoms, np.full(len(atoms), 2.0), angle)
+    Fo, _ = P.oracle_forces()
+    assert rel(F, Fo) < 2e-2
+    assert abs(pe - P.o.s.pot_eng) <= 1e-4 * max(1.0, abs(P.o.s.pot_eng))
+
+
 def test_bonded_one_based_indices(lib):
     P, bonds, bends, dihs = chains()
     P.g.zero_forces()
