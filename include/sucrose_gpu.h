@@ -447,13 +447,19 @@ int sg_peak_fma(sg_ctx* ctx, int32_t fp64, double* tflops);
  * whose device memory comes from their own pool, OpenACC / CUDA Fortran
  * programs that keep RX, RY, RZ and FX, FY, FZ resident on the device.
  *
- * Evaluates lj_ / lj12_ / ljw_ / wca_ (params->kind) over the half list
- * (pair_i[k] < pair_j[k], 0-based) and ADDS the forces into fx, fy, fz and
- * {pot_eng, pair virial} into pot_virial[0..1], like the reference's pair
- * loop (README.md:86-103). rx..rz, pair_i, pair_j, fx..fz and pot_virial are
- * DEVICE pointers owned by the caller; box and params are host memory; the
- * work is enqueued on `stream` (a cudaStream_t, NULL for the default stream)
- * and the call returns without waiting.
+ * Evaluates lj_ / lj12_ / ljw_ / wca_ (params->kind) over a half list that
+ * names each unordered pair once, in any order and either way round, and
+ * ADDS the forces into fx, fy, fz and {pot_eng, pair virial} into
+ * pot_virial[0..1], like the reference's pair loop (README.md:86-103): the
+ * force of pair k acts on pair_i[k] with r = r_i - r_j, and its negative on
+ * pair_j[k]. Indices are 0-based, or 1-based (Fortran's RX(1..N)) when
+ * one_based is nonzero. A pair whose index lies outside the n particles, or
+ * whose two indices are equal, is skipped; when bad_pairs is not NULL the call
+ * sets *bad_pairs (a DEVICE int32) to the number of pairs it skipped.
+ * rx..rz, pair_i, pair_j, fx..fz, pot_virial and bad_pairs are DEVICE
+ * pointers owned by the caller; box and params are host memory; the work is
+ * enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the
+ * call returns without waiting.
  *
  * It allocates nothing: its scratch is a fixed device array inside the
  * library (about 2.1 MiB, held by every GPU that loads the library until the
@@ -464,9 +470,9 @@ int sg_peak_fma(sg_ctx* ctx, int32_t fp64, double* tflops);
  * (other streams, other host threads) race and must be serialised by the
  * caller. err (may be NULL) receives a message on failure. */
 int sg_lj_forces_noalloc(int32_t n, const double* rx, const double* ry, const double* rz, const int32_t* pair_i,
-                         const int32_t* pair_j, int64_t npairs, const double box[3], int32_t periodic,
-                         const sg_pair_params* params, double* fx, double* fy, double* fz, double* pot_virial,
-                         void* stream, char* err, int32_t err_len);
+                         const int32_t* pair_j, int64_t npairs, int32_t one_based, const double box[3],
+                         int32_t periodic, const sg_pair_params* params, double* fx, double* fy, double* fz,
+                         double* pot_virial, int32_t* bad_pairs, void* stream, char* err, int32_t err_len);
 
 /* ---- Philox4x32-10 (fortran/xmath.f90:42-113) -------------------------------- */
 /* Host-side single block, for callers that mirror philox_uniform. */

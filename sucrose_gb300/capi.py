@@ -147,8 +147,9 @@ SIGNATURES = [
     ("sg_step_kernel_count", C.c_int, [_P, _I64]),
     ("sg_peak_fma", C.c_int, [_P, C.c_int32, _D]),
     ("sg_lj_forces_noalloc", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                       C.c_int64, _D, C.c_int32, C.POINTER(PairParams), C.c_void_p, C.c_void_p,
-                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int32]),
+                                       C.c_int64, C.c_int32, _D, C.c_int32, C.POINTER(PairParams), C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
+                                       C.c_int32]),
     ("sg_philox4x32", None, [_U32, _U32, _U32]),
     ("sg_philox4x32_device", C.c_int, [_P, C.c_int64, _U32, _U32, _U32]),
     ("sg_philox_normal_3seq_device", C.c_int, [_P, C.c_int64, _I32, _D]),

@@ -30,6 +30,7 @@ struct NoallocScratch {
     float4 acc[SG_NOALLOC_MAX_N];                 // per-particle force sums (FP32)
     double partials[SG_NOALLOC_MAX_BLOCKS * 2];   // per-block PE and virial
     unsigned int done;                            // blocks finished (last block reduces)
+    unsigned int bad;                             // pairs skipped for a bad index
 };
 
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
@@ -80,42 +81,65 @@ __device__ __forceinline__ void lj_pair(const LJ64& p, float3 r, float3& f, floa
     vir = coeff * rsq;
 }
 
-// One lane per pair, 32 consecutive pairs per warp; I-side sums by segmented
-// shuffle scan over runs of equal i, J-side by float4 atomics into the
-// scratch accumulator; PE and virial per block in FP64, finished by the last
-// block, which adds them to out2[0..1].
+// One lane per pair, 32 consecutive pairs per warp; I-side sums by a
+// segmented shuffle scan over runs of equal i, J-side by float4 atomics into
+// the scratch accumulator; PE and virial per block in FP64, finished by the
+// last block, which adds them to out2[0..1].
+//
+// The caller's list may hold the pairs of one i in any order, so a run is a
+// maximal stretch of adjacent lanes with the same i, and the scan carries a
+// head flag: a lane stops adding from below once its partial sum has reached
+// the first lane of its run. The last lane of each run flushes its run's sum,
+// so an i that appears in two separate runs of a warp is flushed twice, each
+// time with only that run's pairs.
+//
+// A pair whose index (after the one_based shift) lies outside [0, n), or
+// whose two indices are equal, is skipped and counted in sc->bad.
 __global__ void __launch_bounds__(256) k_pair_noalloc(const double* __restrict__ rx, const double* __restrict__ ry,
                                                       const double* __restrict__ rz, const int* __restrict__ pi_,
-                                                      const int* __restrict__ pj_, long long np, LJ64 p, float3 box,
-                                                      float3 inv_box, int periodic, NoallocScratch* sc,
-                                                      double* out2) {
+                                                      const int* __restrict__ pj_, long long np, int n, int base_index,
+                                                      LJ64 p, float3 box, float3 inv_box, int periodic,
+                                                      NoallocScratch* sc, double* out2) {
     const int lane = threadIdx.x & 31;
     const long long gwarp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     float pe_t = 0.f, vir_t = 0.f;
     for (long long base = gwarp * 32; base < np; base += nwarps * 32) {
         const long long t = base + lane;
-        const bool valid = t < np;
-        int i = -1, j = 0;
+        int i = -1;
         float3 f = make_float3(0.f, 0.f, 0.f);
-        if (valid) {
-            i = pi_[t];
-            j = pj_[t];
-            float3 r = make_float3((float)(rx[i] - rx[j]), (float)(ry[i] - ry[j]), (float)(rz[i] - rz[j]));
-            r = min_image(r, box, inv_box, periodic);
-            float pe, vir;
-            lj_pair(p, r, f, pe, vir);
-            pe_t += pe;
-            vir_t += vir;
-            atomicAdd(&sc->acc[j], make_float4(-f.x, -f.y, -f.z, 0.f));
+        if (t < np) {
+            // unsigned: a negative or huge index wraps above n and is refused
+            const unsigned ii = (unsigned)pi_[t] - (unsigned)base_index;
+            const unsigned jj = (unsigned)pj_[t] - (unsigned)base_index;
+            if (ii < (unsigned)n && jj < (unsigned)n && ii != jj) {
+                i = (int)ii;
+                float3 r = make_float3((float)(rx[ii] - rx[jj]), (float)(ry[ii] - ry[jj]), (float)(rz[ii] - rz[jj]));
+                r = min_image(r, box, inv_box, periodic);
+                float pe, vir;
+                lj_pair(p, r, f, pe, vir);
+                pe_t += pe;
+                vir_t += vir;
+                atomicAdd(&sc->acc[jj], make_float4(-f.x, -f.y, -f.z, 0.f));
+            } else {
+                atomicAdd(&sc->bad, 1u);
+            }
         }
+        // head flag: lane 0, or a lane whose i differs from the lane below
+        const int iprev = __shfl_up_sync(0xffffffffu, i, 1);
+        bool head = (lane == 0) || (iprev != i);
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int io = __shfl_up_sync(0xffffffffu, i, o);
             const float fx = __shfl_up_sync(0xffffffffu, f.x, o);
             const float fy = __shfl_up_sync(0xffffffffu, f.y, o);
             const float fz = __shfl_up_sync(0xffffffffu, f.z, o);
-            if (lane >= o && io == i) { f.x += fx; f.y += fy; f.z += fz; }
+            const bool hup = __shfl_up_sync(0xffffffffu, head, o);
+            if (lane >= o && !head) {
+                f.x += fx;
+                f.y += fy;
+                f.z += fz;
+                head = hup;
+            }
         }
         const int inext = __shfl_down_sync(0xffffffffu, i, 1);
         if ((lane == 31 || inext != i) && i >= 0) atomicAdd(&sc->acc[i], make_float4(f.x, f.y, f.z, 0.f));
@@ -124,8 +148,10 @@ __global__ void __launch_bounds__(256) k_pair_noalloc(const double* __restrict__
     block_reduce_finish<2>(e, sc->partials, &sc->done, out2);
 }
 
-__global__ void k_noalloc_add(int n, const NoallocScratch* __restrict__ sc, double* fx, double* fy, double* fz) {
+__global__ void k_noalloc_add(int n, const NoallocScratch* __restrict__ sc, double* fx, double* fy, double* fz,
+                              int* bad_pairs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && bad_pairs) *bad_pairs = (int)sc->bad;
     if (i >= n) return;
     const float4 a = sc->acc[i];
     fx[i] += a.x;
@@ -144,10 +170,10 @@ int fail(char* err, int len, int code, const char* msg) {
 }  // namespace
 
 extern "C" int sg_lj_forces_noalloc(int32_t n, const double* rx, const double* ry, const double* rz,
-                                    const int32_t* pair_i, const int32_t* pair_j, int64_t npairs,
+                                    const int32_t* pair_i, const int32_t* pair_j, int64_t npairs, int32_t one_based,
                                     const double box[3], int32_t periodic, const sg_pair_params* params, double* fx,
-                                    double* fy, double* fz, double* pot_virial, void* stream, char* err,
-                                    int32_t err_len) {
+                                    double* fy, double* fz, double* pot_virial, int32_t* bad_pairs, void* stream,
+                                    char* err, int32_t err_len) {
     if (!params || !box) return fail(err, err_len, SG_EINVAL, "params and box are required");
     if (params->kind != SG_LJ && params->kind != SG_LJ12 && params->kind != SG_LJW && params->kind != SG_WCA)
         return fail(err, err_len, SG_EINVAL, "sg_lj_forces_noalloc supports SG_LJ, SG_LJ12, SG_LJW and SG_WCA only");
@@ -201,7 +227,7 @@ extern "C" int sg_lj_forces_noalloc(int32_t n, const double* rx, const double* r
                                : make_float3(0.f, 0.f, 0.f);
     // the scratch keeps the previous call's contents: clear what must start at zero
     if (cudaMemsetAsync(sc->acc, 0, sizeof(float4) * (size_t)n, s) != cudaSuccess ||
-        cudaMemsetAsync(&sc->done, 0, sizeof(unsigned int), s) != cudaSuccess)
+        cudaMemsetAsync(&sc->done, 0, 2 * sizeof(unsigned int), s) != cudaSuccess)
         return fail(err, err_len, SG_ECUDA, "cudaMemsetAsync on the scratch failed");
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -209,9 +235,9 @@ extern "C" int sg_lj_forces_noalloc(int32_t n, const double* rx, const double* r
     if (grid > 4LL * sms) grid = 4LL * sms;
     if (grid > SG_NOALLOC_MAX_BLOCKS) grid = SG_NOALLOC_MAX_BLOCKS;
     if (grid < 1) grid = 1;
-    k_pair_noalloc<<<(int)grid, 256, 0, s>>>(rx, ry, rz, pair_i, pair_j, (long long)npairs, p, bf, ib, periodic ? 1 : 0,
-                                             sc, pot_virial);
-    k_noalloc_add<<<(n + 255) / 256, 256, 0, s>>>(n, sc, fx, fy, fz);
+    k_pair_noalloc<<<(int)grid, 256, 0, s>>>(rx, ry, rz, pair_i, pair_j, (long long)npairs, n, one_based ? 1 : 0, p,
+                                             bf, ib, periodic ? 1 : 0, sc, pot_virial);
+    k_noalloc_add<<<(n + 255) / 256, 256, 0, s>>>(n, sc, fx, fy, fz, bad_pairs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(err, err_len, SG_ECUDA, cudaGetErrorString(e));
     return SG_OK;
