@@ -4,14 +4,19 @@ Workload (default "ecp"): N = 65536 biaxial ellipsoids, semi-axes (1.5, 1, 0.5)
 (full axes sig = (3, 2, 1)), packing fraction 0.35 (number density 0.1114),
 repulsive ECP (ecpr) with the plain Newton contact solve, Nose-Hoover chains
 of length 3 on translation and rotation, T* = 1.2, dt = 0.001, Verlet list
-rc 3.0 + skin 0.3. Synthetic, seeded: an aligned lattice equilibrated on the
-device with Langevin dynamics before timing (the reference publishes no
-placement routine and no benchmark data set).
+rc 3.0 + skin 0.3. Synthetic, seeded: uniform random orientations and
+non-overlapping positions from the isotropic placement
+(configs.isotropic_placement: growth from a fifth of full size with overlap
+relaxation), thermal velocities and angular momenta; the reference publishes
+no placement routine and no benchmark data set. Both arms start from the same
+bits of that state.
 
 A step is one full timestep (integrators, list check with conditional
 rebuild, forces) launched as one captured CUDA graph. value = listed pairs x
 steps / device time of those steps; e2e repeats the measurement through the
-C ABI with FP64 host arrays copied in and out every step.
+C ABI with FP64 host arrays copied in and out every step. The default line
+also carries the Gay-Berne fluid ("gb") and the 4096-replica ensemble
+("replicas") as sub-objects, each with its own roofline and CPU baseline.
 """
 import argparse
 import json
@@ -30,12 +35,19 @@ sys.path.insert(0, ROOT)
 TAU_PS = 2.156  # argon LJ time unit sigma*sqrt(m/eps) in ps (sigma 3.405 A, eps/kB 119.8 K, m 39.948 u)
 
 WORKLOADS = {
-    "ecp": dict(workload="ecp_biaxial_ecpr_nhc_N65536_phi0.35", counts=(32, 32, 64), sig=(3.0, 2.0, 1.0),
+    "ecp": dict(workload="ecp_biaxial_ecpr_nhc_N65536_phi0.35", n=65536, sig=(3.0, 2.0, 1.0),
                 eps=(1.0, 1.0, 1.0), density=0.1114, kind="ECPR", cutoff=3.0, list_cutoff=3.0, skin=0.3,
-                integrator="NH", T=1.2, dt=0.001, tilt=0.2),
-    "gb": dict(workload="gay_berne_3_5_2_1_langevin_N32768_rho0.30", counts=(64, 32, 16), sig=(1.0, 1.0, 3.0),
+                integrator="NH", T=1.2, dt=0.001, seed=1003),
+    "gb": dict(workload="gay_berne_3_5_2_1_langevin_N32768_rho0.30", n=32768, sig=(1.0, 1.0, 3.0),
                eps=(1.0, 1.0, 0.2), density=0.30, kind="GB", cutoff=4.0, list_cutoff=6.0, skin=0.4,
-               integrator="LANGEVIN", T=1.0, dt=0.002, tilt=0.15, mu=2, nu=1),
+               integrator="LANGEVIN", T=1.0, dt=0.002, mu=2, nu=1, seed=1002),
+}
+
+# one metric string per workload, printed identically by both arms
+METRICS = {
+    "ecp": "ECP pair-evals/s (ecpr, N=65536, phi=0.35)",
+    "gb": "GB pair-evals/s (GB(3,5,2,1), N=32768, rho=0.30)",
+    "replicas": "replica-ensemble pair-evals/s (4096 LJ + GB replicas)",
 }
 
 
@@ -55,6 +67,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary measurements")
     ap.add_argument("--no-mlp", action="store_true", help="skip the learned-guess leg")
+    ap.add_argument("--no-sub", action="store_true", help="skip the gb and replicas sub-objects of the ecp line")
+    ap.add_argument("--profile-case", default=None, help="run one small profiling case and exit (see PROFILE_CASES)")
+    ap.add_argument("--reps", type=int, default=3, help="launches of the profiled kernels (--profile-case)")
+    ap.add_argument("--state-equil", type=int, default=0,
+                    help="untimed Langevin steps from the placed state before timing (ecp, gb)")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000)
     ap.add_argument("--mlp-epochs", type=int, default=3)
     return ap.parse_args()
@@ -115,18 +132,36 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------- workload ---
-def make_system(w, seed=1003):
-    from sucrose_gb300 import GpuSystem, capi, configs
-    r, q, box = configs.aligned_lattice(w["counts"], w["sig"], w["density"], seed=seed, jitter=0.02, tilt=w["tilt"])
+def initial_state(w, seed=None):
+    """The workload's seeded initial state, the same bits in both arms:
+    isotropic non-overlapping placement (uniform orientations), velocities by
+    the reference's set_velocity_to_temperature convention, thermal
+    body-frame angular momenta. Returns r, q, box, v, l, placement report."""
+    from sucrose_gb300 import configs
+    seed = w["seed"] if seed is None else seed
+    r, q, box, rep = configs.isotropic_placement(w["n"], w["sig"], w["density"], seed=seed)
     n = len(r)
     v = configs.velocities_to_temperature(n, w["T"], seed)
-    I = configs.default_inertia(w["sig"])
-    l = configs.angular_momenta(q, I, w["T"], seed)
-    g = GpuSystem(n, box)
+    l = configs.angular_momenta(q, configs.default_inertia(w["sig"]), w["T"], seed)
+    return r, q, box, v, l, rep
+
+
+def long_axis(w):
+    return int(np.argmax(w["sig"]))
+
+
+def make_system(w, seed=None):
+    from sucrose_gb300 import GpuSystem
+    t0 = time.perf_counter()
+    r, q, box, v, l, rep = initial_state(w, seed)
+    t_place = time.perf_counter() - t0
+    g = GpuSystem(len(r), box)
     g.set_particles(sig=w["sig"], eps=w["eps"])
     g.upload(r=r, q=q, v=v, l=l)
     g.init_nlist(w["skin"], w["list_cutoff"], trigger_mode=1)
-    return g, box
+    info = {"placement_s": t_place, "placement_sweeps": int(rep.sweeps),
+            "placement_min_contact_ratio": float(rep.min_contact_ratio)}
+    return g, box, info
 
 
 def pair_params(g, w, solver):
@@ -142,9 +177,12 @@ FLAGS = 0   # step-graph flags (capi.STEP_FLAT under --flat-graph)
 # committed ncu captures of these workloads (traffic is not measurable from
 # inside a timed run)
 NCU_TRAFFIC = {
-    "EC": {"bytes": 12.60e6, "source": "profiles/k_pair_ecp_newton_N65536.md: ncu, 0.46 M listed pairs (lattice state)"},
-    "GB": {"bytes": 45.26e6, "source": "profiles/k_pair_gb_filtered_N32768.md: ncu, 5.32 M listed pairs (lattice state)"},
-    "COULOMB": {"bytes": 65.06e6, "source": "profiles/k_pair_coulomb_charged_N131072.md: ncu, 7.57 M listed pairs"},
+    "EC": {"bytes": 12.60e6, "pairs": 0.46e6,
+           "source": "profiles/k_pair_ecp_newton_N65536.md: ncu, 0.46 M listed pairs"},
+    "GB": {"bytes": 45.26e6, "pairs": 5.32e6,
+           "source": "profiles/k_pair_gb_filtered_N32768.md: ncu, 5.32 M listed pairs"},
+    "COULOMB": {"bytes": 65.06e6, "pairs": 7.57e6,
+                "source": "profiles/k_pair_coulomb_charged_N131072.md: ncu, 7.57 M listed pairs"},
 }
 
 
@@ -245,8 +283,8 @@ def force_error_vs_fp64(g, w, pp, nthreads=None):
     s.rx[:], s.ry[:], s.rz[:] = r.T
     s.qw[:], s.qx[:], s.qy[:], s.qz[:] = q.T
     kind = getattr(O, w["kind"])
-    out = s.pair_batch(O.pair_params(kind, cutoff=w["cutoff"], solver=O.SOLVER_TIGHT), pi, pj,
-                       nthreads or os.cpu_count() or 1)
+    out = s.pair_batch(O.pair_params(kind, cutoff=w["cutoff"], solver=O.SOLVER_TIGHT, mu=w.get("mu"), nu=w.get("nu")),
+                       pi, pj, nthreads or os.cpu_count() or 1)
     Fo = np.zeros((g.n, 3))
     To = np.zeros((g.n, 3))
     np.add.at(Fo, pi, out[:, 1:4])
@@ -318,53 +356,49 @@ def mlp_leg(a, g, w, torch, stream, flush, npairs):
 
 
 # -------------------------------------------------------------------- ours ---
-def run_ours(a):
+def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, extras_on=True):
+    """One ellipsoid workload (ecp or gb) from the shared seeded state: the
+    captured step timed on the device, the force kernel alone, e2e through
+    the C ABI with host arrays, the CPU baseline. Returns the JSON line."""
     import torch
-    import __graft_entry__
-    __graft_entry__.build_library()
-    from sucrose_gb300 import capi
-
-    from sucrose_gb300 import ranks
-    rank, world, local = ranks.rank_info()
-    torch.cuda.set_device(local)
-    w = WORKLOADS[a.config]
+    from sucrose_gb300 import capi, configs, ranks
+    w = WORKLOADS[name]
+    steps = steps or a.steps
     # replicas only: every rank runs its own independent system
-    g, box = make_system(w, seed=ranks.replica_seed(1003, rank))
+    g, box, info = make_system(w, seed=ranks.replica_seed(w["seed"], rank))
+    p2_initial = configs.nematic_order(g.download()[1], long_axis(w))
     stream = torch.cuda.ExternalStream(g.stream_ptr())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    pp = pair_params(g, w, a.solver)
-    pp_eq = pair_params(g, w, "newton" if a.solver != "brent" else "brent")
-
-    # untimed equilibration (Langevin, rotations on) from the aligned lattice
-    configure(g, w, pp_eq, langevin=True, first_step=1)
-    g.step(a.equil)
-    g.step_check()
-    tune = g.autotune(pp, reps=5)      # launch shape of the pair kernel on the equilibrated list
-    configure(g, w, pp)
+    solver = a.solver if name == "ecp" else "newton"
+    pp = pair_params(g, w, solver)
+    if a.state_equil:
+        # optional untimed Langevin steps from the placed state
+        configure(g, w, pair_params(g, w, "newton"), langevin=True, first_step=1)
+        g.step(a.state_equil)
+        g.step_check()
+    tune = g.autotune(pp, reps=5)      # launch shape of the pair kernel on the live list
+    configure(g, w, pp, first_step=a.state_equil + 1)
     g.step(max(a.warmup, 3))
     g.step_check()
     kernels_per_step = g.step_kernel_count()
     p_before = g.npairs()
     builds0 = g.nlist_builds()
-
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        t_dev = timed_steps(g, torch, stream, a.steps, flush)
+        t_dev = timed_steps(g, torch, stream, steps, flush)
     g.step_check()
     p_after = g.npairs()
     builds = g.nlist_builds() - builds0
     npairs = 0.5 * (p_before + p_after)
     if dist is not None:
         t_dev = ranks.max_over_ranks(t_dev, device="cuda")
-    ms_per_step = 1e3 * t_dev / a.steps
-    value = npairs * a.steps * world / t_dev
-    steps_per_s = a.steps / t_dev
+    ms_per_step = 1e3 * t_dev / steps
+    value = npairs * steps * world / t_dev
+    steps_per_s = steps / t_dev
     ns_day = steps_per_s * w["dt"] * TAU_PS * 1e-3 * 86400.0
+    p2_timed = configs.nematic_order(g.download()[1], long_axis(w))
 
     # dominant kernel: the pair-force kernel timed alone (same stream, L2 flushed)
     _, _, st = g.pair_forces(pp, want_stats=True)
@@ -391,7 +425,7 @@ def run_ours(a):
     ptrs = [h.ctypes.data_as(D) for h in host]
     L = g.L
     energies = np.zeros(4)
-    e_steps = max(10, a.steps // 4)
+    e_steps = max(10, steps // 4)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e_steps):
@@ -405,37 +439,37 @@ def run_ours(a):
     d2h = 13 * 8 * n + 32
 
     extras = {}
-    if not a.no_extras and rank == 0:
+    if extras_on and rank == 0:
         extras["force_kernel_pair_evals_per_s"] = npairs / t_force
         extras["force_kernel_ms"] = 1e3 * t_force
         if w["kind"].startswith("ECP"):
             extras["newton_mean_evals_per_pair"] = mean_evals
+            extras["newton_iter_hist"] = [int(x) for x in st.iter_hist]
+            extras["newton_fp64_refined_frac"] = st.fp64_refined / max(st.pairs, 1)
+            extras["nonconverged"] = int(st.nonconverged)
         else:
             extras["pairs_in_range_frac"] = st.solver_evals / max(st.pairs, 1)
-        extras["newton_iter_hist"] = [int(x) for x in st.iter_hist]
-        extras["newton_fp64_refined_frac"] = st.fp64_refined / max(st.pairs, 1)
-        extras["nonconverged"] = int(st.nonconverged)
         extras["fp64_peak_tflops_measured"] = g.peak_fma(True)
         extras["list_rebuilds_in_timed_region"] = int(builds)
         extras["stage_ms_eager"] = g.step_stage_times(20)
-        extras["autotune"] = {"block": tune.block, "filter": tune.filter,
-                              "variant_ms": {f"b{b}_f{f}": float(tune.ms[k]) for k, (b, f) in
-                                             enumerate(((256, 0), (128, 0), (256, 1), (128, 1))[:tune.candidates])}}
-        if a.config == "ecp" and a.solver == "newton":
+        extras["autotune"] = {"pick": {"block": tune.block, "filter": tune.filter},
+                              "variant_ms": tune_variants(tune)}
+        extras["force_error_vs_fp64"] = force_error_vs_fp64(g, w, pp)
+        if name == "ecp" and a.solver == "newton":
             # residual check variants of the same kernel
-            for mode, name in ((2, "double_float"), (0, "none")):
+            for mode, mname in ((2, "double_float"), (0, "none")):
                 pv = pair_params(g, w, "newton")
                 pv.fp64_check = mode
                 tv = statistics.median(timed_forces(g, torch, stream, pv, 10, flush))
-                extras[f"newton_check_{name}_force_kernel_ms"] = 1e3 * tv
-                extras[f"newton_check_{name}_pair_evals_per_s"] = npairs / tv
+                extras[f"newton_check_{mname}_force_kernel_ms"] = 1e3 * tv
+                extras[f"newton_check_{mname}_pair_evals_per_s"] = npairs / tv
             pb = pair_params(g, w, "brent")
             _, _, stb = g.pair_forces(pb, want_stats=True)
             tb = statistics.median(timed_forces(g, torch, stream, pb, 5, flush))
             extras["brent_compat_force_kernel_ms"] = 1e3 * tb
             extras["brent_compat_pair_evals_per_s"] = npairs / tb
             extras["brent_mean_evals_per_pair"] = stb.solver_evals / max(stb.pairs, 1)
-            extras["force_error_vs_fp64"] = force_error_vs_fp64(g, w, pp)
+            extras["nh_modes"] = nh_modes(g, w, pp, torch, stream, flush)
             if not a.no_mlp:
                 extras["mlp"] = mlp_leg(a, g, w, torch, stream, flush, npairs)
 
@@ -447,29 +481,87 @@ def run_ours(a):
         cpu = {"value": cpu_rate, "unit": "pair-evals/s", "cores": 1, "kind": "port",
                "sample": f"{m} listed pairs of this workload's list, {routine}, FP64, "
                          f"oracle restatement built -O3 -ffast-math, 1 thread"}
+    g.close()
+    kname = "k_pair<PotECP>" if w["kind"].startswith("ECP") else "k_pair<PotGB>"
+    line = {
+        "metric": METRICS[name],
+        "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": steps, "warmup": a.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 (fp64 sums and residual check)",
+        "data": "synthetic (seeded isotropic placement, the same state as the reference arm)",
+        "config": {"workload": w["workload"], "n": n, "listed_pairs": npairs, "solver": solver,
+                   "dt": w["dt"], "T": w["T"], "seed": w["seed"],
+                   "integrator": "Nose-Hoover chains (3) on translation and rotation" if w["integrator"] == "NH"
+                   else "Langevin on translation and rotation",
+                   "timed": "the full MD step (integrators, list check with conditional rebuild, forces), "
+                            "one captured CUDA graph per step",
+                   "nematic_P2_initial": p2_initial, "nematic_P2_timed_state": p2_timed, **info,
+                   "untimed_equilibration_steps": a.state_equil,
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": "replicas only" if world > 1 else "single GPU"},
+        "ns_per_day": ns_day, "tau_per_day": steps_per_s * w["dt"] * 86400.0,
+        "e2e": {"value": e2e_value, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(kernels_per_step * steps),
+        "roofline": {"bound": "fp32", "kernel": kname, "achieved": achieved, "peak": peak32,
+                     "unit": "TFLOP/s", "frac": achieved / peak32,
+                     "peak_source": "measured FMA throughput (sg_peak_fma) on this GPU",
+                     "traffic": NCU_TRAFFIC[w["kind"][:2]]["bytes"] * st.pairs / NCU_TRAFFIC[w["kind"][:2]]["pairs"],
+                     "traffic_source": NCU_TRAFFIC[w["kind"][:2]]["source"]
+                     + " (scaled to this launch's listed pairs)"},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    line.update(extras)
+    return line
+
+
+def tune_variants(tune):
+    """The autotuner's timed launch variants, by block size and range filter."""
+    shapes = ((256, 0), (128, 0), (256, 1), (128, 1))
+    return {f"b{b}_f{f}": float(tune.ms[k]) for k, (b, f) in enumerate(shapes[:tune.candidates])}
+
+
+def nh_modes(g, w, pp, torch, stream, flush, steps=20):
+    """The Nose-Hoover step in both modes on the same state: the reference's
+    per-particle chain recurrence (mode 0) and the standard chain (mode 1)."""
+    from sucrose_gb300 import capi
+    r, q, v, l = g.download()
+    out = {}
+    for mode, label in ((capi.INT_NH_REF, "reference_per_particle_chain"), (capi.INT_NH, "standard_chain")):
+        g.upload(r=r, q=q, v=v, l=l)
+        g.build_nlist()
+        g.configure_step(pp, integrator=mode, dt=w["dt"], target_temp=w["T"], rotations=1,
+                         rot_chain=0 if mode == capi.INT_NH_REF else 1, flags=FLAGS)
+        g.step(3)
+        g.step_check()
+        t = timed_steps(g, torch, stream, steps, flush)
+        g.step_check()
+        out[label] = {"ms_per_step": 1e3 * t / steps}
+    g.upload(r=r, q=q, v=v, l=l)
+    g.build_nlist()
+    configure(g, w, pp)
+    return out
+
+
+def run_ours(a):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from sucrose_gb300 import ranks
+    rank, world, local = ranks.rank_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.barrier()
+    line = ellipsoid_line(a, a.config, rank, world, local, dist, extras_on=not a.no_extras)
+    if a.config == "ecp" and not a.no_extras and not a.no_sub:
+        # the other two headline workloads, each timed over fewer steps
+        sub = min(a.steps, 50)
+        line["gb"] = ellipsoid_line(a, "gb", rank, world, local, dist, steps=sub, extras_on=rank == 0)
+        line["replicas"] = replicas_line(a, rank, world, local, dist, steps=min(a.steps, 20))
     if rank == 0:
-        line = {
-            "metric": "ECP pair-evals/s (plain Newton contact solve, full MD step)" if a.config == "ecp"
-            else "GB pair-evals/s (full MD step)",
-            "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
-            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp32 (fp64 sums and residual check)", "data": "synthetic (seeded lattice, device-equilibrated)",
-            "config": {"workload": w["workload"], "n": g.n, "listed_pairs": npairs, "solver": a.solver,
-                       "dt": w["dt"], "T": w["T"], "l2": "flushed between timed steps (256 MB write)",
-                       "parallelism": "replicas only" if world > 1 else "single GPU"},
-            "ns_per_day": ns_day, "tau_per_day": steps_per_s * w["dt"] * 86400.0,
-            "e2e": {"value": e2e_value, "unit": "pair-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": int(kernels_per_step * a.steps),
-            "roofline": {"bound": "fp32", "kernel": "k_pair<PotECP>" if w["kind"].startswith("ECP") else "k_pair<PotGB>",
-                         "achieved": achieved, "peak": peak32,
-                         "unit": "TFLOP/s", "frac": achieved / peak32,
-                         "peak_source": "measured FMA throughput (sg_peak_fma) on this GPU",
-                         "traffic": NCU_TRAFFIC[w["kind"][:2]]["bytes"],
-                         "traffic_source": NCU_TRAFFIC[w["kind"][:2]]["source"]},
-            "cpu_baseline": cpu,
-            "clocks": clk.summary(),
-        }
-        line.update(extras)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -980,15 +1072,25 @@ def replica_pair_params():
 
 
 def run_replicas(a):
-    """Batched replicas: one captured step advances all 4096 replicas; the
-    same replicas as 4096 single-system contexts, each stepped by its own
-    captured graph one after another, give the sequential-launch comparison."""
     import torch
     import __graft_entry__
     __graft_entry__.build_library()
-    from sucrose_gb300 import GpuSystem, capi, configs, ranks
+    from sucrose_gb300 import ranks
     rank, world, local = ranks.rank_info()
     torch.cuda.set_device(local)
+    line = replicas_line(a, rank, world, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def replicas_line(a, rank=0, world=1, local=0, dist=None, steps=None):
+    """Batched replicas: one captured step advances all 4096 replicas; the
+    same replicas as 4096 single-system contexts, each stepped by its own
+    captured graph one after another, give the sequential-launch comparison.
+    Returns the JSON line."""
+    import torch
+    from sucrose_gb300 import GpuSystem, capi, configs, ranks
+    steps = steps or steps
     W = REPLICAS
     t0 = time.perf_counter()
     e = configs.replica_ensemble(a.nrep, seed=ranks.replica_seed(W["seed"], rank))
@@ -1027,19 +1129,21 @@ def run_replicas(a):
     p_before = g.npairs()
     builds0 = g.nlist_builds()
     rep_builds0 = g.rep_nlist_builds()
+    if dist is not None:
+        dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        t_dev = timed_steps(g, torch, stream, a.steps, flush)
+        t_dev = timed_steps(g, torch, stream, steps, flush)
     g.step_check()
     npairs = 0.5 * (p_before + g.npairs())
     builds = g.nlist_builds() - builds0
     rep_builds = g.rep_nlist_builds() - rep_builds0
     fam_of = np.asarray(e["family"])
-    rebuilt_per_step = {name: float(rep_builds[fam_of == f].sum()) / a.steps for f, name in ((0, "LJ"), (1, "GB"))}
+    rebuilt_per_step = {name: float(rep_builds[fam_of == f].sum()) / steps for f, name in ((0, "LJ"), (1, "GB"))}
     if world > 1:
         t_dev = ranks.max_over_ranks(t_dev, device="cuda")
-    ms_per_step = 1e3 * t_dev / a.steps
-    value = npairs * a.steps * world / t_dev
+    ms_per_step = 1e3 * t_dev / steps
+    value = npairs * steps * world / t_dev
 
     # where a step's time goes: the same step enqueued stage by stage (no graph)
     stages = ("lgv_initial", "list_check_and_rebuild", "zero_forces", "pair_LJ", "pair_GB", "lgv_final")
@@ -1131,7 +1235,7 @@ def run_replicas(a):
             s.step_check()
             s.close()
         seq = {"ms_per_step": 1e3 * t_seq, "contexts": len(singles), "setup_s": t_seq_setup,
-               "batched_speedup": t_seq / (t_dev / a.steps),
+               "batched_speedup": t_seq / (t_dev / steps),
                "how": "one context and one captured step graph per replica, launched one after another from the "
                       "host each step (each context on its own stream); host wall clock over 3 steps with device "
                       "synchronisation at both ends"}
@@ -1142,8 +1246,8 @@ def run_replicas(a):
     if rank == 0:
         nrep_total = len(e["n"]) * world
         line = {
-            "metric": "replica-ensemble pair-evals/s (4096 LJ + GB replicas, one captured step for all)",
-            "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "metric": METRICS["replicas"],
+            "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": steps, "warmup": a.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32 (fp64 sums)", "data": "synthetic (seeded replica ensemble, device-equilibrated)",
             "config": {"workload": W["workload"], "replicas": len(e["n"]), "particles": int(n),
@@ -1152,10 +1256,10 @@ def run_replicas(a):
                        "dt": dt, "integrator": "Langevin (translation + rotation), per-replica T and Philox key",
                        "l2": "inputs larger than L2 (and a 256 MB write between timed steps)",
                        "parallelism": "replicas only" if world > 1 else "single GPU"},
-            "replica_steps_per_s": nrep_total * a.steps / t_dev,
+            "replica_steps_per_s": nrep_total * steps / t_dev,
             "e2e": {"value": npairs * e_steps / t_e2e, "unit": "pair-evals/s", "h2d_bytes_per_step": 13 * 8 * n,
                     "d2h_bytes_per_step": 13 * 8 * n + 32},
-            "gpu_launches": int(kernels_per_step * a.steps),
+            "gpu_launches": int(kernels_per_step * steps),
             "roofline": {"bound": "fp32", "kernel": f"k_pair<Pot{top}> (replica family range)",
                          "achieved": fam[top]["tflops"], "peak": peak32, "unit": "TFLOP/s",
                          "frac": fam[top]["tflops"] / peak32,
@@ -1170,7 +1274,8 @@ def run_replicas(a):
             "sequential_single_system": seq,
             "host_setup_s": t_setup_host,
         }
-        print(json.dumps(line), flush=True)
+    g.close()
+    return line if rank == 0 else None
 
 
 def replica_cpu_systems(e, stride=97):
@@ -1221,11 +1326,12 @@ def replica_cpu_sample(e, seconds, nthreads=1):
                       "reference's lj_ / gb_ restated in C++ (FP64), oracle built -O3 -ffast-math"}
 
 
-def run_reference_replicas(a):
+def reference_replicas_line(a, steps=None):
     """Reference arm for the replica ensemble: the restated lj_ / gb_ on the
     host cores (OpenMP), each step one pass over a fixed sample of whole
     replicas."""
     from sucrose_gb300 import configs
+    steps = steps or a.steps
     e = configs.replica_ensemble(a.nrep, seed=REPLICAS["seed"])
     systems = replica_cpu_systems(e)
     nth = os.cpu_count() or 1
@@ -1240,41 +1346,35 @@ def run_reference_replicas(a):
         for s, pp, pi, pj in chosen[:2]:
             s.pair_batch(pp, pi, pj, nth)
     t0 = time.perf_counter()
-    for _ in range(a.steps):
+    for _ in range(steps):
         for s, pp, pi, pj in chosen:
             s.pair_batch(pp, pi, pj, nth)
     dt = time.perf_counter() - t0
-    value = per_step * a.steps / dt
-    line = {"impl": "reference", "metric": "replica-ensemble pair-evals/s (4096 LJ + GB replicas, one captured step for all)",
-            "value": value, "unit": "pair-evals/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-            "ms_per_step": 1e3 * dt / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    value = per_step * steps / dt
+    line = {"impl": "reference", "metric": METRICS["replicas"],
+            "value": value, "unit": "pair-evals/s", "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp64", "data": "synthetic (seeded replica ensemble, lattice state)",
             "config": {"workload": REPLICAS["workload"], "replicas_sampled": len(chosen), "per_step_pairs": per_step},
             "cpu_baseline": {"value": value, "unit": "pair-evals/s", "cores": nth, "kind": "port",
                              "sample": f"{len(chosen)} whole replicas per step ({per_step} pairs); the reference "
                                        "lj_ / gb_ restated in C++, OpenMP"},
             "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # --------------------------------------------------------------- reference ---
-def run_reference(a):
-    """The reference's pair routine restated on the CPU (its Fortran has no
-    compiler here), all host threads, on this workload's geometry."""
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    if a.config == "replicas":
-        return run_reference_replicas(a)
-    if a.config == "charged":
-        return run_reference_charged(a)
-    if a.config in ("constrained", "polymer"):
-        return run_reference_constrained(a)
+def reference_ellipsoid_line(a, name, steps=None):
+    """The reference's pair routine (ecpr_ with its Brent solve and per-pair
+    setup, or gb_) restated on the CPU (its Fortran has no compiler here), on
+    all host threads, over the whole listed pair set of the same seeded state
+    the GPU arm starts from (the list built by a k-d tree with the
+    reference's acceptance test), once per step."""
     import oracle as O
     from scipy.spatial import cKDTree
-    from sucrose_gb300 import configs
-    w = WORKLOADS[a.config]
-    r, q, box = configs.aligned_lattice(w["counts"], w["sig"], w["density"], seed=1003, jitter=0.02, tilt=w["tilt"])
+    w = WORKLOADS[name]
+    steps = steps or a.steps
+    r, q, box, v, l, rep = initial_state(w)
     n = len(r)
     rw = (r + box / 2.0) % box
     tree = cKDTree(rw, boxsize=box)
@@ -1289,33 +1389,162 @@ def run_reference(a):
     kind = getattr(O, w["kind"])
     pp = O.pair_params(kind, cutoff=w["cutoff"], solver=O.SOLVER_BRENT, mu=w.get("mu"), nu=w.get("nu"))
     nth = os.cpu_count() or 1
-    per_step = min(len(pi), 200000)
     for _ in range(a.warmup):
-        s.pair_batch(pp, pi[:per_step // 10], pj[:per_step // 10], nth)
+        s.pair_batch(pp, pi[:len(pi) // 10], pj[:len(pj) // 10], nth)
     t0 = time.perf_counter()
-    for k in range(a.steps):
-        off = (k * per_step) % max(1, len(pi) - per_step + 1)
-        s.pair_batch(pp, pi[off:off + per_step], pj[off:off + per_step], nth)
+    for k in range(steps):
+        s.pair_batch(pp, pi, pj, nth)
     dt = time.perf_counter() - t0
-    value = per_step * a.steps / dt
-    line = {"impl": "reference", "metric": "ECP pair-evals/s" if a.config == "ecp" else "GB pair-evals/s",
-            "value": value, "unit": "pair-evals/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-            "ms_per_step": 1e3 * dt / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp64", "data": "synthetic (seeded lattice)",
-            "config": {"workload": w["workload"], "n": n, "listed_pairs": int(len(pi)), "per_step_pairs": per_step},
+    value = len(pi) * steps / dt
+    routine = "ecpr_: Brent, per-pair setup" if name == "ecp" else "gb_ (mu 2, nu 1)"
+    return {"impl": "reference", "metric": METRICS[name],
+            "value": value, "unit": "pair-evals/s", "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * dt / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64", "data": "synthetic (seeded isotropic placement, the same state as the GPU arm)",
+            "config": {"workload": w["workload"], "n": n, "listed_pairs": int(len(pi)), "seed": w["seed"],
+                       "timed": "the reference pair routine over every listed pair, once per step",
+                       "placement_sweeps": int(rep.sweeps)},
             "cpu_baseline": {"value": value, "unit": "pair-evals/s", "cores": nth, "kind": "port",
-                             "sample": f"{per_step} pairs per step of the {len(pi)}-pair list; the reference pair "
-                                       "routine (" + ("ecpr_: Brent, per-pair setup" if a.config == "ecp" else "gb_")
-                                       + ", FP64) restated in C++, OpenMP"},
+                             "sample": f"all {len(pi)} listed pairs per step; the reference pair routine ("
+                                       + routine + ", FP64) restated in C++, OpenMP"},
             "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    if a.config == "replicas":
+        print(json.dumps(reference_replicas_line(a)), flush=True)
+        return
+    if a.config == "charged":
+        return run_reference_charged(a)
+    if a.config in ("constrained", "polymer"):
+        return run_reference_constrained(a)
+    import __graft_entry__
+    __graft_entry__.build_library()     # the seeded placement runs on the device (input set-up only)
+    line = reference_ellipsoid_line(a, a.config)
+    if a.config == "ecp" and not a.no_extras and not a.no_sub:
+        line["gb"] = reference_ellipsoid_line(a, "gb", steps=min(a.steps, 50))
+        line["replicas"] = reference_replicas_line(a, steps=min(a.steps, 20))
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------- profile cases ---
+PROFILE_CASES = """Small, self-contained launches of each kernel family, for profiling:
+python bench.py --profile-case <case> [--reps K]. Each case builds one seeded
+system at the size of its benchmark workload (the same isotropic ECP and GB
+states as the benchmark), runs one untimed launch sequence, then K launches
+of the kernels of interest and exits. A profiler selects the kernel with its
+own filter (for example ncu -k regex:k_pair -c 2). Cases:
+  ecp       ECP (3,2,1) ellipsoids, N = 65 536, repulsive kind, Newton solve
+  ecp_mlp   the same with the learned guess (weights from a short training)
+  gb        Gay-Berne (3,5,2,1), N = 32 768, filtered launch
+  lj        Lennard-Jones fcc, N = 32 000
+  list      neighbour-list rebuild of the ECP system (forced, every launch)
+  gb_list   neighbour-list rebuild of the Gay-Berne system (list radius 6.4)
+  langevin  Langevin step (initial + final) with rotations, N = 32 768
+  nhc       Nose-Hoover chain step with rotations, N = 65 536
+  mlp_train one MLP training step on 65 536 samples
+  ecp_step  captured Nose-Hoover steps of the ECP system (list build as
+            flag-gated kernels, so that a profiler sees every kernel)
+  replicas  captured steps of --nrep replicas (LJ + GB), same flag"""
+
+
+def profile_case(a):
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from sucrose_gb300 import GpuSystem, capi, configs
+    case = a.profile_case
+    g = p = None
+    if case in ("ecp", "ecp_mlp", "list", "nhc", "ecp_step", "mlp_train"):
+        w = WORKLOADS["ecp"]
+        g, _, _ = make_system(w)
+        p = pair_params(g, w, "newton")
+    elif case in ("gb", "langevin", "gb_list"):
+        w = WORKLOADS["gb"]
+        g, _, _ = make_system(w)
+        p = pair_params(g, w, "newton")
+    elif case == "lj":
+        r, q, box = configs.fcc_lattice(20, 0.8442)
+        g = GpuSystem(len(r), box)
+        g.upload(r=r, v=configs.velocities_to_temperature(len(r), 0.722, 15))
+        g.init_nlist(0.3, 2.5, trigger_mode=1)
+        p = g.params(capi.LJ, cutoff=2.5)
+    elif case != "replicas":
+        raise SystemExit("unknown case " + case + "\n" + PROFILE_CASES)
+    reps = a.reps
+    if case in ("ecp", "gb", "lj"):
+        for _ in range(1 + reps):
+            g.zero_forces()
+            g.pair_forces(p)
+    elif case == "ecp_mlp":
+        from sucrose_gb300 import mlp
+
+        def langevin(T):
+            g.configure_step(p, integrator=capi.INT_LANGEVIN, dt=0.001, target_temp=T, rotations=1)
+
+        X, y = mlp.generate(g, p, langevin, samples=200_000, every=10, equil=20)
+        mlp.train(g, X, y, epochs=1, batch=65536, lr=2e-3, seed=1)
+        g.build_nlist()
+        pm = pair_params(g, WORKLOADS["ecp"], "mlp")
+        for _ in range(1 + reps):
+            g.zero_forces()
+            g.pair_forces(pm)
+    elif case in ("list", "gb_list"):
+        for _ in range(1 + reps):
+            g.build_nlist()
+    elif case == "langevin":
+        g.zero_forces()
+        g.pair_forces(p)
+        for k in range(1 + reps):
+            g.lgv_initial(0.002, k + 1, damping=1.0, target_temp=1.0)
+            g.lgv_final(0.002, damping=1.0)
+    elif case == "nhc":
+        g.zero_forces()
+        g.pair_forces(p)
+        for _ in range(1 + reps):
+            g.nht_initial(0.001, 1.2, 0.0, mode=1, rot_chain=1)
+            g.qq_initial(0.001)
+            g.nht_final(0.001, 1.2, 0.0, mode=1, rot_chain=1)
+            g.qq_final(0.001)
+    elif case == "ecp_step":
+        g.configure_step(p, integrator=capi.INT_NH, dt=0.001, target_temp=1.2, rotations=1, rot_chain=1,
+                         flags=capi.STEP_FLAT)
+        g.step(1 + reps)
+    elif case == "mlp_train":
+        from sucrose_gb300 import mlp
+
+        def langevin(T):
+            g.configure_step(p, integrator=capi.INT_LANGEVIN, dt=0.001, target_temp=T, rotations=1)
+
+        X, y = mlp.generate(g, p, langevin, samples=65536, every=2, equil=2)
+        mlp.train(g, X, y, epochs=1 + reps, batch=65536, lr=2e-3, seed=1)
+    elif case == "replicas":
+        e = configs.replica_ensemble(a.nrep, seed=REPLICAS["seed"])
+        sig, eps, inert, v0, l0 = replica_arrays(e)
+        g = GpuSystem.replicas(e["n"], e["box"], e["family"], e["temp"], e["key"])
+        g.set_particles(mass=1.0, sig=sig, eps=eps, inertia=inert)
+        g.upload(r=e["r"], q=e["q"], v=v0, l=l0)
+        LJ, GB = configs.LJ_REPLICA, configs.GB_REPLICA
+        g.init_rep_nlist([LJ["skin"], GB["skin"], 0.3], [LJ["list_cutoff"], GB["list_cutoff"], 3.0], trigger_mode=1)
+        pairs = replica_pair_params()
+        g.configure_step_pairs(pairs, integrator=capi.INT_LANGEVIN, dt=REPLICAS["dt"], damping=1.0, rotations=1,
+                               flags=capi.STEP_FLAT)
+        if a.rep_equil:   # untimed steps first, until replicas start to rebuild their lists
+            g.step(a.rep_equil)
+        g.step(1 + reps)
+    g.synchronize()
+    print("profile case", case, "done")
 
 
 if __name__ == "__main__":
     args = parse()
     if args.flat_graph:
         FLAGS = 1
-    if args.impl == "reference":
+    if args.profile_case:
+        profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.config == "replicas":
         run_replicas(args)

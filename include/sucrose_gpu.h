@@ -474,6 +474,28 @@ int sg_lj_forces_noalloc(int32_t n, const double* rx, const double* ry, const do
                          int32_t periodic, const sg_pair_params* params, double* fx, double* fy, double* fz,
                          double* pot_virial, int32_t* bad_pairs, void* stream, char* err, int32_t err_len);
 
+/* ---- seeded isotropic ellipsoid placement ---------------------------------- */
+/* No counterpart in the reference, whose only generator is the FCC lattice
+ * (fortran/system.f90:438-523). n hard ellipsoids of the given semi-axes in a
+ * periodic box centred on 0, built on the current device: positions start
+ * uniform in the box and orientations uniform on the unit 3-sphere (Philox
+ * words of the seed); the ellipsoids grow from a fifth of their size to full
+ * size while Jacobi sweeps move and turn every overlapping pair apart
+ * (Perram-Wertheim test and its gradient) until no pair is closer than gap
+ * times contact. The same seed gives the same bits on every run (per-particle
+ * sums in fixed point). r_out: n x 3, q_out: n x 4 (w, x, y, z), HOST arrays.
+ * Returns SG_ENOCONV if the sweeps could not relax the packing (too dense),
+ * SG_ECUTOFF_GT_HALFBOX if the box is narrower than about four semi-axes. */
+typedef struct {
+    int32_t stages;              /* growth steps taken                         */
+    int32_t sweeps;              /* Jacobi sweeps in all                       */
+    int64_t overlaps;            /* pairs closer than gap x contact at the end */
+    double min_contact_ratio;    /* min |r| / contact distance over close pairs */
+    double final_scale;          /* size reached, 1 on success                 */
+} sg_place_report;
+int sg_place_isotropic(int64_t n, const double semi_axes[3], const double box[3], uint64_t seed, double gap,
+                       double* r_out, double* q_out, sg_place_report* rep);
+
 /* ---- Philox4x32-10 (fortran/xmath.f90:42-113) -------------------------------- */
 /* Host-side single block, for callers that mirror philox_uniform. */
 void sg_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

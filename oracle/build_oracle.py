@@ -11,7 +11,8 @@ Produces, with plain g++ and no build system:
                                    src/system.cpp, src/integrators.cpp) plus
                                    ref_shim.cpp, when the reference tree is present.
 The reference's Fortran cannot be built: no Fortran compiler exists in this
-image or on the GPU host.
+image or on the GPU host. The reference tree is read from the directory named
+by the SUCROSE_REFERENCE environment variable, else from /root/reference.
 """
 import os
 import subprocess
@@ -20,7 +21,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = "/root/reference"
+REFERENCE_ROOT = os.environ.get("SUCROSE_REFERENCE", "/root/reference")
 
 STRICT = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
 FAST = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffast-math", "-fopenmp"]

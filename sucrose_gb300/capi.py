@@ -50,6 +50,11 @@ class TuneResult(C.Structure):
                 ("ms", C.c_float * 4)]
 
 
+class PlaceReport(C.Structure):
+    _fields_ = [("stages", C.c_int32), ("sweeps", C.c_int32), ("overlaps", C.c_int64),
+                ("min_contact_ratio", C.c_double), ("final_scale", C.c_double)]
+
+
 class EcpStats(C.Structure):
     _fields_ = [("pairs", C.c_int64), ("solver_evals", C.c_int64), ("nonconverged", C.c_int64),
                 ("fallbacks", C.c_int64), ("iter_hist", C.c_int64 * 24), ("fp64_refined", C.c_int64)]
@@ -150,6 +155,7 @@ SIGNATURES = [
                                        C.c_int64, C.c_int32, _D, C.c_int32, C.POINTER(PairParams), C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
                                        C.c_int32]),
+    ("sg_place_isotropic", C.c_int, [C.c_int64, _D, _D, C.c_uint64, C.c_double, _D, _D, C.POINTER(PlaceReport)]),
     ("sg_philox4x32", None, [_U32, _U32, _U32]),
     ("sg_philox4x32_device", C.c_int, [_P, C.c_int64, _U32, _U32, _U32]),
     ("sg_philox_normal_3seq_device", C.c_int, [_P, C.c_int64, _I32, _D]),

@@ -76,3 +76,31 @@ def jittered_fcc(cells, density, seed, amp=0.08):
 
 def ellipsoids(counts, sig, density, seed, tilt, jitter=0.03):
     return configs.aligned_lattice(counts, sig, density, seed=seed, jitter=jitter, tilt=tilt)
+
+
+def kdtree_reference_pairs(r, box, cutoff, skin):
+    """The reference's half list at sizes where its O(N^2) build is too slow:
+    candidates from a periodic k-d tree (a superset, radius widened by 1e-6),
+    then build_nlist's own acceptance test on each (system.f90:977-1000):
+    FP64 difference, ANINT minimum image (ties away from zero), and the strict
+    (x^2 + y^2) + z^2 < (rc+skin)^2. Returns (pi, pj) 0-based, i < j, in row
+    order. Checked against the oracle's O(N^2) build in tests/test_oracle.py."""
+    from scipy.spatial import cKDTree
+    r = np.asarray(r, dtype=np.float64)
+    box = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)).copy()
+    rl = cutoff + skin
+    w = np.mod(r + box / 2.0, box)
+    w = np.minimum(w, np.nextafter(box, 0.0))
+    cand = cKDTree(w, boxsize=box).query_pairs(rl * (1.0 + 1e-6), output_type="ndarray")
+    if len(cand) == 0:
+        return np.zeros(0, np.int32), np.zeros(0, np.int32)
+    cand.sort(axis=1)
+    i, j = cand[:, 0], cand[:, 1]
+    d = r[i] - r[j]
+    x = d / box
+    d = d - np.sign(x) * np.floor(np.abs(x) + 0.5) * box
+    rsq = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+    keep = rsq < rl * rl
+    i, j = i[keep], j[keep]
+    o = np.lexsort((j, i))
+    return i[o].astype(np.int32), j[o].astype(np.int32)

@@ -104,6 +104,48 @@ def test_nose_hoover(lib, mode):
     np.testing.assert_allclose(st[:6], list(P.o.s.eta) + list(P.o.s.p_eta), rtol=1e-6, atol=1e-9)
 
 
+def test_nose_hoover_rotational_chain_against_the_oracle(lib):
+    """The standard chain on translation and rotation (rot_chain = 1, the
+    thermostat of the ECP benchmark) against the oracle's translational chain
+    plus its rotational chain (or_nhr_half: the same propagator on
+    G1 = sum L_b^2 / I - 3 N T, scaling every angular momentum): particle
+    state, all twelve chain variables and the kinetic energy, both halves."""
+    P = state(7)
+    P.o.s.target_temp = 1.2
+    # first chain momenta of order Q1 / dt, so that one half step scales the
+    # velocities and angular momenta by about 1e-3 (far above the tolerance)
+    chain = np.array([0.01, -0.02, 0.03, 1.0e4, 3.0, -2.0, -0.01, 0.02, 0.0, 2.0e4, 5.0, -3.0])
+
+    def run(sys, rot_chain, oracle):
+        sys.g.nht_state(chain)
+        for k in range(3):
+            sys.o.s.eta[k], sys.o.s.p_eta[k] = chain[k], chain[3 + k]
+            sys.o.s.eta_r[k], sys.o.s.p_eta_r[k] = chain[6 + k], chain[9 + k]
+        sys.g.nht_initial(0.001, 1.2, mode=1, rot_chain=rot_chain)
+        if oracle:
+            sys.o.nht_initial(0.001, mode=1)
+            sys.o.nhr_half(0.001)
+            compare_state(sys, tol=5e-6)
+            np.testing.assert_allclose(sys.g.nht_state(), oracle_chain(sys), rtol=1e-6, atol=1e-9)
+        ke = sys.g.nht_final(0.001, 1.2, mode=1, rot_chain=rot_chain)
+        if oracle:
+            sys.o.nht_final(0.001, mode=1)
+            sys.o.nhr_half(0.001)
+            compare_state(sys, tol=5e-6)
+            np.testing.assert_allclose(sys.g.nht_state(), oracle_chain(sys), rtol=1e-6, atol=1e-9)
+            assert abs(ke - sys.o.s.kin_eng) < 1e-5 * sys.o.s.kin_eng
+
+    def oracle_chain(sys):
+        o = sys.o.s
+        return np.array(list(o.eta) + list(o.p_eta) + list(o.eta_r) + list(o.p_eta_r))
+
+    run(P, 1, True)
+    # the rotational chain did act: without it the angular momenta differ
+    Q = state(7)
+    run(Q, 0, False)
+    assert rel(Q.g.download()[3], P.g.download()[3]) > 1e-4
+
+
 def test_thermo(lib):
     r, q, box = jittered_fcc(3, 0.8442, seed=1)
     v = configs.velocities_to_temperature(108, 0.722, 15)

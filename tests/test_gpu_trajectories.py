@@ -1,0 +1,94 @@
+"""Statistical trajectory tests: what a long run must conserve or sample.
+
+Per-call parity against the oracle cannot reach these (FP32 trajectories
+leave any FP64 one within ~10^3 steps), and the rotational Nose-Hoover chain
+has no reference implementation, so its physical pin is equipartition:
+  * the README example (FCC 3^3 at rho 0.8442, T 0.722, seed 15, truncated
+    and shifted LJ at rc 2.5, dt 5e-4) over its full 20 000 NVE steps:
+    the total energy stays constant (README.md:83-115);
+  * Langevin on translation and rotation (integrators.f90:507-676): the mean
+    translational and rotational kinetic energies are 3/2 N T each;
+  * the standard Nose-Hoover chains on translation and rotation: the mean
+    translational kinetic energy is (3N - 3) T / 2 (the chain's n_dof,
+    integrators.f90:303-392) and the rotational one 3/2 N T.
+All runs use the captured step, as the benchmark does.
+"""
+import numpy as np
+import pytest
+
+from helpers import lj_fcc
+from sucrose_gb300 import GpuSystem, capi, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def test_readme_nve_energy_conservation(lib):
+    r, q, box, v = lj_fcc()
+    g = GpuSystem(108, box)
+    g.upload(r=r, v=v)
+    g.init_nlist(0.3, 2.5)
+    g.configure_step(g.params(capi.LJ, cutoff=2.5), integrator=capi.INT_NVE, dt=0.0005)
+    E, K = [], []
+    for _ in range(200):              # 200 x 100 = the README's 20 000 steps
+        g.step(100)
+        e = g.energies()
+        E.append(e[0] + e[2])
+        K.append(e[2])
+    g.step_check()
+    E, K = np.array(E), np.array(K)
+    scale = K.mean()
+    assert np.all(np.isfinite(E))
+    # the lattice melts (kinetic energy moves into the potential) while the
+    # total stays put: fluctuation and drift far below the kinetic scale
+    assert np.ptp(K) > 0.1 * scale
+    assert np.std(E) < 2e-4 * scale
+    assert abs(E[-20:].mean() - E[:20].mean()) < 5e-4 * scale
+
+
+def fluid(seed, T=1.2):
+    """1000 ECP (3, 2, 1) ellipsoids at packing fraction 0.2 (isotropic
+    placement), Maxwell-Boltzmann velocities with zero net momentum and
+    thermal angular momenta at T."""
+    sig = (3.0, 2.0, 1.0)
+    n = 1000
+    r, q, box, _ = configs.isotropic_placement(n, sig, 0.2 / (np.pi / 6 * 6.0), seed=seed)
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=(n, 3)) * np.sqrt(T)
+    v -= v.mean(0)
+    I = configs.default_inertia(sig)
+    l = configs.angular_momenta(q, I, T, seed)
+    g = GpuSystem(n, box)
+    g.set_particles(sig=sig, inertia=I)
+    g.upload(r=r, q=q, v=v, l=l)
+    g.init_nlist(0.3, 3.0)
+    return g, g.params(capi.ECPR, cutoff=3.0, solver=capi.SOLVER_NEWTON), n
+
+
+def sample_kinetic(g, equil, steps, every=20):
+    g.step(equil)
+    kt, kr = [], []
+    for _ in range(steps // every):
+        g.step(every)
+        e = g.energies()
+        kt.append(e[2])
+        kr.append(e[3])
+    g.step_check()
+    return np.mean(kt), np.mean(kr)
+
+
+def test_langevin_equipartition(lib):
+    T = 1.2
+    g, pp, n = fluid(31, T)
+    g.configure_step(pp, integrator=capi.INT_LANGEVIN, dt=0.001, target_temp=T, damping=1.0, rotations=1)
+    kt, kr = sample_kinetic(g, 5000, 40000)
+    assert abs(kt / (1.5 * n * T) - 1.0) < 0.02
+    assert abs(kr / (1.5 * n * T) - 1.0) < 0.02
+
+
+def test_nose_hoover_chains_equipartition(lib):
+    T = 1.2
+    g, pp, n = fluid(32, T)
+    g.configure_step(pp, integrator=capi.INT_NH, dt=0.001, target_temp=T, rotations=1, rot_chain=1)
+    kt, kr = sample_kinetic(g, 10000, 40000)
+    assert abs(kt / (0.5 * (3 * n - 3) * T) - 1.0) < 0.025
+    assert abs(kr / (1.5 * n * T) - 1.0) < 0.025

@@ -252,3 +252,25 @@ def test_fp32_prediction_budget():
     s.forces(pp, pi, pj, prec=32)
     F32 = np.stack([s.fx, s.fy, s.fz], 1)
     assert np.linalg.norm(F32 - F64) / np.linalg.norm(F64) < 1e-5
+
+
+def test_kdtree_reference_pairs_match_the_oracle_build():
+    """The k-d tree list used by the full-size tests equals the oracle's
+    O(N^2) build_nlist restatement, near-threshold pairs across the
+    periodic boundary included."""
+    from helpers import kdtree_reference_pairs
+    rng = np.random.default_rng(17)
+    box = np.array([21.0, 19.5, 23.0])
+    base = rng.uniform(-box / 2, box / 2, size=(400, 3))
+    d = rng.normal(size=(400, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    partner = base + d * (2.8 + rng.uniform(-3e-6, 3e-6, size=(400, 1)))
+    partner -= box * np.round(partner / box)
+    r = np.concatenate([base, partner, rng.uniform(-box / 2, box / 2, size=(1200, 3))])
+    r = r.astype(np.float32).astype(np.float64)
+    s = O.System(len(r), box)
+    s.rx[:], s.ry[:], s.rz[:] = r.T
+    opi, opj = s.pairs(2.5, 0.3)
+    kpi, kpj = kdtree_reference_pairs(r, box, 2.5, 0.3)
+    assert len(opi) > 1000
+    assert np.array_equal(opi, kpi) and np.array_equal(opj, kpj)
