@@ -62,7 +62,9 @@ def parse():
     ap.add_argument("--rep-equil", type=int, default=300, help="untimed equilibration steps (config replicas)")
     ap.add_argument("--flat-graph", action="store_true",
                     help="list build as flag-gated kernels instead of a conditional graph node (for ncu launch lists)")
-    ap.add_argument("--solver", default="newton", choices=["newton", "brent", "mlp"])
+    ap.add_argument("--solver", default="support", choices=["support", "newton", "brent", "mlp"],
+                    help="ECP contact solve: Newton from the support-function start (default), from 1/2, "
+                         "the reference's Brent, or from the learned guess")
     ap.add_argument("--equil", type=int, default=1500, help="untimed Langevin equilibration steps")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary measurements")
@@ -70,6 +72,8 @@ def parse():
     ap.add_argument("--no-sub", action="store_true", help="skip the gb and replicas sub-objects of the ecp line")
     ap.add_argument("--profile-case", default=None, help="run one small profiling case and exit (see PROFILE_CASES)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the profiled kernels (--profile-case)")
+    ap.add_argument("--ecp-path", default=None, choices=["split", "fused"],
+                    help="ECP profile cases: the split Newton path or the one-kernel path (default: untuned)")
     ap.add_argument("--state-equil", type=int, default=0,
                     help="untimed Langevin steps from the placed state before timing (ecp, gb)")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000)
@@ -167,7 +171,8 @@ def make_system(w, seed=None):
 def pair_params(g, w, solver):
     from sucrose_gb300 import capi
     kind = getattr(capi, w["kind"])
-    s = {"newton": capi.SOLVER_NEWTON, "brent": capi.SOLVER_BRENT_COMPAT, "mlp": capi.SOLVER_MLP_NEWTON}[solver]
+    s = {"newton": capi.SOLVER_NEWTON, "support": capi.SOLVER_NEWTON_SUPPORT, "brent": capi.SOLVER_BRENT_COMPAT,
+         "mlp": capi.SOLVER_MLP_NEWTON}[solver]
     return g.params(kind, cutoff=w["cutoff"], mu=w.get("mu", 0), nu=w.get("nu", 0), solver=s)
 
 
@@ -196,23 +201,24 @@ def configure(g, w, pp, langevin=False, first_step=1):
                          flags=FLAGS)
 
 
-def pair_flops(kind, listed, in_range, mean_evals=0.0):
+def pair_flops(kind, listed, in_range, mean_evals=0.0, support=False):
     """Algorithmic FP32 flops of one pair-force launch, counted from the kernel
     sources (FMA = 2 flops, sqrt / rsqrt / division = 1). Every listed pair
     pays the distance and, for Gay-Berne, the orientation terms up to the range
     test; pairs in range pay the force and torque terms."""
     if kind.startswith("ECP"):
-        return ecp_flops_per_pair(mean_evals) * listed
+        return ecp_flops_per_pair(mean_evals, support) * listed
     if kind.startswith("GB"):
         return 80.0 * listed + 240.0 * in_range
     return 20.0 * listed + 20.0 * in_range
 
 
-def ecp_flops_per_pair(mean_evals):
+def ecp_flops_per_pair(mean_evals, support=False):
     """Algorithmic FP32 flops of one ECP pair (Newton), counted from the kernel
     source: setup 60, per Newton evaluation 110, final factorisation 30, force
-    and torque terms 420 (FMA = 2 flops, rsqrt/div = 1)."""
-    return 60.0 + 110.0 * mean_evals + 30.0 + 420.0
+    and torque terms 420 (FMA = 2 flops, rsqrt/div = 1); the support-function
+    start adds 44 (two quadratic forms, two square roots, one division)."""
+    return 60.0 + (44.0 if support else 0.0) + 110.0 * mean_evals + 30.0 + 420.0
 
 
 def timed_steps(g, torch, stream, steps, flush):
@@ -406,7 +412,7 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
     tf = timed_forces(g, torch, stream, pp, 20, flush)
     t_force = statistics.median(tf)
     peak32 = g.peak_fma(False)
-    flops = pair_flops(w["kind"], st.pairs, st.solver_evals, mean_evals)
+    flops = pair_flops(w["kind"], st.pairs, st.solver_evals, mean_evals, support=solver == "support")
     achieved = flops / t_force / 1e12
 
     # e2e: FP64 host arrays in and out through the C ABI every step
@@ -449,16 +455,27 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
             extras["nonconverged"] = int(st.nonconverged)
         else:
             extras["pairs_in_range_frac"] = st.solver_evals / max(st.pairs, 1)
+            extras["pairs_near_contact_frac"] = st.fallbacks / max(st.pairs, 1)
         extras["fp64_peak_tflops_measured"] = g.peak_fma(True)
         extras["list_rebuilds_in_timed_region"] = int(builds)
-        extras["stage_ms_eager"] = g.step_stage_times(20)
-        extras["autotune"] = {"pick": {"block": tune.block, "filter": tune.filter},
-                              "variant_ms": tune_variants(tune)}
+        extras["stage_ms_in_graph"] = g.step_stage_times(20)
+        ecp = w["kind"].startswith("ECP")
+        extras["autotune"] = {"pick": {"block": tune.block, ("split" if ecp else "filter"): tune.filter},
+                              "variant_ms": tune_variants(tune, ecp)}
         extras["force_error_vs_fp64"] = force_error_vs_fp64(g, w, pp)
-        if name == "ecp" and a.solver == "newton":
+        if name == "ecp" and a.solver in ("newton", "support"):
+            # Newton from lambda = 1/2 on the same list (the support start is the headline)
+            if a.solver == "support":
+                ph = pair_params(g, w, "newton")
+                _, _, sth = g.pair_forces(ph, want_stats=True)
+                th = statistics.median(timed_forces(g, torch, stream, ph, 10, flush))
+                extras["newton_half_start"] = {
+                    "force_kernel_ms": 1e3 * th, "pair_evals_per_s": npairs / th,
+                    "mean_evals_per_pair": sth.solver_evals / max(sth.pairs, 1),
+                    "iter_hist": [int(x) for x in sth.iter_hist]}
             # residual check variants of the same kernel
             for mode, mname in ((2, "double_float"), (0, "none")):
-                pv = pair_params(g, w, "newton")
+                pv = pair_params(g, w, a.solver)
                 pv.fp64_check = mode
                 tv = statistics.median(timed_forces(g, torch, stream, pv, 10, flush))
                 extras[f"newton_check_{mname}_force_kernel_ms"] = 1e3 * tv
@@ -515,10 +532,12 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
     return line
 
 
-def tune_variants(tune):
-    """The autotuner's timed launch variants, by block size and range filter."""
+def tune_variants(tune, ecp=False):
+    """The autotuner's timed launch variants, by block size and range filter
+    (ECP: the one-kernel path or the split Newton path)."""
     shapes = ((256, 0), (128, 0), (256, 1), (128, 1))
-    return {f"b{b}_f{f}": float(tune.ms[k]) for k, (b, f) in enumerate(shapes[:tune.candidates])}
+    tag = (lambda f: "split" if f else "fused") if ecp else (lambda f: f"f{f}")
+    return {f"b{b}_{tag(f)}": float(tune.ms[k]) for k, (b, f) in enumerate(shapes[:tune.candidates])}
 
 
 def nh_modes(g, w, pp, torch, stream, flush, steps=20):
@@ -862,7 +881,7 @@ def run_constrained(a):
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"},
             "cpu_baseline": None,
             "clocks": clk.summary(),
-            "stage_ms_eager": stages,
+            "stage_ms_in_graph": stages,
             "constraint_stats_timed": cst,
             "list_rebuilds_in_timed_region": int(builds),
             "autotune": {"block": tune.block, "filter": tune.filter},
@@ -1268,7 +1287,7 @@ def replicas_line(a, rank=0, world=1, local=0, dist=None, steps=None):
             "clocks": clk.summary(),
             "families": fam,
             "autotune": tunes,
-            "stage_ms_eager": breakdown,
+            "stage_ms_in_graph": breakdown,
             "list_rebuilds_in_timed_region": int(builds),
             "replicas_rebuilt_per_step": rebuilt_per_step,
             "sequential_single_system": seq,
@@ -1460,7 +1479,9 @@ def profile_case(a):
     if case in ("ecp", "ecp_mlp", "list", "nhc", "ecp_step", "mlp_train"):
         w = WORKLOADS["ecp"]
         g, _, _ = make_system(w)
-        p = pair_params(g, w, "newton")
+        p = pair_params(g, w, a.solver if a.solver in ("newton", "support") else "newton")
+        if a.ecp_path:
+            g.set_launch(p.kind, 256, 1 if a.ecp_path == "split" else 0)
     elif case in ("gb", "langevin", "gb_list"):
         w = WORKLOADS["gb"]
         g, _, _ = make_system(w)

@@ -36,7 +36,8 @@ module sucrose_gpu
         SG_DH = 5, SG_COULOMB = 6, SG_DIPOLE = 7, SG_GB = 10, SG_GBR = 11, SG_GBW = 12, SG_GBC = 13, &
         SG_GBWC = 14, SG_ECP = 20, SG_ECPR = 21, SG_ECPW = 22, SG_ECPC = 23, SG_ECPWC = 24
     ! sg_ecp_solver
-    integer(c_int32_t), parameter :: SG_SOLVER_BRENT_COMPAT = 0, SG_SOLVER_NEWTON = 1, SG_SOLVER_MLP_NEWTON = 2
+    integer(c_int32_t), parameter :: SG_SOLVER_BRENT_COMPAT = 0, SG_SOLVER_NEWTON = 1, SG_SOLVER_MLP_NEWTON = 2, &
+        SG_SOLVER_NEWTON_SUPPORT = 3
     ! sg_integrator and step flags
     integer(c_int32_t), parameter :: SG_INT_NVE = 0, SG_INT_LANGEVIN = 1, SG_INT_NH = 2, SG_INT_NH_REF = 3
     integer(c_int32_t), parameter :: SG_STEP_FLAT = 1, SG_STEP_REACTION_FIELD = 2, SG_STEP_CONSTRAINTS = 4, &

@@ -66,8 +66,11 @@ typedef enum {
 /* ECP contact-parameter solvers. */
 typedef enum {
     SG_SOLVER_BRENT_COMPAT = 0,  /* the reference's Brent (fortran/force.f90:1046-1172), FP64, same lambda bits */
-    SG_SOLVER_NEWTON = 1,        /* Newton on dS/dlambda, FP32, FP64 residual check            */
-    SG_SOLVER_MLP_NEWTON = 2     /* MLP initial guess, <= 3 Newton steps, else the plain Newton */
+    SG_SOLVER_NEWTON = 1,        /* Newton on dS/dlambda from lambda = 1/2, FP32, FP64 residual check */
+    SG_SOLVER_MLP_NEWTON = 2,    /* MLP initial guess, <= 3 Newton steps, else the plain Newton */
+    SG_SOLVER_NEWTON_SUPPORT = 3 /* the same Newton from lambda = h_A / (h_A + h_B), h the support
+                                    functions sqrt(r.A r), sqrt(r.B r) of the two ellipsoids along r
+                                    (the maximiser for spheres); same tolerance and check */
 } sg_ecp_solver;
 
 /* Parameters of one pair-force call (the arguments of *_calculate_forces). */
@@ -98,7 +101,9 @@ typedef struct {
     int64_t pairs;          /* pairs evaluated                                      */
     int64_t solver_evals;   /* ECP: total objective / Newton evaluations; LJ, GB: pairs in range */
     int64_t nonconverged;   /* pairs whose solve hit its iteration cap              */
-    int64_t fallbacks;      /* MLP path: pairs that fell back to the plain Newton   */
+    int64_t fallbacks;      /* MLP path: pairs that fell back to the plain Newton;
+                               GB kinds: pairs evaluated in the near-contact class
+                               (contact distance in double-float)                */
     int64_t iter_hist[24];  /* Newton iterations per pair (last bin: >= 23)         */
     int64_t fp64_refined;   /* Newton: pairs that needed the FP64-residual correction */
 } sg_ecp_stats;
@@ -398,10 +403,11 @@ int sg_step_configure_pairs(sg_ctx* ctx, const sg_step_config* cfg, const sg_pai
 int sg_step(sg_ctx* ctx, int32_t nsteps);
 /* Wait, then report list overflow (SG_ECAPACITY) or a non-finite energy (SG_ENAN). */
 int sg_step_check(sg_ctx* ctx);
-/* Run nsteps steps eagerly (not from the graph) with CUDA events between the
- * stages and return the mean milliseconds of: initial half step, constraints a,
- * list check and rebuild, force zeroing, pair forces, final half step,
- * constraints b (the constraint stages are 0 without SG_STEP_CONSTRAINTS). */
+/* Run nsteps steps (one eager step, then a captured step with an event-record
+ * node between its stages, launched nsteps times) and return the mean
+ * milliseconds of: initial half step, constraints a, list check and rebuild,
+ * force zeroing, pair forces, final half step, constraints b (the constraint
+ * stages are 0 without SG_STEP_CONSTRAINTS). */
 int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[7]);
 /* Kernel launches in one captured step (after the first sg_step call). */
 int sg_step_kernel_count(sg_ctx* ctx, int64_t* count);
@@ -423,17 +429,24 @@ int sg_mlp_set_inline(sg_ctx* ctx, int32_t inline_guess);
 /* ---- autotuner of the pair kernels (no counterpart in the reference) ------- */
 typedef struct {
     int32_t block;       /* chosen threads per block                            */
-    int32_t filter;      /* chosen: 1 = range filter + per-warp in-range queue   */
+    int32_t filter;      /* chosen: 1 = range filter + per-warp in-range queue;
+                            2 = Gay-Berne replicas: one replica per block, its
+                            records staged in shared memory (replaces (256, 0));
+                            ECP kinds: 1 = split Newton path (solve kernel, then
+                            force kernel), 0 = one kernel per pair              */
     int32_t candidates;  /* variants timed (ms[0..candidates-1])                 */
     int32_t reserved;
-    float ms[4];         /* mean launch time of (256,0) (128,0) (256,1) (128,1)  */
+    float ms[4];         /* mean launch time of (256,0) (128,0) (256,1) (128,1);
+                            GB replicas: (256,2) in place of (256,0)           */
 } sg_tune_result;
 /* Time each launch variant of the params' pair kernel on the current list
  * (reps launches each), keep the fastest for this context's (kind, size,
  * density) bucket. Forces, torques and energy accumulators are restored.
  * Captured steps are re-captured at their next sg_step. */
 int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* params, int32_t reps, sg_tune_result* out);
-/* Set a launch variant by hand (block 128 or 256; filter ignored for ECP). */
+/* Set a launch variant by hand (block 128 or 256; filter 0, 1, or 2 for
+ * the Gay-Berne replica tiles; for ECP kinds, filter selects the split Newton
+ * path, which the Brent solver ignores). */
 int sg_pair_set_launch(sg_ctx* ctx, int32_t kind, int32_t block, int32_t filter);
 
 /* Measured FP32 (fp64 = 0) or FP64 (fp64 = 1) FMA throughput of this GPU in

@@ -18,7 +18,7 @@ LJ, LJ12, LJW, WCA = 0, 1, 2, 3
 MORSE, DH, COULOMB, DIPOLE = 4, 5, 6, 7
 GB, GBR, GBW, GBC, GBWC = 10, 11, 12, 13, 14
 ECP, ECPR, ECPW, ECPC, ECPWC = 20, 21, 22, 23, 24
-SOLVER_BRENT_COMPAT, SOLVER_NEWTON, SOLVER_MLP_NEWTON = 0, 1, 2
+SOLVER_BRENT_COMPAT, SOLVER_NEWTON, SOLVER_MLP_NEWTON, SOLVER_NEWTON_SUPPORT = 0, 1, 2, 3
 
 
 class PairParams(C.Structure):

@@ -1,0 +1,74 @@
+// Double-float arithmetic on the FP32 pipe: a value is hi + lo with
+// |lo| <= ulp(hi) / 2, about 48 significant bits. Error-free transformations
+// (Knuth's two-sum, the FMA two-product) carry each rounding error into lo.
+// Used where FP32 cancellation would be amplified past the force tolerance
+// and FP64 (1/64 of the FP32 rate on GB300) would be too slow.
+#pragma once
+
+#include "sg_internal.cuh"
+
+struct dfl {
+    float hi, lo;
+};
+
+SG_DEV dfl df_of(float a) { return {a, 0.f}; }
+// a + b exactly (any magnitudes)
+SG_DEV dfl df_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+// a + b exactly, when |a| >= |b|
+SG_DEV dfl df_fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+// a * b exactly
+SG_DEV dfl df_two_prod(float a, float b) {
+    const float p = a * b;
+    return {p, fmaf(a, b, -p)};
+}
+SG_DEV dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
+SG_DEV dfl df_add(dfl a, dfl b) {
+    const dfl s = df_two_sum(a.hi, b.hi);
+    return df_fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+SG_DEV dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+SG_DEV dfl df_mul(dfl a, dfl b) {
+    const dfl p = df_two_prod(a.hi, b.hi);
+    return df_fast_two_sum(p.hi, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo)));
+}
+SG_DEV dfl df_mul_f(dfl a, float b) {
+    const dfl p = df_two_prod(a.hi, b);
+    return df_fast_two_sum(p.hi, fmaf(a.lo, b, p.lo));
+}
+// a / b: the FP32 quotient, then one correction from the double-float residual
+SG_DEV dfl df_div(dfl a, dfl b) {
+    const float rb = __frcp_rn(b.hi);
+    const float q1 = a.hi * rb;
+    const dfl r = df_sub(a, df_mul_f(b, q1));
+    return df_fast_two_sum(q1, r.hi * rb);
+}
+SG_DEV dfl df_sqrt(dfl a) {
+    const float s = sqrtf(a.hi);
+    const dfl p = df_two_prod(s, s);
+    return df_fast_two_sum(s, (((a.hi - p.hi) - p.lo) + a.lo) * (0.5f / s));
+}
+// a . b of two FP32 vectors
+SG_DEV dfl df_dot3(float3 a, float3 b) {
+    const dfl x = df_two_prod(a.x, b.x), y = df_two_prod(a.y, b.y), z = df_two_prod(a.z, b.z);
+    const dfl s = df_two_sum(x.hi, y.hi);
+    const dfl t = df_two_sum(s.hi, z.hi);
+    return df_fast_two_sum(t.hi, ((x.lo + y.lo) + z.lo) + (s.lo + t.lo));
+}
+// a . (b + bl) with bl the low parts of a double-float vector
+SG_DEV dfl df_dot3_lo(float3 a, float3 b, float3 bl) {
+    dfl d = df_dot3(a, b);
+    return df_fast_two_sum(d.hi, d.lo + fmaf(a.x, bl.x, fmaf(a.y, bl.y, a.z * bl.z)));
+}
+// (a + al) . (b + bl), both double-float vectors
+SG_DEV dfl df_dot3_dd(float3 a, float3 al, float3 b, float3 bl) {
+    dfl d = df_dot3(a, b);
+    const float c = fmaf(a.x, bl.x, fmaf(a.y, bl.y, fmaf(a.z, bl.z, fmaf(al.x, b.x, fmaf(al.y, b.y, al.z * b.z)))));
+    return df_fast_two_sum(d.hi, d.lo + c);
+}

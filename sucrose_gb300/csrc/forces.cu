@@ -12,8 +12,10 @@ namespace {
 int launch_forces(sg_ctx* ctx, const sg_pair_params* p) {
     if (!ctx || !p) return SG_EINVAL;
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "pair forces need sg_nlist_init first");
-    SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 4, 0, sizeof(double) * 2, ctx->stream));
-    SG_CUDA(ctx, cudaMemsetAsync(ctx->stats, 0, sizeof(unsigned long long) * 32, ctx->stream));
+    if (!ctx->step_fused) {   // the fused step's initial half step zeroed them
+        SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 4, 0, sizeof(double) * 2, ctx->stream));
+        SG_CUDA(ctx, cudaMemsetAsync(ctx->stats, 0, sizeof(unsigned long long) * 32, ctx->stream));
+    }
     ctx->launch_family = p->kind < 10 ? 0 : (p->kind < 20 ? 1 : 2);
     if (ctx->nrep && ctx->fam_pstart[ctx->launch_family] == ctx->fam_pstart[ctx->launch_family + 1])
         return SG_OK;   // no replica of this family

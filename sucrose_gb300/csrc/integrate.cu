@@ -6,6 +6,7 @@
 
 #include "sg_internal.cuh"
 #include "philox.cuh"
+#include "step_epi.cuh"
 
 namespace {
 
@@ -169,7 +170,7 @@ struct LgvConst {
 __global__ void k_lgv_initial(int n, LgvConst c, Geo g, float4* __restrict__ pos, float4* __restrict__ vel,
                               const float4* __restrict__ force, float4* __restrict__ quat, float4* __restrict__ angm,
                               const float4* __restrict__ torque, const float4* __restrict__ inert,
-                              const float4* __restrict__ inert_inv, int rotations) {
+                              const float4* __restrict__ inert_inv, int rotations, StepEpi epi) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float h = 0.5f * c.dt;
@@ -202,8 +203,12 @@ __global__ void k_lgv_initial(int n, LgvConst c, Geo g, float4* __restrict__ pos
     v.z = c.ed * v.z + amp * n1c;
     p = wrap_pos(make_float3(p.x + h * v.x, p.y + h * v.y, p.z + h * v.z), g, i);
     vel[i] = v;
-    pos[i] = make_float4(p.x, p.y, p.z, r.w);
-    if (!rotations) return;
+    const float4 pn = make_float4(p.x, p.y, p.z, r.w);
+    pos[i] = pn;
+    if (!rotations) {
+        if (epi.on) step_epilogue(epi, i, pn, quat[i]);
+        return;
+    }
     float4 L4 = angm[i], T = torque[i], I4 = inert[i], Ii = inert_inv[i];
     float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
     Rot rm;
@@ -215,14 +220,16 @@ __global__ void k_lgv_initial(int n, LgvConst c, Geo g, float4* __restrict__ pos
     Lb.z = c.kk12 * Lb.z + c.kk2 * sqrtf(rot_ampf * I4.z) * n2c;
     L = rot_apply_t(rm, Lb);
     angm[i] = make_float4(L.x, L.y, L.z, 0.f);
-    quat[i] = q_advance(q, qd, c.dt);
+    const float4 qn = q_advance(q, qd, c.dt);
+    quat[i] = qn;
+    if (epi.on) step_epilogue(epi, i, pn, qn);
 }
 
 __global__ void k_lgv_final(int n, float dt, float4* __restrict__ vel, const float4* __restrict__ force,
                             const float4* __restrict__ shape, const float4* __restrict__ quat,
                             float4* __restrict__ angm, const float4* __restrict__ torque,
                             const float4* __restrict__ inert_inv, int rotations, double* partials, unsigned int* done,
-                            double* acc) {
+                            double* acc, int* step_inc) {
     double e[2] = {0.0, 0.0};
     const float h = 0.5f * dt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -238,7 +245,10 @@ __global__ void k_lgv_final(int n, float dt, float4* __restrict__ vel, const flo
             e[1] += kin_rot_of(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z));
         }
     }
-    block_reduce_finish<2>(e, partials, done, acc);
+    // step_inc (captured step): the sums are stored, and the step counter advances
+    if (block_reduce_finish<2>(e, partials, done, acc, nullptr, step_inc != nullptr) && step_inc &&
+        threadIdx.x == 0)
+        *step_inc += 1;
 }
 
 // ------------------------------------------------------------ Nose-Hoover --
@@ -374,7 +384,7 @@ __global__ void k_nhc_sum_chain(int n, float dt, int kick, float4* __restrict__ 
             e[1] += 2.0 * kin_rot_of(quat[i], make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z));
         }
     }
-    if (block_reduce_finish<2>(e, partials, done, nh + 14)) {
+    if (block_reduce_finish<2>(e, partials, done, nh + 14, nullptr, true)) {
         __syncthreads();
         __threadfence_block();
         nhc_chain_threads(c, nh, rot);
@@ -387,7 +397,7 @@ __global__ void k_nhc_initial_fused(int n, const double* nh, float dt, Geo g, fl
                                     float4* __restrict__ vel, const float4* __restrict__ force,
                                     float4* __restrict__ quat, float4* __restrict__ angm,
                                     const float4* __restrict__ torque, const float4* __restrict__ inert_inv,
-                                    int rot_chain, int rotations) {
+                                    int rot_chain, int rotations, StepEpi epi) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float sc = (float)nh[12];
@@ -402,20 +412,24 @@ __global__ void k_nhc_initial_fused(int n, const double* nh, float dt, Geo g, fl
     const float h = 0.5f * dt, im = v.w;
     v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
     float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g, i);
-    pos[i] = make_float4(p.x, p.y, p.z, r.w);
+    const float4 pn = make_float4(p.x, p.y, p.z, r.w);
+    pos[i] = pn;
     vel[i] = v;
+    float4 qn = quat[i];
     if (rotations) {
         const float4 T = torque[i], Ii = inert_inv[i];
         float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
         Rot rm;
         float3 Lb;
-        const float4 q = quat[i];
+        const float4 q = qn;
         float4 qd = q_midpoint(q, L, make_float3(Ii.x, Ii.y, Ii.z), dt, rm, Lb);
-        quat[i] = q_advance(q, qd, dt);
+        qn = q_advance(q, qd, dt);
+        quat[i] = qn;
         angm[i] = make_float4(L.x, L.y, L.z, 0.f);
     } else if (rot_chain) {
         angm[i] = L4;
     }
+    if (epi.on) step_epilogue(epi, i, pn, qn);
 }
 
 // Chain scaling, then the rotational half kick; KE = sum 0.5 m v^2 and KE_rot
@@ -424,7 +438,7 @@ __global__ void k_nhc_final_fused(int n, const double* nh, float dt, float4* __r
                                   const float4* __restrict__ shape, const float4* __restrict__ quat,
                                   float4* __restrict__ angm, const float4* __restrict__ torque,
                                   const float4* __restrict__ inert_inv, int rot_chain, int rotations, double* partials,
-                                  unsigned int* done, double* acc) {
+                                  unsigned int* done, double* acc, int* step_inc) {
     double e[2] = {0.0, 0.0};
     const float h = 0.5f * dt;
     const float sc = (float)nh[12];
@@ -447,7 +461,9 @@ __global__ void k_nhc_final_fused(int n, const double* nh, float dt, float4* __r
             }
         }
     }
-    block_reduce_finish<2>(e, partials, done, acc);
+    // the sums are stored; step_inc (captured step): the step counter advances
+    if (block_reduce_finish<2>(e, partials, done, acc, nullptr, true) && step_inc && threadIdx.x == 0)
+        *step_inc += 1;
 }
 
 // scale v (and L), then optionally the VV kick + drift (initial step)
@@ -639,9 +655,11 @@ int sg_lgv_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double 
     c.temp_int = (uint32_t)(int32_t)(target_temp * 1000.0);
     c.k0 = key ? key[0] : SG_PHILOX_KEY0;
     c.k1 = key ? key[1] : SG_PHILOX_KEY1;
+    StepEpi epi;
+    if (int rc = make_step_epi(ctx, epi)) return rc;
     k_lgv_initial<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, c, make_geo(ctx), ctx->pos, ctx->vel,
                                                                  ctx->force, ctx->quat, ctx->angm, ctx->torque,
-                                                                 ctx->inert, ctx->inert_inv, ctx->lgv_rotations);
+                                                                 ctx->inert, ctx->inert_inv, ctx->lgv_rotations, epi);
     SG_LAUNCH_CHECK(ctx, "k_lgv_initial");
     return SG_OK;
 }
@@ -649,12 +667,13 @@ int sg_lgv_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double 
 int sg_lgv_final(sg_ctx* ctx, double dt, double damping, double* kin_eng, double* kin_rot) {
     (void)damping;
     if (!ctx) return SG_EINVAL;
-    SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double) * 2, ctx->stream));
+    if (!ctx->step_fused) SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double) * 2, ctx->stream));
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
     k_lgv_final<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->vel, ctx->force, ctx->shape, ctx->quat,
                                               ctx->angm, ctx->torque, ctx->inert_inv, ctx->lgv_rotations, ctx->partials,
-                                              ctx->done_counter, ctx->acc + 2);
+                                              ctx->done_counter, ctx->acc + 2,
+                                              ctx->step_fused ? ctx->step_dev : nullptr);
     SG_LAUNCH_CHECK(ctx, "k_lgv_final");
     if (int rc = read_acc(ctx, 2, kin_eng)) return rc;
     return read_acc(ctx, 3, kin_rot);
@@ -720,16 +739,17 @@ int sg_nhc_step_initial(sg_ctx* ctx, double dt, double target_temp, double coupl
     if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "Nose-Hoover chains are per system: not available on a replica context");
     if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
     NhConst c = nh_const(ctx, dt, target_temp, coupling);
-    SG_CUDA(ctx, cudaMemsetAsync(ctx->nh + 14, 0, sizeof(double) * 2, ctx->stream));
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
     k_nhc_sum_chain<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, 0, ctx->vel, ctx->force, ctx->shape, ctx->quat,
                                                   ctx->angm, ctx->inert_inv, rot_chain, c, ctx->partials,
                                                   ctx->done_counter, ctx->nh);
+    StepEpi epi;
+    if (int rc = make_step_epi(ctx, epi)) return rc;
     k_nhc_initial_fused<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, (float)dt, make_geo(ctx),
                                                                        ctx->pos, ctx->vel, ctx->force, ctx->quat,
                                                                        ctx->angm, ctx->torque, ctx->inert_inv,
-                                                                       rot_chain, rotations);
+                                                                       rot_chain, rotations, epi);
     SG_LAUNCH_CHECK(ctx, "k_nhc_initial_fused");
     return SG_OK;
 }
@@ -740,16 +760,15 @@ int sg_nhc_step_final(sg_ctx* ctx, double dt, double target_temp, double couplin
     if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "Nose-Hoover chains are per system: not available on a replica context");
     if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
     NhConst c = nh_const(ctx, dt, target_temp, coupling);
-    SG_CUDA(ctx, cudaMemsetAsync(ctx->nh + 14, 0, sizeof(double) * 2, ctx->stream));
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
     k_nhc_sum_chain<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, 1, ctx->vel, ctx->force, ctx->shape, ctx->quat,
                                                   ctx->angm, ctx->inert_inv, rot_chain, c, ctx->partials,
                                                   ctx->done_counter, ctx->nh);
-    SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double) * 2, ctx->stream));
     k_nhc_final_fused<<<grid, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, (float)dt, ctx->vel, ctx->shape, ctx->quat,
                                                     ctx->angm, ctx->torque, ctx->inert_inv, rot_chain, rotations,
-                                                    ctx->partials, ctx->done_counter, ctx->acc + 2);
+                                                    ctx->partials, ctx->done_counter, ctx->acc + 2,
+                                                    ctx->step_fused ? ctx->step_dev : nullptr);
     SG_LAUNCH_CHECK(ctx, "k_nhc_final_fused");
     return SG_OK;
 }

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "sg_internal.cuh"
+#include "step_epi.cuh"
 
 namespace {
 
@@ -120,45 +121,13 @@ __device__ __forceinline__ int cell_of(float4 p, const ListGeom& g, int& cx, int
 // ---------------------------------------------------------------- trigger --
 // needs_rebuild (system.f90:1005-1039) in FP64 on the FP32 state: any
 // particle with 4 |dr|^2 > trigger_sq requests a rebuild (the maximum over
-// particles exceeds the bound iff some particle does).
-__global__ void k_check(int n, const float4* __restrict__ pos, const float4* __restrict__ last, ListGeom g0,
-                        double trigger_sq, int* flags, RepDev rp, int* rep_flag) {
+// particles exceeds the bound iff some particle does). The test itself is
+// check_displacement (step_epi.cuh), which the captured step also runs inside
+// its initial half step.
+__global__ void k_check(int n, const float4* __restrict__ pos, CheckArgs c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    ListGeom g = g0;
-    int r = 0;
-    if (rp.rep_of) {
-        r = rp.rep_of[i];
-        g = geom_for(g0, rp, r);
-        trigger_sq = rp.trig[r];
-    }
-    float4 a = pos[i], b = last[i];
-    {
-        // FP32 screen: decide in FP32 when clear of the bound by 1e-3 relative
-        float fx = a.x - b.x, fy = a.y - b.y, fz = a.z - b.z;
-        if (g.periodic) {
-            fx -= roundf(fx * g.inv_box.x) * g.box.x;
-            fy -= roundf(fy * g.inv_box.y) * g.box.y;
-            fz -= roundf(fz * g.inv_box.z) * g.box.z;
-        }
-        const float f4 = 4.f * (fx * fx + fy * fy + fz * fz);
-        if (f4 < (float)trigger_sq * 0.999f && fabsf(fx) < 0.25f * g.box.x && fabsf(fy) < 0.25f * g.box.y &&
-            fabsf(fz) < 0.25f * g.box.z)
-            return;
-    }
-    double dx = __dsub_rn((double)a.x, (double)b.x), dy = __dsub_rn((double)a.y, (double)b.y),
-           dz = __dsub_rn((double)a.z, (double)b.z);
-    if (g.periodic) {
-        dx = __dsub_rn(dx, __dmul_rn(round(__ddiv_rn(dx, g.bx)), g.bx));
-        dy = __dsub_rn(dy, __dmul_rn(round(__ddiv_rn(dy, g.by)), g.by));
-        dz = __dsub_rn(dz, __dmul_rn(round(__ddiv_rn(dz, g.bz)), g.bz));
-    }
-    double rr = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    if (__dmul_rn(4.0, rr) > trigger_sq) {
-        // a replica context rebuilds only the replicas whose particles moved
-        if (rp.rep_of) rep_flag[r] = 1;
-        flags[F_REBUILD] = 1;
-    }
+    check_displacement(i, pos[i], c);
 }
 
 __global__ void k_begin(int* flags, int* cell_count, int* cell_fill, int ncells) {
@@ -717,9 +686,7 @@ int build_sync(sg_ctx* ctx) {
 }  // namespace
 
 int sg_nlist_enqueue_check(sg_ctx* ctx) {
-    ListGeom g = make_geom(ctx);
-    k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->nl.pos_last, g, ctx->nl.trigger_sq,
-                                                           ctx->nl.dev_flags, ctx->rep, ctx->nl.rep_flag);
+    k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, check_args(ctx));
     SG_LAUNCH_CHECK(ctx, "k_check");
     return SG_OK;
 }
@@ -939,11 +906,9 @@ int sg_nlist_build(sg_ctx* ctx) {
 int sg_nlist_needs_rebuild(sg_ctx* ctx, int32_t* flag) {
     if (!ctx || !flag) return SG_EINVAL;
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_nlist_needs_rebuild");
-    ListGeom g = make_geom(ctx);
     k_clear_request<<<clear_grid(ctx), 256, 0, ctx->stream>>>(ctx->nl.dev_flags, ctx->nl.rep_flag, ctx->nrep,
                                                               nullptr);
-    k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->nl.pos_last, g, ctx->nl.trigger_sq,
-                                                           ctx->nl.dev_flags, ctx->rep, ctx->nl.rep_flag);
+    k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, check_args(ctx));
     SG_LAUNCH_CHECK(ctx, "k_check");
     int f = 0;
     SG_CUDA(ctx, cudaMemcpyAsync(&f, ctx->nl.dev_flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -957,9 +922,7 @@ int sg_nlist_needs_rebuild(sg_ctx* ctx, int32_t* flag) {
 int sg_nlist_update(sg_ctx* ctx) {
     if (!ctx) return SG_EINVAL;
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_nlist_update");
-    ListGeom g = make_geom(ctx);
-    k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->nl.pos_last, g, ctx->nl.trigger_sq,
-                                                           ctx->nl.dev_flags, ctx->rep, ctx->nl.rep_flag);
+    k_check<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, check_args(ctx));
     SG_LAUNCH_CHECK(ctx, "k_check");
     return enqueue_build(ctx);
 }

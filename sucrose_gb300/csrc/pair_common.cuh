@@ -8,9 +8,10 @@
 //   * the I-side terms are summed across lanes with a segmented shuffle scan
 //     (segments = runs of equal i), and the last lane of each run issues one
 //     float4 atomic,
-//   * PE and the pair virial r_ij . F_ij are summed per thread in FP32, per
-//     warp in double-float, then per block in FP64, and finished
-//     deterministically by the last block (block_reduce_finish_f).
+//   * PE and the pair virial r_ij . F_ij are summed per thread and per warp
+//     in double-float (FP32 two-sums), then per block in FP64, and finished
+//     deterministically by the last block (block_reduce_finish_f), so the
+//     totals do not depend on which pairs a thread happened to evaluate.
 // The grid is persistent (a multiple of the SM count); the pair count is read
 // from device memory so the launch needs no host synchronisation.
 #pragma once
@@ -31,6 +32,14 @@ template <class P, class = void>
 struct ExactFilter : std::true_type {};
 template <class P>
 struct ExactFilter<P, std::void_t<decltype(P::kExactFilter)>> : std::integral_constant<bool, P::kExactFilter> {};
+
+//   kTwoClass (false): its range test returns a class (0 out of range, 1 in
+//     range, 2 in range and near contact) and the near-contact pairs queue
+//     separately for eval_r<true>, a more precise evaluation.
+template <class P, class = void>
+struct TwoClass : std::false_type {};
+template <class P>
+struct TwoClass<P, std::void_t<decltype(P::kTwoClass)>> : std::integral_constant<bool, P::kTwoClass> {};
 
 struct PairOut {
     float3 f;    // force on I (FXIJ)
@@ -62,6 +71,26 @@ struct PairLaunch {
     double* acc_total;           // running sums since the last zero_forces
     unsigned long long* stats;   // solver statistics (ECP) or listed / in-range counts (LJ, GB)
 };
+
+// Storage index and particles of lane `lane`'s pair in the 32-pair chunk that
+// starts at row-order index `base`; pairs outside [b0, np) are invalid.
+SG_DEV void pair_fetch(const PairLaunch& L, int base, int lane, int np, int b0, int& t, int& i, int& j,
+                       bool& valid) {
+    const int v = base + lane;
+    valid = v < np && v >= b0;
+    t = v;
+    i = -1;
+    j = 0;
+    if (valid) {
+        if (L.sec) {
+            int r = L.chunk_rep[base >> 5];
+            while (r + 1 < L.nrep && L.row_off[L.rep_off[r + 1]] <= v) ++r;
+            t = (int)(L.sec[r] + (long long)(v - L.row_off[L.rep_off[r]]));
+        }
+        i = L.pair_i[t];
+        j = L.pair_j[t];
+    }
+}
 
 SG_DEV void atomic_add_f3(float4* p, float3 v) {
     atomicAdd(p, make_float4(v.x, v.y, v.z, 0.f));
@@ -100,12 +129,27 @@ SG_DEV void segmented_scatter_i(const PairLaunch& L, int i, float3 f, float3 t) 
 #define SG_NSTATS 32
 #define SG_PAIR_MAX_BLOCK 256
 
+// Per-thread double-float sums of the pair energy and virial.
+struct EnergySums {
+    float pe = 0.f, pe_lo = 0.f, vir = 0.f, vir_lo = 0.f;
+    SG_DEV void add(float p, float v) {
+        float s = pe + p, bb = s - pe;
+        pe_lo += (pe - (s - bb)) + (p - bb);
+        pe = s;
+        s = vir + v;
+        bb = s - vir;
+        vir_lo += (vir - (s - bb)) + (v - bb);
+        vir = s;
+    }
+};
+
 // One pair per lane, evaluated and scattered (all 32 lanes call it).
 // i, j: the pair's particles (loaded by the caller; ignored when !valid).
 // COUNT: 0 nothing, 1 listed and in-range pairs, 2 in-range pairs only.
 // HAS_R: r_ij comes from the in-range queue (QueueR potentials).
-template <class Pot, int COUNT, bool HAS_R = false>
-SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int j, bool valid, float& pe, float& vir,
+// PRECISE: the near-contact class of a kTwoClass potential.
+template <class Pot, int COUNT, bool HAS_R = false, bool PRECISE = false>
+SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int j, bool valid, EnergySums& es,
                          unsigned long long* sh_stats, float3 rq = make_float3(0.f, 0.f, 0.f)) {
     const int lane = threadIdx.x & 31;
     PairOut o;
@@ -120,7 +164,9 @@ SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int 
         j = 0;
     }
     // called by every lane (warp-cooperative potentials need all 32)
-    if constexpr (HAS_R)
+    if constexpr (HAS_R && TwoClass<Pot>::value)
+        pot.template eval_r<PRECISE>(valid, valid ? i : 0, j, rq, o);
+    else if constexpr (HAS_R)
         pot.eval_r(valid, valid ? i : 0, j, rq, o);
     else
         pot.eval(valid, valid ? i : 0, j, t, o, sh_stats);
@@ -136,23 +182,118 @@ SG_DEV void pair_process(const PairLaunch& L, const Pot& pot, int t, int i, int 
         atomic_add_f3(&L.force[j], make_float3(-o.f.x, -o.f.y, -o.f.z));
         if (Pot::kTorque) atomic_add_f3(&L.torque[j], o.tj);
     }
-    pe += o.pe;
-    vir += o.vir;
+    es.add(o.pe, o.vir);
     segmented_scatter_i<Pot::kTorque>(L, i, o.f, o.ti);
 }
 
-// FILTER: a cheap range test runs on every listed pair first; the pairs in
-// range queue up per warp (in list order, so rows stay contiguous) and are
-// evaluated 32 at a time, so no lane idles on an out-of-range pair.
+// Per-warp queues of in-range pairs for the filtered kernels: a cheap range
+// test runs on every listed pair first; the pairs in range queue up (in list
+// order, so rows stay contiguous) and are evaluated 32 at a time, so no lane
+// idles on an out-of-range pair. kTwoClass potentials keep a second queue for
+// their near-contact class. Slots: storage index, i, j [, r_ij]; 64 per queue.
+template <class Pot>
+struct PairQueues {
+    static constexpr bool kQR = QueueR<Pot>::value;
+    static constexpr bool kExact = ExactFilter<Pot>::value;
+    static constexpr bool k2 = TwoClass<Pot>::value;
+    static constexpr int kQW = kQR ? 6 : 3;   // words per slot
+    static constexpr int kNQ = k2 ? 2 : 1;    // queues per warp
+    static constexpr int kWords = 64 * kQW * kNQ;   // shared words per warp
+    static constexpr int kCnt = (Pot::kCountActive && !kExact) ? 2 : 0;
+    int* qbase;   // this warp's queues: t at +0, i at +64, j at +128, r_ij x, y, z at +192, +256, +320
+    int qn[2];
+    int lane;
+
+    SG_DEV void init(int* warp_words) {
+        qbase = warp_words;
+        qn[0] = qn[1] = 0;
+        lane = threadIdx.x & 31;
+    }
+    // queue k: append this lane's pair when keep (list order kept)
+    SG_DEV void push(int k, bool keep, int t, int i, int j, float3 rr) {
+        int* q = qbase + k * 64 * kQW;
+        const unsigned km = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            const int slot = qn[k] + __popc(km & ((1u << lane) - 1u));
+            q[slot] = t;
+            q[64 + slot] = i;
+            q[128 + slot] = j;
+            if constexpr (kQR) {
+                float* qr = reinterpret_cast<float*>(q + 192);
+                qr[slot] = rr.x;
+                qr[64 + slot] = rr.y;
+                qr[128 + slot] = rr.z;
+            }
+        }
+        qn[k] += __popc(km);
+        __syncwarp();
+    }
+    // queue K: evaluate its first 32 pairs (or the last n < 32) and shift the rest down
+    template <int K>
+    SG_DEV void drain(int n, const PairLaunch& L, const Pot& pot, EnergySums& es, unsigned long long* sh_stats) {
+        int* q = qbase + K * 64 * kQW;
+        [[maybe_unused]] float* qr = reinterpret_cast<float*>(q + 192);
+        const bool ok = lane < n;
+        const int tq = ok ? q[lane] : 0, iq = ok ? q[64 + lane] : 0, jq = ok ? q[128 + lane] : 0;
+        float3 rq = make_float3(0.f, 0.f, 0.f);
+        if constexpr (kQR)
+            if (ok) rq = make_float3(qr[lane], qr[64 + lane], qr[128 + lane]);
+        __syncwarp();
+        if (n == 32 && lane < qn[K] - 32) {
+            q[lane] = q[32 + lane];
+            q[64 + lane] = q[96 + lane];
+            q[128 + lane] = q[160 + lane];
+            if constexpr (kQR) {
+                qr[lane] = qr[32 + lane];
+                qr[64 + lane] = qr[96 + lane];
+                qr[128 + lane] = qr[160 + lane];
+            }
+        }
+        __syncwarp();
+        qn[K] -= n;
+        pair_process<Pot, kCnt, kQR, K == 1>(L, pot, tq, iq, jq, ok, es, sh_stats, rq);
+    }
+    // one listed pair per lane: range test, counters, queue, evaluate full batches
+    SG_DEV void feed(const PairLaunch& L, const Pot& pot, int t, int i, int j, bool valid, EnergySums& es,
+                     unsigned long long* sh_stats) {
+        float3 rr = make_float3(0.f, 0.f, 0.f);
+        int cls;
+        if constexpr (k2)
+            cls = valid ? pot.in_range_r(i, j, rr) : 0;
+        else if constexpr (kQR)
+            cls = (valid && pot.in_range_r(i, j, rr)) ? 1 : 0;
+        else
+            cls = (valid && pot.in_range(i, j)) ? 1 : 0;
+        const unsigned vm = __ballot_sync(0xffffffffu, valid), km = __ballot_sync(0xffffffffu, cls != 0);
+        if (Pot::kCountActive && lane == 0) {
+            atomicAdd(&sh_stats[0], (unsigned long long)__popc(vm));
+            if (kExact && km) atomicAdd(&sh_stats[1], (unsigned long long)__popc(km));
+        }
+        if constexpr (k2) {   // stats[3]: pairs of the near-contact class
+            const unsigned k2m = __ballot_sync(0xffffffffu, cls == 2);
+            if (lane == 0 && k2m) atomicAdd(&sh_stats[3], (unsigned long long)__popc(k2m));
+        }
+        push(0, cls == 1, t, i, j, rr);
+        if constexpr (k2) push(1, cls == 2, t, i, j, rr);
+        if (qn[0] >= 32) drain<0>(32, L, pot, es, sh_stats);
+        if constexpr (k2)
+            if (qn[1] >= 32) drain<1>(32, L, pot, es, sh_stats);
+    }
+    // the queues' last pairs (qn is warp-uniform)
+    SG_DEV void flush(const PairLaunch& L, const Pot& pot, EnergySums& es, unsigned long long* sh_stats) {
+        if (qn[0] > 0) drain<0>(qn[0], L, pot, es, sh_stats);
+        if constexpr (k2)
+            if (qn[1] > 0) drain<1>(qn[1], L, pot, es, sh_stats);
+    }
+};
+
+// FILTER: the range test and per-warp queues of PairQueues.
 template <class Pot, bool FILTER>
 __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFiltered : Pot::kMinBlocks)
     k_pair(PairLaunch L, Pot pot) {
-    constexpr bool kQR = QueueR<Pot>::value;
-    constexpr bool kExact = ExactFilter<Pot>::value;
-    constexpr int kQW = kQR ? 6 : 3;   // queue words per slot
+    using Q = PairQueues<Pot>;
     __shared__ unsigned long long sh_stats[SG_NSTATS];
-    // per-warp queue of in-range pairs: storage index, i, j [, r_ij] (64 slots each)
-    __shared__ int sh_queue[FILTER ? SG_PAIR_MAX_BLOCK * 2 * kQW : 1];
+    __shared__ int sh_queue[FILTER ? (SG_PAIR_MAX_BLOCK / 32) * Q::kWords : 1];
     constexpr bool kSh = Pot::kStats || Pot::kCountActive;
     if (kSh) {
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x) sh_stats[k] = 0ull;
@@ -163,103 +304,32 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFil
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int np = *L.npairs;
     const int b0 = L.begin ? *L.begin : 0;
-    float pe = 0.f, vir = 0.f;
-    int* qt = sh_queue + (FILTER ? (threadIdx.x >> 5) * 64 * kQW : 0);
-    int* qi = qt + 64;
-    int* qj = qt + 128;
-    float* qr = reinterpret_cast<float*>(qt + 192);   // x, y, z at +0, +64, +128 (kQR only)
-    int qn = 0;
+    EnergySums es;
+    Q q;
+    q.init(sh_queue + (FILTER ? (threadIdx.x >> 5) * Q::kWords : 0));
     // replica sections: warps walk whole 32-pair chunks, whose first replica is tabulated
     const int bstart = L.sec ? (b0 & ~31) : b0;
     const int stride = nwarps * 32;
-    // storage index and particles of this lane's pair in the chunk at `base`
-    auto fetch = [&](int base, int& t, int& i, int& j, bool& valid) {
-        const int v = base + lane;
-        valid = v < np && v >= b0;
-        t = v;
-        i = -1;
-        j = 0;
-        if (valid) {
-            if (L.sec) {
-                int r = L.chunk_rep[base >> 5];
-                while (r + 1 < L.nrep && L.row_off[L.rep_off[r + 1]] <= v) ++r;
-                t = (int)(L.sec[r] + (long long)(v - L.row_off[L.rep_off[r]]));
-            }
-            i = L.pair_i[t];
-            j = L.pair_j[t];
-        }
-    };
     int tn, in_, jn;
     bool vn;
-    fetch(bstart + gwarp * 32, tn, in_, jn, vn);
+    pair_fetch(L, bstart + gwarp * 32, lane, np, b0, tn, in_, jn, vn);
     for (int base = bstart + gwarp * 32; base < np; base += stride) {
         const int t = tn, i = in_, j = jn;
         const bool valid = vn;
-        if (base + stride < np) fetch(base + stride, tn, in_, jn, vn);   // next chunk's indices in flight
-        if constexpr (!FILTER) {
-            pair_process<Pot, Pot::kCountActive ? 1 : 0>(L, pot, t, i, j, valid, pe, vir, sh_stats);
-        } else {
-            float3 rr = make_float3(0.f, 0.f, 0.f);
-            bool keep;
-            if constexpr (kQR)
-                keep = valid && pot.in_range_r(i, j, rr);
-            else
-                keep = valid && pot.in_range(i, j);
-            const unsigned vm = __ballot_sync(0xffffffffu, valid), km = __ballot_sync(0xffffffffu, keep);
-            if (Pot::kCountActive && lane == 0) {
-                atomicAdd(&sh_stats[0], (unsigned long long)__popc(vm));
-                if (kExact && km) atomicAdd(&sh_stats[1], (unsigned long long)__popc(km));
-            }
-            if (keep) {
-                const int slot = qn + __popc(km & ((1u << lane) - 1u));
-                qt[slot] = t;
-                qi[slot] = i;
-                qj[slot] = j;
-                if constexpr (kQR) {
-                    qr[slot] = rr.x;
-                    qr[64 + slot] = rr.y;
-                    qr[128 + slot] = rr.z;
-                }
-            }
-            qn += __popc(km);
-            __syncwarp();
-            if (qn >= 32) {
-                const int tq = qt[lane], iq = qi[lane], jq = qj[lane];
-                float3 rq = make_float3(0.f, 0.f, 0.f);
-                if constexpr (kQR) rq = make_float3(qr[lane], qr[64 + lane], qr[128 + lane]);
-                __syncwarp();
-                if (lane < qn - 32) {
-                    qt[lane] = qt[32 + lane];
-                    qi[lane] = qi[32 + lane];
-                    qj[lane] = qj[32 + lane];
-                    if constexpr (kQR) {
-                        qr[lane] = qr[32 + lane];
-                        qr[64 + lane] = qr[96 + lane];
-                        qr[128 + lane] = qr[160 + lane];
-                    }
-                }
-                __syncwarp();
-                qn -= 32;
-                pair_process<Pot, (Pot::kCountActive && !kExact) ? 2 : 0, kQR>(L, pot, tq, iq, jq, true, pe, vir,
-                                                                                 sh_stats, rq);
-            }
-        }
+        if (base + stride < np) pair_fetch(L, base + stride, lane, np, b0, tn, in_, jn, vn);   // next indices in flight
+        if constexpr (!FILTER)
+            pair_process<Pot, Pot::kCountActive ? 1 : 0>(L, pot, t, i, j, valid, es, sh_stats);
+        else
+            q.feed(L, pot, t, i, j, valid, es, sh_stats);
     }
-    if (FILTER && qn > 0) {   // qn is warp-uniform
-        const bool ok = lane < qn;
-        float3 rq = make_float3(0.f, 0.f, 0.f);
-        if constexpr (kQR)
-            if (ok) rq = make_float3(qr[lane], qr[64 + lane], qr[128 + lane]);
-        pair_process<Pot, (Pot::kCountActive && !kExact) ? 2 : 0, kQR>(
-            L, pot, ok ? qt[lane] : 0, ok ? qi[lane] : 0, ok ? qj[lane] : 0, ok, pe, vir, sh_stats, rq);
-    }
+    if constexpr (FILTER) q.flush(L, pot, es, sh_stats);
     if (kSh) {
         __syncthreads();
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x)
             if (sh_stats[k]) atomicAdd(&L.stats[k], sh_stats[k]);
     }
-    const float e[2] = {pe, vir};
-    block_reduce_finish_f<2>(e, L.partials, L.done, L.acc, L.acc_total);
+    const float e[2] = {es.pe, es.vir}, elo[2] = {es.pe_lo, es.vir_lo};
+    block_reduce_finish_f<2>(e, L.partials, L.done, L.acc, L.acc_total, elo);
 }
 
 // Launch shape of the pair kernels: block size and the range filter. The
@@ -281,10 +351,9 @@ int launch_pair_v(sg_ctx* ctx, PairLaunch L, Pot pot, int block) {
     return SG_OK;
 }
 
-// Launch helper: persistent grid sized from occupancy.
-template <class Pot>
-int launch_pair(sg_ctx* ctx, Pot pot, int kind) {
-    if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "pair forces need sg_nlist_init first");
+// The list walk of this context's pair kernels: the whole list, or in a
+// replica context the rows of the launch family's replicas.
+inline PairLaunch make_pair_launch(sg_ctx* ctx) {
     PairLaunch L;
     L.pair_i = ctx->nl.pair_i;
     L.pair_j = ctx->nl.pair_j;
@@ -309,6 +378,15 @@ int launch_pair(sg_ctx* ctx, Pot pot, int kind) {
     L.acc = ctx->acc + 4;
     L.acc_total = ctx->acc;
     L.stats = ctx->stats;
+    L.partials = nullptr;
+    return L;
+}
+
+// Launch helper: persistent grid sized from occupancy.
+template <class Pot>
+int launch_pair(sg_ctx* ctx, Pot pot, int kind) {
+    if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "pair forces need sg_nlist_init first");
+    PairLaunch L = make_pair_launch(ctx);
     const PairTune tune = sg_pair_tune_for(ctx, kind, Pot::kFilterable);
     if (Pot::kFilterable && tune.filter) return launch_pair_v<Pot, Pot::kFilterable>(ctx, L, pot, tune.block);
     return launch_pair_v<Pot, false>(ctx, L, pot, tune.block);
@@ -396,6 +474,24 @@ SG_DEV float min_image_precise(float a, float c, float L, float iL, float Llo, i
     if (!periodic) return d + e;
     const float n = roundf(d * iL);
     return __fsub_rn(d, n * L) + (e - n * Llo);
+}
+
+// r_ij = a - c by the minimum image of the box of i, to ~1e-12 absolute
+// (min_image_precise), from positions already loaded.
+SG_DEV float3 pair_rij_of_precise(float3 a, float3 c, int i, const BoxF& b) {
+    float3 L = b.box, iL = b.inv_box, lo = b.box_lo;
+    int per = b.periodic;
+    if (b.rep_of) {
+        const int r = b.rep_of[i];
+        const float4 bx = b.rbox[r], ib = b.rinv[r], bl = b.rbox_lo[r];
+        L = make_float3(bx.x, bx.y, bx.z);
+        iL = make_float3(ib.x, ib.y, ib.z);
+        lo = make_float3(bl.x, bl.y, bl.z);
+        per = 1;
+    }
+    return make_float3(min_image_precise(a.x, c.x, L.x, iL.x, lo.x, per),
+                       min_image_precise(a.y, c.y, L.y, iL.y, lo.y, per),
+                       min_image_precise(a.z, c.z, L.z, iL.z, lo.z, per));
 }
 
 // pair_rij for the contact-distance potentials (ECP): see min_image_precise.

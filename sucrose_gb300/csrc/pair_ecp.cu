@@ -19,6 +19,12 @@
 //   NEWTON        Newton on S'(l) = (1-2l) r.K - l(1-l) K.D.K (D = B_R - A_R)
 //                 in FP32 with bracketing, from l = 1/2, then an FP64 check
 //                 of |S'| (one step of FP64 iterative refinement of K).
+//   NEWTON_SUPPORT the same Newton from l = h_A / (h_A + h_B), where
+//                 h_A = sqrt(r.A_R r) and h_B = sqrt(r.B_R r) are |r| times
+//                 the support functions of the two ellipsoids along r: the
+//                 maximiser of S for two spheres, and on random orientations
+//                 2.9 instead of 3.5 evaluations per pair, 4 instead of 6 for
+//                 the slowest pair of 32.
 //   MLP_NEWTON    the same Newton from the learned guess, at most three
 //                 steps, else the plain Newton (counted as a fallback).
 #include <cmath>
@@ -34,10 +40,20 @@
 #endif
 #include "pair_common.cuh"
 #include "ecp_mlp.cuh"
+#include "step_epi.cuh"
 
-// Internal solver id: Newton from a guess already stored in the per-pair
-// lambda array (the tensor-core guess pass of mlp_tc.cu).
-#define SOLVER_MLP_PRE 3
+// Internal solver ids. SOLVER_MLP_PRE: Newton from a guess already stored in
+// the per-pair lambda array (the tensor-core guess pass of mlp_tc.cu).
+// SOLVER_GIVEN: the force kernel of the split Newton path, which starts from
+// the lambda that k_ecp_solve stored (negative: that solve hit its cap).
+#define SOLVER_MLP_PRE 10
+#define SOLVER_GIVEN 11
+
+// Minimum resident blocks of 256 threads the force kernel of the split path
+// (SOLVER_GIVEN) is compiled for.
+#ifndef SG_ECP_FORCE_MIN_BLOCKS
+#define SG_ECP_FORCE_MIN_BLOCKS 3
+#endif
 
 namespace {
 
@@ -47,66 +63,7 @@ __global__ void k_ecp_prep(int n, const float4* __restrict__ quat, const float4*
                            double* __restrict__ prep64) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const float4 q = quat[p];
-    const float w = q.x, x = q.y, y = q.z, z = q.w;
-    // rows of the reference's U (rotation_matrix form, :1244-1252): body axes in the lab frame
-    float u[3][3];
-    u[0][0] = w * w + x * x - y * y - z * z; u[0][1] = 2.f * (x * y + w * z); u[0][2] = 2.f * (x * z - w * y);
-    u[1][0] = 2.f * (x * y - w * z); u[1][1] = w * w - x * x + y * y - z * z; u[1][2] = 2.f * (y * z + w * x);
-    u[2][0] = 2.f * (x * z + w * y); u[2][1] = 2.f * (y * z - w * x); u[2][2] = w * w - x * x - y * y + z * z;
-    const float4 s4 = shape[p], e4 = eshape[p];
-    const float sg[3] = {s4.x, s4.y, s4.z};
-    const float ep[3] = {e4.x, e4.y, e4.z};
-    const float e0 = fmaxf(fmaxf(ep[0], ep[1]), ep[2]);
-    float s2[3], E[3];
-    for (int k = 0; k < 3; ++k) {
-        float h = 0.5f * sg[k];
-        s2[k] = h * h;
-        E[k] = powf(e0 / ep[k], muinv) * 0.25f;
-    }
-    float A[6], B[6];
-    const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
-    for (int m = 0; m < 6; ++m) {
-        float a = 0.f, b = 0.f;
-        for (int k = 0; k < 3; ++k) {
-            float uu = u[k][ia[m]] * u[k][ib[m]];
-            a += s2[k] * uu;
-            b += E[k] * uu;
-        }
-        A[m] = a;
-        B[m] = b;
-    }
-    const float st = (sg[0] * sg[1] + sg[2] * sg[2]) * sqrtf(2.f * sg[0] * sg[1]) * 0.125f;
-    prep[4 * p + 0] = make_float4(A[0], A[1], A[2], A[3]);
-    prep[4 * p + 1] = make_float4(A[4], A[5], B[0], B[1]);
-    prep[4 * p + 2] = make_float4(B[2], B[3], B[4], B[5]);
-    prep[4 * p + 3] = make_float4(u[2][0], u[2][1], u[2][2], st);
-    if (prep64) {
-        // A_R in FP64 with the reference's operation order (xmath.f90:194-208, :262-279)
-        const double W = w, X = x, Y = y, Z = z;
-        double r[3][3];
-        r[0][0] = __dsub_rn(__dsub_rn(__dadd_rn(__dmul_rn(W, W), __dmul_rn(X, X)), __dmul_rn(Y, Y)), __dmul_rn(Z, Z));
-        r[0][1] = __dmul_rn(2.0, __dadd_rn(__dmul_rn(X, Y), __dmul_rn(W, Z)));
-        r[0][2] = __dmul_rn(2.0, __dsub_rn(__dmul_rn(X, Z), __dmul_rn(W, Y)));
-        r[1][0] = __dmul_rn(2.0, __dsub_rn(__dmul_rn(X, Y), __dmul_rn(W, Z)));
-        r[1][1] = __dsub_rn(__dadd_rn(__dsub_rn(__dmul_rn(W, W), __dmul_rn(X, X)), __dmul_rn(Y, Y)), __dmul_rn(Z, Z));
-        r[1][2] = __dmul_rn(2.0, __dadd_rn(__dmul_rn(Y, Z), __dmul_rn(W, X)));
-        r[2][0] = __dmul_rn(2.0, __dadd_rn(__dmul_rn(X, Z), __dmul_rn(W, Y)));
-        r[2][1] = __dmul_rn(2.0, __dsub_rn(__dmul_rn(Y, Z), __dmul_rn(W, X)));
-        r[2][2] = __dadd_rn(__dsub_rn(__dsub_rn(__dmul_rn(W, W), __dmul_rn(X, X)), __dmul_rn(Y, Y)), __dmul_rn(Z, Z));
-        double b[3];
-        for (int k = 0; k < 3; ++k) {
-            double h = __ddiv_rn((double)sg[k], 2.0);
-            b[k] = __dmul_rn(h, h);
-        }
-        for (int m = 0; m < 6; ++m) {
-            const int c1 = ia[m], c2 = ib[m];
-            double t0 = __dmul_rn(__dmul_rn(r[0][c1], b[0]), r[0][c2]);
-            double t1 = __dmul_rn(__dmul_rn(r[1][c1], b[1]), r[1][c2]);
-            double t2 = __dmul_rn(__dmul_rn(r[2][c1], b[2]), r[2][c2]);
-            prep64[6 * (size_t)p + m] = __dadd_rn(__dadd_rn(t0, t1), t2);
-        }
-    }
+    ecp_prep_one(p, quat[p], shape[p], eshape[p], muinv, prep, prep64);
 }
 
 // ------------------------------------------------------------- 3x3 SPD ----
@@ -238,6 +195,12 @@ __device__ double ref_brent(const DPair& pair, int& nevals) {
 }
 
 // -------------------------------------------------------- Newton (FP32) ----
+// Start of the support-function Newton: h_A / (h_A + h_B) with h_X = sqrt(r.X r).
+SG_DEV float support_guess(const float* A, const float* B, float3 r) {
+    const float ha = sqrtf(dot3(r, symv(A, r))), hb = sqrtf(dot3(r, symv(B, r)));
+    return ha / (ha + hb);
+}
+
 // Bracketed Newton on S'(l) in FP32. Quadratic convergence makes the step
 // after one of size < step_tol land at the FP32 noise floor, so that step is
 // taken, K is recomputed at the new lambda, and the loop ends.
@@ -296,7 +259,7 @@ SG_DEV NewtonResult newton_solve(const float* A, const float* D, float3 r, float
 // refined K. With K accurate to ~1e-13 the FP32 dot products contribute
 // ~1e-7 of r.K to S' (ten times under the 1e-6 bound); without the refinement
 // the FP32 solve alone leaves an error of the order of the bound.
-//   mode 1: e in FP64 (6 + 12 DFMA, no division);
+//   mode 1: e in FP64 (nine FP64 FMAs; operands widened on the integer pipe);
 //   mode 2: e in double-float arithmetic on the FP32 pipe (error-free
 //           products and sums, ~48-bit significand), no FP64 instruction.
 // Returns s1 = S' and rK = r.K (the check is |s1| <= tol rK) and S'' (FP32).
@@ -306,16 +269,60 @@ SG_DEV void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
+// Exact FP32 -> FP64 widening on the integer pipe: the exponent is rebiased
+// and the significand shifted into place, the same bits the conversion
+// instruction gives for every normal number, infinity and NaN (zero and
+// subnormals give a signed zero). On GB300 the conversion instructions share
+// the FP64 pipe, which runs at 1/64 of the FP32 rate.
+SG_DEV double widen(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned e = u & 0x7f800000u, sgn = u & 0x80000000u, m = (u >> 3) & 0x000fffffu;
+    unsigned hi = sgn | ((e >> 3) + (896u << 20)) | m, lo = u << 29;
+    if (e == 0u) { hi = sgn; lo = 0u; }
+    if (e == 0x7f800000u) hi = sgn | 0x7ff00000u | m;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// FP64 -> FP32 on the integer pipe, truncating the significand (relative
+// error below 2^-23); magnitudes under the FP32 normal range give a signed
+// zero, over it a NaN. For residuals that enter only as small corrections.
+SG_DEV float narrow_trunc(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned sgn = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+    unsigned u = sgn | ((unsigned)e << 23) | ((hi & 0x000fffffu) << 3) | (lo >> 29);
+    if (e <= 0) u = sgn;
+    if (e >= 255) u = sgn | 0x7fc00000u;
+    return __uint_as_float(u);
+}
+
+// e = r - G K in FP64 arithmetic. G = A + lam D is formed exactly as gh + gl
+// on the FP32 pipe (gh = fl(A + lam D); gl its rounding error, to 2^-48 |G|);
+// r, gh and K are widened exactly, so every product gh_ij K_j is exact in FP64
+// and the row sums r_i - sum_j gh_ij K_j carry one FP64 rounding per term:
+// nine FP64 FMAs per pair. The small part gl K (~2^-24 |r|) is added in FP32.
 SG_DEV float3 lin_residual_fp64(const float* A, const float* D, float3 r, float lam, float3 K) {
-    const double L = lam;
-    double g[6];
+    double G[6];
+    float gl[6];
 #pragma unroll
-    for (int m = 0; m < 6; ++m) g[m] = fma(L, (double)D[m], (double)A[m]);
-    const double kx = K.x, ky = K.y, kz = K.z;
-    const double ex = (double)r.x - fma(g[0], kx, fma(g[1], ky, g[2] * kz));
-    const double ey = (double)r.y - fma(g[1], kx, fma(g[3], ky, g[4] * kz));
-    const double ez = (double)r.z - fma(g[2], kx, fma(g[4], ky, g[5] * kz));
-    return make_float3((float)ex, (float)ey, (float)ez);
+    for (int m = 0; m < 6; ++m) {
+        const float p = lam * D[m];
+        const float pe = fmaf(lam, D[m], -p);
+        float sh, se;
+        two_sum(A[m], p, sh, se);
+        G[m] = widen(sh);
+        gl[m] = se + pe;
+    }
+    const double kx = widen(K.x), ky = widen(K.y), kz = widen(K.z);
+    double ex = fma(-G[0], kx, widen(r.x));
+    double ey = fma(-G[1], kx, widen(r.y));
+    double ez = fma(-G[2], kx, widen(r.z));
+    ex = fma(-G[1], ky, ex); ey = fma(-G[3], ky, ey); ez = fma(-G[4], ky, ez);
+    ex = fma(-G[2], kz, ex); ey = fma(-G[4], kz, ey); ez = fma(-G[5], kz, ez);
+    const float cx = gl[0] * K.x + gl[1] * K.y + gl[2] * K.z;
+    const float cy = gl[1] * K.x + gl[3] * K.y + gl[4] * K.z;
+    const float cz = gl[2] * K.x + gl[4] * K.y + gl[5] * K.z;
+    return make_float3(narrow_trunc(ex) - cx, narrow_trunc(ey) - cy, narrow_trunc(ez) - cz);
 }
 
 SG_DEV float3 lin_residual_df(const float* A, const float* D, float3 r, float lam, float3 K) {
@@ -382,7 +389,10 @@ struct PotECP {
     static constexpr bool kCountActive = false;
     static constexpr bool kFilterable = false;
     static constexpr int kMinBlocks =
-        (SOLVER == SG_SOLVER_NEWTON || SOLVER == SOLVER_MLP_PRE) ? SG_ECP_MIN_BLOCKS : 1;
+        (SOLVER == SG_SOLVER_NEWTON || SOLVER == SG_SOLVER_NEWTON_SUPPORT || SOLVER == SOLVER_MLP_PRE)
+            ? SG_ECP_MIN_BLOCKS
+        : SOLVER == SOLVER_GIVEN                                ? SG_ECP_FORCE_MIN_BLOCKS
+                                                                : 1;
     static constexpr int kMinBlocksFiltered = 1;   // not filterable
     int prefiltered;
     SG_DEV bool in_range(int, int) const { return true; }
@@ -445,18 +455,33 @@ SG_DEV float PotECP<SOLVER>::solve_lambda(int i, int j, float3 r, const float* A
         }
         return lam;
     }
-    constexpr bool kGuess = (SOLVER == SG_SOLVER_MLP_NEWTON || SOLVER == SOLVER_MLP_PRE);
-    const int budget = kGuess ? 3 : max_iter;
-    NewtonResult nr = newton_solve(A, D, r, lam0, budget, step_tol);
-    evals = nr.iters;
-    if (kGuess && !nr.converged) {
-        fallback = true;
-        nr = newton_solve(A, D, r, 0.5f, max_iter, step_tol);
-        evals += nr.iters;
+    NewtonResult nr;
+    if constexpr (SOLVER == SOLVER_GIVEN) {
+        // lambda from k_ecp_solve (negative: its solve hit the iteration cap);
+        // the factor and K at that lambda are those of its last evaluation
+        lam = fabsf(lam0);
+        nonconv = lam0 < 0.f;
+        float g[6];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) g[m] = fmaf(lam, D[m], A[m]);
+        nr.c = chol(g);
+        nr.K = chol_solve(nr.c, r);
+        nr.lam = lam;
+    } else {
+        constexpr bool kGuess = (SOLVER == SG_SOLVER_MLP_NEWTON || SOLVER == SOLVER_MLP_PRE);
+        const int budget = kGuess ? 3 : max_iter;
+        if (SOLVER == SG_SOLVER_NEWTON_SUPPORT) lam0 = support_guess(A, Bm, r);
+        nr = newton_solve(A, D, r, lam0, budget, step_tol);
+        evals = nr.iters;
+        if (kGuess && !nr.converged) {
+            fallback = true;
+            nr = newton_solve(A, D, r, 0.5f, max_iter, step_tol);
+            evals += nr.iters;
+        }
+        iters = nr.iters;
+        lam = nr.lam;
+        nonconv = !nr.converged;
     }
-    iters = nr.iters;
-    lam = nr.lam;
-    nonconv = !nr.converged;
     KRlo = make_float3(0.f, 0.f, 0.f);
     if (fp64_check) {
         float s2, rK;
@@ -491,8 +516,9 @@ template <int SOLVER>
 SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, unsigned long long* sh) const {
     const float3 r = pair_rij_precise(pos, i, j, b);   // invalid lanes evaluate (0,0): never used
     float lam0 = 0.5f;
-    if (SOLVER == SOLVER_MLP_PRE) {
-        // the guess of the tensor-core pass, stored where this pair's lambda goes
+    if (SOLVER == SOLVER_MLP_PRE || SOLVER == SOLVER_GIVEN) {
+        // the guess of the tensor-core pass, or the solved lambda, stored where
+        // this pair's lambda goes
         lam0 = valid ? lam_out[t] : 0.5f;
     }
     if (SOLVER == SG_SOLVER_MLP_NEWTON) {
@@ -518,7 +544,7 @@ SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, un
     float lam = 0.5f;
     if (valid) {
         lam = solve_lambda(i, j, r, A, Bm, lam0, cR, KR, KRlo, evals, iters, nonconv, fallback, refined);
-        if (lam_out) lam_out[t] = lam;
+        if (lam_out && (SOLVER != SOLVER_GIVEN || refined || nonconv)) lam_out[t] = lam;
     }
     {
         // warp-aggregated solver statistics into the block's shared counters
@@ -529,12 +555,14 @@ SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, un
         const unsigned nc = __popc(__ballot_sync(full, valid && nonconv));
         const unsigned fb = __popc(__ballot_sync(full, valid && fallback));
         const unsigned rf = __popc(__ballot_sync(full, valid && refined));
-        const unsigned key = valid ? min(iters, 23u) : 255u;
-        const unsigned peers = __match_any_sync(full, key);
-        if (key != 255u && lane == __ffs(peers) - 1) atomicAdd(&sh[4 + key], (unsigned long long)__popc(peers));
+        if (SOLVER != SOLVER_GIVEN) {   // the split path's solve kernel keeps the histogram
+            const unsigned key = valid ? min(iters, 23u) : 255u;
+            const unsigned peers = __match_any_sync(full, key);
+            if (key != 255u && lane == __ffs(peers) - 1) atomicAdd(&sh[4 + key], (unsigned long long)__popc(peers));
+        }
         if (lane == 0) {
             atomicAdd(&sh[0], (unsigned long long)np);
-            atomicAdd(&sh[1], (unsigned long long)ev);
+            if (ev) atomicAdd(&sh[1], (unsigned long long)ev);
             if (nc) atomicAdd(&sh[2], (unsigned long long)nc);
             if (fb) atomicAdd(&sh[3], (unsigned long long)fb);
             if (rf) atomicAdd(&sh[28], (unsigned long long)rf);
@@ -660,6 +688,97 @@ SG_DEV void PotECP<SOLVER>::eval(bool valid, int i, int j, int t, PairOut& o, un
     o.vir = dot3(r, F);
 }
 
+// ------------------------------------------------- split Newton: solve ----
+// The Newton solve of the split path: lambda for every listed pair and the
+// solver statistics, nothing else. Its registers are those of the Newton loop
+// alone, so it keeps many more warps resident than a kernel that also holds
+// the force terms; the force kernel (PotECP<SOLVER_GIVEN>) then starts from
+// the stored lambda with the same work for every pair, the residual check
+// included. lambda is stored negated when the solve hit its iteration cap.
+struct EcpSolveArgs {
+    const float4* __restrict__ pos;
+    const float4* __restrict__ prep;
+    float* __restrict__ lam;   // in: the learned guess (SOLVER_MLP_PRE); out: lambda
+    BoxF b;
+    int max_iter;
+    float step_tol;
+};
+
+template <int SOLVER>
+__global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK) k_ecp_solve(PairLaunch L, EcpSolveArgs a) {
+    constexpr bool kGuess = SOLVER == SOLVER_MLP_PRE;
+    __shared__ unsigned long long sh[SG_NSTATS];
+    for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x) sh[k] = 0ull;
+    __syncthreads();
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int np = *L.npairs;
+    const int b0 = L.begin ? *L.begin : 0;
+    const int bstart = L.sec ? (b0 & ~31) : b0;
+    for (int base = bstart + gwarp * 32; base < np; base += nwarps * 32) {
+        int t, i, j;
+        bool valid;
+        pair_fetch(L, base, lane, np, b0, t, i, j, valid);
+        unsigned evals = 0, iters = 0;
+        bool fallback = false;
+        if (valid) {
+            const float3 r = pair_rij_precise(a.pos, i, j, a.b);
+            const float4 pi0 = a.prep[4 * i], pi1 = a.prep[4 * i + 1];
+            const float4 pj0 = a.prep[4 * j], pj1 = a.prep[4 * j + 1];
+            const float A[6] = {pi0.x, pi0.y, pi0.z, pi0.w, pi1.x, pi1.y};
+            const float D[6] = {pj0.x - A[0], pj0.y - A[1], pj0.z - A[2], pj0.w - A[3], pj1.x - A[4], pj1.y - A[5]};
+            const float B[6] = {pj0.x, pj0.y, pj0.z, pj0.w, pj1.x, pj1.y};
+            const float lam0 = kGuess                                 ? a.lam[t]
+                               : SOLVER == SG_SOLVER_NEWTON_SUPPORT ? support_guess(A, B, r)
+                                                                      : 0.5f;
+            NewtonResult nr = newton_solve(A, D, r, lam0, kGuess ? 3 : a.max_iter, a.step_tol);
+            evals = nr.iters;
+            if (kGuess && !nr.converged) {
+                fallback = true;
+                nr = newton_solve(A, D, r, 0.5f, a.max_iter, a.step_tol);
+                evals += nr.iters;
+            }
+            iters = nr.iters;
+            a.lam[t] = nr.converged ? nr.lam : -nr.lam;
+        }
+        // warp-aggregated: evaluations, fallbacks, iteration histogram
+        const unsigned ev = __reduce_add_sync(full, evals);
+        const unsigned fb = __popc(__ballot_sync(full, fallback));
+        const unsigned key = valid ? min(iters, 23u) : 255u;
+        const unsigned peers = __match_any_sync(full, key);
+        if (key != 255u && lane == __ffs(peers) - 1) atomicAdd(&sh[4 + key], (unsigned long long)__popc(peers));
+        if (lane == 0) {
+            if (ev) atomicAdd(&sh[1], (unsigned long long)ev);
+            if (fb) atomicAdd(&sh[3], (unsigned long long)fb);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x)
+        if (sh[k]) atomicAdd(&L.stats[k], sh[k]);
+}
+
+template <int SOLVER>
+int launch_ecp_solve(sg_ctx* ctx, const sg_pair_params* p) {
+    if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "pair forces need sg_nlist_init first");
+    PairLaunch L = make_pair_launch(ctx);
+    EcpSolveArgs a;
+    a.pos = ctx->pos;
+    a.prep = ctx->ecp_prep;
+    a.lam = ctx->ecp_lambda;
+    a.b = make_boxf(ctx);
+    a.max_iter = p->newton_max_iter > 0 ? p->newton_max_iter : 20;
+    a.step_tol = 1e-4f;
+    const int block = SG_PAIR_MAX_BLOCK;
+    int grid = sg_grid_for(ctx, (const void*)k_ecp_solve<SOLVER>, block, 0);
+    const int64_t max_useful = (ctx->nl.pair_capacity + block - 1) / block;
+    if (grid > max_useful) grid = (int)std::max<int64_t>(1, max_useful);
+    k_ecp_solve<SOLVER><<<grid, block, 0, ctx->stream>>>(L, a);
+    SG_LAUNCH_CHECK(ctx, "k_ecp_solve");
+    return SG_OK;
+}
+
 template <int SOLVER>
 int launch_ecp(sg_ctx* ctx, const sg_pair_params* p, int mu, int nu) {
     PotECP<SOLVER> pot;
@@ -709,7 +828,8 @@ int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p) {
     const int brent = p->solver == SG_SOLVER_BRENT_COMPAT;
     if (p->solver == SG_SOLVER_MLP_NEWTON && !ctx->mlp_ready)
         return sg_fail(ctx, SG_ENOTREADY, "MLP solver selected but no weights were set (sg_mlp_set_weights)");
-    if (int rc = sg_ecp_prepare(ctx, p, brent)) return rc;
+    if (!(ctx->step_prep_kind == SG_PREP_ECP && !brent))   // else written by the step's initial half step
+        if (int rc = sg_ecp_prepare(ctx, p, brent)) return rc;
     if (ctx->ecp_lambda_cap < ctx->nl.pair_capacity) {
         ctx->graph_epoch++;
         if (ctx->ecp_lambda) cudaFree(ctx->ecp_lambda);
@@ -717,14 +837,25 @@ int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p) {
         SG_CUDA(ctx, cudaMalloc(&ctx->ecp_lambda, sizeof(float) * (size_t)ctx->nl.pair_capacity));
         ctx->ecp_lambda_cap = ctx->nl.pair_capacity;
     }
+    const bool split = sg_pair_tune_for(ctx, p->kind, false).filter != 0;
     switch (p->solver) {
         case SG_SOLVER_BRENT_COMPAT: return launch_ecp<SG_SOLVER_BRENT_COMPAT>(ctx, p, mu, nu);
-        case SG_SOLVER_NEWTON: return launch_ecp<SG_SOLVER_NEWTON>(ctx, p, mu, nu);
+        case SG_SOLVER_NEWTON:
+            if (!split) return launch_ecp<SG_SOLVER_NEWTON>(ctx, p, mu, nu);
+            // split path: the Newton solve, then the forces from its lambda
+            if (int rc = launch_ecp_solve<SG_SOLVER_NEWTON>(ctx, p)) return rc;
+            return launch_ecp<SOLVER_GIVEN>(ctx, p, mu, nu);
+        case SG_SOLVER_NEWTON_SUPPORT:
+            if (!split) return launch_ecp<SG_SOLVER_NEWTON_SUPPORT>(ctx, p, mu, nu);
+            if (int rc = launch_ecp_solve<SG_SOLVER_NEWTON_SUPPORT>(ctx, p)) return rc;
+            return launch_ecp<SOLVER_GIVEN>(ctx, p, mu, nu);
         case SG_SOLVER_MLP_NEWTON:
             if (ctx->mlp_inline) return launch_ecp<SG_SOLVER_MLP_NEWTON>(ctx, p, mu, nu);
             // tensor-core guess pass, then Newton from it
             if (int rc = sg_mlp_guess_tc_launch(ctx, ctx->ecp_lambda)) return rc;
-            return launch_ecp<SOLVER_MLP_PRE>(ctx, p, mu, nu);
+            if (!split) return launch_ecp<SOLVER_MLP_PRE>(ctx, p, mu, nu);
+            if (int rc = launch_ecp_solve<SOLVER_MLP_PRE>(ctx, p)) return rc;
+            return launch_ecp<SOLVER_GIVEN>(ctx, p, mu, nu);
         default: return sg_fail(ctx, SG_EINVAL, "unknown ECP solver %d", p->solver);
     }
 }

@@ -76,7 +76,7 @@ struct sg_nlist_state {
 // Launch shape of a pair kernel (chosen by the autotuner).
 struct PairTune {
     int block = 256;   // threads per block (128 or 256)
-    int filter = 0;    // range filter + per-warp queue of in-range pairs
+    int filter = 0;    // range filter + per-warp queue of in-range pairs; ECP kinds: the split Newton path
 };
 
 struct sg_ctx {
@@ -124,6 +124,20 @@ struct sg_ctx {
     int mlp_ready = 0;
     int* mlp_tc_err = nullptr;       // device flag: a tensor-core completion wait ran out
     int mlp_inline = 0;              // 1: the ECP kernel evaluates the guess itself (mma.sync)
+    // Captured-step fusion, set while a step is being enqueued: the initial
+    // half step also runs the list's displacement test, zeroes forces,
+    // torques and the accumulators, and (step_prep_kind) writes the pair
+    // potential's per-particle prep; the final half step stores its sums and
+    // advances the step counter.
+    // Gay-Berne replica tiles (k_pair_gb_tile): the GB family's replicas,
+    // largest first, a work counter and a finished-blocks counter, and the
+    // largest replica's particle count.
+    int* gb_tile_order = nullptr;
+    int gb_tile_count = 0;
+    int gb_tile_maxn = 0;
+    int step_fused = 0;
+    int step_prep_kind = 0;          // SG_PREP_NONE / _ECP / _GB (step_epi.cuh)
+    float step_prep_muinv = 1.f;
     int mlp_tc_test_no_mma = 0;      // failure-path test: the next guess pass issues no MMA
     void* mlp_work = nullptr;        // training workspace (mlp_train.cu)
     int mlp_adam_t = 0;
@@ -245,9 +259,10 @@ SG_DEV float3 min_image(float3 d, float3 box, float3 inv_box, int periodic) {
 // called by every thread of the block. partials holds gridDim.x * K slots.
 // Block sums from one value per warp (held by lane 0), then the grid sum in
 // the block that arrives last. Returns true in that block (block-uniform).
+// store: acc[k] = total instead of acc[k] += total (no zeroing pass needed).
 template <int K>
 __device__ bool block_finish_from_warps(const double (&wv)[K], double* partials, unsigned int* done, double* acc,
-                                        double* acc_also) {
+                                        double* acc_also, bool store = false) {
     __shared__ double sh[32][K];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
@@ -290,7 +305,8 @@ __device__ bool block_finish_from_warps(const double (&wv)[K], double* partials,
         if (threadIdx.x < K) {
             double t = 0.0;
             for (int w = 0; w < nw; ++w) t += sh[w][threadIdx.x];
-            acc[threadIdx.x] += t;
+            if (store) acc[threadIdx.x] = t;
+            else acc[threadIdx.x] += t;
             if (acc_also) acc_also[threadIdx.x] += t;
         }
         if (threadIdx.x == 0) *done = 0u;
@@ -301,7 +317,7 @@ __device__ bool block_finish_from_warps(const double (&wv)[K], double* partials,
 // Per-thread FP64 values: warp sums by shuffles, then block_finish_from_warps.
 template <int K>
 __device__ bool block_reduce_finish(double (&v)[K], double* partials, unsigned int* done, double* acc,
-                                    double* acc_also = nullptr) {
+                                    double* acc_also = nullptr, bool store = false) {
     double wv[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -310,7 +326,7 @@ __device__ bool block_reduce_finish(double (&v)[K], double* partials, unsigned i
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         wv[k] = x;
     }
-    return block_finish_from_warps<K>(wv, partials, done, acc, acc_also);
+    return block_finish_from_warps<K>(wv, partials, done, acc, acc_also, store);
 }
 
 // The same for per-thread FP32 sums (pair energies and virials): the warp
@@ -318,13 +334,14 @@ __device__ bool block_reduce_finish(double (&v)[K], double* partials, unsigned i
 // on the FP32 pipe, and FP64 takes over from one value per warp, so the
 // result matches an FP64 sum of the FP32 terms to ~1e-14 relative while the
 // FP64 pipe sees 1/32 of the additions.
+// vlo (optional): low parts of per-thread double-float sums v + vlo.
 template <int K>
 __device__ bool block_reduce_finish_f(const float (&v)[K], double* partials, unsigned int* done, double* acc,
-                                      double* acc_also = nullptr) {
+                                      double* acc_also = nullptr, const float* vlo = nullptr) {
     double w[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        float hi = v[k], lo = 0.f;
+        float hi = v[k], lo = vlo ? vlo[k] : 0.f;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const float ho = __shfl_down_sync(0xffffffffu, hi, o);

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "sg_internal.cuh"
+#include "step_epi.cuh"
 
 namespace {
 
@@ -18,15 +19,17 @@ __global__ void k_set_rebuild_condition(cudaGraphConditionalHandle h, const int*
 // step; the build kernels sit in the body of a conditional graph node that
 // executes only when a rebuild was requested, so a step without a rebuild
 // launches none of them. Outside capture the flag-gated kernels are enqueued.
-int enqueue_list_update(sg_ctx* ctx, bool flat) {
+// checked: the displacement test already ran (in the fused initial half step).
+int enqueue_list_update(sg_ctx* ctx, bool flat, bool checked) {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
     cudaGraph_t cg = nullptr;
     const cudaGraphNode_t* deps = nullptr;
     const cudaGraphEdgeData* edges = nullptr;
     size_t nd = 0;
     SG_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &edges, &nd));
-    if (flat || st != cudaStreamCaptureStatusActive) return sg_nlist_update(ctx);
-    if (int rc = sg_nlist_enqueue_check(ctx)) return rc;
+    if (flat || st != cudaStreamCaptureStatusActive) return checked ? sg_nlist_enqueue_build(ctx) : sg_nlist_update(ctx);
+    if (!checked)
+        if (int rc = sg_nlist_enqueue_check(ctx)) return rc;
     cudaGraphConditionalHandle h;
     SG_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &edges, &nd));
     SG_CUDA(ctx, cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault));
@@ -56,6 +59,44 @@ int enqueue_list_update(sg_ctx* ctx, bool flat) {
     return SG_OK;
 }
 
+// Whether the step can run in its fused form (four kernels and the rebuild
+// node), and which per-particle prep its initial half step writes: the
+// Langevin and standard Nose-Hoover integrators without constraints; the
+// prep when the pair sets are all ECP kinds with a Newton solver, or all
+// Gay-Berne kinds, with one exponent mu.
+void plan_fusion(sg_ctx* ctx, const sg_step_config& c) {
+    ctx->step_fused = 0;
+    ctx->step_prep_kind = SG_PREP_NONE;
+    if ((c.flags & SG_STEP_CONSTRAINTS) || !(c.integrator == SG_INT_LANGEVIN || c.integrator == SG_INT_NH)) return;
+    ctx->step_fused = 1;
+    bool ecp = false, gb = false, other_ecp = false, same_mu = true;
+    int mu = -1;
+    for (int k = 0; k < ctx->step_npairs; ++k) {
+        const sg_pair_params& p = ctx->step_pairs[k];
+        int m;
+        if (p.kind >= SG_ECP) {
+            ecp = true;
+            if (p.solver == SG_SOLVER_BRENT_COMPAT) other_ecp = true;
+            m = (p.mu == 0 && p.nu == 0) ? 2 : p.mu;
+        } else if (p.kind >= SG_GB) {
+            gb = true;
+            m = (p.mu == 0 && p.nu == 0) ? 1 : p.mu;
+        } else {
+            continue;
+        }
+        if (mu >= 0 && m != mu) same_mu = false;
+        mu = m;
+    }
+    if (!same_mu || mu < 1 || (ecp && gb) || other_ecp) return;
+    if (ecp) ctx->step_prep_kind = SG_PREP_ECP;
+    if (gb) ctx->step_prep_kind = SG_PREP_GB;
+    ctx->step_prep_muinv = 1.f / (float)mu;
+}
+
+// An event-record node when the stream is being captured (a plain record
+// there would only mark a capture dependency), an ordinary record otherwise.
+void record_event(cudaEvent_t e, cudaStream_t s) { cudaEventRecordWithFlags(e, s, cudaEventRecordExternal); }
+
 // ev (optional): 6 events recorded before the initial half step, the list
 // update, the force zeroing, the pair stage, the final half step and the
 // step counter (eager steps only; sg_step_stage_times).
@@ -63,8 +104,10 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
     const double dt = c.dt;
     ctx->lgv_step_dev = ctx->step_dev;
     ctx->lgv_rotations = c.rotations;
+    plan_fusion(ctx, c);
+    const bool fused = ctx->step_fused != 0;
     int rc = SG_OK;
-    if (ev) cudaEventRecord(ev[0], ctx->stream);
+    if (ev) record_event(ev[0], ctx->stream);
     const bool con = (c.flags & SG_STEP_CONSTRAINTS) != 0;
     if (con) rc = sg_constraints_save(ctx);
     if (!rc) switch (c.integrator) {
@@ -81,18 +124,18 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
             break;
         default: rc = sg_fail(ctx, SG_EINVAL, "unknown integrator %d", c.integrator);
     }
-    if (ev) cudaEventRecord(ev[1], ctx->stream);
+    if (ev) record_event(ev[1], ctx->stream);
     if (!rc && con) rc = sg_constraints_a(ctx, dt);
-    if (ev) cudaEventRecord(ev[2], ctx->stream);
-    if (!rc) rc = enqueue_list_update(ctx, (c.flags & SG_STEP_FLAT) != 0);
-    if (ev) cudaEventRecord(ev[3], ctx->stream);
-    if (!rc) rc = sg_zero_forces(ctx);
-    if (ev) cudaEventRecord(ev[4], ctx->stream);
+    if (ev) record_event(ev[2], ctx->stream);
+    if (!rc) rc = enqueue_list_update(ctx, (c.flags & SG_STEP_FLAT) != 0, fused);
+    if (ev) record_event(ev[3], ctx->stream);
+    if (!rc && !fused) rc = sg_zero_forces(ctx);
+    if (ev) record_event(ev[4], ctx->stream);
     for (int k = 0; !rc && k < ctx->step_npairs; ++k) rc = sg_pair_forces_async(ctx, &ctx->step_pairs[k]);
     if (!rc && (c.flags & SG_STEP_REACTION_FIELD)) rc = sg_reaction_field_eval_async(ctx);
     for (int k = 0; !rc && (c.flags & SG_STEP_BONDED) && k < 6; ++k)
         if (ctx->bonded_n[k]) rc = sg_bonded_forces_async(ctx, k);
-    if (ev) cudaEventRecord(ev[5], ctx->stream);
+    if (ev) record_event(ev[5], ctx->stream);
     if (!rc) {
         switch (c.integrator) {
             case SG_INT_NVE: rc = sg_vv_final(ctx, dt, nullptr); if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr); break;
@@ -103,16 +146,18 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
                 if (!rc && c.rotations) rc = sg_qq_final(ctx, dt, nullptr);
         }
     }
-    if (ev) cudaEventRecord(ev[6], ctx->stream);
+    if (ev) record_event(ev[6], ctx->stream);
     if (!rc && con) rc = sg_constraints_b(ctx, dt);
-    if (ev) cudaEventRecord(ev[7], ctx->stream);
-    if (!rc) {
+    if (ev) record_event(ev[7], ctx->stream);
+    if (!rc && !fused) {   // the fused final half step advances the counter itself
         k_step_incr<<<1, 1, 0, ctx->stream>>>(ctx->step_dev);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) rc = sg_cuda_check(ctx, e, "k_step_incr");
     }
     ctx->lgv_step_dev = nullptr;
     ctx->lgv_rotations = 1;
+    ctx->step_fused = 0;
+    ctx->step_prep_kind = SG_PREP_NONE;
     return rc;
 }
 
@@ -197,20 +242,38 @@ int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[7]) {
     if (!ctx || !out_ms || nsteps < 1) return SG_EINVAL;
     if (!ctx->step_ready) return sg_fail(ctx, SG_ENOTREADY, "sg_step_configure must precede sg_step_stage_times");
     const sg_step_config& c = *reinterpret_cast<const sg_step_config*>(ctx->step_cfg);
-    std::vector<cudaEvent_t> ev(8 * (size_t)nsteps);
+    // one step captured with an event-record node between the stages, so the
+    // stages are timed as the captured step runs them (no host launch gaps)
+    cudaEvent_t ev[8];
     for (auto& e : ev) SG_CUDA(ctx, cudaEventCreate(&e));
-    int rc = SG_OK;
-    for (int s = 0; s < nsteps && !rc; ++s) rc = enqueue_step(ctx, c, ev.data() + 8 * s);
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    for (int k = 0; k < 7; ++k) out_ms[k] = 0.0;
+    int rc = enqueue_step(ctx, c);   // eager step: every buffer allocated before the capture
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!rc) e = cudaStreamSynchronize(ctx->stream);
     if (!rc && e == cudaSuccess) {
-        for (int s = 0; s < nsteps; ++s)
-            for (int k = 0; k < 7; ++k) {
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, ev[8 * s + k], ev[8 * s + k + 1]);
-                out_ms[k] += ms / nsteps;
-            }
+        const unsigned epoch = ctx->graph_epoch;
+        e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            rc = enqueue_step(ctx, c, ev);
+            e = cudaStreamEndCapture(ctx->stream, &graph);
+        }
+        if (!rc && e == cudaSuccess && epoch != ctx->graph_epoch)
+            rc = sg_fail(ctx, SG_ECUDA, "a buffer was reallocated while capturing the step");
+        if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
     }
+    for (int k = 0; k < 7; ++k) out_ms[k] = 0.0;
+    for (int s = 0; s < nsteps && !rc && e == cudaSuccess; ++s) {
+        e = cudaGraphLaunch(exec, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        for (int k = 0; k < 7 && e == cudaSuccess; ++k) {
+            float ms = 0.f;
+            e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            out_ms[k] += ms / nsteps;
+        }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
     for (auto& x : ev) cudaEventDestroy(x);
     if (rc) return rc;
     if (e != cudaSuccess) return sg_cuda_check(ctx, e, "sg_step_stage_times");

@@ -2,7 +2,11 @@
 // reference). The variants are the block size (128 or 256 threads) and, for
 // potentials with a cheap range test (LJ family, Gay-Berne family), whether
 // the kernel filters the list first and evaluates only the in-range pairs,
-// 32 per warp. The best variant depends on the potential, the share of
+// 32 per warp; for the ECP kinds with a Newton solver the second axis is the
+// split path (a solve kernel, then a force kernel from the stored lambda)
+// against the one kernel that solves and evaluates each pair. Gay-Berne
+// replicas add the replica tiles (records staged in shared memory per
+// replica), which take the place of the unfiltered 256-thread variant. The best variant depends on the potential, the share of
 // listed pairs that are in range and the system size, so it is measured on
 // the live list and cached per (kind, particle-count bucket, density bucket).
 #include <cmath>
@@ -27,8 +31,11 @@ PairTune sg_pair_tune_for(sg_ctx* ctx, int kind, bool filterable) {
     PairTune t;
     t.block = 256;
     // default before tuning: filter the Gay-Berne kinds, whose range test is
-    // a small part of the pair's work and often fails
+    // a small part of the pair's work and often fails; the ECP kinds solve and
+    // evaluate each pair in one kernel (measured faster on the benchmark list)
     t.filter = filterable && kind >= SG_GB && kind < SG_ECP;
+    // Gay-Berne replicas: the replica tiles (k_pair_gb_tile)
+    if (t.filter && ctx->nrep) t.filter = 2;
     return t;
 }
 
@@ -39,7 +46,7 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
     if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "sg_nlist_init must precede sg_pair_autotune");
     if (reps < 1) reps = 5;
     const int n = ctx->n;
-    const bool filterable = p->kind < SG_ECP;
+    const bool filterable = p->kind < SG_ECP || p->solver != SG_SOLVER_BRENT_COMPAT;
     // keep the caller's forces, torques and accumulators
     float4* save = nullptr;
     double acc[8];
@@ -61,7 +68,8 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const long long key = tune_key(ctx, p->kind);
-    const PairTune cand[4] = {{256, 0}, {128, 0}, {256, 1}, {128, 1}};
+    const bool tiles = ctx->nrep && p->kind >= SG_GB && p->kind < SG_ECP;
+    const PairTune cand[4] = {{256, tiles ? 2 : 0}, {128, tiles ? 0 : 0}, {256, 1}, {128, 1}};
     const int ncand = filterable ? 4 : 2;
     float best = 1e30f;
     PairTune pick = cand[0];
@@ -109,10 +117,10 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
 }
 
 int sg_pair_set_launch(sg_ctx* ctx, int32_t kind, int32_t block, int32_t filter) {
-    if (!ctx || (block != 128 && block != 256)) return SG_EINVAL;
+    if (!ctx || (block != 128 && block != 256) || filter < 0 || filter > 2) return SG_EINVAL;
     PairTune t;
     t.block = block;
-    t.filter = (filter && kind < SG_ECP) ? 1 : 0;
+    t.filter = filter;
     ctx->tune[tune_key(ctx, kind)] = t;
     ctx->graph_epoch++;
     return SG_OK;

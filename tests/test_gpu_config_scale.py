@@ -90,9 +90,10 @@ def test_gay_berne_full_size_list_and_forces(lib):
     assert abs(pe - peo) <= 1e-5 * abs(peo)
 
 
-def test_ecp_full_size_list_and_forces(lib):
+@pytest.mark.parametrize("solver", [capi.SOLVER_NEWTON, capi.SOLVER_NEWTON_SUPPORT], ids=["half", "support"])
+def test_ecp_full_size_list_and_forces(lib, solver):
     # positions and box 3 % closer: tens of thousands of pairs in contact
-    npairs, F, T, pe, Fo, To, peo, active = full_size(ECP, "ECPR", solver=capi.SOLVER_NEWTON, squeeze=0.97)
+    npairs, F, T, pe, Fo, To, peo, active = full_size(ECP, "ECPR", solver=solver, squeeze=0.97)
     assert npairs > 400_000 and active > 10_000
     assert rel(F, Fo) < 1e-5
     assert rel(T, To) < 1e-5

@@ -209,3 +209,60 @@ def test_fused_nose_hoover_step_matches_separate_calls(lib):
     # and the captured graph keeps stepping
     a.step(3)
     a.step_check()
+
+
+def _gb_system(seed=6):
+    sig, eps = (1.0, 1.0, 3.0), (1.0, 1.0, 0.2)
+    r, q, box = ellipsoids((16, 16, 8), sig, 0.3, seed=seed, tilt=0.05)
+    n = len(r)
+    v = configs.velocities_to_temperature(n, 1.0, seed)
+    I = configs.default_inertia(sig)
+    l = configs.angular_momenta(q, I, 1.0, seed)
+    from sucrose_gb300 import GpuSystem
+    g = GpuSystem(n, box)
+    g.set_particles(sig=sig, eps=eps, inertia=I)
+    g.upload(r=f32(r), q=f32(q), v=f32(v), l=f32(l))
+    g.init_nlist(0.4, 6.0, trigger_mode=1)
+    return g
+
+
+@pytest.mark.parametrize("flat", [0, 1], ids=["conditional", "flat"])
+def test_fused_langevin_step_matches_separate_calls(lib, flat):
+    """The captured Langevin step, whose initial half step also runs the list
+    test, zeroes the forces and writes the Gay-Berne prep, against the drop-in
+    entry points called one by one; then a step whose list test requests a
+    rebuild."""
+    from sucrose_gb300 import capi
+    dt, T = 0.002, 1.0
+    a, b = _gb_system(), _gb_system()
+    p = a.params(capi.GB, cutoff=4.0, mu=2, nu=1)
+    for g in (a, b):
+        g.zero_forces()
+        g.pair_forces(p)
+    a.configure_step(p, integrator=capi.INT_LANGEVIN, dt=dt, target_temp=T, damping=1.0, rotations=1,
+                     first_step=7, flags=flat)
+    a.step(1)                       # the first step runs eagerly through the same kernels as the graph
+    a.synchronize()
+    b.lgv_initial(dt, 7, damping=1.0, target_temp=T)
+    b.update_nlist()
+    b.zero_forces()
+    pe_b, _ = b.pair_forces(p)
+    ke_b, kr_b = b.lgv_final(dt, damping=1.0)
+    sa, sb = a.download(), b.download()
+    for x, y in zip(sa, sb):
+        assert np.array_equal(x, y) or rel(x, y) < 1e-6
+    fa, ta = a.forces()
+    fb, tb = b.forces()
+    assert rel(fa, fb) < 1e-6 and rel(ta, tb) < 1e-6
+    e = a.energies()
+    assert abs(e[0] - pe_b) < 1e-6 * abs(pe_b)
+    assert abs(e[2] - ke_b) < 1e-6 * ke_b and abs(e[3] - kr_b) < 1e-6 * kr_b
+    # a displacement beyond the skin: the fused test requests the rebuild
+    builds = a.nlist_builds()
+    r, q, v, l = a.download()
+    a.upload(r=r, q=q, v=v + 150.0, l=l)   # a uniform drift of 0.3 per step
+    a.step(1)
+    a.step_check()
+    assert a.nlist_builds() == builds + 1
+    a.step(3)
+    a.step_check()

@@ -63,15 +63,49 @@ ECP_KINDS = [(capi.ECP, O.ECP, {}), (capi.ECPR, O.ECPR, {}), (capi.ECPW, O.ECPW,
 
 
 @pytest.mark.parametrize("kd,ko,kw", ECP_KINDS)
-def test_ecp_newton_vs_converged_fp64(lib, kd, ko, kw):
+@pytest.mark.parametrize("split", [1, 0], ids=["split", "fused"])
+@pytest.mark.parametrize("check", [1, 2], ids=["fp64", "double_float"])
+def test_ecp_newton_vs_converged_fp64(lib, kd, ko, kw, split, check):
+    # split: Newton solve kernel, then the force kernel from its lambda (the
+    # default); fused: one kernel solves and evaluates each pair
     P = ecp_state()
+    P.g.set_launch(kd, 256, split)
     pdev = P.g.params(kd, cutoff=3.0, solver=capi.SOLVER_NEWTON, **kw)
+    pdev.fp64_check = check
     por = O.pair_params(ko, cutoff=3.0, solver=O.SOLVER_TIGHT, **kw)
     F, T, pe, Fo, To, peo, st = compare(P, pdev, por, 3.0, 0.3)
     assert np.linalg.norm(Fo) > 0
     assert rel(F, Fo) < TOL and rel(T, To) < TOL
     assert abs(pe - peo) <= TOL * max(abs(peo), 1e-12)
     assert st.nonconverged == 0 and st.pairs == len(P.o.pairs(3.0, 0.3)[0])
+
+
+@pytest.mark.parametrize("kd,ko,kw", ECP_KINDS)
+@pytest.mark.parametrize("split", [1, 0], ids=["split", "fused"])
+def test_ecp_newton_support_start_vs_converged_fp64(lib, kd, ko, kw, split):
+    # Newton from the support-function start: same tolerance, same bound
+    P = ecp_state(seed=5)
+    P.g.set_launch(kd, 256, split)
+    pdev = P.g.params(kd, cutoff=3.0, solver=capi.SOLVER_NEWTON_SUPPORT, **kw)
+    por = O.pair_params(ko, cutoff=3.0, solver=O.SOLVER_TIGHT, **kw)
+    F, T, pe, Fo, To, peo, st = compare(P, pdev, por, 3.0, 0.3)
+    assert rel(F, Fo) < TOL and rel(T, To) < TOL
+    assert abs(pe - peo) <= TOL * max(abs(peo), 1e-12)
+    assert st.nonconverged == 0 and st.pairs == len(P.o.pairs(3.0, 0.3)[0])
+
+
+def test_ecp_support_start_saves_evaluations(lib):
+    # the support-function start needs fewer Newton evaluations than 1/2 on
+    # random orientations, and lands on the same lambda
+    P = ecp_state(seed=11, tilt=3.0, counts=(8, 10, 16))
+    P.g.init_nlist(0.3, 3.0)
+    out = {}
+    for solver in (capi.SOLVER_NEWTON, capi.SOLVER_NEWTON_SUPPORT):
+        P.g.zero_forces()
+        _, _, st = P.g.pair_forces(P.g.params(capi.ECPR, cutoff=3.0, solver=solver), want_stats=True)
+        out[solver] = (st.solver_evals / st.pairs, P.g.ecp_lambda().astype(np.float64))
+    assert out[capi.SOLVER_NEWTON_SUPPORT][0] < out[capi.SOLVER_NEWTON][0] - 0.2
+    assert np.max(np.abs(out[capi.SOLVER_NEWTON_SUPPORT][1] - out[capi.SOLVER_NEWTON][1])) < 4e-6
 
 
 @pytest.mark.parametrize("kd,ko,kw", ECP_KINDS)
@@ -97,11 +131,12 @@ def test_ecp_brent_lambda_bits(lib):
     assert np.array_equal(lam_dev, lam_ref.astype(np.float32))
 
 
-def test_ecp_newton_lambda_accuracy(lib):
+@pytest.mark.parametrize("solver", [capi.SOLVER_NEWTON, capi.SOLVER_NEWTON_SUPPORT], ids=["half", "support"])
+def test_ecp_newton_lambda_accuracy(lib, solver):
     P = ecp_state(seed=8)
     P.g.init_nlist(0.3, 3.0)
     P.g.zero_forces()
-    P.g.pair_forces(P.g.params(capi.ECPR, solver=capi.SOLVER_NEWTON))
+    P.g.pair_forces(P.g.params(capi.ECPR, solver=solver))
     lam_dev = P.g.ecp_lambda().astype(np.float64)
     pi, pj = P.g.raw_pairs()
     lam_ref, _ = P.o.forces(O.pair_params(O.ECPR, solver=O.SOLVER_TIGHT), pi, pj, want_lambda=True)

@@ -11,7 +11,8 @@ has no reference implementation, so its physical pin is equipartition:
   * the standard Nose-Hoover chains on translation and rotation: the mean
     translational kinetic energy is (3N - 3) T / 2 (the chain's n_dof,
     integrators.f90:303-392) and the rotational one 3/2 N T.
-All runs use the captured step, as the benchmark does.
+All runs use the captured step, as the benchmark does, and the skin rebuild
+trigger (trigger mode 1).
 """
 import numpy as np
 import pytest
@@ -26,7 +27,11 @@ def test_readme_nve_energy_conservation(lib):
     r, q, box, v = lj_fcc()
     g = GpuSystem(108, box)
     g.upload(r=r, v=v)
-    g.init_nlist(0.3, 2.5)
+    # rebuild on the skin (trigger 1): the reference's own trigger waits for a
+    # displacement of (rc + skin) / 2, by which time pairs have entered the
+    # cut-off unlisted and the energy jumps (tests/test_gpu_philox_nlist.py
+    # pins that trigger against the reference's decision)
+    g.init_nlist(0.3, 2.5, trigger_mode=1)
     g.configure_step(g.params(capi.LJ, cutoff=2.5), integrator=capi.INT_NVE, dt=0.0005)
     E, K = [], []
     for _ in range(200):              # 200 x 100 = the README's 20 000 steps
@@ -60,7 +65,7 @@ def fluid(seed, T=1.2):
     g = GpuSystem(n, box)
     g.set_particles(sig=sig, inertia=I)
     g.upload(r=r, q=q, v=v, l=l)
-    g.init_nlist(0.3, 3.0)
+    g.init_nlist(0.3, 3.0, trigger_mode=1)
     return g, g.params(capi.ECPR, cutoff=3.0, solver=capi.SOLVER_NEWTON), n
 
 
