@@ -9,9 +9,10 @@
 // reference's exact FP64 operation sequence (no contraction).
 //
 // Layout in HBM: per-particle rows of at most max_nb neighbours are written
-// column-major into nb_pad (k * n + i), then compacted into the flattened pair
-// arrays pair_i / pair_j, rows in particle order, which every pair kernel
-// walks 32 pairs per warp.
+// column-major into nb_pad (k * n + i; row-major, i * max_nb + k, by the
+// warp-per-row search of a system with dense cells), then compacted into the
+// flattened pair arrays pair_i / pair_j, rows in particle order, which every
+// pair kernel walks 32 pairs per warp.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -179,8 +180,11 @@ __global__ void k_fill(int n, const int* __restrict__ particle_cell, const int* 
 // Order each cell's particles by index so that rows are deterministic: one
 // warp per cell, each member placed at its rank (the number of smaller
 // indices in the cell; indices are distinct).
+// pos_cell (optional): the members' positions in the same order, so that the
+// row search reads a cell's candidates with contiguous loads.
 __global__ void k_sort_cells(int ncells, const int* __restrict__ cell_start, const int* __restrict__ cell_unsorted,
-                             int* cell_particles, const int* flags) {
+                             int* cell_particles, const int* flags, const float4* __restrict__ pos,
+                             float4* __restrict__ pos_cell) {
     if (!flags[F_REBUILD]) return;
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -191,6 +195,7 @@ __global__ void k_sort_cells(int ncells, const int* __restrict__ cell_start, con
         int rank = 0;
         for (int t = b; t < e; ++t) rank += cell_unsorted[t] < v;
         cell_particles[b + rank] = v;
+        if (pos_cell) pos_cell[b + rank] = pos[v];
     }
 }
 
@@ -286,35 +291,25 @@ __global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g0,
     row_done(i, cnt, cap, nb_count, flags, rp, pr);
 }
 
-// The same rows with one warp per particle, for dense cells: the lanes test
-// 32 members of a cell at once and the accepted ones are appended in member
-// order (ballot, then each accepting lane's rank among them), so each row is
-// exactly the one the thread-per-particle kernel writes.
-__global__ void __launch_bounds__(256) k_rows_cells_warp(int n, const float4* __restrict__ pos, ListGeom g0,
-                                                         const int* __restrict__ cell_start,
-                                                         const int* __restrict__ cell_particles, int max_nb,
-                                                         int* nb_pad, int* nb_count, int* flags, RepDev rp, PadRep pr,
-                                                         const int* rep_flag) {
+// The same rows with one warp per particle, for one system with dense cells:
+// the lanes test 32 members of a cell at once and the accepted ones are
+// appended in member order (ballot, then each accepting lane's rank among
+// them), so each row holds exactly what the thread-per-particle kernel
+// writes. Warps take rows in cell order, so the warps of a block search the
+// same 27 cells and find their candidates (cell-ordered positions, read with
+// contiguous loads) in L1; a chunk whose members all have indices <= i is
+// passed over (members are sorted). Row i is written row-major (i * max_nb).
+__global__ void __launch_bounds__(256) k_rows_cells_warp(int n, ListGeom g, const int* __restrict__ cell_start,
+                                                         const int* __restrict__ cell_particles,
+                                                         const float4* __restrict__ pos_cell, int max_nb,
+                                                         int* nb_pad, int* nb_count, int* flags) {
     if (!flags[F_REBUILD]) return;
     const int lane = threadIdx.x & 31;
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-    // persistent: each warp takes rows gwarp, gwarp + nwarps, ... (rows of
-    // replicas that keep their list are skipped at once)
-    for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n; i += nwarps) {   // warp-uniform
-        if (rp.rep_of && !rep_flag[rp.rep_of[i]]) continue;
-        const float4 pi = pos[i];
-        ListGeom g = g0;
-        int first_cell = 0;
-        size_t base, stride;
-        int cap;
-        pad_slot(n, i, max_nb, rp, pr, base, stride, cap);
-        if (rp.rep_of) {
-            const int r = rp.rep_of[i];
-            const int4 gr = rp.grid[r];
-            if (!gr.x) continue;   // all-pairs replicas: k_rows_cells
-            g = geom_for(g0, rp, r);
-            first_cell = gr.w;
-        }
+    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {   // warp-uniform
+        const int i = cell_particles[w];
+        const float4 pi = pos_cell[w];
+        const size_t base = (size_t)i * max_nb;
         int cnt = 0;
         int cx, cy, cz;
         cell_of(pi, g, cx, cy, cz);
@@ -324,27 +319,45 @@ __global__ void __launch_bounds__(256) k_rows_cells_warp(int n, const float4* __
                 const int yy = wrapc(cy + dy, g.nc[1]);
                 for (int dx = -1; dx <= 1; ++dx) {
                     const int xx = wrapc(cx + dx, g.nc[0]);
-                    const int c = first_cell + (zz * g.nc[1] + yy) * g.nc[0] + xx;
+                    const int c = (zz * g.nc[1] + yy) * g.nc[0] + xx;
                     const int b = cell_start[c], e = cell_start[c + 1];
                     for (int k0 = b; k0 < e; k0 += 32) {
                         const int k = k0 + lane;
-                        int j = 0;
-                        bool acc = false;
-                        if (k < e) {
-                            j = cell_particles[k];
-                            acc = j > i && accept_pair(pi, pos[j], g);
-                        }
+                        const int j = k < e ? cell_particles[k] : -1;
+                        if (!__any_sync(0xffffffffu, j > i)) continue;
+                        const bool acc = j > i && accept_pair(pi, pos_cell[k], g);
                         const unsigned m = __ballot_sync(0xffffffffu, acc);
                         if (acc) {
                             const int slot = cnt + __popc(m & ((1u << lane) - 1u));
-                            if (slot < cap) nb_pad[base + (size_t)slot * stride] = j;
+                            if (slot < max_nb) nb_pad[base + slot] = j;
                         }
                         cnt += __popc(m);
                     }
                 }
             }
         }
-        if (lane == 0) row_done(i, cnt, cap, nb_count, flags, rp, pr);
+        if (lane == 0) {
+            nb_count[i] = min(cnt, max_nb);
+            if (cnt > max_nb) atomicMax(&flags[F_OVERFLOW], cnt);
+        }
+    }
+}
+
+// Row-major padded rows (k_rows_cells_warp) into the flattened pair arrays:
+// a warp per row, contiguous on both sides.
+__global__ void __launch_bounds__(256) k_compact_rows(int n, int max_nb, const int* __restrict__ nb_pad,
+                                                      const int* __restrict__ nb_count,
+                                                      const int* __restrict__ row_off, int* pair_i, int* pair_j,
+                                                      const int* flags) {
+    if (!flags[F_REBUILD]) return;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n; i += nwarps) {
+        const int c = nb_count[i], o = row_off[i];
+        for (int k = lane; k < c; k += 32) {
+            pair_i[o + k] = i;
+            pair_j[o + k] = nb_pad[(size_t)i * max_nb + k];
+        }
     }
 }
 
@@ -629,13 +642,15 @@ int enqueue_build(sg_ctx* ctx) {
         k_fill<<<nb, 256, 0, ctx->stream>>>(n, nl.particle_cell, nl.cell_start, nl.cell_fill, nl.cell_unsorted,
                                             nl.dev_flags);
         k_sort_cells<<<(nl.ncells + 7) / 8, 256, 0, ctx->stream>>>(nl.ncells, nl.cell_start, nl.cell_unsorted,
-                                                                    nl.cell_particles, nl.dev_flags);
-        // one large system with dense cells: a warp per row; sparse cells or many
-    // small replicas rebuilding at once: a thread per row
+                                                                    nl.cell_particles, nl.dev_flags, ctx->pos,
+                                                                    nl.dense_cells ? nl.pos_cell : nullptr);
+        // one large system with dense cells: a warp per row (rows row-major,
+        // compacted a warp per row); sparse cells or many small replicas
+        // rebuilding at once: a thread per row
         if (nl.dense_cells)
             k_rows_cells_warp<<<(int)std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 8 * ctx->num_sms), 256, 0,
-                                ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb, nl.nb_pad,
-                                               nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag);
+                                ctx->stream>>>(n, g, nl.cell_start, nl.cell_particles, nl.pos_cell, nl.max_nb,
+                                               nl.nb_pad, nl.nb_count, nl.dev_flags);
         else
             k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
                                                       nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag,
@@ -646,9 +661,13 @@ int enqueue_build(sg_ctx* ctx) {
         k_rows_all<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
     }
     if (int rc = scan(ctx, nl.nb_count, n, nl.row_off, nl.dev_flags + F_NPAIRS, nl.dev_flags)) return rc;
-    k_compact<<<(n + COMPACT_BLOCK - 1) / COMPACT_BLOCK, COMPACT_BLOCK, 0, ctx->stream>>>(
-        n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off, nl.pair_i, nl.pair_j, nl.dev_flags, ctx->rep, pad,
-        nl.rep_flag);
+    if (nl.use_cells && nl.dense_cells)
+        k_compact_rows<<<16 * ctx->num_sms, 256, 0, ctx->stream>>>(n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off,
+                                                                   nl.pair_i, nl.pair_j, nl.dev_flags);
+    else
+        k_compact<<<(n + COMPACT_BLOCK - 1) / COMPACT_BLOCK, COMPACT_BLOCK, 0, ctx->stream>>>(
+            n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off, nl.pair_i, nl.pair_j, nl.dev_flags, ctx->rep, pad,
+            nl.rep_flag);
     if (ctx->nrep)
         k_chunk_rep<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(nl.row_off, ctx->rep.off, ctx->nrep, nl.dev_flags,
                                                               nl.chunk_rep);
@@ -696,7 +715,7 @@ int sg_nlist_enqueue_build(sg_ctx* ctx) { return enqueue_build(ctx); }
 int sg_nlist_free(sg_ctx* ctx) {
     sg_nlist_state& nl = ctx->nl;
     void* bufs[] = {nl.cell_count, nl.cell_start, nl.cell_fill, nl.cell_particles, nl.particle_cell, nl.nb_count,
-                    nl.nb_pad, nl.row_off, nl.scan_tmp, nl.pair_i, nl.pair_j, nl.dev_flags, nl.pos_last,
+                    nl.nb_pad, nl.row_off, nl.scan_tmp, nl.pair_i, nl.pair_j, nl.dev_flags, nl.pos_last, nl.pos_cell,
                     nl.rep_max_nb, nl.rep_pad_off, nl.rep_need, nl.rep_flag, nl.rep_builds, nl.cell_unsorted,
                     nl.chunk_rep, nl.row_block_order};
     for (void* b : bufs)
@@ -801,6 +820,7 @@ static int alloc_list(sg_ctx* ctx, int max_nb) {
     SG_CUDA(ctx, cudaMalloc(&nl.cell_fill, sizeof(int) * (size_t)nl.ncells));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_particles, sizeof(int) * (size_t)n));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_unsorted, sizeof(int) * (size_t)n));
+    SG_CUDA(ctx, cudaMalloc(&nl.pos_cell, sizeof(float4) * (size_t)n));
     SG_CUDA(ctx, cudaMalloc(&nl.particle_cell, sizeof(int) * (size_t)n));
     SG_CUDA(ctx, cudaMalloc(&nl.nb_count, sizeof(int) * (size_t)n));
     SG_CUDA(ctx, cudaMalloc(&nl.row_off, sizeof(int) * ((size_t)n + 1)));

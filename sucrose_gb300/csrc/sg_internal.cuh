@@ -52,7 +52,8 @@ struct sg_nlist_state {
     int* cell_particles = nullptr;   // [n]
     int* particle_cell = nullptr;    // [n]
     int* nb_count = nullptr;         // [n]
-    int* nb_pad = nullptr;           // [max_nb * n], column-major (k * n + i)
+    int* nb_pad = nullptr;           // [max_nb * n], column-major (k * n + i); dense cells: row-major
+    float4* pos_cell = nullptr;      // [n] positions in cell order (dense cells)
     int* row_off = nullptr;          // [n + 1]
     int* scan_tmp = nullptr;         // block sums of the scan
     int* pair_i = nullptr;           // [pair_capacity]
