@@ -343,14 +343,21 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, 2) k_pair_gb_tile(PairLaunc
         pr.b.periodic = 1;
         const int v0 = L.row_off[o], cnt = L.row_off[o + nr] - v0;
         const long long s0 = L.sec[r];
+        // the pair indices stream from DRAM: the next chunk's are loaded before
+        // this chunk is tested
+        auto fetch = [&](int base, int& t, int& i, int& j, bool& valid) {
+            valid = base + lane < cnt;
+            t = (int)(s0 + base + lane);
+            i = valid ? __ldcs(L.pair_i + t) : -1;
+            j = valid ? __ldcs(L.pair_j + t) : 0;
+        };
+        int tn, in_, jn;
+        bool vn;
+        fetch(warp * 32, tn, in_, jn, vn);
         for (int base = warp * 32; base < cnt; base += nw * 32) {
-            const bool valid = base + lane < cnt;
-            const int t = (int)(s0 + base + lane);
-            int i = -1, j = 0;
-            if (valid) {
-                i = L.pair_i[t];
-                j = L.pair_j[t];
-            }
+            const int t = tn, i = in_, j = jn;
+            const bool valid = vn;
+            if (base + nw * 32 < cnt) fetch(base + nw * 32, tn, in_, jn, vn);
             q.feed(L, pr, t, i, j, valid, es, sh_stats);
         }
         q.flush(L, pr, es, sh_stats);

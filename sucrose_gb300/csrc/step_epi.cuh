@@ -14,6 +14,7 @@
 
 #include <cmath>
 
+#include "dfloat.cuh"
 #include "sg_internal.cuh"
 
 // ------------------------------------------------------------ list trigger --
@@ -171,17 +172,18 @@ SG_DEV void gb_prep_one(int n, int p, float4 at, float4 q, float4 s, float4 e, f
     const float lpar = s.z, lprp = s.x;
     const float ep = powf(e.x, muinv), ez = powf(e.z, muinv);
     const float xhi = (ep - ez) / (ep + ez);
-    // u and chi in FP64 as hi + lo (the precise class of near-contact pairs)
-    const double W = w, X = x, Y = y, Z = z, lp = lpar, lq = lprp;
-    const double ux = 2.0 * (X * Z + W * Y), uy = 2.0 * (Y * Z - W * X), uz = W * W - X * X - Y * Y + Z * Z;
-    const double chi64 = (lp * lp - lq * lq) / (lp * lp + lq * lq);
-    const float chi = (float)chi64;
-    const float3 u = make_float3((float)ux, (float)uy, (float)uz);
+    // u and chi as hi + lo to ~48 bits (the precise class of near-contact
+    // pairs), in double-float arithmetic on the FP32 pipe: the products of the
+    // FP32 quaternion and shape components are exact there
+    const dfl ux = df_mul_f(df_add(df_two_prod(x, z), df_two_prod(w, y)), 2.f);
+    const dfl uy = df_mul_f(df_sub(df_two_prod(y, z), df_two_prod(w, x)), 2.f);
+    const dfl uz = df_add(df_sub(df_two_prod(w, w), df_two_prod(x, x)), df_sub(df_two_prod(z, z), df_two_prod(y, y)));
+    const dfl pp = df_two_prod(lpar, lpar), qq = df_two_prod(lprp, lprp);
+    const dfl chi = df_div(df_sub(pp, qq), df_add(pp, qq));
     prep[2 * p] = make_float4(at.x, at.y, at.z, lprp);
-    prep[2 * p + 1] = make_float4(u.x, u.y, u.z, chi);
+    prep[2 * p + 1] = make_float4(ux.hi, uy.hi, uz.hi, chi.hi);
     prep[2 * (size_t)n + p] = make_float4(xhi, 1.f / e.z, 0.f, 0.f);
-    prep[3 * (size_t)n + p] = make_float4((float)(ux - (double)u.x), (float)(uy - (double)u.y),
-                                          (float)(uz - (double)u.z), (float)(chi64 - (double)chi));
+    prep[3 * (size_t)n + p] = make_float4(ux.lo, uy.lo, uz.lo, chi.lo);
 }
 
 // ------------------------------------------------------- step epilogue ----
