@@ -535,7 +535,9 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
 def tune_variants(tune, ecp=False):
     """The autotuner's timed launch variants, by block size and range filter
     (ECP: the one-kernel path or the split Newton path)."""
-    shapes = ((256, 0), (128, 0), (256, 1), (128, 1))
+    shapes = ((256, 0), (128, 0), (256, 1), (128, 1), (64, 0), (64, 1))
+    if tune.candidates == 3:
+        shapes = ((256, 0), (128, 0), (64, 0))
     tag = (lambda f: "split" if f else "fused") if ecp else (lambda f: f"f{f}")
     return {f"b{b}_{tag(f)}": float(tune.ms[k]) for k, (b, f) in enumerate(shapes[:tune.candidates])}
 

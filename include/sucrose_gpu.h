@@ -428,7 +428,7 @@ int sg_mlp_set_inline(sg_ctx* ctx, int32_t inline_guess);
 
 /* ---- autotuner of the pair kernels (no counterpart in the reference) ------- */
 typedef struct {
-    int32_t block;       /* chosen threads per block                            */
+    int32_t block;       /* chosen threads per block (64, 128 or 256)           */
     int32_t filter;      /* chosen: 1 = range filter + per-warp in-range queue;
                             2 = Gay-Berne replicas: one replica per block, its
                             records staged in shared memory (replaces (256, 0));
@@ -436,15 +436,17 @@ typedef struct {
                             force kernel), 0 = one kernel per pair              */
     int32_t candidates;  /* variants timed (ms[0..candidates-1])                 */
     int32_t reserved;
-    float ms[4];         /* mean launch time of (256,0) (128,0) (256,1) (128,1);
-                            GB replicas: (256,2) in place of (256,0)           */
+    float ms[8];         /* mean launch time of the variants (block, filter), in
+                            order (256,0) (128,0) (256,1) (128,1) (64,0) (64,1);
+                            GB replicas: (256,2) in place of (256,0); kinds
+                            without the second axis: (256,0) (128,0) (64,0)  */
 } sg_tune_result;
 /* Time each launch variant of the params' pair kernel on the current list
  * (reps launches each), keep the fastest for this context's (kind, size,
  * density) bucket. Forces, torques and energy accumulators are restored.
  * Captured steps are re-captured at their next sg_step. */
 int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* params, int32_t reps, sg_tune_result* out);
-/* Set a launch variant by hand (block 128 or 256; filter 0, 1, or 2 for
+/* Set a launch variant by hand (block 64, 128 or 256; filter 0, 1, or 2 for
  * the Gay-Berne replica tiles; for ECP kinds, filter selects the split Newton
  * path, which the Brent solver ignores). */
 int sg_pair_set_launch(sg_ctx* ctx, int32_t kind, int32_t block, int32_t filter);

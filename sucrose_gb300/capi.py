@@ -47,7 +47,7 @@ BEND, DIH, COSINE_BEND, COSINE_DIH, ANGLE_BEND, ANGLE_DIH = range(6)
 
 class TuneResult(C.Structure):
     _fields_ = [("block", C.c_int32), ("filter", C.c_int32), ("candidates", C.c_int32), ("reserved", C.c_int32),
-                ("ms", C.c_float * 4)]
+                ("ms", C.c_float * 8)]
 
 
 class PlaceReport(C.Structure):

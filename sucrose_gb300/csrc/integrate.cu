@@ -285,8 +285,10 @@ __device__ __forceinline__ double exp_chain(double x) {
 // chain element: with h = exp(-x/2), exp(-x) = h^2 and exprel(-x) is
 // (h^2 - 1)/(-x), or for |x| <= 0.01 h times the even series
 // sinh(x/2)/(x/2) = sum (x/2)^2k / (2k+1)!, so the two share it.
-__device__ void u4(double t, int j_start, int j_stop, int stride, double* p, const double* iHB, double sum,
-                   double ndof, double T) {
+// p: the chain momenta in registers (the caller's local copy).
+__device__ __forceinline__ void u4(double t, int j_start, int j_stop, int stride, double (&p)[3], const double* iHB,
+                                   double sum, double ndof, double T) {
+#pragma unroll
     for (int j = j_start; stride > 0 ? j <= j_stop : j >= j_stop; j += stride) {
         double gj = (j == 1) ? (sum - ndof * T) : ((p[j - 2] * p[j - 2] * iHB[j - 2]) - T);
         if (j == 3) {
@@ -330,15 +332,31 @@ __global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* _
 // entry (zeroed by the host before the reduction). Writes the scale factors.
 // The translational chain (which = 0) and the rotational chain (which = 1)
 // are independent, and the caller runs them in two different warps.
+// The chain state is read once into registers and written back at the end:
+// one thread runs the chain's dependent FP64 sequence, and a global load
+// between its steps (L2 latency after each store) would cost more than the
+// arithmetic.
 __device__ void nhc_chain_one(const NhConst& c, double* nh, int which) {
     double* eta = nh + 6 * which;
-    double* p = eta + 3;
+    double e[3], p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        e[k] = eta[k];
+        p[k] = eta[3 + k];
+    }
     const double* iHB = which ? c.iHBr : c.iHB;
+    const double ih[3] = {iHB[0], iHB[1], iHB[2]};
     const double K = nh[14 + which];
-    u4(c.dt / 4.0, 3, 1, -1, p, iHB, K, which ? c.nrot : c.ndof, c.T);
-    const double sc = exp_chain(-0.5 * c.dt * p[0] * iHB[0]);
-    for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] * iHB[k];
-    u4(c.dt / 4.0, 1, 3, 1, p, iHB, K * sc * sc, which ? c.nrot : c.ndof, c.T);
+    u4(c.dt / 4.0, 3, 1, -1, p, ih, K, which ? c.nrot : c.ndof, c.T);
+    const double sc = exp_chain(-0.5 * c.dt * p[0] * ih[0]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) e[k] = e[k] + 0.5 * c.dt * p[k] * ih[k];
+    u4(c.dt / 4.0, 1, 3, 1, p, ih, K * sc * sc, which ? c.nrot : c.ndof, c.T);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        eta[k] = e[k];
+        eta[3 + k] = p[k];
+    }
     nh[12 + which] = sc;
     if (!which) nh[16] = K * sc * sc;
 }
@@ -503,13 +521,21 @@ __global__ void k_kick(int n, float dt, float4* __restrict__ vel, const float4* 
 // The reference's per-particle chain (integrators.f90:324-352, :372-390): a
 // serial recurrence over particles in index order. The O(N) SUM that the
 // reference repeats at every particle is carried as a running FP64 sum,
-// updated by each particle's change; per-particle terms are in FP64.
+// updated by each particle's change; per-particle terms are in FP64. The
+// chain state stays in registers for the whole sweep (written back at the
+// end), the divisions by the chain masses are products with their
+// reciprocals and the exponential is exp_chain.
 __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, float4* __restrict__ pos,
                             float4* __restrict__ vel, const float4* __restrict__ force,
                             const float4* __restrict__ shape) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double* eta = nh;
-    double* p = nh + 3;
+    double eta[3], p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        eta[k] = nh[k];
+        p[k] = nh[3 + k];
+    }
+    const double ih[3] = {c.iHB[0], c.iHB[1], c.iHB[2]};
     double K = nh[14];
     double ke = 0.0;
     const double h = 0.5 * c.dt;
@@ -524,15 +550,16 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
             vx = (float)vx; vy = (float)vy; vz = (float)vz;
             K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
         }
-        u4(c.dt / 4.0, 3, 1, -1, p, c.iHB, K, c.ndof, c.T);
-        const double sc = exp(-0.5 * c.dt * p[0] / c.HB[0]);
+        u4(c.dt / 4.0, 3, 1, -1, p, ih, K, c.ndof, c.T);
+        const double sc = exp_chain(-0.5 * c.dt * p[0] * ih[0]);
         {
             const double ox = vx, oy = vy, oz = vz;
             vx = (float)(vx * sc); vy = (float)(vy * sc); vz = (float)(vz * sc);
             K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
         }
-        for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] / c.HB[k];
-        u4(c.dt / 4.0, 1, 3, 1, p, c.iHB, K, c.ndof, c.T);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] * ih[k];
+        u4(c.dt / 4.0, 1, 3, 1, p, ih, K, c.ndof, c.T);
         if (initial) {
             const double ox = vx, oy = vy, oz = vz;
             vx = (float)(vx + h * (f.x * im)); vy = (float)(vy + h * (f.y * im)); vz = (float)(vz + h * (f.z * im));
@@ -545,6 +572,11 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
             ke += 0.5 * m * (vx * vx + vy * vy + vz * vz);
         }
         vel[i] = make_float4((float)vx, (float)vy, (float)vz, v.w);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        nh[k] = eta[k];
+        nh[3 + k] = p[k];
     }
     nh[14] = K;
     nh[17] = ke;

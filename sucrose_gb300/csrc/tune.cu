@@ -1,5 +1,5 @@
 // Autotuner of the pair kernels' launch shape (no counterpart in the
-// reference). The variants are the block size (128 or 256 threads) and, for
+// reference). The variants are the block size (64, 128 or 256 threads) and, for
 // potentials with a cheap range test (LJ family, Gay-Berne family), whether
 // the kernel filters the list first and evaluates only the in-range pairs,
 // 32 per warp; for the ECP kinds with a Newton solver the second axis is the
@@ -69,13 +69,16 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
     cudaEventCreate(&e1);
     const long long key = tune_key(ctx, p->kind);
     const bool tiles = ctx->nrep && p->kind >= SG_GB && p->kind < SG_ECP;
-    const PairTune cand[4] = {{256, tiles ? 2 : 0}, {128, tiles ? 0 : 0}, {256, 1}, {128, 1}};
-    const int ncand = filterable ? 4 : 2;
+    // block size 256, 128 or 64 x the second axis (range filter; ECP: split path)
+    const PairTune cand[6] = {{256, tiles ? 2 : 0}, {128, 0}, {256, 1}, {128, 1}, {64, 0}, {64, 1}};
+    const int order_unfiltered[3] = {0, 1, 4};
+    const int ncand = filterable ? 6 : 3;
     float best = 1e30f;
     PairTune pick = cand[0];
     int rc = SG_OK;
     sg_tune_result res{};
-    for (int c = 0; c < ncand && !rc; ++c) {
+    for (int v = 0; v < ncand && !rc; ++v) {
+        const int c = filterable ? v : order_unfiltered[v];
         ctx->tune[key] = cand[c];
         rc = sg_pair_forces_async(ctx, p);   // warm-up (allocations, caches)
         float tot = 0.f;
@@ -89,7 +92,7 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
             tot += ms;
         }
         const float ms = tot / reps;
-        res.ms[c] = ms;
+        res.ms[v] = ms;
         if (!rc && ms < best) {
             best = ms;
             pick = cand[c];
@@ -117,7 +120,7 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
 }
 
 int sg_pair_set_launch(sg_ctx* ctx, int32_t kind, int32_t block, int32_t filter) {
-    if (!ctx || (block != 128 && block != 256) || filter < 0 || filter > 2) return SG_EINVAL;
+    if (!ctx || (block != 64 && block != 128 && block != 256) || filter < 0 || filter > 2) return SG_EINVAL;
     PairTune t;
     t.block = block;
     t.filter = filter;

@@ -12,7 +12,7 @@ from helpers import ellipsoids, f32, jittered_fcc, rel
 from sucrose_gb300 import GpuSystem, capi, configs
 
 pytestmark = pytest.mark.gpu
-VARIANTS = [(256, 0), (128, 0), (256, 1), (128, 1)]
+VARIANTS = [(256, 0), (128, 0), (256, 1), (128, 1), (64, 0), (64, 1)]
 
 
 def lj_system():
@@ -82,8 +82,8 @@ def test_autotune_restores_state(lib):
     F0, T0 = g.forces()
     e0 = g.energies()
     res = g.autotune(p, reps=3)
-    assert res.candidates == 4 and res.block in (128, 256) and res.filter in (0, 1)
-    assert all(res.ms[k] > 0 for k in range(4))
+    assert res.candidates == 6 and res.block in (64, 128, 256) and res.filter in (0, 1)
+    assert all(res.ms[k] > 0 for k in range(6))
     F1, T1 = g.forces()
     assert np.array_equal(F0, F1) and np.array_equal(T0, T1)
     assert np.array_equal(e0, g.energies())
