@@ -84,10 +84,18 @@ SG_DEV float4 q_midpoint(float4 q, float3 L, float3 Iinv, float dt, Rot& rm, flo
     return make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// Renormalisation in FP64: the sum of squares of the exactly widened
+// components in FP64, 1 / sqrt(s) by one FP64 Newton step from the FP32
+// estimate (about 43 correct bits, far below the FP32 rounding of the
+// result), the products rounded to FP32. An FP64 square root and division
+// cost some forty instructions of the FP64 pipe (1/64 of the FP32 rate on
+// GB300) per particle; this form costs about sixteen.
 SG_DEV float4 q_advance(float4 q, float4 qd, float dt) {
-    double w = (double)(q.x + dt * qd.x), x = (double)(q.y + dt * qd.y), y = (double)(q.z + dt * qd.z),
-           z = (double)(q.w + dt * qd.w);
-    double inv = 1.0 / sqrt(w * w + x * x + y * y + z * z);
+    const double w = (double)(q.x + dt * qd.x), x = (double)(q.y + dt * qd.y), y = (double)(q.z + dt * qd.z),
+                 z = (double)(q.w + dt * qd.w);
+    const double s = fma(w, w, fma(x, x, fma(y, y, z * z)));
+    double inv = (double)rsqrtf((float)s);
+    inv = inv * fma(-0.5 * s * inv, inv, 1.5);
     return make_float4((float)(w * inv), (float)(x * inv), (float)(y * inv), (float)(z * inv));
 }
 
@@ -281,11 +289,17 @@ __device__ __forceinline__ double exp_chain(double x) {
 }
 
 // u4_propagator: G1 from the supplied sum (m v^2 or L_b^2/I), with
-// exprel(y) = (e^y - 1)/y (integrators.f90:233-301). One FP64 exponential per
-// chain element: with h = exp(-x/2), exp(-x) = h^2 and exprel(-x) is
-// (h^2 - 1)/(-x), or for |x| <= 0.01 h times the even series
-// sinh(x/2)/(x/2) = sum (x/2)^2k / (2k+1)!, so the two share it.
-// p: the chain momenta in registers (the caller's local copy).
+// exprel(y) = (e^y - 1)/y (integrators.f90:233-301). The chain momenta, the
+// forces G_j and the products p e^-x + t G c stay in FP64. F32: the two
+// factors e^-x and c = exprel(-x), which multiply FP64 values and need only
+// FP32's relative precision once per half step, are evaluated in FP32 (one
+// thread runs this chain, and a dependent FP64 operation costs ~14 times an
+// FP32 one on GB300): with h = e^(-x/2), e^-x = h^2 and c = h sinh(x/2)/(x/2),
+// the even series in (x/2)^2 (no cancellation for small x); for |x| >= 1 the
+// FP64 forms. The reference-compat chain, applied once per particle, keeps
+// them in FP64 (F32 = false): its N applications would accumulate the FP32
+// rounding.
+template <bool F32 = true>
 __device__ __forceinline__ void u4(double t, int j_start, int j_stop, int stride, double (&p)[3], const double* iHB,
                                    double sum, double ndof, double T) {
 #pragma unroll
@@ -295,17 +309,30 @@ __device__ __forceinline__ void u4(double t, int j_start, int j_stop, int stride
             p[2] = p[2] + t * gj;
         } else {
             const double x = t * p[j] * iHB[j];
-            const double h = exp_chain(-0.5 * x);
-            const double ex = h * h;
-            double c;
-            if (fabs(x) > 0.01) {
-                c = (ex - 1.0) / (-x);
+            double ex, c;
+            if (!F32) {
+                const double h = exp_chain(-0.5 * x);
+                ex = h * h;
+                if (fabs(x) > 0.01) {
+                    c = (ex - 1.0) / (-x);
+                } else {
+                    const double g[5] = {1.0 / 1, 1.0 / 6, 1.0 / 120, 1.0 / 5040, 1.0 / 362880};
+                    const double y = (0.5 * x) * (0.5 * x);
+                    double f = g[4];
+                    for (int k = 3; k >= 0; --k) f = f * y + g[k];
+                    c = h * f;
+                }
+            } else if (fabs(x) < 1.0) {
+                const float xf = (float)x, u = 0.5f * xf, y = u * u;
+                const float h = expf(-u);
+                // sinh(u)/u = 1 + y/6 + y^2/120 + y^3/5040 + y^4/362880 (|u| < 0.5: < 1e-9 left)
+                const float sh = fmaf(fmaf(fmaf(fmaf(y, 1.f / 362880.f, 1.f / 5040.f), y, 1.f / 120.f), y, 1.f / 6.f), y,
+                                      1.f);
+                ex = (double)(h * h);
+                c = (double)(h * sh);
             } else {
-                const double g[5] = {1.0 / 1, 1.0 / 6, 1.0 / 120, 1.0 / 5040, 1.0 / 362880};
-                const double y = (0.5 * x) * (0.5 * x);
-                double f = g[4];
-                for (int k = 3; k >= 0; --k) f = f * y + g[k];
-                c = h * f;
+                ex = exp(-x);
+                c = (ex - 1.0) / (-x);
             }
             p[j - 1] = p[j - 1] * ex + t * gj * c;
         }
@@ -550,7 +577,7 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
             vx = (float)vx; vy = (float)vy; vz = (float)vz;
             K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
         }
-        u4(c.dt / 4.0, 3, 1, -1, p, ih, K, c.ndof, c.T);
+        u4<false>(c.dt / 4.0, 3, 1, -1, p, ih, K, c.ndof, c.T);
         const double sc = exp_chain(-0.5 * c.dt * p[0] * ih[0]);
         {
             const double ox = vx, oy = vy, oz = vz;
@@ -559,7 +586,7 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] * ih[k];
-        u4(c.dt / 4.0, 1, 3, 1, p, ih, K, c.ndof, c.T);
+        u4<false>(c.dt / 4.0, 1, 3, 1, p, ih, K, c.ndof, c.T);
         if (initial) {
             const double ox = vx, oy = vy, oz = vz;
             vx = (float)(vx + h * (f.x * im)); vy = (float)(vy + h * (f.y * im)); vz = (float)(vz + h * (f.z * im));
