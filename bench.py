@@ -504,7 +504,7 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
         "metric": METRICS[name],
         "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": steps, "warmup": a.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 (fp64 sums and residual check)",
+        "dtype": "fp32 (fp64 totals and residual check)",
         "data": "synthetic (seeded isotropic placement, the same state as the reference arm)",
         "config": {"workload": w["workload"], "n": n, "listed_pairs": npairs, "solver": solver,
                    "dt": w["dt"], "T": w["T"], "seed": w["seed"],
@@ -738,7 +738,7 @@ def run_charged(a):
             "metric": "charged pair-evals/s (WCA + switched Coulomb, full MD step)",
             "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp32 (fp64 sums)", "data": "synthetic (seeded FCC lattice, +-1 charges, device-equilibrated)",
+            "dtype": "fp32 (fp64 totals)", "data": "synthetic (seeded FCC lattice, +-1 charges, device-equilibrated)",
             "config": {"workload": w["workload"], "n": n, "listed_pairs": npairs, "pair_sets": ["WCA", "COULOMB"],
                        "dt": w["dt"], "T": w["T"], "cutoff": w["cutoff"], "skin": w["skin"],
                        "l2": "flushed between timed steps (256 MB write)",
@@ -866,7 +866,7 @@ def run_constrained(a):
             "metric": w["metric"],
             "value": value, "unit": "constraint-solves/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp32 (fp64 sums)", "data": "synthetic (seeded molecule lattice, device-equilibrated)",
+            "dtype": "fp32 (fp64 totals)", "data": "synthetic (seeded molecule lattice, device-equilibrated)",
             "config": {"workload": w["workload"], "n": n, "constraints": nc,
                        "bonded_terms": {int(k): int(len(at)) for k, at, _, _ in terms},
                        "listed_pairs": npairs, "dt": w["dt"], "T": w["T"],
@@ -1270,7 +1270,7 @@ def replicas_line(a, rank=0, world=1, local=0, dist=None, steps=None):
             "metric": METRICS["replicas"],
             "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": steps, "warmup": a.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp32 (fp64 sums)", "data": "synthetic (seeded replica ensemble, device-equilibrated)",
+            "dtype": "fp32 (fp64 totals)", "data": "synthetic (seeded replica ensemble, device-equilibrated)",
             "config": {"workload": W["workload"], "replicas": len(e["n"]), "particles": int(n),
                        "listed_pairs": npairs, "lj_replicas": int(np.sum(e["family"] == 0)),
                        "gb_replicas": int(np.sum(e["family"] == 1)), "count_redraws": int(e["redraws"]),

@@ -4,7 +4,8 @@
  * One context (sg_ctx) owns one system's device state on one GPU and one CUDA
  * stream. State is FP32 structure-of-arrays in HBM (float4 position,
  * quaternion, velocity, angular momentum, force, torque, shape, energy scales,
- * inertia); energy, virial and kinetic-energy reductions are FP64.
+ * inertia); energy, virial and kinetic-energy totals are FP64 (kinetic terms
+ * and their partial sums in double-float, ~48 bits).
  *
  * Host arrays crossing this boundary are FP64 structure-of-arrays of length N
  * in the reference's own layout (module globals RX..RZ, QW..QZ, VX..VZ, LX..LZ,

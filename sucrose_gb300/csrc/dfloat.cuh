@@ -72,3 +72,89 @@ SG_DEV dfl df_dot3_dd(float3 a, float3 al, float3 b, float3 bl) {
     const float c = fmaf(a.x, bl.x, fmaf(a.y, bl.y, fmaf(a.z, bl.z, fmaf(al.x, b.x, fmaf(al.y, b.y, al.z * b.z)))));
     return df_fast_two_sum(d.hi, d.lo + c);
 }
+
+// ------------------------------------------------ double-float grid sums --
+// Warp sum of K double-float values by shuffles (lane 0 holds the result).
+template <int K>
+SG_DEV void df_warp_sum(dfl (&v)[K]) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const dfl w = {__shfl_down_sync(0xffffffffu, v[k].hi, o), __shfl_down_sync(0xffffffffu, v[k].lo, o)};
+            v[k] = df_add(v[k], w);
+        }
+    }
+}
+
+// Grid sum of K per-thread double-float values, every level in double-float
+// on the FP32 pipe: warps by shuffles, the block from one value per warp, the
+// block partials (hi, lo pairs in the slots of partials, gridDim.x * K of
+// them) in the block that finishes last, in a fixed order. FP64 appears once,
+// for the result: out[k] = total (store) or out[k] += total. tot (optional,
+// shared memory): the totals for the finishing block's own threads after a
+// __syncthreads. Every thread of the block calls it; returns true in the
+// finishing block (block-uniform).
+template <int K>
+__device__ bool block_reduce_finish_df(dfl (&v)[K], double* partials, unsigned int* done, double* out, bool store,
+                                       double* tot = nullptr) {
+    __shared__ float2 sh[32][K];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    float2* part = reinterpret_cast<float2*>(partials);
+    df_warp_sum<K>(v);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) sh[warp][k] = make_float2(v[k].hi, v[k].lo);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        dfl t[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) t[k] = lane < nw ? dfl{sh[lane][k].x, sh[lane][k].y} : dfl{0.f, 0.f};
+        df_warp_sum<K>(t);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) part[(size_t)blockIdx.x * K + k] = make_float2(t[k].hi, t[k].lo);
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    dfl s[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] = dfl{0.f, 0.f};
+    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float2 p = __ldcg(part + (size_t)b * K + k);   // L2: written by other blocks
+            s[k] = df_add(s[k], dfl{p.x, p.y});
+        }
+    }
+    df_warp_sum<K>(s);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) sh[warp][k] = make_float2(s[k].hi, s[k].lo);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        dfl t[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) t[k] = lane < nw ? dfl{sh[lane][k].x, sh[lane][k].y} : dfl{0.f, 0.f};
+        df_warp_sum<K>(t);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const double d = (double)t[k].hi + (double)t[k].lo;
+                if (store) out[k] = d;
+                else out[k] += d;
+                if (tot) tot[k] = d;
+            }
+            *done = 0u;
+        }
+    }
+    return true;
+}

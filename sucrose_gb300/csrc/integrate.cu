@@ -1,7 +1,8 @@
 // Integrators of the reference's verlet, quaternion, langevin and nose_hoover
 // modules (fortran/integrators.f90:1-392, :494-676) on FP32 state, one thread
-// per particle, kinetic-energy sums in FP64 (block partials finished by the
-// last block). Quaternion renormalisation is done in FP64.
+// per particle. Kinetic-energy terms and their sums in double-float on the
+// FP32 pipe (block partials finished by the last block, FP64 for the result);
+// quaternion renormalisation beyond FP32 precision in double-float.
 #include <cmath>
 
 #include "sg_internal.cuh"
@@ -84,25 +85,35 @@ SG_DEV float4 q_midpoint(float4 q, float3 L, float3 Iinv, float dt, Rot& rm, flo
     return make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// Renormalisation in FP64: the sum of squares of the exactly widened
-// components in FP64, 1 / sqrt(s) by one FP64 Newton step from the FP32
-// estimate (about 43 correct bits, far below the FP32 rounding of the
-// result), the products rounded to FP32. An FP64 square root and division
-// cost some forty instructions of the FP64 pipe (1/64 of the FP32 rate on
-// GB300) per particle; this form costs about sixteen.
+// Renormalisation to beyond FP32 precision, on the FP32 pipe (FP64 runs at
+// 1/64 of its rate on GB300): s = |q|^2 in double-float (squares exact by FMA
+// two-products), 1 / sqrt(s) = r0 (1 + e/2) by one Newton step from the FP32
+// estimate r0 with e = 1 - s r0^2 formed from the double-float s (about 44
+// correct bits), each component rounded once, w r0 + w r0 e/2 in one FMA.
 SG_DEV float4 q_advance(float4 q, float4 qd, float dt) {
-    const double w = (double)(q.x + dt * qd.x), x = (double)(q.y + dt * qd.y), y = (double)(q.z + dt * qd.z),
-                 z = (double)(q.w + dt * qd.w);
-    const double s = fma(w, w, fma(x, x, fma(y, y, z * z)));
-    double inv = (double)rsqrtf((float)s);
-    inv = inv * fma(-0.5 * s * inv, inv, 1.5);
-    return make_float4((float)(w * inv), (float)(x * inv), (float)(y * inv), (float)(z * inv));
+    const float w = q.x + dt * qd.x, x = q.y + dt * qd.y, y = q.z + dt * qd.z, z = q.w + dt * qd.w;
+    const dfl s = df_add(df_dot3(make_float3(w, x, y), make_float3(w, x, y)), df_two_prod(z, z));
+    const float r0 = rsqrtf(s.hi);
+    const dfl sr2 = df_mul(s, df_two_prod(r0, r0));
+    const float c = 0.5f * ((1.f - sr2.hi) - sr2.lo) * r0;
+    return make_float4(fmaf(w, r0, w * c), fmaf(x, r0, x * c), fmaf(y, r0, y * c), fmaf(z, r0, z * c));
 }
 
-SG_DEV double kin_rot_of(float4 q, float3 L, float3 Iinv) {
+// Kinetic terms in double-float on the FP32 pipe; the sums take them through
+// block_reduce_finish_df, so FP64 appears once per reduction, not per particle.
+// m |v|^2: the squares exact, their sum and the product with m to ~48 bits.
+SG_DEV dfl mv2_df(float m, float4 v) {
+    const float3 u = make_float3(v.x, v.y, v.z);
+    return df_mul_f(df_dot3(u, u), m);
+}
+SG_DEV dfl df_half(dfl a) { return {0.5f * a.hi, 0.5f * a.lo}; }
+// 2 KE_rot = sum_k L_b,k^2 / I_k with L_b = R L the body-frame angular
+// momentum (integrators.f90:190-215): the squares rounded to FP32, their
+// products with 1/I_k exact, the sum in double-float.
+SG_DEV dfl kin_rot2_df(float4 q, float3 L, float3 Iinv) {
     Rot r = rot_of(q.x, q.y, q.z, q.w);
     float3 Lb = rot_apply(r, L);
-    return 0.5 * ((double)(Lb.x * Lb.x) * Iinv.x + (double)(Lb.y * Lb.y) * Iinv.y + (double)(Lb.z * Lb.z) * Iinv.z);
+    return df_dot3(make_float3(Lb.x * Lb.x, Lb.y * Lb.y, Lb.z * Lb.z), Iinv);
 }
 
 // ------------------------------------------------------------------- VV ----
@@ -121,16 +132,16 @@ __global__ void k_vv_initial(int n, float dt, Geo g, float4* __restrict__ pos, f
 // final half kick; KE = sum 0.5 m v^2 (mass from shape.w)
 __global__ void k_vv_final(int n, float dt, float4* __restrict__ vel, const float4* __restrict__ force,
                            const float4* __restrict__ shape, double* partials, unsigned int* done, double* acc) {
-    double e[1] = {0.0};
+    dfl e[1] = {{0.f, 0.f}};
     const float h = 0.5f * dt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 v = vel[i], f = force[i];
         const float im = v.w;
         v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
         vel[i] = v;
-        e[0] += 0.5 * (double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        e[0] = df_add(e[0], df_half(mv2_df(shape[i].w, v)));
     }
-    block_reduce_finish<1>(e, partials, done, acc);
+    block_reduce_finish_df<1>(e, partials, done, acc, false);
 }
 
 // --------------------------------------------------------------- rotation --
@@ -151,15 +162,15 @@ __global__ void k_qq_initial(int n, float dt, float4* __restrict__ quat, float4*
 __global__ void k_qq_final(int n, float dt, const float4* __restrict__ quat, float4* __restrict__ angm,
                            const float4* __restrict__ torque, const float4* __restrict__ inert_inv, double* partials,
                            unsigned int* done, double* acc) {
-    double e[1] = {0.0};
+    dfl e[1] = {{0.f, 0.f}};
     const float h = 0.5f * dt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 L4 = angm[i], T = torque[i], Ii = inert_inv[i];
         float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
         angm[i] = make_float4(L.x, L.y, L.z, 0.f);
-        e[0] += kin_rot_of(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z));
+        e[0] = df_add(e[0], df_half(kin_rot2_df(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z))));
     }
-    block_reduce_finish<1>(e, partials, done, acc);
+    block_reduce_finish_df<1>(e, partials, done, acc, false);
 }
 
 // --------------------------------------------------------------- Langevin --
@@ -238,31 +249,32 @@ __global__ void k_lgv_final(int n, float dt, float4* __restrict__ vel, const flo
                             float4* __restrict__ angm, const float4* __restrict__ torque,
                             const float4* __restrict__ inert_inv, int rotations, double* partials, unsigned int* done,
                             double* acc, int* step_inc) {
-    double e[2] = {0.0, 0.0};
+    dfl e[2] = {{0.f, 0.f}, {0.f, 0.f}};
     const float h = 0.5f * dt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 v = vel[i], f = force[i];
         const float im = v.w;
         v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
         vel[i] = v;
-        e[0] += 0.5 * (double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        e[0] = df_add(e[0], df_half(mv2_df(shape[i].w, v)));
         if (rotations) {
             float4 L4 = angm[i], T = torque[i], Ii = inert_inv[i];
             float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
             angm[i] = make_float4(L.x, L.y, L.z, 0.f);
-            e[1] += kin_rot_of(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z));
+            e[1] = df_add(e[1], df_half(kin_rot2_df(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z))));
         }
     }
     // step_inc (captured step): the sums are stored, and the step counter advances
-    if (block_reduce_finish<2>(e, partials, done, acc, nullptr, step_inc != nullptr) && step_inc &&
-        threadIdx.x == 0)
+    if (block_reduce_finish_df<2>(e, partials, done, acc, step_inc != nullptr) && step_inc && threadIdx.x == 0)
         *step_inc += 1;
 }
 
 // ------------------------------------------------------------ Nose-Hoover --
 // integrators.f90:233-301; chain length 3. nh layout: [0..2] eta, [3..5] p_eta,
 // [6..8] eta_r, [9..11] p_eta_r, [12] translational scale, [13] rotational
-// scale, [14] sum m v^2 scratch, [15] sum L_b^2/I scratch.
+// scale, [14] sum m v^2 scratch, [15] sum L_b^2/I scratch, [16] the scaled
+// sum m v^2, [17] the compat sweep's KE, [18] the two scales rounded to FP32
+// (a float pair: the particle kernels read them without an FP64 conversion).
 struct NhConst {
     double dt, T, ndof, nrot;
     double HB[3], HBr[3];
@@ -343,16 +355,16 @@ __global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* _
                           const float4* __restrict__ quat, const float4* __restrict__ angm,
                           const float4* __restrict__ inert_inv, int rot, double* partials, unsigned int* done,
                           double* dst) {
-    double e[2] = {0.0, 0.0};
+    dfl e[2] = {{0.f, 0.f}, {0.f, 0.f}};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 v = vel[i];
-        e[0] += (double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        e[0] = df_add(e[0], mv2_df(shape[i].w, v));
         if (rot) {
             float4 L = angm[i], Ii = inert_inv[i];
-            e[1] += 2.0 * kin_rot_of(quat[i], make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z));
+            e[1] = df_add(e[1], kin_rot2_df(quat[i], make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z)));
         }
     }
-    block_reduce_finish<2>(e, partials, done, dst);
+    block_reduce_finish_df<2>(e, partials, done, dst, false);
 }
 
 // Standard NHC half step on the chain(s): nh[14], nh[15] hold the sums on
@@ -363,7 +375,8 @@ __global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* _
 // one thread runs the chain's dependent FP64 sequence, and a global load
 // between its steps (L2 latency after each store) would cost more than the
 // arithmetic.
-__device__ void nhc_chain_one(const NhConst& c, double* nh, int which) {
+// K: the sum (m v^2 or L_b^2/I) for this chain.
+__device__ void nhc_chain_one(const NhConst& c, double* nh, int which, double K) {
     double* eta = nh + 6 * which;
     double e[3], p[3];
 #pragma unroll
@@ -373,7 +386,6 @@ __device__ void nhc_chain_one(const NhConst& c, double* nh, int which) {
     }
     const double* iHB = which ? c.iHBr : c.iHB;
     const double ih[3] = {iHB[0], iHB[1], iHB[2]};
-    const double K = nh[14 + which];
     u4(c.dt / 4.0, 3, 1, -1, p, ih, K, which ? c.nrot : c.ndof, c.T);
     const double sc = exp_chain(-0.5 * c.dt * p[0] * ih[0]);
 #pragma unroll
@@ -385,22 +397,31 @@ __device__ void nhc_chain_one(const NhConst& c, double* nh, int which) {
         eta[3 + k] = p[k];
     }
     nh[12 + which] = sc;
+    reinterpret_cast<float*>(nh + 18)[which] = (float)sc;
     if (!which) nh[16] = K * sc * sc;
 }
 
-// threads 0 (translation) and 32 (rotation, or the unit scale without it)
-__device__ void nhc_chain_threads(const NhConst& c, double* nh, int rot) {
-    if (threadIdx.x == 0) nhc_chain_one(c, nh, 0);
+// threads 0 (translation) and 32 (rotation, or the unit scale without it).
+// tot: the two sums (shared memory), else nh[14], nh[15].
+__device__ void nhc_chain_threads(const NhConst& c, double* nh, int rot, const double* tot) {
+    if (threadIdx.x == 0) nhc_chain_one(c, nh, 0, tot ? tot[0] : nh[14]);
     if (threadIdx.x == 32) {
-        if (rot) nhc_chain_one(c, nh, 1);
-        else nh[13] = 1.0;
+        if (rot) {
+            nhc_chain_one(c, nh, 1, tot ? tot[1] : nh[15]);
+        } else {
+            nh[13] = 1.0;
+            reinterpret_cast<float*>(nh + 18)[1] = 1.f;
+        }
     }
 }
 
 __global__ void k_nhc_chain(NhConst c, double* nh, int rot) {
     if (blockIdx.x != 0) return;
-    nhc_chain_threads(c, nh, rot);
+    nhc_chain_threads(c, nh, rot, nullptr);
 }
+
+// the translational and rotational scales as FP32 (nh[18])
+SG_DEV float2 nh_scale_f(const double* nh) { return *reinterpret_cast<const float2*>(nh + 18); }
 
 // ---- fused Nose-Hoover step (the captured step's form) -----------------------
 // The same arithmetic as the separate entry points, in fewer passes:
@@ -413,7 +434,7 @@ __global__ void k_nhc_sum_chain(int n, float dt, int kick, float4* __restrict__ 
                                 const float4* __restrict__ shape, const float4* __restrict__ quat,
                                 const float4* __restrict__ angm, const float4* __restrict__ inert_inv, int rot,
                                 NhConst c, double* partials, unsigned int* done, double* nh) {
-    double e[2] = {0.0, 0.0};
+    dfl e[2] = {{0.f, 0.f}, {0.f, 0.f}};
     const float h = 0.5f * dt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 v = vel[i];
@@ -423,16 +444,16 @@ __global__ void k_nhc_sum_chain(int n, float dt, int kick, float4* __restrict__ 
             v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
             vel[i] = v;
         }
-        e[0] += (double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        e[0] = df_add(e[0], mv2_df(shape[i].w, v));
         if (rot) {
             float4 L = angm[i], Ii = inert_inv[i];
-            e[1] += 2.0 * kin_rot_of(quat[i], make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z));
+            e[1] = df_add(e[1], kin_rot2_df(quat[i], make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z)));
         }
     }
-    if (block_reduce_finish<2>(e, partials, done, nh + 14, nullptr, true)) {
+    __shared__ double tot[2];
+    if (block_reduce_finish_df<2>(e, partials, done, nh + 14, true, tot)) {
         __syncthreads();
-        __threadfence_block();
-        nhc_chain_threads(c, nh, rot);
+        nhc_chain_threads(c, nh, rot, tot);
     }
 }
 
@@ -445,12 +466,13 @@ __global__ void k_nhc_initial_fused(int n, const double* nh, float dt, Geo g, fl
                                     int rot_chain, int rotations, StepEpi epi) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float sc = (float)nh[12];
+    const float2 scf = nh_scale_f(nh);
+    const float sc = scf.x;
     float4 v = vel[i];
     v.x *= sc; v.y *= sc; v.z *= sc;
     float4 L4 = angm[i];
     if (rot_chain) {
-        const float sr = (float)nh[13];
+        const float sr = scf.y;
         L4 = make_float4(L4.x * sr, L4.y * sr, L4.z * sr, L4.w);
     }
     const float4 f = force[i], r = pos[i];
@@ -484,15 +506,16 @@ __global__ void k_nhc_final_fused(int n, const double* nh, float dt, float4* __r
                                   float4* __restrict__ angm, const float4* __restrict__ torque,
                                   const float4* __restrict__ inert_inv, int rot_chain, int rotations, double* partials,
                                   unsigned int* done, double* acc, int* step_inc) {
-    double e[2] = {0.0, 0.0};
+    dfl e[2] = {{0.f, 0.f}, {0.f, 0.f}};
     const float h = 0.5f * dt;
-    const float sc = (float)nh[12];
-    const float sr = rot_chain ? (float)nh[13] : 1.f;
+    const float2 scf = nh_scale_f(nh);
+    const float sc = scf.x;
+    const float sr = rot_chain ? scf.y : 1.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 v = vel[i];
         v.x *= sc; v.y *= sc; v.z *= sc;
         vel[i] = v;
-        e[0] += 0.5 * ((double)shape[i].w * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z));
+        e[0] = df_add(e[0], df_half(mv2_df(shape[i].w, v)));
         if (rot_chain || rotations) {
             float4 L4 = angm[i];
             if (rot_chain) L4 = make_float4(L4.x * sr, L4.y * sr, L4.z * sr, L4.w);
@@ -500,14 +523,14 @@ __global__ void k_nhc_final_fused(int n, const double* nh, float dt, float4* __r
                 const float4 T = torque[i], Ii = inert_inv[i];
                 const float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
                 angm[i] = make_float4(L.x, L.y, L.z, 0.f);
-                e[1] += kin_rot_of(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z));
+                e[1] = df_add(e[1], df_half(kin_rot2_df(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z))));
             } else {
                 angm[i] = L4;
             }
         }
     }
     // the sums are stored; step_inc (captured step): the step counter advances
-    if (block_reduce_finish<2>(e, partials, done, acc, nullptr, true) && step_inc && threadIdx.x == 0)
+    if (block_reduce_finish_df<2>(e, partials, done, acc, true) && step_inc && threadIdx.x == 0)
         *step_inc += 1;
 }
 
@@ -517,11 +540,12 @@ __global__ void k_nhc_apply(int n, const double* nh, int do_vv, float dt, Geo g,
                             int rot) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float sc = (float)nh[12];
+    const float2 scf = nh_scale_f(nh);
+    const float sc = scf.x;
     float4 v = vel[i];
     v.x *= sc; v.y *= sc; v.z *= sc;
     if (rot) {
-        const float sr = (float)nh[13];
+        const float sr = scf.y;
         float4 L = angm[i];
         angm[i] = make_float4(L.x * sr, L.y * sr, L.z * sr, L.w);
     }
