@@ -251,17 +251,33 @@ __global__ void k_lgv_final(int n, float dt, float4* __restrict__ vel, const flo
                             double* acc, int* step_inc) {
     dfl e[2] = {{0.f, 0.f}, {0.f, 0.f}};
     const float h = 0.5f * dt;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 v = vel[i], f = force[i];
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    // the first particle's inputs that the pair stage before does not write
+    float4 v0{}, s0{}, L0{}, I0{}, q0{};
+    if (i0 < n) {
+        v0 = vel[i0];
+        s0 = shape[i0];
+        if (rotations) {
+            L0 = angm[i0];
+            I0 = inert_inv[i0];
+            q0 = quat[i0];
+        }
+    }
+    pdl_wait();
+    for (int i = i0; i < n; i += stride) {
+        const bool first = i == i0;
+        float4 v = first ? v0 : vel[i];
+        const float4 f = force[i];
         const float im = v.w;
         v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
         vel[i] = v;
-        e[0] = df_add(e[0], df_half(mv2_df(shape[i].w, v)));
+        e[0] = df_add(e[0], df_half(mv2_df((first ? s0 : shape[i]).w, v)));
         if (rotations) {
-            float4 L4 = angm[i], T = torque[i], Ii = inert_inv[i];
+            const float4 L4 = first ? L0 : angm[i], T = torque[i], Ii = first ? I0 : inert_inv[i];
+            const float4 q = first ? q0 : quat[i];
             float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
             angm[i] = make_float4(L.x, L.y, L.z, 0.f);
-            e[1] = df_add(e[1], df_half(kin_rot2_df(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z))));
+            e[1] = df_add(e[1], df_half(kin_rot2_df(q, L, make_float3(Ii.x, Ii.y, Ii.z))));
         }
     }
     // step_inc (captured step): the sums are stored, and the step counter advances
@@ -436,18 +452,33 @@ __global__ void k_nhc_sum_chain(int n, float dt, int kick, float4* __restrict__ 
                                 NhConst c, double* partials, unsigned int* done, double* nh) {
     dfl e[2] = {{0.f, 0.f}, {0.f, 0.f}};
     const float h = 0.5f * dt;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 v = vel[i];
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    // the first particle's inputs, none of which the pair stage before writes
+    float4 v0{}, s0{}, q0{}, L0{}, I0{};
+    if (i0 < n) {
+        v0 = vel[i0];
+        s0 = shape[i0];
+        if (rot) {
+            q0 = quat[i0];
+            L0 = angm[i0];
+            I0 = inert_inv[i0];
+        }
+    }
+    pdl_wait();
+    pdl_trigger();
+    for (int i = i0; i < n; i += stride) {
+        const bool first = i == i0;
+        float4 v = first ? v0 : vel[i];
         if (kick) {
             const float4 f = force[i];
             const float im = v.w;
             v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
             vel[i] = v;
         }
-        e[0] = df_add(e[0], mv2_df(shape[i].w, v));
+        e[0] = df_add(e[0], mv2_df((first ? s0 : shape[i]).w, v));
         if (rot) {
-            float4 L = angm[i], Ii = inert_inv[i];
-            e[1] = df_add(e[1], kin_rot2_df(quat[i], make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z)));
+            const float4 L = first ? L0 : angm[i], Ii = first ? I0 : inert_inv[i], q = first ? q0 : quat[i];
+            e[1] = df_add(e[1], kin_rot2_df(q, make_float3(L.x, L.y, L.z), make_float3(Ii.x, Ii.y, Ii.z)));
         }
     }
     __shared__ double tot[2];
@@ -466,29 +497,33 @@ __global__ void k_nhc_initial_fused(int n, const double* nh, float dt, Geo g, fl
                                     int rot_chain, int rotations, StepEpi epi) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    // the particle's state, which the sums and chain before do not write
+    float4 v = vel[i], L4 = angm[i];
+    const float4 f = force[i], r = pos[i], q = quat[i];
+    float4 T{}, Ii{};
+    if (rotations) {
+        T = torque[i];
+        Ii = inert_inv[i];
+    }
+    pdl_wait();
     const float2 scf = nh_scale_f(nh);
     const float sc = scf.x;
-    float4 v = vel[i];
     v.x *= sc; v.y *= sc; v.z *= sc;
-    float4 L4 = angm[i];
     if (rot_chain) {
         const float sr = scf.y;
         L4 = make_float4(L4.x * sr, L4.y * sr, L4.z * sr, L4.w);
     }
-    const float4 f = force[i], r = pos[i];
     const float h = 0.5f * dt, im = v.w;
     v.x += h * (f.x * im); v.y += h * (f.y * im); v.z += h * (f.z * im);
     float3 p = wrap_pos(make_float3(r.x + dt * v.x, r.y + dt * v.y, r.z + dt * v.z), g, i);
     const float4 pn = make_float4(p.x, p.y, p.z, r.w);
     pos[i] = pn;
     vel[i] = v;
-    float4 qn = quat[i];
+    float4 qn = q;
     if (rotations) {
-        const float4 T = torque[i], Ii = inert_inv[i];
         float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
         Rot rm;
         float3 Lb;
-        const float4 q = qn;
         float4 qd = q_midpoint(q, L, make_float3(Ii.x, Ii.y, Ii.z), dt, rm, Lb);
         qn = q_advance(q, qd, dt);
         quat[i] = qn;
@@ -508,22 +543,36 @@ __global__ void k_nhc_final_fused(int n, const double* nh, float dt, float4* __r
                                   unsigned int* done, double* acc, int* step_inc) {
     dfl e[2] = {{0.f, 0.f}, {0.f, 0.f}};
     const float h = 0.5f * dt;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    // the first particle's inputs that the sums and chain before do not write
+    float4 s0{}, L0{}, T0{}, I0{}, q0{};
+    if (i0 < n) {
+        s0 = shape[i0];
+        if (rot_chain || rotations) L0 = angm[i0];
+        if (rotations) {
+            T0 = torque[i0];
+            I0 = inert_inv[i0];
+            q0 = quat[i0];
+        }
+    }
+    pdl_wait();
     const float2 scf = nh_scale_f(nh);
     const float sc = scf.x;
     const float sr = rot_chain ? scf.y : 1.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = i0; i < n; i += stride) {
+        const bool first = i == i0;
         float4 v = vel[i];
         v.x *= sc; v.y *= sc; v.z *= sc;
         vel[i] = v;
-        e[0] = df_add(e[0], df_half(mv2_df(shape[i].w, v)));
+        e[0] = df_add(e[0], df_half(mv2_df((first ? s0 : shape[i]).w, v)));
         if (rot_chain || rotations) {
-            float4 L4 = angm[i];
+            float4 L4 = first ? L0 : angm[i];
             if (rot_chain) L4 = make_float4(L4.x * sr, L4.y * sr, L4.z * sr, L4.w);
             if (rotations) {
-                const float4 T = torque[i], Ii = inert_inv[i];
+                const float4 T = first ? T0 : torque[i], Ii = first ? I0 : inert_inv[i], q = first ? q0 : quat[i];
                 const float3 L = make_float3(L4.x + h * T.x, L4.y + h * T.y, L4.z + h * T.z);
                 angm[i] = make_float4(L.x, L.y, L.z, 0.f);
-                e[1] = df_add(e[1], df_half(kin_rot2_df(quat[i], L, make_float3(Ii.x, Ii.y, Ii.z))));
+                e[1] = df_add(e[1], df_half(kin_rot2_df(q, L, make_float3(Ii.x, Ii.y, Ii.z))));
             } else {
                 angm[i] = L4;
             }
@@ -753,11 +802,13 @@ int sg_lgv_final(sg_ctx* ctx, double dt, double damping, double* kin_eng, double
     if (!ctx->step_fused) SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double) * 2, ctx->stream));
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
-    k_lgv_final<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->vel, ctx->force, ctx->shape, ctx->quat,
-                                              ctx->angm, ctx->torque, ctx->inert_inv, ctx->lgv_rotations, ctx->partials,
-                                              ctx->done_counter, ctx->acc + 2,
-                                              ctx->step_fused ? ctx->step_dev : nullptr);
-    SG_LAUNCH_CHECK(ctx, "k_lgv_final");
+    // in the fused step the pair stage's kernels come directly before: this
+    // kernel's loads of the particle state overlap their tail
+    const bool pdl = ctx->step_fused && !ctx->step_events;
+    SG_CUDA(ctx, launch_pdl(pdl, k_lgv_final, grid, 256, 0, ctx->stream, ctx->n, (float)dt, ctx->vel, ctx->force,
+                            ctx->shape, ctx->quat, ctx->angm, ctx->torque, ctx->inert_inv, ctx->lgv_rotations,
+                            ctx->partials, ctx->done_counter, ctx->acc + 2,
+                            ctx->step_fused ? ctx->step_dev : nullptr));
     if (int rc = read_acc(ctx, 2, kin_eng)) return rc;
     return read_acc(ctx, 3, kin_rot);
 }
@@ -829,11 +880,11 @@ int sg_nhc_step_initial(sg_ctx* ctx, double dt, double target_temp, double coupl
                                                   ctx->done_counter, ctx->nh);
     StepEpi epi;
     if (int rc = make_step_epi(ctx, epi)) return rc;
-    k_nhc_initial_fused<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, (float)dt, make_geo(ctx),
-                                                                       ctx->pos, ctx->vel, ctx->force, ctx->quat,
-                                                                       ctx->angm, ctx->torque, ctx->inert_inv,
-                                                                       rot_chain, rotations, epi);
-    SG_LAUNCH_CHECK(ctx, "k_nhc_initial_fused");
+    // programmatic dependent launch: the particle loads overlap the chain
+    SG_CUDA(ctx, launch_pdl(true, k_nhc_initial_fused, (ctx->n + 255) / 256, 256, 0, ctx->stream, ctx->n,
+                            (const double*)ctx->nh, (float)dt, make_geo(ctx), ctx->pos, ctx->vel,
+                            (const float4*)ctx->force, ctx->quat, ctx->angm, (const float4*)ctx->torque,
+                            (const float4*)ctx->inert_inv, (int)rot_chain, (int)rotations, epi));
     return SG_OK;
 }
 
@@ -845,14 +896,17 @@ int sg_nhc_step_final(sg_ctx* ctx, double dt, double target_temp, double couplin
     NhConst c = nh_const(ctx, dt, target_temp, coupling);
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
-    k_nhc_sum_chain<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, 1, ctx->vel, ctx->force, ctx->shape, ctx->quat,
-                                                  ctx->angm, ctx->inert_inv, rot_chain, c, ctx->partials,
-                                                  ctx->done_counter, ctx->nh);
-    k_nhc_final_fused<<<grid, 256, 0, ctx->stream>>>(ctx->n, ctx->nh, (float)dt, ctx->vel, ctx->shape, ctx->quat,
-                                                    ctx->angm, ctx->torque, ctx->inert_inv, rot_chain, rotations,
-                                                    ctx->partials, ctx->done_counter, ctx->acc + 2,
-                                                    ctx->step_fused ? ctx->step_dev : nullptr);
-    SG_LAUNCH_CHECK(ctx, "k_nhc_final_fused");
+    // programmatic dependent launches: the sums' particle loads overlap the
+    // pair stage's tail, the final half's loads the sums and chain
+    SG_CUDA(ctx, launch_pdl(!ctx->step_events, k_nhc_sum_chain, grid, 256, 0, ctx->stream, ctx->n, (float)dt, 1,
+                            ctx->vel, (const float4*)ctx->force, (const float4*)ctx->shape,
+                            (const float4*)ctx->quat, (const float4*)ctx->angm, (const float4*)ctx->inert_inv,
+                            (int)rot_chain, c, ctx->partials, ctx->done_counter, ctx->nh));
+    SG_CUDA(ctx, launch_pdl(true, k_nhc_final_fused, grid, 256, 0, ctx->stream, ctx->n, (const double*)ctx->nh,
+                            (float)dt, ctx->vel, (const float4*)ctx->shape, (const float4*)ctx->quat, ctx->angm,
+                            (const float4*)ctx->torque, (const float4*)ctx->inert_inv, (int)rot_chain,
+                            (int)rotations, ctx->partials, ctx->done_counter, ctx->acc + 2,
+                            ctx->step_fused ? ctx->step_dev : nullptr));
     return SG_OK;
 }
 

@@ -323,6 +323,10 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFil
             q.feed(L, pot, t, i, j, valid, es, sh_stats);
     }
     if constexpr (FILTER) q.flush(L, pot, es, sh_stats);
+    // the pairs are done: a kernel launched after this one with programmatic
+    // serialisation (the final half step) may start loading what this one
+    // does not write
+    pdl_trigger();
     if (kSh) {
         __syncthreads();
         for (int k = threadIdx.x; k < SG_NSTATS; k += blockDim.x)

@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, 2) k_pair_gb_tile(PairLaunc
         }
         q.flush(L, pr, es, sh_stats);
     }
+    pdl_trigger();   // the final half step may start loading (see k_pair)
     if (threadIdx.x == 0 && atomicAdd(&T.ctr[1], 1) == (int)gridDim.x - 1) {
         T.ctr[0] = 0;   // every block has left the loop
         T.ctr[1] = 0;

@@ -7,11 +7,42 @@
 #include <cstring>
 #include <string>
 #include <map>
+#include <utility>
 #include <vector>
 
 #include "../../include/sucrose_gpu.h"
 
 #define SG_DEV __device__ __forceinline__
+
+// ------------------------------------------- programmatic dependent launch --
+// A kernel launched by launch_pdl may be scheduled while the kernel before it
+// in the stream is still running, once every block of that kernel has called
+// pdl_trigger() (or exited). Its blocks then load what the earlier kernel does
+// not write, and pdl_wait() (griddepcontrol.wait) returns once the earlier
+// grid has completed and its writes are visible; every read of data that grid
+// writes, and every write, comes after it. pdl_wait returns at once in a
+// kernel launched the ordinary way. A kernel calls pdl_trigger only after its
+// own pdl_wait, so that its dependents never overlap the grid before it.
+SG_DEV void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+SG_DEV void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// k<<<grid, block, smem, s>>>(args...) with programmatic stream serialisation
+// (pdl = true) or as an ordinary launch.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(bool pdl, void (*k)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // ------------------------------------------------------------------ context --
 // Per-replica tables of a batched context (sg_create_replicas). A context
@@ -137,6 +168,7 @@ struct sg_ctx {
     int gb_tile_count = 0;
     int gb_tile_maxn = 0;
     int step_fused = 0;
+    int step_events = 0;             // the step is captured with event nodes between its stages
     int step_prep_kind = 0;          // SG_PREP_NONE / _ECP / _GB (step_epi.cuh)
     float step_prep_muinv = 1.f;
     int mlp_tc_test_no_mma = 0;      // failure-path test: the next guess pass issues no MMA

@@ -105,6 +105,7 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
     ctx->lgv_step_dev = ctx->step_dev;
     ctx->lgv_rotations = c.rotations;
     plan_fusion(ctx, c);
+    ctx->step_events = ev != nullptr;
     const bool fused = ctx->step_fused != 0;
     int rc = SG_OK;
     if (ev) record_event(ev[0], ctx->stream);
@@ -157,6 +158,7 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
     ctx->lgv_step_dev = nullptr;
     ctx->lgv_rotations = 1;
     ctx->step_fused = 0;
+    ctx->step_events = 0;
     ctx->step_prep_kind = SG_PREP_NONE;
     return rc;
 }
