@@ -72,8 +72,8 @@ def parse():
     ap.add_argument("--no-sub", action="store_true", help="skip the gb and replicas sub-objects of the ecp line")
     ap.add_argument("--profile-case", default=None, help="run one small profiling case and exit (see PROFILE_CASES)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the profiled kernels (--profile-case)")
-    ap.add_argument("--ecp-path", default=None, choices=["split", "fused"],
-                    help="ECP profile cases: the split Newton path or the one-kernel path (default: untuned)")
+    ap.add_argument("--ecp-path", default=None, choices=["split", "fused", "filtered"],
+                    help="ECP profile cases: the split Newton path, the one-kernel path or the one kernel behind the support-function range test (default: untuned)")
     ap.add_argument("--state-equil", type=int, default=0,
                     help="untimed Langevin steps from the placed state before timing (ecp, gb)")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000)
@@ -201,13 +201,19 @@ def configure(g, w, pp, langevin=False, first_step=1):
                          flags=FLAGS)
 
 
-def pair_flops(kind, listed, in_range, mean_evals=0.0, support=False):
+def pair_flops(kind, listed, in_range, mean_evals=0.0, support=False, solved=None):
     """Algorithmic FP32 flops of one pair-force launch, counted from the kernel
     sources (FMA = 2 flops, sqrt / rsqrt / division = 1). Every listed pair
     pays the distance and, for Gay-Berne, the orientation terms up to the range
-    test; pairs in range pay the force and torque terms."""
+    test; pairs in range pay the force and torque terms. ECP: `solved` pairs
+    (all listed ones unless the support-filtered launch turned some away) pay
+    the contact solve and the force terms, mean_evals Newton evaluations each;
+    with the filter every listed pair pays its test (70: the distance, two
+    quadratic forms, two square roots)."""
     if kind.startswith("ECP"):
-        return ecp_flops_per_pair(mean_evals, support) * listed
+        if solved is None or solved >= listed:
+            return ecp_flops_per_pair(mean_evals, support) * listed
+        return 70.0 * listed + ecp_flops_per_pair(mean_evals, support) * solved
     if kind.startswith("GB"):
         return 80.0 * listed + 240.0 * in_range
     return 20.0 * listed + 20.0 * in_range
@@ -302,13 +308,16 @@ def force_error_vs_fp64(g, w, pp, nthreads=None):
     return {"force": nf(F, Fo), "torque": nf(T, To), "pot_eng": abs(pe - peo) / max(abs(peo), 1e-300)}
 
 
-def mlp_leg(a, g, w, torch, stream, flush, npairs):
+def mlp_leg(a, g, w, torch, stream, flush, npairs, tune):
     """Train the learned guess on plain-Newton samples at T* 0.8, 1.2, 1.6 and
-    time the MLP-guess path against the plain path on the same state."""
+    time the MLP-guess path against the plain path on the same state, both
+    with the one-kernel launch that solves every pair (the samples need every
+    pair's lambda); the tuned launch is restored at the end."""
     import ctypes
     from sucrose_gb300 import capi, mlp
     r, q, v, l = g.download()          # restore the timed state afterwards
     newton = pair_params(g, w, "newton")
+    g.set_launch(newton.kind, 256, 0)
 
     def langevin(T):
         g.configure_step(newton, integrator=capi.INT_LANGEVIN, dt=w["dt"], target_temp=T, damping=1.0, rotations=1)
@@ -348,6 +357,7 @@ def mlp_leg(a, g, w, torch, stream, flush, npairs):
     g.step(5)
     g.step_check()
     t_step = timed_steps(g, torch, stream, 50, flush)
+    g.set_launch(newton.kind, tune.block, tune.filter)
     return {"samples": a.mlp_samples, "epochs": a.mlp_epochs, "train_mse": hist, "gen_s": t_gen, "train_s": t_train,
             "force_kernel_ms": 1e3 * tm, "pair_evals_per_s_force_kernel": npairs / tm,
             "guess_pass_ms_tcgen05": 1e3 * t_guess,
@@ -408,11 +418,15 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
 
     # dominant kernel: the pair-force kernel timed alone (same stream, L2 flushed)
     _, _, st = g.pair_forces(pp, want_stats=True)
-    mean_evals = st.solver_evals / max(st.pairs, 1)
+    # ECP: pairs solved (iteration bin 0 holds the pairs the support-filtered
+    # launch turned away) and Newton evaluations per solved pair
+    solved = st.pairs - int(st.iter_hist[0]) if w["kind"].startswith("ECP") else st.pairs
+    mean_evals = st.solver_evals / max(solved, 1)
     tf = timed_forces(g, torch, stream, pp, 20, flush)
     t_force = statistics.median(tf)
     peak32 = g.peak_fma(False)
-    flops = pair_flops(w["kind"], st.pairs, st.solver_evals, mean_evals, support=solver == "support")
+    flops = pair_flops(w["kind"], st.pairs, st.solver_evals, mean_evals, support=solver == "support",
+                       solved=solved)
     achieved = flops / t_force / 1e12
 
     # e2e: FP64 host arrays in and out through the C ABI every step
@@ -449,7 +463,8 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
         extras["force_kernel_pair_evals_per_s"] = npairs / t_force
         extras["force_kernel_ms"] = 1e3 * t_force
         if w["kind"].startswith("ECP"):
-            extras["newton_mean_evals_per_pair"] = mean_evals
+            extras["newton_mean_evals_per_solved_pair"] = mean_evals
+            extras["pairs_solved_frac"] = solved / max(st.pairs, 1)
             extras["newton_iter_hist"] = [int(x) for x in st.iter_hist]
             extras["newton_fp64_refined_frac"] = st.fp64_refined / max(st.pairs, 1)
             extras["nonconverged"] = int(st.nonconverged)
@@ -460,8 +475,10 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
         extras["list_rebuilds_in_timed_region"] = int(builds)
         extras["stage_ms_in_graph"] = g.step_stage_times(20)
         ecp = w["kind"].startswith("ECP")
-        extras["autotune"] = {"pick": {"block": tune.block, ("split" if ecp else "filter"): tune.filter},
-                              "variant_ms": tune_variants(tune, ecp)}
+        pick = {"block": tune.block, "filter": tune.filter}
+        if ecp:
+            pick["path"] = {0: "fused", 1: "split", 2: "support_filtered"}[tune.filter]
+        extras["autotune"] = {"pick": pick, "variant_ms": tune_variants(tune, ecp)}
         extras["force_error_vs_fp64"] = force_error_vs_fp64(g, w, pp)
         if name == "ecp" and a.solver in ("newton", "support"):
             # Newton from lambda = 1/2 on the same list (the support start is the headline)
@@ -471,7 +488,7 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
                 th = statistics.median(timed_forces(g, torch, stream, ph, 10, flush))
                 extras["newton_half_start"] = {
                     "force_kernel_ms": 1e3 * th, "pair_evals_per_s": npairs / th,
-                    "mean_evals_per_pair": sth.solver_evals / max(sth.pairs, 1),
+                    "mean_evals_per_solved_pair": sth.solver_evals / max(sth.pairs - int(sth.iter_hist[0]), 1),
                     "iter_hist": [int(x) for x in sth.iter_hist]}
             # residual check variants of the same kernel
             for mode, mname in ((2, "double_float"), (0, "none")):
@@ -488,7 +505,7 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
             extras["brent_mean_evals_per_pair"] = stb.solver_evals / max(stb.pairs, 1)
             extras["nh_modes"] = nh_modes(g, w, pp, torch, stream, flush)
             if not a.no_mlp:
-                extras["mlp"] = mlp_leg(a, g, w, torch, stream, flush, npairs)
+                extras["mlp"] = mlp_leg(a, g, w, torch, stream, flush, npairs, tune)
 
     cpu = None
     if rank == 0:
@@ -534,11 +551,15 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
 
 def tune_variants(tune, ecp=False):
     """The autotuner's timed launch variants, by block size and range filter
-    (ECP: the one-kernel path or the split Newton path)."""
+    (ECP: the one-kernel path, the split Newton path, or the one kernel behind
+    the support-function range test)."""
     shapes = ((256, 0), (128, 0), (256, 1), (128, 1), (64, 0), (64, 1))
     if tune.candidates == 3:
         shapes = ((256, 0), (128, 0), (64, 0))
-    tag = (lambda f: "split" if f else "fused") if ecp else (lambda f: f"f{f}")
+    if tune.candidates == 8:
+        shapes = ((256, 2), (128, 2), (256, 0), (128, 0), (256, 1), (128, 1), (64, 2), (64, 0))
+    names = {0: "fused", 1: "split", 2: "support_filtered"}
+    tag = (lambda f: names[f]) if ecp else (lambda f: f"f{f}")
     return {f"b{b}_{tag(f)}": float(tune.ms[k]) for k, (b, f) in enumerate(shapes[:tune.candidates])}
 
 
@@ -1483,7 +1504,7 @@ def profile_case(a):
         g, _, _ = make_system(w)
         p = pair_params(g, w, a.solver if a.solver in ("newton", "support") else "newton")
         if a.ecp_path:
-            g.set_launch(p.kind, 256, 1 if a.ecp_path == "split" else 0)
+            g.set_launch(p.kind, 256, {"fused": 0, "split": 1, "filtered": 2}[a.ecp_path])
     elif case in ("gb", "langevin", "gb_list"):
         w = WORKLOADS["gb"]
         g, _, _ = make_system(w)

@@ -105,7 +105,9 @@ typedef struct {
     int64_t fallbacks;      /* MLP path: pairs that fell back to the plain Newton;
                                GB kinds: pairs evaluated in the near-contact class
                                (contact distance in double-float)                */
-    int64_t iter_hist[24];  /* Newton iterations per pair (last bin: >= 23)         */
+    int64_t iter_hist[24];  /* Newton iterations per pair (last bin: >= 23); bin 0:
+                               pairs the support-filtered launch turned away
+                               unsolved (beyond any contact)                       */
     int64_t fp64_refined;   /* Newton: pairs that needed the FP64-residual correction */
 } sg_ecp_stats;
 
@@ -203,7 +205,9 @@ int sg_pair_forces_async(sg_ctx* ctx, const sg_pair_params* params);
 /* Device accumulators: pot_eng, pair virial, kin_eng, kin_rot (FP64). */
 int sg_read_energies(sg_ctx* ctx, double out[4]);
 /* Per-pair contact parameter of the last ECP call, in the device list order
- * that sg_nlist_pairs returns (debug / parity). */
+ * that sg_nlist_pairs returns (debug / parity). After a call with the
+ * support-filtered launch (sg_pair_set_launch filter 2), pairs that it did not
+ * solve read NaN. */
 int sg_ecp_lambda(sg_ctx* ctx, float* lam, int64_t capacity);
 
 /* ---- integrators (fortran/integrators.f90) ----------------------------------- */
@@ -433,14 +437,18 @@ typedef struct {
     int32_t filter;      /* chosen: 1 = range filter + per-warp in-range queue;
                             2 = Gay-Berne replicas: one replica per block, its
                             records staged in shared memory (replaces (256, 0));
-                            ECP kinds: 1 = split Newton path (solve kernel, then
-                            force kernel), 0 = one kernel per pair              */
+                            ECP kinds: 0 = one kernel per pair, 1 = split Newton
+                            path (solve kernel, then force kernel), 2 = one
+                            kernel behind the support-function range test (pairs
+                            beyond h_A + h_B + reach - sigma are not solved)   */
     int32_t candidates;  /* variants timed (ms[0..candidates-1])                 */
     int32_t reserved;
     float ms[8];         /* mean launch time of the variants (block, filter), in
                             order (256,0) (128,0) (256,1) (128,1) (64,0) (64,1);
-                            GB replicas: (256,2) in place of (256,0); kinds
-                            without the second axis: (256,0) (128,0) (64,0)  */
+                            GB replicas: (256,2) in place of (256,0); ECP with a
+                            Newton solver: (256,2) (128,2) (256,0) (128,0)
+                            (256,1) (128,1) (64,2) (64,0); kinds without the
+                            second axis: (256,0) (128,0) (64,0)              */
 } sg_tune_result;
 /* Time each launch variant of the params' pair kernel on the current list
  * (reps launches each), keep the fastest for this context's (kind, size,
@@ -448,8 +456,9 @@ typedef struct {
  * Captured steps are re-captured at their next sg_step. */
 int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* params, int32_t reps, sg_tune_result* out);
 /* Set a launch variant by hand (block 64, 128 or 256; filter 0, 1, or 2 for
- * the Gay-Berne replica tiles; for ECP kinds, filter selects the split Newton
- * path, which the Brent solver ignores). */
+ * the Gay-Berne replica tiles; for ECP kinds, filter 1 selects the split
+ * Newton path and 2 the support-filtered one kernel, both of which the Brent
+ * solver ignores). */
 int sg_pair_set_launch(sg_ctx* ctx, int32_t kind, int32_t block, int32_t filter);
 
 /* Measured FP32 (fp64 = 0) or FP64 (fp64 = 1) FMA throughput of this GPU in

@@ -412,6 +412,10 @@ int sg_mlp_features(sg_ctx* ctx, void* x_bf16, float* y, int64_t capacity, int64
     int64_t k = 0;
     if (int rc = sg_nlist_count(ctx, &k)) return rc;
     if (!ctx->ecp_lambda) return sg_fail(ctx, SG_ENOTREADY, "no ECP call has produced lambda yet");
+    if (ctx->ecp_lambda_partial)
+        return sg_fail(ctx, SG_ENOTREADY,
+                       "the last ECP call used the support-filtered launch, which leaves lambda of the pairs it "
+                       "does not solve unset: select another launch (sg_pair_set_launch filter 0) to collect samples");
     const float3 box = make_float3((float)ctx->box[0], (float)ctx->box[1], (float)ctx->box[2]);
     const float3 ib = make_float3((float)(1.0 / ctx->box[0]), (float)(1.0 / ctx->box[1]), (float)(1.0 / ctx->box[2]));
     const long long n = std::min<long long>(k, capacity);

@@ -273,6 +273,16 @@ struct PairQueues {
             const unsigned k2m = __ballot_sync(0xffffffffu, cls == 2);
             if (lane == 0 && k2m) atomicAdd(&sh_stats[3], (unsigned long long)__popc(k2m));
         }
+        if constexpr (Pot::kStats) {
+            // solver statistics (ECP): a pair turned away counts as listed with
+            // no solve (iteration bin 0), and the potential is told of it
+            const unsigned rm = vm & ~km;
+            if (lane == 0 && rm) {
+                atomicAdd(&sh_stats[0], (unsigned long long)__popc(rm));
+                atomicAdd(&sh_stats[4], (unsigned long long)__popc(rm));
+            }
+            if (valid && cls == 0) pot.filtered_out(t);
+        }
         push(0, cls == 1, t, i, j, rr);
         if constexpr (k2) push(1, cls == 2, t, i, j, rr);
         if (qn[0] >= 32) drain<0>(32, L, pot, es, sh_stats);

@@ -387,15 +387,36 @@ struct PotECP {
     static constexpr bool kTorque = true;
     static constexpr bool kStats = true;
     static constexpr bool kCountActive = false;
-    static constexpr bool kFilterable = false;
+    // the Newton solvers take the support-function range test (in_range)
+    static constexpr bool kFilterable = SOLVER == SG_SOLVER_NEWTON || SOLVER == SG_SOLVER_NEWTON_SUPPORT;
+    static constexpr bool kExactFilter = false;
     static constexpr int kMinBlocks =
         (SOLVER == SG_SOLVER_NEWTON || SOLVER == SG_SOLVER_NEWTON_SUPPORT || SOLVER == SOLVER_MLP_PRE)
             ? SG_ECP_MIN_BLOCKS
         : SOLVER == SOLVER_GIVEN                                ? SG_ECP_FORCE_MIN_BLOCKS
                                                                 : 1;
-    static constexpr int kMinBlocksFiltered = 1;   // not filterable
+    static constexpr int kMinBlocksFiltered = SG_ECP_MIN_BLOCKS;
     int prefiltered;
-    SG_DEV bool in_range(int, int) const { return true; }
+    // Range test of the filtered launch, a superset of the pairs eval keeps.
+    // The Perram-Wertheim contact distance along r is at most h_A + h_B, the
+    // two ellipsoids' support functions along r (h_X = sqrt(r.X r) / |r| with
+    // X = U^T S^2 U): at that separation a plane normal to r separates them.
+    // A pair with |r| >= h_A + h_B + (reach - sigma) is inactive in eval, and
+    // skips the contact solve. The bound is widened by 2e-4 relative + 1e-4
+    // for the FP32 rounding of r, h and sigma; NaN keeps the pair.
+    SG_DEV bool in_range(int i, int j) const {
+        const float3 r = pair_rij(pos, i, j, b);
+        const float4 a0 = prep[4 * i], a1 = prep[4 * i + 1], b0 = prep[4 * j], b1 = prep[4 * j + 1];
+        const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
+        const float B[6] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y};
+        const float rsq = dot3(r, r);
+        const float hs = (sqrtf(dot3(r, symv(A, r))) + sqrtf(dot3(r, symv(B, r)))) * rsqrtf(rsq);
+        return !(rsq * rsqrtf(rsq) >= (hs + reach_extra) * 1.0002f + 1e-4f);
+    }
+    // a listed pair that in_range turned away: its lambda reads NaN (not solved)
+    SG_DEV void filtered_out(int t) const {
+        if (lam_out) lam_out[t] = __int_as_float(0x7fc00000);
+    }
     const float4* __restrict__ pos;
     const float4* __restrict__ quat;
     const float4* __restrict__ shape;
@@ -407,6 +428,7 @@ struct PotECP {
     double bx, by, bz;
     int kind, mu, nu, max_iter, fp64_check;
     float cutoff, wf, chirality, tol, step_tol;
+    float reach_extra;   // reach - sigma: cutoff - 1 (+ wf welded), 0 for the repulsive kind
     bool weld, chiral, rep;
 
     SG_DEV void eval(bool valid, int i, int j, int t, PairOut& o, unsigned long long* sh) const;
@@ -805,6 +827,11 @@ int launch_ecp(sg_ctx* ctx, const sg_pair_params* p, int mu, int nu) {
     pot.weld = (p->kind == SG_ECPW || p->kind == SG_ECPWC);
     pot.chiral = (p->kind == SG_ECPC || p->kind == SG_ECPWC);
     pot.rep = (p->kind == SG_ECPR);
+    pot.reach_extra = pot.rep ? 0.f : pot.cutoff - 1.f + (pot.weld ? pot.wf : 0.f);
+    const PairTune tune = sg_pair_tune_for(ctx, p->kind, false);
+    // the support-filtered launch (tune.filter 2) leaves lambda unset (NaN)
+    // for the pairs it does not solve
+    ctx->ecp_lambda_partial = PotECP<SOLVER>::kFilterable && tune.filter == 2;
     return launch_pair(ctx, pot, p->kind);
 }
 
@@ -837,7 +864,9 @@ int sg_launch_pair_ecp(sg_ctx* ctx, const sg_pair_params* p) {
         SG_CUDA(ctx, cudaMalloc(&ctx->ecp_lambda, sizeof(float) * (size_t)ctx->nl.pair_capacity));
         ctx->ecp_lambda_cap = ctx->nl.pair_capacity;
     }
-    const bool split = sg_pair_tune_for(ctx, p->kind, false).filter != 0;
+    // launch shape, second axis: 0 one kernel, 1 split (solve, then forces),
+    // 2 one kernel behind the support-function range test (Newton solvers)
+    const bool split = sg_pair_tune_for(ctx, p->kind, false).filter == 1;
     switch (p->solver) {
         case SG_SOLVER_BRENT_COMPAT: return launch_ecp<SG_SOLVER_BRENT_COMPAT>(ctx, p, mu, nu);
         case SG_SOLVER_NEWTON:

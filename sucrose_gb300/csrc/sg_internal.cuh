@@ -167,6 +167,7 @@ struct sg_ctx {
     int* gb_tile_order = nullptr;
     int gb_tile_count = 0;
     int gb_tile_maxn = 0;
+    int ecp_lambda_partial = 0;      // the last ECP call left lambda unset (NaN) for unsolved pairs
     int step_fused = 0;
     int step_events = 0;             // the step is captured with event nodes between its stages
     int step_prep_kind = 0;          // SG_PREP_NONE / _ECP / _GB (step_epi.cuh)

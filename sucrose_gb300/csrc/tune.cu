@@ -4,7 +4,8 @@
 // the kernel filters the list first and evaluates only the in-range pairs,
 // 32 per warp; for the ECP kinds with a Newton solver the second axis is the
 // split path (a solve kernel, then a force kernel from the stored lambda)
-// against the one kernel that solves and evaluates each pair. Gay-Berne
+// against the one kernel that solves and evaluates each pair, and the one
+// kernel behind the support-function range test (filter 2). Gay-Berne
 // replicas add the replica tiles (records staged in shared memory per
 // replica), which take the place of the unfiltered 256-thread variant. The best variant depends on the potential, the share of
 // listed pairs that are in range and the system size, so it is measured on
@@ -69,17 +70,21 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
     cudaEventCreate(&e1);
     const long long key = tune_key(ctx, p->kind);
     const bool tiles = ctx->nrep && p->kind >= SG_GB && p->kind < SG_ECP;
-    // block size 256, 128 or 64 x the second axis (range filter; ECP: split path)
+    const bool ecp = p->kind >= SG_ECP && filterable;
+    // block size 256, 128 or 64 x the second axis (range filter; ECP: split
+    // path, support-filtered kernel)
     const PairTune cand[6] = {{256, tiles ? 2 : 0}, {128, 0}, {256, 1}, {128, 1}, {64, 0}, {64, 1}};
+    const PairTune cand_ecp[8] = {{256, 2}, {128, 2}, {256, 0}, {128, 0}, {256, 1}, {128, 1}, {64, 2}, {64, 0}};
     const int order_unfiltered[3] = {0, 1, 4};
-    const int ncand = filterable ? 6 : 3;
+    const int ncand = ecp ? 8 : filterable ? 6 : 3;
     float best = 1e30f;
-    PairTune pick = cand[0];
+    PairTune pick = ecp ? cand_ecp[0] : cand[0];
     int rc = SG_OK;
     sg_tune_result res{};
     for (int v = 0; v < ncand && !rc; ++v) {
         const int c = filterable ? v : order_unfiltered[v];
-        ctx->tune[key] = cand[c];
+        const PairTune tv = ecp ? cand_ecp[v] : cand[c];
+        ctx->tune[key] = tv;
         rc = sg_pair_forces_async(ctx, p);   // warm-up (allocations, caches)
         float tot = 0.f;
         for (int k = 0; k < reps && !rc; ++k) {
@@ -95,7 +100,7 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
         res.ms[v] = ms;
         if (!rc && ms < best) {
             best = ms;
-            pick = cand[c];
+            pick = tv;
         }
     }
     ctx->tune[key] = pick;

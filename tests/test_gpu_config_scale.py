@@ -60,9 +60,10 @@ def test_isotropic_placement(lib, sig, density):
     assert not np.array_equal(r, other)
 
 
-def full_size(w, kind, solver=None, mu=None, nu=None, squeeze=1.0):
+def full_size(w, kind, solver=None, mu=None, nu=None, squeeze=1.0, launch=None):
     """The benchmark's placed state (positions and box scaled by `squeeze`,
-    so that repulsive pairs overlap), its list and forces on both sides."""
+    so that repulsive pairs overlap), its list and forces on both sides.
+    launch: (block, filter) of the pair kernel (sg_pair_set_launch)."""
     r, q, box, rep = configs.isotropic_placement(w["n"], w["sig"], w["density"], seed=w["seed"])
     assert rep.overlaps == 0
     P = Pair(r * squeeze, q, box * squeeze, sig=w["sig"], eps=w["eps"])
@@ -72,6 +73,8 @@ def full_size(w, kind, solver=None, mu=None, nu=None, squeeze=1.0):
     assert len(gpi) == len(opi)
     assert np.array_equal(gpi, opi) and np.array_equal(gpj, opj)
     kw = {} if mu is None else {"mu": mu, "nu": nu}
+    if launch is not None:
+        P.g.set_launch(getattr(capi, kind), *launch)
     P.g.zero_forces()
     pe, _ = P.g.pair_forces(P.g.params(getattr(capi, kind), cutoff=w["cutoff"],
                                        **({"solver": solver} if solver is not None else {}), **kw))
@@ -90,10 +93,12 @@ def test_gay_berne_full_size_list_and_forces(lib):
     assert abs(pe - peo) <= 1e-5 * abs(peo)
 
 
-@pytest.mark.parametrize("solver", [capi.SOLVER_NEWTON, capi.SOLVER_NEWTON_SUPPORT], ids=["half", "support"])
-def test_ecp_full_size_list_and_forces(lib, solver):
-    # positions and box 3 % closer: tens of thousands of pairs in contact
-    npairs, F, T, pe, Fo, To, peo, active = full_size(ECP, "ECPR", solver=solver, squeeze=0.97)
+@pytest.mark.parametrize("solver,filt", [(capi.SOLVER_NEWTON, 0), (capi.SOLVER_NEWTON_SUPPORT, 0),
+                                         (capi.SOLVER_NEWTON_SUPPORT, 2)], ids=["half", "support", "support_filtered"])
+def test_ecp_full_size_list_and_forces(lib, solver, filt):
+    # positions and box 3 % closer: tens of thousands of pairs in contact;
+    # filt 2: the support-function range test in front of the solve
+    npairs, F, T, pe, Fo, To, peo, active = full_size(ECP, "ECPR", solver=solver, squeeze=0.97, launch=(256, filt))
     assert npairs > 400_000 and active > 10_000
     assert rel(F, Fo) < 1e-5
     assert rel(T, To) < 1e-5

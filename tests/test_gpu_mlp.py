@@ -63,6 +63,33 @@ def test_inference_kernel_matches_training_forward(lib):
     assert np.max(np.abs(pred - inf)) < 2e-3
 
 
+def test_features_refused_after_support_filtered_call(lib):
+    """The support-filtered launch leaves lambda unset for the pairs it does
+    not solve: collecting training samples after it is refused, and works
+    again after a call that solves every pair."""
+    import ctypes as C
+    import torch
+    P = small_ecp(seed=5)
+    g = P.g
+    p = g.params(capi.ECPR, solver=capi.SOLVER_NEWTON)
+    k = g.npairs()
+    X = torch.empty((k, 16), dtype=torch.bfloat16, device="cuda")
+    y = torch.empty(k, dtype=torch.float32, device="cuda")
+    cnt = C.c_int64(0)
+    feats = lambda: g.L.sg_mlp_features(g.ctx, C.c_void_p(X.data_ptr()), C.c_void_p(y.data_ptr()), k,
+                                        C.byref(cnt))
+    g.set_launch(capi.ECPR, 256, 2)
+    g.zero_forces()
+    g.pair_forces(p)
+    assert np.isnan(g.ecp_lambda()).any()
+    assert feats() == capi.SG_ENOTREADY
+    g.set_launch(capi.ECPR, 256, 0)
+    g.zero_forces()
+    g.pair_forces(p)
+    assert feats() == capi.SG_OK and cnt.value == k
+    assert not np.isnan(y.cpu().numpy()).any()
+
+
 def test_tensor_core_guess_matches_warp_mma_guess(lib):
     """tcgen05 pass (TMEM accumulators) against the warp-level mma.sync path and
     the training forward: the same BF16 operands and FP32 accumulation, so the

@@ -63,11 +63,12 @@ ECP_KINDS = [(capi.ECP, O.ECP, {}), (capi.ECPR, O.ECPR, {}), (capi.ECPW, O.ECPW,
 
 
 @pytest.mark.parametrize("kd,ko,kw", ECP_KINDS)
-@pytest.mark.parametrize("split", [1, 0], ids=["split", "fused"])
+@pytest.mark.parametrize("split", [1, 0, 2], ids=["split", "fused", "filtered"])
 @pytest.mark.parametrize("check", [1, 2], ids=["fp64", "double_float"])
 def test_ecp_newton_vs_converged_fp64(lib, kd, ko, kw, split, check):
-    # split: Newton solve kernel, then the force kernel from its lambda (the
-    # default); fused: one kernel solves and evaluates each pair
+    # split: Newton solve kernel, then the force kernel from its lambda; fused:
+    # one kernel solves and evaluates each pair; filtered: the same behind the
+    # support-function range test
     P = ecp_state()
     P.g.set_launch(kd, 256, split)
     pdev = P.g.params(kd, cutoff=3.0, solver=capi.SOLVER_NEWTON, **kw)
@@ -81,7 +82,7 @@ def test_ecp_newton_vs_converged_fp64(lib, kd, ko, kw, split, check):
 
 
 @pytest.mark.parametrize("kd,ko,kw", ECP_KINDS)
-@pytest.mark.parametrize("split", [1, 0], ids=["split", "fused"])
+@pytest.mark.parametrize("split", [1, 0, 2], ids=["split", "fused", "filtered"])
 def test_ecp_newton_support_start_vs_converged_fp64(lib, kd, ko, kw, split):
     # Newton from the support-function start: same tolerance, same bound
     P = ecp_state(seed=5)
@@ -92,6 +93,55 @@ def test_ecp_newton_support_start_vs_converged_fp64(lib, kd, ko, kw, split):
     assert rel(F, Fo) < TOL and rel(T, To) < TOL
     assert abs(pe - peo) <= TOL * max(abs(peo), 1e-12)
     assert st.nonconverged == 0 and st.pairs == len(P.o.pairs(3.0, 0.3)[0])
+
+
+def _support_sum(P, pi, pj):
+    """h_A + h_B along r_ij in FP64: the ellipsoids' support functions, with the
+    body axes as the rows of the rotation matrix of each quaternion."""
+    w, x, y, z = P.q.T.astype(np.float64)
+    R = np.stack([np.stack([w * w + x * x - y * y - z * z, 2 * (x * y + w * z), 2 * (x * z - w * y)], -1),
+                  np.stack([2 * (x * y - w * z), w * w - x * x + y * y - z * z, 2 * (y * z + w * x)], -1),
+                  np.stack([2 * (x * z + w * y), 2 * (y * z - w * x), w * w - x * x - y * y + z * z], -1)], 1)
+    d = P.r[pj].astype(np.float64) - P.r[pi].astype(np.float64)
+    d -= np.round(d / P.box) * P.box
+    rm = np.linalg.norm(d, axis=1)
+    n = d / rm[:, None]
+    semi = 0.5 * np.asarray(ECP_SIG)
+    h = lambda k: np.linalg.norm(semi * np.einsum("mij,mj->mi", R[k], n), axis=1)
+    return rm, h(pi) + h(pj)
+
+
+@pytest.mark.parametrize("kd,extra", [(capi.ECPR, 0.0), (capi.ECP, 2.0)], ids=["ecpr", "ecp"])
+def test_ecp_support_filter(lib, kd, extra):
+    """The support-filtered launch: the same forces as the launch that solves
+    every pair; the pairs it turns away are beyond h_A + h_B + (reach - sigma)
+    in FP64, count in iteration bin 0 and read NaN as lambda; the others carry
+    the lambda of the full launch."""
+    P = ecp_state(seed=8)
+    P.g.init_nlist(0.3, 3.0)
+    p = P.g.params(kd, cutoff=3.0, solver=capi.SOLVER_NEWTON_SUPPORT)
+    out = {}
+    for filt in (0, 2):
+        P.g.set_launch(kd, 256, filt)
+        P.g.zero_forces()
+        pe, _, st = P.g.pair_forces(p, want_stats=True)
+        out[filt] = (pe, *P.g.forces(), st, P.g.ecp_lambda().astype(np.float64))
+    pe0, F0, T0, st0, lam0 = out[0]
+    pe2, F2, T2, st2, lam2 = out[2]
+    assert np.linalg.norm(F0) > 0
+    assert rel(F2, F0) < 3e-6 and rel(T2, T0) < 3e-6
+    assert abs(pe2 - pe0) <= 1e-6 * max(abs(pe0), 1e-12)
+    k = P.g.npairs()
+    away = np.isnan(lam2)
+    assert st0.pairs == st2.pairs == k and st0.iter_hist[0] == 0
+    # repulsive kind: contact only, most listed pairs are beyond the bound;
+    # cutoff 3 (reach = sigma + 2): few are
+    assert st2.iter_hist[0] == away.sum() and (0.3 * k if kd == capi.ECPR else 0) <= away.sum() < k
+    assert sum(st2.iter_hist) == k and st2.solver_evals < st0.solver_evals
+    assert np.max(np.abs(lam2[~away] - lam0[~away])) < 1e-6
+    pi, pj = P.g.raw_pairs()
+    rm, hs = _support_sum(P, pi, pj)
+    assert np.all(rm[away] >= hs[away] + extra)
 
 
 def test_ecp_support_start_saves_evaluations(lib):

@@ -1,7 +1,8 @@
 """Launch variants of the pair kernels and the autotuner.
 
-Every variant (block 128 / 256, with or without the range filter; for ECP,
-the split Newton path or the one-kernel path) must give
+Every variant (block 64 / 128 / 256, with or without the range filter; for
+ECP, the split Newton path, the one-kernel path or the one kernel behind the
+support-function range test) must give
 the same forces, torques and energies (only the order of float atomics
 differs), the same listed / in-range counts, and the autotuner must leave the
 caller's forces and accumulators as they were."""
@@ -13,6 +14,7 @@ from sucrose_gb300 import GpuSystem, capi, configs
 
 pytestmark = pytest.mark.gpu
 VARIANTS = [(256, 0), (128, 0), (256, 1), (128, 1), (64, 0), (64, 1)]
+ECP_VARIANTS = VARIANTS + [(256, 2), (128, 2), (64, 2)]
 
 
 def lj_system():
@@ -35,7 +37,8 @@ def gb_system(kind=capi.GB, sig=(1.0, 1.0, 3.0)):
 
 
 def ecp_system():
-    r, q, box = ellipsoids((6, 8, 12), (3.0, 2.0, 1.0), 0.1114, seed=3, tilt=0.4)
+    # a compressed lattice (density 0.13): pairs in contact for the repulsive kind
+    r, q, box = ellipsoids((6, 8, 12), (3.0, 2.0, 1.0), 0.13, seed=3, tilt=0.4)
     g = GpuSystem(len(r), box)
     g.set_particles(sig=(3.0, 2.0, 1.0))
     g.upload(r=f32(r), q=f32(q))
@@ -61,10 +64,15 @@ def test_variants_agree(lib, make):
         assert ref[4][0] == g.npairs() and ref[4][1] >= ref[4][0]
     else:                    # solver_evals: pairs in range
         assert ref[4][0] == g.npairs() and 0 < ref[4][1] <= ref[4][0]
-    for v in VARIANTS[1:]:
+    ecp = p.kind >= capi.ECP
+    if ecp:
+        assert np.linalg.norm(ref[2]) > 0
+    for v in (ECP_VARIANTS if ecp else VARIANTS)[1:]:
         pe, vir, F, T, counts = forces_with(g, p, *v)
-        # the filter's range test and eval's may round differently on the boundary
-        assert counts[0] == ref[4][0] and abs(counts[1] - ref[4][1]) <= 2, v
+        if ecp and v[1] == 2:   # the support filter: fewer pairs solved
+            assert counts[0] == ref[4][0] and counts[1] < ref[4][1], v
+        else:   # the filter's range test and eval's may round differently on the boundary
+            assert counts[0] == ref[4][0] and abs(counts[1] - ref[4][1]) <= 2, v
         assert abs(pe - ref[0]) <= 1e-6 * max(1.0, abs(ref[0])), v
         assert abs(vir - ref[1]) <= 1e-6 * max(1.0, abs(ref[1])), v
         # float atomics in another order: ~1e-7 per pair force, amplified where
@@ -92,6 +100,22 @@ def test_autotune_restores_state(lib):
     pe = g.pair_forces(p)[0]
     F2, _ = g.forces()
     assert rel(F2, F0) < 1e-6
+    g.close()
+
+
+def test_autotune_ecp_variants(lib):
+    """ECP with a Newton solver: eight variants (the support-filtered kernel,
+    the one kernel, the split path), the state restored."""
+    g, p = ecp_system()
+    p.solver = capi.SOLVER_NEWTON_SUPPORT
+    g.zero_forces()
+    g.pair_forces(p)
+    F0, T0 = g.forces()
+    res = g.autotune(p, reps=2)
+    assert res.candidates == 8 and res.block in (64, 128, 256) and res.filter in (0, 1, 2)
+    assert all(res.ms[k] > 0 for k in range(8))
+    F1, T1 = g.forces()
+    assert np.array_equal(F0, F1) and np.array_equal(T0, T1)
     g.close()
 
 
