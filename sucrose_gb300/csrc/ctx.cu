@@ -109,7 +109,8 @@ int sg_destroy(sg_ctx* ctx) {
     void* bufs[] = {ctx->pos, ctx->quat, ctx->vel, ctx->angm, ctx->force, ctx->torque, ctx->shape, ctx->eshape,
                     ctx->inert, ctx->inert_inv, ctx->acc, ctx->partials, ctx->done_counter, ctx->stats, ctx->nh,
                     ctx->ecp_prep, ctx->ecp_prep64, ctx->ecp_lambda, ctx->mlp_w, ctx->mlp_wbf16, ctx->mlp_tc_err,
-                    ctx->rf_dip, ctx->rf_mark, ctx->rf_cnt, ctx->rf_field, ctx->mc_scratch, ctx->gb_tile_order};
+                    ctx->rf_dip, ctx->rf_mark, ctx->rf_cnt, ctx->rf_field, ctx->mc_scratch, ctx->gb_tile_order,
+                    ctx->pair_surv};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);

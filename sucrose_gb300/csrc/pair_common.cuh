@@ -70,6 +70,11 @@ struct PairLaunch {
     double* acc;                 // per-call sums: acc[0] += PE, acc[1] += virial
     double* acc_total;           // running sums since the last zero_forces
     unsigned long long* stats;   // solver statistics (ECP) or listed / in-range counts (LJ, GB)
+    // two-pass filtered launch (k_pair_compact): pair_i / pair_j are the
+    // compacted pairs, tmap[v] the list storage index of compacted pair v, and
+    // the block that finishes last zeroes *count_reset (the compacted count)
+    const int* tmap;
+    int* count_reset;
 };
 
 // Storage index and particles of lane `lane`'s pair in the 32-pair chunk that
@@ -89,6 +94,7 @@ SG_DEV void pair_fetch(const PairLaunch& L, int base, int lane, int np, int b0, 
         }
         i = L.pair_i[t];
         j = L.pair_j[t];
+        if (L.tmap) t = L.tmap[t];
     }
 }
 
@@ -343,7 +349,83 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFil
             if (sh_stats[k]) atomicAdd(&L.stats[k], sh_stats[k]);
     }
     const float e[2] = {es.pe, es.vir}, elo[2] = {es.pe_lo, es.vir_lo};
-    block_reduce_finish_f<2>(e, L.partials, L.done, L.acc, L.acc_total, elo);
+    if (block_reduce_finish_f<2>(e, L.partials, L.done, L.acc, L.acc_total, elo) && L.count_reset &&
+        threadIdx.x == 0)
+        *L.count_reset = 0;   // every block has read the compacted count
+}
+
+// First pass of the two-pass filtered launch: the range test of every listed
+// pair, and the pairs that pass written in list order to (tmap, ci, cj) from
+// *count on, one atomic per block and round (a round: blockDim.x * P
+// consecutive pairs, P per thread, whose index loads and gathers are in
+// flight together). A round's pairs stay together and in row order, so the
+// second pass, k_pair over the compacted pairs, keeps the segmented scatter's
+// locality and every lane of its warps busy. Pairs turned away are counted as
+// listed with no solve (stats[0], stats[4]) and handed to the potential's
+// filtered_out. 256 threads: the round's 8 x P warp counts fit one warp scan.
+constexpr int SG_COMPACT_P = 4;
+template <class Pot>
+__global__ void __launch_bounds__(256) k_pair_compact(PairLaunch L, Pot pot, int* __restrict__ count,
+                                                     int* __restrict__ tmap, int* __restrict__ ci,
+                                                     int* __restrict__ cj) {
+    constexpr int P = SG_COMPACT_P;
+    static_assert(8 * P <= 32, "one warp scans the round's counts");
+    __shared__ int sh_n[8 * P];
+    __shared__ unsigned long long sh_away;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) sh_away = 0ull;
+    const int np = *L.npairs;
+    unsigned away = 0;
+    const int per_round = 256 * P;
+    for (int base0 = blockIdx.x * per_round; base0 < np; base0 += gridDim.x * per_round) {   // block-uniform
+        int t[P], i[P], j[P];
+        bool valid[P];
+#pragma unroll
+        for (int k = 0; k < P; ++k) pair_fetch(L, base0 + (warp * P + k) * 32, lane, np, 0, t[k], i[k], j[k], valid[k]);
+        unsigned km[P];
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            const bool keep = valid[k] && pot.in_range(i[k], j[k]);
+            km[k] = __ballot_sync(full, keep);
+            const unsigned vm = __ballot_sync(full, valid[k]);
+            if (valid[k] && !keep) pot.filtered_out(t[k]);
+            away += __popc(vm & ~km[k]);
+            if (lane == 0) sh_n[warp * P + k] = __popc(km[k]);
+        }
+        __syncthreads();
+        if (warp == 0) {   // exclusive scan of the 8 P counts, one atomic for the round
+            const int c = sh_n[lane];
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(full, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int total = __shfl_sync(full, incl, 31);
+            int base = 0;
+            if (lane == 0 && total) base = atomicAdd(count, total);
+            base = __shfl_sync(full, base, 0);
+            sh_n[lane] = base + incl - c;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            if (km[k] & (1u << lane)) {
+                const int slot = sh_n[warp * P + k] + __popc(km[k] & ((1u << lane) - 1u));
+                tmap[slot] = t[k];
+                ci[slot] = i[k];
+                cj[slot] = j[k];
+            }
+        }
+        __syncthreads();   // sh_n is rewritten by the next round
+    }
+    if (lane == 0 && away) atomicAdd(&sh_away, (unsigned long long)away);
+    __syncthreads();
+    if (threadIdx.x == 0 && sh_away) {
+        atomicAdd(&L.stats[0], sh_away);
+        atomicAdd(&L.stats[4], sh_away);
+    }
 }
 
 // Launch shape of the pair kernels: block size and the range filter. The
@@ -393,7 +475,44 @@ inline PairLaunch make_pair_launch(sg_ctx* ctx) {
     L.acc_total = ctx->acc;
     L.stats = ctx->stats;
     L.partials = nullptr;
+    L.tmap = nullptr;
+    L.count_reset = nullptr;
     return L;
+}
+
+// The two-pass filtered launch of a potential with a superset range test
+// (single systems): k_pair_compact, then k_pair over the compacted pairs. The
+// compacted arrays hold up to the list's pair capacity.
+template <class Pot>
+int launch_pair_two_pass(sg_ctx* ctx, Pot pot, int block) {
+    if (!ctx->nl.initialized) return sg_fail(ctx, SG_ENOTREADY, "pair forces need sg_nlist_init first");
+    PairLaunch L = make_pair_launch(ctx);
+    const int64_t cap = ctx->nl.pair_capacity;
+    if (ctx->pair_surv_cap < cap) {
+        ctx->graph_epoch++;
+        if (ctx->pair_surv) cudaFree(ctx->pair_surv);
+        ctx->pair_surv = nullptr;
+        ctx->pair_surv_cap = 0;
+        SG_CUDA(ctx, cudaMalloc(&ctx->pair_surv, sizeof(int) * (size_t)(32 + 3 * cap)));
+        SG_CUDA(ctx, cudaMemsetAsync(ctx->pair_surv, 0, sizeof(int) * 32, ctx->stream));
+        ctx->pair_surv_cap = cap;
+    }
+    int* count = ctx->pair_surv;
+    int* tmap = count + 32;
+    int* ci = tmap + cap;
+    int* cj = ci + cap;
+    pot.prefiltered = 0;
+    int grid = sg_grid_for(ctx, (const void*)k_pair_compact<Pot>, 256, 0);
+    const int64_t rounds = (cap + 256 * SG_COMPACT_P - 1) / (256 * SG_COMPACT_P);
+    if (grid > rounds) grid = (int)std::max<int64_t>(1, rounds);
+    k_pair_compact<Pot><<<grid, 256, 0, ctx->stream>>>(L, pot, count, tmap, ci, cj);
+    SG_LAUNCH_CHECK(ctx, "k_pair_compact");
+    L.pair_i = ci;
+    L.pair_j = cj;
+    L.npairs = count;
+    L.tmap = tmap;
+    L.count_reset = count;
+    return launch_pair_v<Pot, false>(ctx, L, pot, block);
 }
 
 // Launch helper: persistent grid sized from occupancy.

@@ -397,21 +397,31 @@ struct PotECP {
                                                                 : 1;
     static constexpr int kMinBlocksFiltered = SG_ECP_MIN_BLOCKS;
     int prefiltered;
-    // Range test of the filtered launch, a superset of the pairs eval keeps.
-    // The Perram-Wertheim contact distance along r is at most h_A + h_B, the
-    // two ellipsoids' support functions along r (h_X = sqrt(r.X r) / |r| with
-    // X = U^T S^2 U): at that separation a plane normal to r separates them.
-    // A pair with |r| >= h_A + h_B + (reach - sigma) is inactive in eval, and
-    // skips the contact solve. The bound is widened by 2e-4 relative + 1e-4
-    // for the FP32 rounding of r, h and sigma; NaN keeps the pair.
+    // Range test of the filtered launch, a superset of the pairs eval keeps,
+    // from two upper bounds on the Perram-Wertheim contact distance sigma:
+    //  (1) sigma <= h_A + h_B, the two ellipsoids' support functions along r
+    //      (h_X = sqrt(r.X r) / |r|, X = U^T S^2 U): at that separation a plane
+    //      normal to r separates them;
+    //  (2) sigma <= |r| / sqrt(F(l0)) for any l, F(l) = l(1-l) r.(A + l(B-A))^-1 r
+    //      the contact function whose maximum over l gives sigma = |r| / sqrt(F*);
+    //      taken at the support start l0 = h_A / (h_A + h_B), one evaluation.
+    // A pair with |r| >= bound + (reach - sigma) is inactive in eval and skips
+    // the contact solve. The bounds are widened (2e-4 and 1e-3 relative, 1e-4)
+    // for the FP32 rounding of r, h, F and sigma; NaN keeps the pair.
     SG_DEV bool in_range(int i, int j) const {
         const float3 r = pair_rij(pos, i, j, b);
         const float4 a0 = prep[4 * i], a1 = prep[4 * i + 1], b0 = prep[4 * j], b1 = prep[4 * j + 1];
         const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
         const float B[6] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y};
-        const float rsq = dot3(r, r);
-        const float hs = (sqrtf(dot3(r, symv(A, r))) + sqrtf(dot3(r, symv(B, r)))) * rsqrtf(rsq);
-        return !(rsq * rsqrtf(rsq) >= (hs + reach_extra) * 1.0002f + 1e-4f);
+        const float rsq = dot3(r, r), rinv = rsqrtf(rsq), rm = rsq * rinv;
+        const float ha = sqrtf(dot3(r, symv(A, r))), hb = sqrtf(dot3(r, symv(B, r)));   // |r| h_A, |r| h_B
+        if (rm >= ((ha + hb) * rinv + reach_extra) * 1.0002f + 1e-4f) return false;
+        const float l0 = ha / (ha + hb);
+        float g[6];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) g[m] = fmaf(l0, B[m] - A[m], A[m]);
+        const float F = l0 * (1.f - l0) * dot3(r, chol_solve(chol(g), r));
+        return !(rm >= (rm * rsqrtf(F) + reach_extra) * 1.001f + 1e-4f);
     }
     // a listed pair that in_range turned away: its lambda reads NaN (not solved)
     SG_DEV void filtered_out(int t) const {
@@ -832,6 +842,10 @@ int launch_ecp(sg_ctx* ctx, const sg_pair_params* p, int mu, int nu) {
     // the support-filtered launch (tune.filter 2) leaves lambda unset (NaN)
     // for the pairs it does not solve
     ctx->ecp_lambda_partial = PotECP<SOLVER>::kFilterable && tune.filter == 2;
+    // single systems: the range test in a pass of its own, then the contact
+    // solve over the compacted pairs; replica contexts: per-warp queues
+    if constexpr (PotECP<SOLVER>::kFilterable)
+        if (tune.filter == 2 && !ctx->nrep) return launch_pair_two_pass(ctx, pot, tune.block);
     return launch_pair(ctx, pot, p->kind);
 }
 

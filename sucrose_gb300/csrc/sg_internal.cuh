@@ -167,7 +167,9 @@ struct sg_ctx {
     int* gb_tile_order = nullptr;
     int gb_tile_count = 0;
     int gb_tile_maxn = 0;
-    int ecp_lambda_partial = 0;      // the last ECP call left lambda unset (NaN) for unsolved pairs
+    int ecp_lambda_partial = 0;
+    int* pair_surv = nullptr;        // two-pass filtered launch: count, then tmap, i, j of the compacted pairs
+    int64_t pair_surv_cap = 0;      // the last ECP call left lambda unset (NaN) for unsolved pairs
     int step_fused = 0;
     int step_events = 0;             // the step is captured with event nodes between its stages
     int step_prep_kind = 0;          // SG_PREP_NONE / _ECP / _GB (step_epi.cuh)

@@ -95,28 +95,31 @@ def test_ecp_newton_support_start_vs_converged_fp64(lib, kd, ko, kw, split):
     assert st.nonconverged == 0 and st.pairs == len(P.o.pairs(3.0, 0.3)[0])
 
 
-def _support_sum(P, pi, pj):
-    """h_A + h_B along r_ij in FP64: the ellipsoids' support functions, with the
-    body axes as the rows of the rotation matrix of each quaternion."""
+def _contact_distance(P, pi, pj, lam):
+    """|r_ij| and the contact distance sigma = |r| / sqrt(F(lambda)) along r_ij
+    in FP64, F(l) = l(1-l) r.((1-l)A + lB)^-1 r with A = R^T S^2 R (the body axes
+    as the rows of each quaternion's rotation matrix, S the semi-axes), at the
+    oracle's converged lambda."""
     w, x, y, z = P.q.T.astype(np.float64)
     R = np.stack([np.stack([w * w + x * x - y * y - z * z, 2 * (x * y + w * z), 2 * (x * z - w * y)], -1),
                   np.stack([2 * (x * y - w * z), w * w - x * x + y * y - z * z, 2 * (y * z + w * x)], -1),
                   np.stack([2 * (x * z + w * y), 2 * (y * z - w * x), w * w - x * x - y * y + z * z], -1)], 1)
+    S2 = np.diag((0.5 * np.asarray(ECP_SIG)) ** 2)
+    A = np.einsum("mki,kl,mlj->mij", R, S2, R)
     d = P.r[pj].astype(np.float64) - P.r[pi].astype(np.float64)
     d -= np.round(d / P.box) * P.box
     rm = np.linalg.norm(d, axis=1)
-    n = d / rm[:, None]
-    semi = 0.5 * np.asarray(ECP_SIG)
-    h = lambda k: np.linalg.norm(semi * np.einsum("mij,mj->mi", R[k], n), axis=1)
-    return rm, h(pi) + h(pj)
+    G = (1 - lam)[:, None, None] * A[pi] + lam[:, None, None] * A[pj]
+    F = lam * (1 - lam) * np.einsum("mi,mi->m", d, np.linalg.solve(G, d[:, :, None])[:, :, 0])
+    return rm, rm / np.sqrt(F)
 
 
-@pytest.mark.parametrize("kd,extra", [(capi.ECPR, 0.0), (capi.ECP, 2.0)], ids=["ecpr", "ecp"])
-def test_ecp_support_filter(lib, kd, extra):
-    """The support-filtered launch: the same forces as the launch that solves
-    every pair; the pairs it turns away are beyond h_A + h_B + (reach - sigma)
-    in FP64, count in iteration bin 0 and read NaN as lambda; the others carry
-    the lambda of the full launch."""
+@pytest.mark.parametrize("kd,ko,extra", [(capi.ECPR, O.ECPR, 0.0), (capi.ECP, O.ECP, 2.0)], ids=["ecpr", "ecp"])
+def test_ecp_support_filter(lib, kd, ko, extra):
+    """The filtered launch: the same forces as the launch that solves every
+    pair; the pairs its range test turns away are beyond sigma + (reach -
+    sigma) at the oracle's converged lambda, count in iteration bin 0 and read
+    NaN as lambda; the others carry the lambda of the full launch."""
     P = ecp_state(seed=8)
     P.g.init_nlist(0.3, 3.0)
     p = P.g.params(kd, cutoff=3.0, solver=capi.SOLVER_NEWTON_SUPPORT)
@@ -134,14 +137,15 @@ def test_ecp_support_filter(lib, kd, extra):
     k = P.g.npairs()
     away = np.isnan(lam2)
     assert st0.pairs == st2.pairs == k and st0.iter_hist[0] == 0
-    # repulsive kind: contact only, most listed pairs are beyond the bound;
+    # repulsive kind: contact only, most listed pairs are turned away;
     # cutoff 3 (reach = sigma + 2): few are
-    assert st2.iter_hist[0] == away.sum() and (0.3 * k if kd == capi.ECPR else 0) <= away.sum() < k
+    assert st2.iter_hist[0] == away.sum() and (0.5 * k if kd == capi.ECPR else 0) <= away.sum() < k
     assert sum(st2.iter_hist) == k and st2.solver_evals < st0.solver_evals
     assert np.max(np.abs(lam2[~away] - lam0[~away])) < 1e-6
     pi, pj = P.g.raw_pairs()
-    rm, hs = _support_sum(P, pi, pj)
-    assert np.all(rm[away] >= hs[away] + extra)
+    lam_ref, _ = P.o.forces(O.pair_params(ko, cutoff=3.0, solver=O.SOLVER_TIGHT), pi, pj, want_lambda=True)
+    rm, sigma = _contact_distance(P, pi, pj, lam_ref)
+    assert np.all(rm[away] >= sigma[away] + extra)
 
 
 def test_ecp_support_start_saves_evaluations(lib):
