@@ -242,15 +242,20 @@ def timed_steps(g, torch, stream, steps, flush):
 
 
 def timed_forces(g, torch, stream, pp, reps, flush):
+    """Device time of one force call (prep and pair kernels), L2 flushed before
+    each: the flush is enqueued first, so that the host has enqueued the
+    call's launches while the device still runs it and the interval between
+    the events holds the call's kernels back to back (an idle device between
+    the events would time the host's launch rate instead)."""
     start = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
     end = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
     with torch.cuda.stream(stream):
         for k in range(reps):
+            flush.add_(1.0)
             g.zero_forces()
             start[k].record(stream)
             g.pair_forces_async(pp)
             end[k].record(stream)
-            flush.add_(1.0)
     torch.cuda.synchronize()
     return [s.elapsed_time(e) / 1e3 for s, e in zip(start, end)]
 

@@ -363,7 +363,9 @@ __global__ void __launch_bounds__(SG_PAIR_MAX_BLOCK, FILTER ? Pot::kMinBlocksFil
 // locality and every lane of its warps busy. Pairs turned away are counted as
 // listed with no solve (stats[0], stats[4]) and handed to the potential's
 // filtered_out. 256 threads: the round's 8 x P warp counts fit one warp scan.
-constexpr int SG_COMPACT_P = 4;
+#ifndef SG_COMPACT_P
+#define SG_COMPACT_P 4
+#endif
 template <class Pot>
 __global__ void __launch_bounds__(256) k_pair_compact(PairLaunch L, Pot pot, int* __restrict__ count,
                                                      int* __restrict__ tmap, int* __restrict__ ci,
@@ -383,19 +385,22 @@ __global__ void __launch_bounds__(256) k_pair_compact(PairLaunch L, Pot pot, int
         bool valid[P];
 #pragma unroll
         for (int k = 0; k < P; ++k) pair_fetch(L, base0 + (warp * P + k) * 32, lane, np, 0, t[k], i[k], j[k], valid[k]);
+        // the P range tests first, with no vote or store between them
+        bool keep[P];
+#pragma unroll
+        for (int k = 0; k < P; ++k) keep[k] = valid[k] && pot.in_range(i[k], j[k]);
         unsigned km[P];
 #pragma unroll
         for (int k = 0; k < P; ++k) {
-            const bool keep = valid[k] && pot.in_range(i[k], j[k]);
-            km[k] = __ballot_sync(full, keep);
+            km[k] = __ballot_sync(full, keep[k]);
             const unsigned vm = __ballot_sync(full, valid[k]);
-            if (valid[k] && !keep) pot.filtered_out(t[k]);
+            if (valid[k] && !keep[k]) pot.filtered_out(t[k]);
             away += __popc(vm & ~km[k]);
             if (lane == 0) sh_n[warp * P + k] = __popc(km[k]);
         }
         __syncthreads();
         if (warp == 0) {   // exclusive scan of the 8 P counts, one atomic for the round
-            const int c = sh_n[lane];
+            const int c = lane < 8 * P ? sh_n[lane] : 0;
             int incl = c;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -406,7 +411,7 @@ __global__ void __launch_bounds__(256) k_pair_compact(PairLaunch L, Pot pot, int
             int base = 0;
             if (lane == 0 && total) base = atomicAdd(count, total);
             base = __shfl_sync(full, base, 0);
-            sh_n[lane] = base + incl - c;
+            if (lane < 8 * P) sh_n[lane] = base + incl - c;
         }
         __syncthreads();
 #pragma unroll

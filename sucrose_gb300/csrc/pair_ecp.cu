@@ -409,8 +409,13 @@ struct PotECP {
     // the contact solve. The bounds are widened (2e-4 and 1e-3 relative, 1e-4)
     // for the FP32 rounding of r, h, F and sigma; NaN keeps the pair.
     SG_DEV bool in_range(int i, int j) const {
-        const float3 r = pair_rij(pos, i, j, b);
-        const float4 a0 = prep[4 * i], a1 = prep[4 * i + 1], b0 = prep[4 * j], b1 = prep[4 * j + 1];
+        float4 a0, a1, b0, b1;
+        ld_f4x2(prep + 4 * i, a0, a1);   // A_R: the first 32 bytes of each record
+        ld_f4x2(prep + 4 * j, b0, b1);
+        return range_test(pos[i], pos[j], a0, a1, b0, b1, i);
+    }
+    SG_DEV bool range_test(float4 pi, float4 pj, float4 a0, float4 a1, float4 b0, float4 b1, int i) const {
+        const float3 r = pair_rij_of(make_float3(pi.x, pi.y, pi.z), make_float3(pj.x, pj.y, pj.z), i, b);
         const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
         const float B[6] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y};
         const float rsq = dot3(r, r), rinv = rsqrtf(rsq), rm = rsq * rinv;

@@ -86,16 +86,31 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
         const PairTune tv = ecp ? cand_ecp[v] : cand[c];
         ctx->tune[key] = tv;
         rc = sg_pair_forces_async(ctx, p);   // warm-up (allocations, caches)
-        float tot = 0.f;
-        for (int k = 0; k < reps && !rc; ++k) {
-            cudaEventRecord(e0, ctx->stream);
-            rc = sg_pair_forces_async(ctx, p);
-            cudaEventRecord(e1, ctx->stream);
-            cudaEventSynchronize(e1);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            tot += ms;
+        // the variant's launches captured once and replayed back to back: the
+        // timing is device time, not the host's launch rate
+        cudaGraph_t gph = nullptr;
+        cudaGraphExec_t gexe = nullptr;
+        if (!rc) {
+            cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                rc = sg_pair_forces_async(ctx, p);
+                e = cudaStreamEndCapture(ctx->stream, &gph);
+            }
+            if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&gexe, gph, 0);
+            if (!rc && e != cudaSuccess) rc = sg_cuda_check(ctx, e, "capture of a launch variant");
         }
+        float tot = 0.f;
+        if (!rc) {
+            cudaGraphLaunch(gexe, ctx->stream);
+            cudaEventRecord(e0, ctx->stream);
+            for (int k = 0; k < reps; ++k) cudaGraphLaunch(gexe, ctx->stream);
+            cudaEventRecord(e1, ctx->stream);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&tot, e0, e1);
+            if (e != cudaSuccess) rc = sg_cuda_check(ctx, e, "timing of a launch variant");
+        }
+        if (gexe) cudaGraphExecDestroy(gexe);
+        if (gph) cudaGraphDestroy(gph);
         const float ms = tot / reps;
         res.ms[v] = ms;
         if (!rc && ms < best) {
