@@ -296,22 +296,29 @@ __global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g0,
     row_done(i, cnt, cap, nb_count, flags, rp, pr);
 }
 
-// The same rows with one warp per particle, for one system with dense cells:
-// the lanes test 32 members of a cell at once and the accepted ones are
-// appended in member order (ballot, then each accepting lane's rank among
-// them), so each row holds exactly what the thread-per-particle kernel
-// writes. Warps take rows in cell order, so the warps of a block search the
-// same 27 cells and find their candidates (cell-ordered positions, read with
-// contiguous loads) in L1; a chunk whose members all have indices <= i is
-// passed over (members are sorted). Row i is written row-major (i * max_nb).
-__global__ void __launch_bounds__(256) k_rows_cells_warp(int n, ListGeom g, const int* __restrict__ cell_start,
-                                                         const int* __restrict__ cell_particles,
-                                                         const float4* __restrict__ pos_cell, int max_nb,
-                                                         int* nb_pad, int* nb_count, int* flags) {
+// The same rows for one system, G lanes per row (G = 8, 16 or 32; 32 / G rows
+// per warp, rows taken in cell order). The three x cells of each (dz, dy) row
+// of the 27-cell stencil are consecutive in cell order, so their members are
+// one contiguous range of cell_particles (two when the stencil wraps in x,
+// listed in the thread-per-row kernel's dx order): nine ranges instead of 27
+// cells, tested G members at a time; the accepted ones are appended in member
+// order (a ballot over the row's lanes, then each accepting lane's rank), so
+// each row holds exactly what the thread-per-particle kernel writes. A chunk
+// whose members all have indices <= i is passed over (members are sorted).
+// Rows are written row-major (i * max_nb). Launched with G = 32 for dense
+// cells (row_lanes_for).
+template <int G>
+__global__ void __launch_bounds__(256) k_rows_xrange(int n, ListGeom g, const int* __restrict__ cell_start,
+                                                     const int* __restrict__ cell_particles,
+                                                     const float4* __restrict__ pos_cell, int max_nb, int* nb_pad,
+                                                     int* nb_count, int* flags) {
+    static_assert(G == 8 || G == 16 || G == 32, "8, 16 or 32 lanes per row");
     if (!flags[F_REBUILD]) return;
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {   // warp-uniform
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), g0 = lane & ~(G - 1);
+    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << g0);
+    const int ngroups = (int)((gridDim.x * blockDim.x) / G);
+    const int nx = g.nc[0];
+    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G); w < n; w += ngroups) {   // group-uniform
         const int i = cell_particles[w];
         const float4 pi = pos_cell[w];
         const size_t base = (size_t)i * max_nb;
@@ -321,19 +328,23 @@ __global__ void __launch_bounds__(256) k_rows_cells_warp(int n, ListGeom g, cons
         for (int dz = -1; dz <= 1; ++dz) {
             const int zz = wrapc(cz + dz, g.nc[2]);
             for (int dy = -1; dy <= 1; ++dy) {
-                const int yy = wrapc(cy + dy, g.nc[1]);
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const int xx = wrapc(cx + dx, g.nc[0]);
-                    const int c = (zz * g.nc[1] + yy) * g.nc[0] + xx;
-                    const int b = cell_start[c], e = cell_start[c + 1];
-                    for (int k0 = b; k0 < e; k0 += 32) {
-                        const int k = k0 + lane;
+                const int row = (zz * g.nc[1] + wrapc(cy + dy, g.nc[1])) * nx;
+                // x cells cx-1 .. cx+1 as ranges of consecutive cells, in dx order
+                int lo0 = cx - 1, hi0 = cx + 1, lo1 = 0, hi1 = -1;
+                if (cx == 0) { lo0 = nx - 1; hi0 = nx - 1; lo1 = 0; hi1 = 1; }
+                else if (cx == nx - 1) { hi0 = nx - 1; lo1 = 0; hi1 = 0; }
+                for (int sgm = 0; sgm < 2; ++sgm) {
+                    const int clo = sgm ? lo1 : lo0, chi = sgm ? hi1 : hi0;
+                    if (chi < clo) continue;
+                    const int b = cell_start[row + clo], e = cell_start[row + chi + 1];
+                    for (int k0 = b; k0 < e; k0 += G) {
+                        const int k = k0 + sub;
                         const int j = k < e ? cell_particles[k] : -1;
-                        if (!__any_sync(0xffffffffu, j > i)) continue;
+                        if (!__any_sync(gmask, j > i)) continue;
                         const bool acc = j > i && accept_pair(pi, pos_cell[k], g);
-                        const unsigned m = __ballot_sync(0xffffffffu, acc);
+                        const unsigned m = __ballot_sync(gmask, acc) >> g0;
                         if (acc) {
-                            const int slot = cnt + __popc(m & ((1u << lane) - 1u));
+                            const int slot = cnt + __popc(m & ((1u << sub) - 1u));
                             if (slot < max_nb) nb_pad[base + slot] = j;
                         }
                         cnt += __popc(m);
@@ -341,14 +352,14 @@ __global__ void __launch_bounds__(256) k_rows_cells_warp(int n, ListGeom g, cons
                 }
             }
         }
-        if (lane == 0) {
+        if (sub == 0) {
             nb_count[i] = min(cnt, max_nb);
             if (cnt > max_nb) atomicMax(&flags[F_OVERFLOW], cnt);
         }
     }
 }
 
-// Row-major padded rows (k_rows_cells_warp) into the flattened pair arrays:
+// Row-major padded rows (k_rows_xrange) into the flattened pair arrays:
 // a warp per row, contiguous on both sides.
 __global__ void __launch_bounds__(256) k_compact_rows(int n, int max_nb, const int* __restrict__ nb_pad,
                                                       const int* __restrict__ nb_count,
@@ -632,6 +643,15 @@ int alloc_rows(sg_ctx* ctx, int max_nb) {
     return SG_OK;
 }
 
+// Lanes per row of a single system's search: 32 (k_rows_xrange) when the
+// stencil's x ranges hold 24 members or more on average (8 per cell); sparser
+// cells, a thread per row (k_rows_cells over cell-ordered positions; measured
+// on the ECP list, 4.2 per cell: 72 us against 91 us for 16 lanes per row).
+int row_lanes_for(int use_cells, int n, int ncells) {
+    if (!use_cells) return 0;
+    return 3.0 * n / std::max(ncells, 1) >= 24.0 ? 32 : 0;
+}
+
 // Enqueue the (flag-gated) build kernels.
 int enqueue_build(sg_ctx* ctx) {
     sg_nlist_state& nl = ctx->nl;
@@ -650,14 +670,14 @@ int enqueue_build(sg_ctx* ctx) {
         k_sort_cells<<<(nl.ncells + 7) / 8, 256, 0, ctx->stream>>>(nl.ncells, nl.cell_start, nl.cell_unsorted,
                                                                     nl.cell_particles, nl.dev_flags, ctx->pos,
                                                                     pos_cell);
-        // one large system with dense cells: a warp per row (rows row-major,
-        // compacted a warp per row); sparse cells or many small replicas
-        // rebuilding at once: a thread per row
-        if (nl.dense_cells)
-            k_rows_cells_warp<<<(int)std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 8 * ctx->num_sms), 256, 0,
-                                ctx->stream>>>(n, g, nl.cell_start, nl.cell_particles, nl.pos_cell, nl.max_nb,
-                                               nl.nb_pad, nl.nb_count, nl.dev_flags);
-        else
+        // one system with dense cells: a warp per row over the stencil's x
+        // ranges (rows row-major, compacted a warp per row); sparse cells, or
+        // many small replicas rebuilding at once: a thread per row
+        if (nl.row_lanes) {
+            const int grid = (int)std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 8 * ctx->num_sms);
+            k_rows_xrange<32><<<grid, 256, 0, ctx->stream>>>(n, g, nl.cell_start, nl.cell_particles, nl.pos_cell,
+                                                             nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
+        } else
             k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
                                                       nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag,
                                                       nl.row_block_order, pos_cell);
@@ -667,7 +687,7 @@ int enqueue_build(sg_ctx* ctx) {
         k_rows_all<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
     }
     if (int rc = scan(ctx, nl.nb_count, n, nl.row_off, nl.dev_flags + F_NPAIRS, nl.dev_flags)) return rc;
-    if (nl.use_cells && nl.dense_cells)
+    if (nl.use_cells && nl.row_lanes)
         k_compact_rows<<<16 * ctx->num_sms, 256, 0, ctx->stream>>>(n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off,
                                                                    nl.pair_i, nl.pair_j, nl.dev_flags);
     else
@@ -767,7 +787,7 @@ int sg_nlist_box_changed(sg_ctx* ctx) {
         nl.use_cells = 0;
     }
     nl.ncells = nl.ncell[0] * nl.ncell[1] * nl.ncell[2];
-    nl.dense_cells = nl.use_cells && ctx->n >= 12 * nl.ncells;
+    nl.row_lanes = row_lanes_for(nl.use_cells, ctx->n, nl.ncells);
     ctx->graph_epoch++;
     return SG_OK;
 }
@@ -803,7 +823,7 @@ int sg_nlist_init(sg_ctx* ctx, double skin, double cutoff, int32_t trigger_mode)
     }
     if (!nl.use_cells) nl.ncell[0] = nl.ncell[1] = nl.ncell[2] = 1;
     nl.ncells = nl.ncell[0] * nl.ncell[1] * nl.ncell[2];
-    nl.dense_cells = nl.use_cells && n >= 12 * nl.ncells;
+    nl.row_lanes = row_lanes_for(nl.use_cells, n, nl.ncells);
     double vol = ctx->box[0] * ctx->box[1] * ctx->box[2];
     double rho = n / vol;
     // rows hold the j > i neighbours in index order, so a particle of low
@@ -889,7 +909,7 @@ int sg_rep_nlist_init(sg_ctx* ctx, const double* skin, const double* cutoff, int
     nl.ncell[0] = nl.ncell[1] = nl.ncell[2] = 1;
     nl.ncells = total_cells;
     // many small lists rebuild at once here: a thread per row keeps every lane busy
-    nl.dense_cells = 0;
+    nl.row_lanes = 0;
     nl.h_rep_max_nb = max_nb_r;
     SG_CUDA(ctx, cudaMalloc(&nl.rep_max_nb, sizeof(int) * R));
     SG_CUDA(ctx, cudaMalloc(&nl.rep_pad_off, sizeof(long long) * R));

@@ -71,7 +71,7 @@ struct sg_nlist_state {
     double rl2 = 0.0;                // (rc+skin)^2 in FP64, the reference's r_skin_sq after a build
     double trigger_sq = 0.0;         // compared with 4 * max displacement^2
     int use_cells = 0;
-    int dense_cells = 0;             // >= 12 particles per cell: one warp per row in the search
+    int row_lanes = 0;               // a single system with dense cells: 32 lanes per row in the search; 0: a thread per row
     int ncell[3] = {0, 0, 0};
     int ncells = 0;
     int ncells_cap = 0;              // cells the arrays were sized for
@@ -84,7 +84,7 @@ struct sg_nlist_state {
     int* particle_cell = nullptr;    // [n]
     int* nb_count = nullptr;         // [n]
     int* nb_pad = nullptr;           // [max_nb * n], column-major (k * n + i); dense cells: row-major
-    float4* pos_cell = nullptr;      // [n] positions in cell order (dense cells)
+    float4* pos_cell = nullptr;      // [n] positions in cell order (single systems)
     int* row_off = nullptr;          // [n + 1]
     int* scan_tmp = nullptr;         // block sums of the scan
     int* pair_i = nullptr;           // [pair_capacity]
