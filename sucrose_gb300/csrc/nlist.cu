@@ -9,16 +9,20 @@
 // reference's exact FP64 operation sequence (no contraction).
 //
 // Layout in HBM: per-particle rows of at most max_nb neighbours are written
-// column-major into nb_pad (k * n + i; row-major, i * max_nb + k, by the
-// warp-per-row search of a system with dense cells), then compacted into the
-// flattened pair arrays pair_i / pair_j, rows in particle order, which every
-// pair kernel walks 32 pairs per warp.
+// into nb_pad (a single system: row-major, i * max_nb + k, by the cooperative
+// build; replica contexts: column-major k * n + i in each replica's section),
+// then compacted into the flattened pair arrays pair_i / pair_j, rows in
+// particle order, which every pair kernel walks 32 pairs per warp.
 #include <algorithm>
 #include <cmath>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "sg_internal.cuh"
 #include "step_epi.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -307,74 +311,84 @@ __global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g0,
 // whose members all have indices <= i is passed over (members are sorted).
 // Rows are written row-major (i * max_nb). Launched with G = 32 for dense
 // cells (row_lanes_for).
+// One row of the x-range search by the G lanes of a group (sub: the lane in
+// the group, g0 its first lane, gmask the group's lanes). Row w of the cell
+// order, written row-major.
 template <int G>
-__global__ void __launch_bounds__(256) k_rows_xrange(int n, ListGeom g, const int* __restrict__ cell_start,
-                                                     const int* __restrict__ cell_particles,
-                                                     const float4* __restrict__ pos_cell, int max_nb, int* nb_pad,
-                                                     int* nb_count, int* flags) {
-    static_assert(G == 8 || G == 16 || G == 32, "8, 16 or 32 lanes per row");
-    if (!flags[F_REBUILD]) return;
-    const int lane = threadIdx.x & 31, sub = lane & (G - 1), g0 = lane & ~(G - 1);
-    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << g0);
-    const int ngroups = (int)((gridDim.x * blockDim.x) / G);
+__device__ __forceinline__ void xrange_row(int w, int sub, int g0, unsigned gmask, const ListGeom& g,
+                                           const int* cell_start, const int* cell_particles, const float4* pos_cell,
+                                           int max_nb, int* nb_pad, int* nb_count, int* flags) {
     const int nx = g.nc[0];
-    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G); w < n; w += ngroups) {   // group-uniform
-        const int i = cell_particles[w];
-        const float4 pi = pos_cell[w];
-        const size_t base = (size_t)i * max_nb;
-        int cnt = 0;
-        int cx, cy, cz;
-        cell_of(pi, g, cx, cy, cz);
-        for (int dz = -1; dz <= 1; ++dz) {
-            const int zz = wrapc(cz + dz, g.nc[2]);
-            for (int dy = -1; dy <= 1; ++dy) {
-                const int row = (zz * g.nc[1] + wrapc(cy + dy, g.nc[1])) * nx;
-                // x cells cx-1 .. cx+1 as ranges of consecutive cells, in dx order
-                int lo0 = cx - 1, hi0 = cx + 1, lo1 = 0, hi1 = -1;
-                if (cx == 0) { lo0 = nx - 1; hi0 = nx - 1; lo1 = 0; hi1 = 1; }
-                else if (cx == nx - 1) { hi0 = nx - 1; lo1 = 0; hi1 = 0; }
-                for (int sgm = 0; sgm < 2; ++sgm) {
-                    const int clo = sgm ? lo1 : lo0, chi = sgm ? hi1 : hi0;
-                    if (chi < clo) continue;
-                    const int b = cell_start[row + clo], e = cell_start[row + chi + 1];
-                    for (int k0 = b; k0 < e; k0 += G) {
-                        const int k = k0 + sub;
-                        const int j = k < e ? cell_particles[k] : -1;
-                        if (!__any_sync(gmask, j > i)) continue;
-                        const bool acc = j > i && accept_pair(pi, pos_cell[k], g);
-                        const unsigned m = __ballot_sync(gmask, acc) >> g0;
-                        if (acc) {
-                            const int slot = cnt + __popc(m & ((1u << sub) - 1u));
-                            if (slot < max_nb) nb_pad[base + slot] = j;
-                        }
-                        cnt += __popc(m);
+    const int i = cell_particles[w];
+    const float4 pi = pos_cell[w];
+    const size_t base = (size_t)i * max_nb;
+    int cnt = 0;
+    int cx, cy, cz;
+    cell_of(pi, g, cx, cy, cz);
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int zz = wrapc(cz + dz, g.nc[2]);
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int row = (zz * g.nc[1] + wrapc(cy + dy, g.nc[1])) * nx;
+            // x cells cx-1 .. cx+1 as ranges of consecutive cells, in dx order
+            int lo0 = cx - 1, hi0 = cx + 1, lo1 = 0, hi1 = -1;
+            if (cx == 0) { lo0 = nx - 1; hi0 = nx - 1; lo1 = 0; hi1 = 1; }
+            else if (cx == nx - 1) { hi0 = nx - 1; lo1 = 0; hi1 = 0; }
+            for (int sgm = 0; sgm < 2; ++sgm) {
+                const int clo = sgm ? lo1 : lo0, chi = sgm ? hi1 : hi0;
+                if (chi < clo) continue;
+                const int b = cell_start[row + clo], e = cell_start[row + chi + 1];
+                for (int k0 = b; k0 < e; k0 += G) {
+                    const int k = k0 + sub;
+                    const int j = k < e ? cell_particles[k] : -1;
+                    if (!__any_sync(gmask, j > i)) continue;
+                    const bool acc = j > i && accept_pair(pi, pos_cell[k], g);
+                    const unsigned m = __ballot_sync(gmask, acc) >> g0;
+                    if (acc) {
+                        const int slot = cnt + __popc(m & ((1u << sub) - 1u));
+                        if (slot < max_nb) nb_pad[base + slot] = j;
+                    }
+                    cnt += __popc(m);
+                }
+            }
+        }
+    }
+    if (sub == 0) {
+        nb_count[i] = min(cnt, max_nb);
+        if (cnt > max_nb) atomicMax(&flags[F_OVERFLOW], cnt);
+    }
+}
+
+// One row of a single system by one thread: row t of the cell order over the
+// 27 cells (cell-ordered candidates, contiguous loads), written row-major.
+__device__ __forceinline__ void cells_row(int t, const ListGeom& g, const int* cell_start, const int* cell_particles,
+                                          const float4* pos_cell, int max_nb, int* nb_pad, int* nb_count,
+                                          int* flags) {
+    const int i = cell_particles[t];
+    const float4 pi = pos_cell[t];
+    const size_t base = (size_t)i * max_nb;
+    int cnt = 0;
+    int cx, cy, cz;
+    cell_of(pi, g, cx, cy, cz);
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int zz = wrapc(cz + dz, g.nc[2]);
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int yy = wrapc(cy + dy, g.nc[1]);
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int c = (zz * g.nc[1] + yy) * g.nc[0] + wrapc(cx + dx, g.nc[0]);
+                const int b = cell_start[c], e = cell_start[c + 1];
+                for (int k = b; k < e; ++k) {
+                    const int j = cell_particles[k];
+                    if (j <= i) continue;
+                    if (accept_pair(pi, pos_cell[k], g)) {
+                        if (cnt < max_nb) nb_pad[base + cnt] = j;
+                        ++cnt;
                     }
                 }
             }
         }
-        if (sub == 0) {
-            nb_count[i] = min(cnt, max_nb);
-            if (cnt > max_nb) atomicMax(&flags[F_OVERFLOW], cnt);
-        }
     }
-}
-
-// Row-major padded rows (k_rows_xrange) into the flattened pair arrays:
-// a warp per row, contiguous on both sides.
-__global__ void __launch_bounds__(256) k_compact_rows(int n, int max_nb, const int* __restrict__ nb_pad,
-                                                      const int* __restrict__ nb_count,
-                                                      const int* __restrict__ row_off, int* pair_i, int* pair_j,
-                                                      const int* flags) {
-    if (!flags[F_REBUILD]) return;
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-    for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n; i += nwarps) {
-        const int c = nb_count[i], o = row_off[i];
-        for (int k = lane; k < c; k += 32) {
-            pair_i[o + k] = i;
-            pair_j[o + k] = nb_pad[(size_t)i * max_nb + k];
-        }
-    }
+    nb_count[i] = min(cnt, max_nb);
+    if (cnt > max_nb) atomicMax(&flags[F_OVERFLOW], cnt);
 }
 
 // All-pairs variant for boxes with fewer than three cells per side and for
@@ -573,6 +587,168 @@ __global__ void k_set_request(int* flags, int* rep_flag, int R) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < R; r += gridDim.x * blockDim.x) rep_flag[r] = 1;
 }
 
+// ------------------------------------------------ single-system rebuild --
+// The whole rebuild of a single system with cells in one cooperative kernel:
+// its phases (bin, scan of the cell counts, fill, sort, row search, scan of
+// the row lengths, compaction, finish) are separated by grid-wide barriers
+// instead of kernel boundaries. A step without a rebuild then runs one
+// launch that exits at its first instruction, where the captured step would
+// otherwise evaluate a graph conditional node or a dozen flag-gated
+// kernels. Arrays written in one phase and read in a later one are read with
+// plain (coherent) loads, never through the read-only path.
+struct CoopBuild {
+    int n, ncells, max_nb, row_lanes;
+    const float4* pos;
+    ListGeom g;
+    int* cell_count;
+    int* cell_fill;
+    int* cell_start;
+    int* cell_unsorted;
+    int* cell_particles;
+    int* particle_cell;
+    float4* pos_cell;
+    int* nb_pad;
+    int* nb_count;
+    int* row_off;
+    int* pair_i;
+    int* pair_j;
+    float4* last;
+    int* flags;
+    int* tmp;   // gridDim.x block totals of the scans
+};
+
+// Exclusive scan of in[0, m) into out[0, m] (out[m] = total, also *total_dst)
+// by the whole grid: each block scans a contiguous tile, the tiles' totals
+// give each block its offset after a grid barrier.
+__device__ __forceinline__ void coop_scan(cg::grid_group& grid, const int* in, int m, int* out, int* total_dst, int* tmp) {
+    __shared__ int sh[32];
+    __shared__ int sh_off;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int T = (m + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int lo = min(m, (int)blockIdx.x * T), hi = min(m, lo + T);
+    const int per = (T + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int tlo = min(hi, lo + (int)threadIdx.x * per), thi = min(hi, tlo + per);
+    int s = 0;
+    for (int k = tlo; k < thi; ++k) s += in[k];
+    int x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int v = lane < nw ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane < nw) sh[lane] = v;
+    }
+    __syncthreads();
+    const int excl = x - s + (w ? sh[w - 1] : 0);
+    const int btot = sh[nw - 1];
+    if (threadIdx.x == 0) tmp[blockIdx.x] = btot;
+    grid.sync();
+    int o = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) o += tmp[b];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) o += __shfl_xor_sync(0xffffffffu, o, d);
+    __syncthreads();
+    if (lane == 0) sh[w] = o;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int k = 0; k < nw; ++k) t += sh[k];
+        sh_off = t;
+    }
+    __syncthreads();
+    int run = sh_off + excl;
+    for (int k = tlo; k < thi; ++k) {
+        const int v = in[k];
+        out[k] = run;
+        run += v;
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        const int tot = sh_off + btot;
+        out[m] = tot;
+        if (total_dst) *total_dst = tot;
+    }
+    __syncthreads();   // sh is reused by the next scan
+}
+
+__global__ void __launch_bounds__(256, 3) k_build_coop(CoopBuild a) {
+    if (!a.flags[F_REBUILD]) return;   // grid-uniform: cleared only after the last barrier
+    cg::grid_group grid = cg::this_grid();
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    const int gw = gt >> 5, nwarps = gs >> 5;
+    // zero the cell counters
+    for (int c = gt; c < a.ncells; c += gs) {
+        a.cell_count[c] = 0;
+        a.cell_fill[c] = 0;
+    }
+    if (gt == 0) a.flags[F_OVERFLOW] = 0;
+    grid.sync();
+    // bin
+    for (int i = gt; i < a.n; i += gs) {
+        int cx, cy, cz;
+        const int c = cell_of(a.pos[i], a.g, cx, cy, cz);
+        a.particle_cell[i] = c;
+        atomicAdd(&a.cell_count[c], 1);
+    }
+    grid.sync();
+    coop_scan(grid, a.cell_count, a.ncells, a.cell_start, nullptr, a.tmp);
+    grid.sync();
+    // members in arrival order
+    for (int i = gt; i < a.n; i += gs) {
+        const int c = a.particle_cell[i];
+        a.cell_unsorted[a.cell_start[c] + atomicAdd(&a.cell_fill[c], 1)] = i;
+    }
+    grid.sync();
+    // each cell's members by index (a warp per cell, each member at its rank),
+    // their positions in the same order
+    for (int c = gw; c < a.ncells; c += nwarps) {
+        const int b = a.cell_start[c], e = a.cell_start[c + 1];
+        for (int k = b + lane; k < e; k += 32) {
+            const int v = a.cell_unsorted[k];
+            int rank = 0;
+            for (int t = b; t < e; ++t) rank += a.cell_unsorted[t] < v;
+            a.cell_particles[b + rank] = v;
+            a.pos_cell[b + rank] = a.pos[v];
+        }
+    }
+    grid.sync();
+    // rows, in cell order: a warp per row (dense cells) or a thread per row
+    if (a.row_lanes == 32) {
+        for (int w = gw; w < a.n; w += nwarps)
+            xrange_row<32>(w, lane, 0, 0xffffffffu, a.g, a.cell_start, a.cell_particles, a.pos_cell, a.max_nb, a.nb_pad,
+                           a.nb_count, a.flags);
+    } else {
+        for (int t = gt; t < a.n; t += gs)
+            cells_row(t, a.g, a.cell_start, a.cell_particles, a.pos_cell, a.max_nb, a.nb_pad, a.nb_count, a.flags);
+    }
+    grid.sync();
+    coop_scan(grid, a.nb_count, a.n, a.row_off, a.flags + F_NPAIRS, a.tmp);
+    grid.sync();
+    // rows into the flat pair arrays (a warp per row, contiguous on both
+    // sides); the positions of this build
+    for (int i = gw; i < a.n; i += nwarps) {
+        const int c = a.nb_count[i], o = a.row_off[i];
+        for (int k = lane; k < c; k += 32) {
+            a.pair_i[o + k] = i;
+            a.pair_j[o + k] = a.nb_pad[(size_t)i * a.max_nb + k];
+        }
+    }
+    for (int i = gt; i < a.n; i += gs) a.last[i] = a.pos[i];
+    if (gt == 0) {
+        a.flags[F_BUILDS] += 1;
+        a.flags[F_REBUILD] = 0;   // every block read it at entry, before the first barrier
+    }
+}
+
 int clear_grid(const sg_ctx* ctx) { return std::max(1, std::min(64, (ctx->nrep + 255) / 256)); }
 
 // (0.4998 min(box))^2 with a margin, as a float that never exceeds the true value
@@ -643,9 +819,24 @@ int alloc_rows(sg_ctx* ctx, int max_nb) {
     return SG_OK;
 }
 
-// Lanes per row of a single system's search: 32 (k_rows_xrange) when the
+// Grid of the cooperative build (every block resident at once) and its
+// scratch, sized once per context.
+int coop_setup(sg_ctx* ctx) {
+    sg_nlist_state& nl = ctx->nl;
+    if (nl.coop_grid) return SG_OK;
+    int per_sm = 0;
+    SG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_build_coop, 256, 0));
+    if (per_sm < 1) return sg_fail(ctx, SG_ECUDA, "the cooperative list build does not fit an SM");
+    const int grid = per_sm * ctx->num_sms;
+    SG_CUDA(ctx, cudaMalloc(&nl.coop_tmp, sizeof(int) * (size_t)(grid + 1)));
+    nl.coop_grid = grid;
+    ctx->graph_epoch++;
+    return SG_OK;
+}
+
+// Lanes per row of a single system's search: 32 (xrange_row) when the
 // stencil's x ranges hold 24 members or more on average (8 per cell); sparser
-// cells, a thread per row (k_rows_cells over cell-ordered positions; measured
+// cells, a thread per row (cells_row over cell-ordered positions; measured
 // on the ECP list, 4.2 per cell: 72 us against 91 us for 16 lanes per row).
 int row_lanes_for(int use_cells, int n, int ncells) {
     if (!use_cells) return 0;
@@ -659,39 +850,55 @@ int enqueue_build(sg_ctx* ctx) {
     ListGeom g = make_geom(ctx);
     const int nb = (n + 255) / 256;
     const PadRep pad{nl.rep_max_nb, nl.rep_pad_off, nl.rep_need};
+    if (nl.use_cells && !ctx->nrep) {
+        // a single system: the cooperative kernel (rows row-major)
+        if (int rc = coop_setup(ctx)) return rc;
+        CoopBuild a;
+        a.n = n;
+        a.ncells = nl.ncells;
+        a.max_nb = nl.max_nb;
+        a.row_lanes = nl.row_lanes;
+        a.pos = ctx->pos;
+        a.g = g;
+        a.cell_count = nl.cell_count;
+        a.cell_fill = nl.cell_fill;
+        a.cell_start = nl.cell_start;
+        a.cell_unsorted = nl.cell_unsorted;
+        a.cell_particles = nl.cell_particles;
+        a.particle_cell = nl.particle_cell;
+        a.pos_cell = nl.pos_cell;
+        a.nb_pad = nl.nb_pad;
+        a.nb_count = nl.nb_count;
+        a.row_off = nl.row_off;
+        a.pair_i = nl.pair_i;
+        a.pair_j = nl.pair_j;
+        a.last = nl.pos_last;
+        a.flags = nl.dev_flags;
+        a.tmp = nl.coop_tmp;
+        void* args[] = {&a};
+        SG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_build_coop, nl.coop_grid, 256, args, 0, ctx->stream));
+        return SG_OK;
+    }
     if (nl.use_cells) {
+        // replica contexts: flag-gated kernels, a thread per row
         k_begin<<<std::max(1, std::min(1024, (nl.ncells + 255) / 256)), 256, 0, ctx->stream>>>(nl.dev_flags, nl.cell_count,
                                                                                                 nl.cell_fill, nl.ncells);
         k_bin<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.particle_cell, nl.cell_count, nl.dev_flags, ctx->rep);
         if (int rc = scan(ctx, nl.cell_count, nl.ncells, nl.cell_start, nullptr, nl.dev_flags)) return rc;
         k_fill<<<nb, 256, 0, ctx->stream>>>(n, nl.particle_cell, nl.cell_start, nl.cell_fill, nl.cell_unsorted,
                                             nl.dev_flags);
-        float4* pos_cell = ctx->nrep ? nullptr : nl.pos_cell;   // single systems: cell-ordered positions
         k_sort_cells<<<(nl.ncells + 7) / 8, 256, 0, ctx->stream>>>(nl.ncells, nl.cell_start, nl.cell_unsorted,
                                                                     nl.cell_particles, nl.dev_flags, ctx->pos,
-                                                                    pos_cell);
-        // one system with dense cells: a warp per row over the stencil's x
-        // ranges (rows row-major, compacted a warp per row); sparse cells, or
-        // many small replicas rebuilding at once: a thread per row
-        if (nl.row_lanes) {
-            const int grid = (int)std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 8 * ctx->num_sms);
-            k_rows_xrange<32><<<grid, 256, 0, ctx->stream>>>(n, g, nl.cell_start, nl.cell_particles, nl.pos_cell,
-                                                             nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
-        } else
-            k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
-                                                      nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag,
-                                                      nl.row_block_order, pos_cell);
-
+                                                                    nullptr);
+        k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
+                                                  nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag,
+                                                  nl.row_block_order, nullptr);
     } else {
         k_begin<<<1, 32, 0, ctx->stream>>>(nl.dev_flags, nl.cell_count, nl.cell_fill, 0);
         k_rows_all<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
     }
     if (int rc = scan(ctx, nl.nb_count, n, nl.row_off, nl.dev_flags + F_NPAIRS, nl.dev_flags)) return rc;
-    if (nl.use_cells && nl.row_lanes)
-        k_compact_rows<<<16 * ctx->num_sms, 256, 0, ctx->stream>>>(n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off,
-                                                                   nl.pair_i, nl.pair_j, nl.dev_flags);
-    else
-        k_compact<<<(n + COMPACT_BLOCK - 1) / COMPACT_BLOCK, COMPACT_BLOCK, 0, ctx->stream>>>(
+    k_compact<<<(n + COMPACT_BLOCK - 1) / COMPACT_BLOCK, COMPACT_BLOCK, 0, ctx->stream>>>(
             n, nl.max_nb, nl.nb_pad, nl.nb_count, nl.row_off, nl.pair_i, nl.pair_j, nl.dev_flags, ctx->rep, pad,
             nl.rep_flag);
     if (ctx->nrep)
@@ -743,7 +950,7 @@ int sg_nlist_free(sg_ctx* ctx) {
     void* bufs[] = {nl.cell_count, nl.cell_start, nl.cell_fill, nl.cell_particles, nl.particle_cell, nl.nb_count,
                     nl.nb_pad, nl.row_off, nl.scan_tmp, nl.pair_i, nl.pair_j, nl.dev_flags, nl.pos_last, nl.pos_cell,
                     nl.rep_max_nb, nl.rep_pad_off, nl.rep_need, nl.rep_flag, nl.rep_builds, nl.cell_unsorted,
-                    nl.chunk_rep, nl.row_block_order};
+                    nl.chunk_rep, nl.row_block_order, nl.coop_tmp};
     for (void* b : bufs)
         if (b) cudaFree(b);
     nl = sg_nlist_state();

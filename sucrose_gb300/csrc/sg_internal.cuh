@@ -71,6 +71,8 @@ struct sg_nlist_state {
     double rl2 = 0.0;                // (rc+skin)^2 in FP64, the reference's r_skin_sq after a build
     double trigger_sq = 0.0;         // compared with 4 * max displacement^2
     int use_cells = 0;
+    int coop_grid = 0;               // blocks of the cooperative single-system build (0: not set up)
+    int* coop_tmp = nullptr;         // its scans' block totals
     int row_lanes = 0;               // a single system with dense cells: 32 lanes per row in the search; 0: a thread per row
     int ncell[3] = {0, 0, 0};
     int ncells = 0;

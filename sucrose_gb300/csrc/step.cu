@@ -16,9 +16,10 @@ __global__ void k_set_rebuild_condition(cudaGraphConditionalHandle h, const int*
 }
 
 // List maintenance inside a captured step: the displacement test runs every
-// step; the build kernels sit in the body of a conditional graph node that
-// executes only when a rebuild was requested, so a step without a rebuild
-// launches none of them. Outside capture the flag-gated kernels are enqueued.
+// step; a single system with cells then runs the cooperative build kernel,
+// which returns at once without a request; a replica context's build kernels
+// sit in the body of a conditional graph node that executes only when a
+// rebuild was requested. Outside capture the flag-gated kernels are enqueued.
 // checked: the displacement test already ran (in the fused initial half step).
 int enqueue_list_update(sg_ctx* ctx, bool flat, bool checked) {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
@@ -27,7 +28,11 @@ int enqueue_list_update(sg_ctx* ctx, bool flat, bool checked) {
     const cudaGraphEdgeData* edges = nullptr;
     size_t nd = 0;
     SG_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &edges, &nd));
-    if (flat || st != cudaStreamCaptureStatusActive) return checked ? sg_nlist_enqueue_build(ctx) : sg_nlist_update(ctx);
+    // a single system with cells rebuilds in one cooperative kernel that exits
+    // at once without a request: no conditional node
+    const bool coop = ctx->nl.use_cells && !ctx->nrep;
+    if (flat || coop || st != cudaStreamCaptureStatusActive)
+        return checked ? sg_nlist_enqueue_build(ctx) : sg_nlist_update(ctx);
     if (!checked)
         if (int rc = sg_nlist_enqueue_check(ctx)) return rc;
     cudaGraphConditionalHandle h;
