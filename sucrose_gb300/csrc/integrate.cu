@@ -291,10 +291,16 @@ __global__ void k_lgv_final(int n, float dt, float4* __restrict__ vel, const flo
 // scale, [14] sum m v^2 scratch, [15] sum L_b^2/I scratch, [16] the scaled
 // sum m v^2, [17] the compat sweep's KE, [18] the two scales rounded to FP32
 // (a float pair: the particle kernels read them without an FP64 conversion).
+// The standard chain's constants in double-float (hi + lo split on the host).
+struct NhDf {
+    dfl t4, hdt, T, ndofT, nrotT;   // dt/4, dt/2, T, ndof T, nrot T
+    dfl iHB[3], iHBr[3];
+};
 struct NhConst {
     double dt, T, ndof, nrot;
     double HB[3], HBr[3];
     double iHB[3], iHBr[3];   // 1 / HB: the chains multiply (an FP64 division is a long serial sequence)
+    NhDf d;
 };
 
 
@@ -317,17 +323,9 @@ __device__ __forceinline__ double exp_chain(double x) {
 }
 
 // u4_propagator: G1 from the supplied sum (m v^2 or L_b^2/I), with
-// exprel(y) = (e^y - 1)/y (integrators.f90:233-301). The chain momenta, the
-// forces G_j and the products p e^-x + t G c stay in FP64. F32: the two
-// factors e^-x and c = exprel(-x), which multiply FP64 values and need only
-// FP32's relative precision once per half step, are evaluated in FP32 (one
-// thread runs this chain, and a dependent FP64 operation costs ~14 times an
-// FP32 one on GB300): with h = e^(-x/2), e^-x = h^2 and c = h sinh(x/2)/(x/2),
-// the even series in (x/2)^2 (no cancellation for small x); for |x| >= 1 the
-// FP64 forms. The reference-compat chain, applied once per particle, keeps
-// them in FP64 (F32 = false): its N applications would accumulate the FP32
-// rounding.
-template <bool F32 = true>
+// exprel(y) = (e^y - 1)/y (integrators.f90:233-301), in FP64: the
+// reference-compat chain, applied once per particle (the standard chain's
+// double-float form is u4_df).
 __device__ __forceinline__ void u4(double t, int j_start, int j_stop, int stride, double (&p)[3], const double* iHB,
                                    double sum, double ndof, double T) {
 #pragma unroll
@@ -337,34 +335,65 @@ __device__ __forceinline__ void u4(double t, int j_start, int j_stop, int stride
             p[2] = p[2] + t * gj;
         } else {
             const double x = t * p[j] * iHB[j];
-            double ex, c;
-            if (!F32) {
-                const double h = exp_chain(-0.5 * x);
-                ex = h * h;
-                if (fabs(x) > 0.01) {
-                    c = (ex - 1.0) / (-x);
-                } else {
-                    const double g[5] = {1.0 / 1, 1.0 / 6, 1.0 / 120, 1.0 / 5040, 1.0 / 362880};
-                    const double y = (0.5 * x) * (0.5 * x);
-                    double f = g[4];
-                    for (int k = 3; k >= 0; --k) f = f * y + g[k];
-                    c = h * f;
-                }
-            } else if (fabs(x) < 1.0) {
-                const float xf = (float)x, u = 0.5f * xf, y = u * u;
-                const float h = expf(-u);
-                // sinh(u)/u = 1 + y/6 + y^2/120 + y^3/5040 + y^4/362880 (|u| < 0.5: < 1e-9 left)
-                const float sh = fmaf(fmaf(fmaf(fmaf(y, 1.f / 362880.f, 1.f / 5040.f), y, 1.f / 120.f), y, 1.f / 6.f), y,
-                                      1.f);
-                ex = (double)(h * h);
-                c = (double)(h * sh);
-            } else {
-                ex = exp(-x);
+            const double h = exp_chain(-0.5 * x);
+            const double ex = h * h;
+            double c;
+            if (fabs(x) > 0.01) {
                 c = (ex - 1.0) / (-x);
+            } else {
+                const double g[5] = {1.0 / 1, 1.0 / 6, 1.0 / 120, 1.0 / 5040, 1.0 / 362880};
+                const double y = (0.5 * x) * (0.5 * x);
+                double f = g[4];
+                for (int k = 3; k >= 0; --k) f = f * y + g[k];
+                c = h * f;
             }
             p[j - 1] = p[j - 1] * ex + t * gj * c;
         }
     }
+}
+
+// The standard chain in double-float arithmetic on the FP32 pipe (~48-bit
+// significands): one thread runs each chain, and a dependent FP64 operation
+// costs it several hundred cycles on GB300, a double-float one a few dozen.
+// u4 as above: G_j, the products and the sums in double-float, the two
+// factors e^-x and exprel(-x) in FP32 (their relative precision enters once
+// per half step, as in the FP64 form).
+SG_DEV void u4_df(dfl t, int j_start, int j_stop, int stride, dfl (&p)[3], const dfl (&iq)[3], dfl K, dfl dofT,
+                  dfl T) {
+#pragma unroll
+    for (int j = j_start; stride > 0 ? j <= j_stop : j >= j_stop; j += stride) {
+        const dfl gj = (j == 1) ? df_sub(K, dofT) : df_sub(df_mul(df_mul(p[j - 2], p[j - 2]), iq[j - 2]), T);
+        if (j == 3) {
+            p[2] = df_add(p[2], df_mul(t, gj));
+        } else {
+            const float x = t.hi * p[j].hi * iq[j].hi;
+            float ex, c;
+            if (fabsf(x) < 1.f) {
+                const float u = 0.5f * x, y = u * u;
+                const float h = expf(-u);
+                // sinh(u)/u = 1 + y/6 + y^2/120 + y^3/5040 + y^4/362880 (|u| < 0.5: < 1e-9 left)
+                const float sh = fmaf(fmaf(fmaf(fmaf(y, 1.f / 362880.f, 1.f / 5040.f), y, 1.f / 120.f), y, 1.f / 6.f), y,
+                                      1.f);
+                ex = h * h;
+                c = h * sh;
+            } else {
+                ex = expf(-x);
+                c = (1.f - ex) / x;
+            }
+            p[j - 1] = df_add(df_mul_f(p[j - 1], ex), df_mul_f(df_mul(t, gj), c));
+        }
+    }
+}
+
+// e^x in double-float: for |x| <= 1e-3, 1 + x + x^2/2 in double-float and
+// x^3 (1/6 + x/24 + x^2/120) in FP32 (the rest of the series is below 2e-21);
+// larger |x| through the FP64 series.
+SG_DEV dfl exp_df(dfl x) {
+    if (!(fabsf(x.hi) <= 1e-3f)) return df_from_double(exp_chain(df_to_double(x)));
+    const float r = fmaf(fmaf(x.hi, 1.f / 120.f, 1.f / 24.f), x.hi, 1.f / 6.f);
+    const float x3r = x.hi * x.hi * x.hi * r;
+    const dfl x2 = df_mul(x, x);
+    return df_add(df_add(df_of(1.f), x), df_add(dfl{0.5f * x2.hi, 0.5f * x2.lo}, df_of(x3r)));
 }
 
 __global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* __restrict__ shape,
@@ -387,34 +416,34 @@ __global__ void k_sum_mv2(int n, const float4* __restrict__ vel, const float4* _
 // entry (zeroed by the host before the reduction). Writes the scale factors.
 // The translational chain (which = 0) and the rotational chain (which = 1)
 // are independent, and the caller runs them in two different warps.
-// The chain state is read once into registers and written back at the end:
-// one thread runs the chain's dependent FP64 sequence, and a global load
-// between its steps (L2 latency after each store) would cost more than the
-// arithmetic.
+// The chain state (FP64 in nh) is read once into double-float registers and
+// written back at the end; the sequence runs in double-float (u4_df).
 // K: the sum (m v^2 or L_b^2/I) for this chain.
-__device__ void nhc_chain_one(const NhConst& c, double* nh, int which, double K) {
+__device__ void nhc_chain_one(const NhConst& c, double* nh, int which, double Kd) {
     double* eta = nh + 6 * which;
-    double e[3], p[3];
+    dfl e[3], p[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        e[k] = eta[k];
-        p[k] = eta[3 + k];
+        e[k] = df_from_double(eta[k]);
+        p[k] = df_from_double(eta[3 + k]);
     }
-    const double* iHB = which ? c.iHBr : c.iHB;
-    const double ih[3] = {iHB[0], iHB[1], iHB[2]};
-    u4(c.dt / 4.0, 3, 1, -1, p, ih, K, which ? c.nrot : c.ndof, c.T);
-    const double sc = exp_chain(-0.5 * c.dt * p[0] * ih[0]);
+    const dfl(&iq)[3] = which ? c.d.iHBr : c.d.iHB;
+    const dfl dofT = which ? c.d.nrotT : c.d.ndofT;
+    const dfl K = df_from_double(Kd);
+    u4_df(c.d.t4, 3, 1, -1, p, iq, K, dofT, c.d.T);
+    const dfl sc = exp_df(df_neg(df_mul(c.d.hdt, df_mul(p[0], iq[0]))));
 #pragma unroll
-    for (int k = 0; k < 3; ++k) e[k] = e[k] + 0.5 * c.dt * p[k] * ih[k];
-    u4(c.dt / 4.0, 1, 3, 1, p, ih, K * sc * sc, which ? c.nrot : c.ndof, c.T);
+    for (int k = 0; k < 3; ++k) e[k] = df_add(e[k], df_mul(c.d.hdt, df_mul(p[k], iq[k])));
+    const dfl K2 = df_mul(K, df_mul(sc, sc));
+    u4_df(c.d.t4, 1, 3, 1, p, iq, K2, dofT, c.d.T);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        eta[k] = e[k];
-        eta[3 + k] = p[k];
+        eta[k] = df_to_double(e[k]);
+        eta[3 + k] = df_to_double(p[k]);
     }
-    nh[12 + which] = sc;
-    reinterpret_cast<float*>(nh + 18)[which] = (float)sc;
-    if (!which) nh[16] = K * sc * sc;
+    nh[12 + which] = df_to_double(sc);
+    reinterpret_cast<float*>(nh + 18)[which] = sc.hi + sc.lo;
+    if (!which) nh[16] = df_to_double(K2);
 }
 
 // threads 0 (translation) and 32 (rotation, or the unit scale without it).
@@ -650,7 +679,7 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
             vx = (float)vx; vy = (float)vy; vz = (float)vz;
             K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
         }
-        u4<false>(c.dt / 4.0, 3, 1, -1, p, ih, K, c.ndof, c.T);
+        u4(c.dt / 4.0, 3, 1, -1, p, ih, K, c.ndof, c.T);
         const double sc = exp_chain(-0.5 * c.dt * p[0] * ih[0]);
         {
             const double ox = vx, oy = vy, oz = vz;
@@ -659,7 +688,7 @@ __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, fl
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] * ih[k];
-        u4<false>(c.dt / 4.0, 1, 3, 1, p, ih, K, c.ndof, c.T);
+        u4(c.dt / 4.0, 1, 3, 1, p, ih, K, c.ndof, c.T);
         if (initial) {
             const double ox = vx, oy = vy, oz = vz;
             vx = (float)(vx + h * (f.x * im)); vy = (float)(vy + h * (f.y * im)); vz = (float)(vz + h * (f.z * im));
@@ -704,6 +733,19 @@ NhConst nh_const(const sg_ctx* ctx, double dt, double T, double coupling) {
     for (int k = 0; k < 3; ++k) {
         c.iHB[k] = 1.0 / c.HB[k];
         c.iHBr[k] = 1.0 / c.HBr[k];
+    }
+    auto split = [](double x) {
+        const float h = (float)x;
+        return dfl{h, (float)(x - (double)h)};
+    };
+    c.d.t4 = split(dt / 4.0);
+    c.d.hdt = split(0.5 * dt);
+    c.d.T = split(T);
+    c.d.ndofT = split(c.ndof * T);
+    c.d.nrotT = split(c.nrot * T);
+    for (int k = 0; k < 3; ++k) {
+        c.d.iHB[k] = split(c.iHB[k]);
+        c.d.iHBr[k] = split(c.iHBr[k]);
     }
     return c;
 }

@@ -269,33 +269,6 @@ SG_DEV void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
-// Exact FP32 -> FP64 widening on the integer pipe: the exponent is rebiased
-// and the significand shifted into place, the same bits the conversion
-// instruction gives for every normal number, infinity and NaN (zero and
-// subnormals give a signed zero). On GB300 the conversion instructions share
-// the FP64 pipe, which runs at 1/64 of the FP32 rate.
-SG_DEV double widen(float x) {
-    const unsigned u = __float_as_uint(x);
-    const unsigned e = u & 0x7f800000u, sgn = u & 0x80000000u, m = (u >> 3) & 0x000fffffu;
-    unsigned hi = sgn | ((e >> 3) + (896u << 20)) | m, lo = u << 29;
-    if (e == 0u) { hi = sgn; lo = 0u; }
-    if (e == 0x7f800000u) hi = sgn | 0x7ff00000u | m;
-    return __hiloint2double((int)hi, (int)lo);
-}
-
-// FP64 -> FP32 on the integer pipe, truncating the significand (relative
-// error below 2^-23); magnitudes under the FP32 normal range give a signed
-// zero, over it a NaN. For residuals that enter only as small corrections.
-SG_DEV float narrow_trunc(double x) {
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    const unsigned sgn = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7ffu) - 896;
-    unsigned u = sgn | ((unsigned)e << 23) | ((hi & 0x000fffffu) << 3) | (lo >> 29);
-    if (e <= 0) u = sgn;
-    if (e >= 255) u = sgn | 0x7fc00000u;
-    return __uint_as_float(u);
-}
-
 // e = r - G K in FP64 arithmetic. G = A + lam D is formed exactly as gh + gl
 // on the FP32 pipe (gh = fl(A + lam D); gl its rounding error, to 2^-48 |G|);
 // r, gh and K are widened exactly, so every product gh_ij K_j is exact in FP64
