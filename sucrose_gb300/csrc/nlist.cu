@@ -597,7 +597,7 @@ __global__ void k_set_request(int* flags, int* rep_flag, int R) {
 // kernels. Arrays written in one phase and read in a later one are read with
 // plain (coherent) loads, never through the read-only path.
 struct CoopBuild {
-    int n, ncells, max_nb, row_lanes;
+    int n, ncells, ncells_cap, max_nb, row_lanes;
     const float4* pos;
     ListGeom g;
     int* cell_count;
@@ -653,7 +653,7 @@ __device__ __forceinline__ void coop_scan(cg::grid_group& grid, const int* in, i
     if (threadIdx.x == 0) tmp[blockIdx.x] = btot;
     grid.sync();
     int o = 0;
-    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) o += tmp[b];
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) o += __ldcg(tmp + b);   // L2: rewritten per scan
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) o += __shfl_xor_sync(0xffffffffu, o, d);
     __syncthreads();
@@ -679,20 +679,15 @@ __device__ __forceinline__ void coop_scan(cg::grid_group& grid, const int* in, i
     __syncthreads();   // sh is reused by the next scan
 }
 
-__global__ void __launch_bounds__(256, 3) k_build_coop(CoopBuild a) {
+__global__ void __launch_bounds__(256, 4) k_build_coop(CoopBuild a) {
     if (!a.flags[F_REBUILD]) return;   // grid-uniform: cleared only after the last barrier
     cg::grid_group grid = cg::this_grid();
     const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
     const int gw = gt >> 5, nwarps = gs >> 5;
-    // zero the cell counters
-    for (int c = gt; c < a.ncells; c += gs) {
-        a.cell_count[c] = 0;
-        a.cell_fill[c] = 0;
-    }
+    // bin (cell_count is zero: the previous build cleared it after its scan)
+    for (int c = gt; c < a.ncells; c += gs) a.cell_fill[c] = 0;
     if (gt == 0) a.flags[F_OVERFLOW] = 0;
-    grid.sync();
-    // bin
     for (int i = gt; i < a.n; i += gs) {
         int cx, cy, cz;
         const int c = cell_of(a.pos[i], a.g, cx, cy, cz);
@@ -702,11 +697,12 @@ __global__ void __launch_bounds__(256, 3) k_build_coop(CoopBuild a) {
     grid.sync();
     coop_scan(grid, a.cell_count, a.ncells, a.cell_start, nullptr, a.tmp);
     grid.sync();
-    // members in arrival order
+    // members in arrival order; the counts are cleared for the next build
     for (int i = gt; i < a.n; i += gs) {
         const int c = a.particle_cell[i];
         a.cell_unsorted[a.cell_start[c] + atomicAdd(&a.cell_fill[c], 1)] = i;
     }
+    for (int c = gt; c < a.ncells_cap; c += gs) a.cell_count[c] = 0;
     grid.sync();
     // each cell's members by index (a warp per cell, each member at its rank),
     // their positions in the same order
@@ -733,13 +729,18 @@ __global__ void __launch_bounds__(256, 3) k_build_coop(CoopBuild a) {
     grid.sync();
     coop_scan(grid, a.nb_count, a.n, a.row_off, a.flags + F_NPAIRS, a.tmp);
     grid.sync();
-    // rows into the flat pair arrays (a warp per row, contiguous on both
-    // sides); the positions of this build
-    for (int i = gw; i < a.n; i += nwarps) {
-        const int c = a.nb_count[i], o = a.row_off[i];
-        for (int k = lane; k < c; k += 32) {
-            a.pair_i[o + k] = i;
-            a.pair_j[o + k] = a.nb_pad[(size_t)i * a.max_nb + k];
+    // rows into the flat pair arrays, contiguous on both sides: a warp per
+    // row for dense cells, 8 lanes per row for sparse ones (rows of ~8)
+    {
+        const int G = a.row_lanes == 32 ? 32 : 8;
+        const int sub = lane & (G - 1);
+        const int ng = gs / G;
+        for (int i = gt / G; i < a.n; i += ng) {
+            const int c = a.nb_count[i], o = a.row_off[i];
+            for (int k = sub; k < c; k += G) {
+                a.pair_i[o + k] = i;
+                a.pair_j[o + k] = a.nb_pad[(size_t)i * a.max_nb + k];
+            }
         }
     }
     for (int i = gt; i < a.n; i += gs) a.last[i] = a.pos[i];
@@ -856,6 +857,7 @@ int enqueue_build(sg_ctx* ctx) {
         CoopBuild a;
         a.n = n;
         a.ncells = nl.ncells;
+        a.ncells_cap = nl.ncells_cap;
         a.max_nb = nl.max_nb;
         a.row_lanes = nl.row_lanes;
         a.pos = ctx->pos;
@@ -876,7 +878,12 @@ int enqueue_build(sg_ctx* ctx) {
         a.flags = nl.dev_flags;
         a.tmp = nl.coop_tmp;
         void* args[] = {&a};
-        SG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_build_coop, nl.coop_grid, 256, args, 0, ctx->stream));
+        // as many blocks as the row search has rows (a thread per row, or a
+        // warp per row for dense cells), up to what is resident at once:
+        // blocks without rows would wait at each barrier while the search runs
+        const int64_t row_threads = (int64_t)n * (nl.row_lanes ? nl.row_lanes : 1);
+        const int grid = (int)std::min<int64_t>(nl.coop_grid, std::max<int64_t>(ctx->num_sms, (row_threads + 255) / 256));
+        SG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_build_coop, grid, 256, args, 0, ctx->stream));
         return SG_OK;
     }
     if (nl.use_cells) {
@@ -1049,6 +1056,8 @@ static int alloc_list(sg_ctx* ctx, int max_nb) {
     int ntiles = std::max((n + SCAN_TILE - 1) / SCAN_TILE, (nl.ncells + SCAN_TILE - 1) / SCAN_TILE) + 2;
     nl.ncells_cap = nl.ncells;
     SG_CUDA(ctx, cudaMalloc(&nl.cell_count, sizeof(int) * (size_t)nl.ncells));
+    // zero before the first build: the cooperative build clears the counts after use
+    SG_CUDA(ctx, cudaMemsetAsync(nl.cell_count, 0, sizeof(int) * (size_t)nl.ncells, ctx->stream));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_start, sizeof(int) * ((size_t)nl.ncells + 1)));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_fill, sizeof(int) * (size_t)nl.ncells));
     SG_CUDA(ctx, cudaMalloc(&nl.cell_particles, sizeof(int) * (size_t)n));
