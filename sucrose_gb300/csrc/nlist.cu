@@ -359,23 +359,29 @@ __device__ __forceinline__ void xrange_row(int w, int sub, int g0, unsigned gmas
 }
 
 // One row of a single system by one thread: row t of the cell order over the
-// 27 cells (cell-ordered candidates, contiguous loads), written row-major.
+// stencil's nine x ranges (as xrange_row, the same order as a walk over the 27
+// cells; cell-ordered candidates, contiguous loads), written row-major.
 __device__ __forceinline__ void cells_row(int t, const ListGeom& g, const int* cell_start, const int* cell_particles,
                                           const float4* pos_cell, int max_nb, int* nb_pad, int* nb_count,
                                           int* flags) {
+    const int nx = g.nc[0];
     const int i = cell_particles[t];
     const float4 pi = pos_cell[t];
     const size_t base = (size_t)i * max_nb;
     int cnt = 0;
     int cx, cy, cz;
     cell_of(pi, g, cx, cy, cz);
+    int lo0 = cx - 1, hi0 = cx + 1, lo1 = 0, hi1 = -1;
+    if (cx == 0) { lo0 = nx - 1; hi0 = nx - 1; lo1 = 0; hi1 = 1; }
+    else if (cx == nx - 1) { hi0 = nx - 1; lo1 = 0; hi1 = 0; }
     for (int dz = -1; dz <= 1; ++dz) {
         const int zz = wrapc(cz + dz, g.nc[2]);
         for (int dy = -1; dy <= 1; ++dy) {
-            const int yy = wrapc(cy + dy, g.nc[1]);
-            for (int dx = -1; dx <= 1; ++dx) {
-                const int c = (zz * g.nc[1] + yy) * g.nc[0] + wrapc(cx + dx, g.nc[0]);
-                const int b = cell_start[c], e = cell_start[c + 1];
+            const int row = (zz * g.nc[1] + wrapc(cy + dy, g.nc[1])) * nx;
+            for (int sgm = 0; sgm < 2; ++sgm) {
+                const int clo = sgm ? lo1 : lo0, chi = sgm ? hi1 : hi0;
+                if (chi < clo) continue;
+                const int b = cell_start[row + clo], e = cell_start[row + chi + 1];
                 for (int k = b; k < e; ++k) {
                     const int j = cell_particles[k];
                     if (j <= i) continue;
