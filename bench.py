@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--reps", type=int, default=3, help="launches of the profiled kernels (--profile-case)")
     ap.add_argument("--ecp-path", default=None, choices=["split", "fused", "filtered"],
                     help="ECP profile cases: the split Newton path, the one-kernel path or the one kernel behind the support-function range test (default: untuned)")
+    ap.add_argument("--launch", default=None,
+                    help="block,filter of the headline pair kernel instead of autotuning (e.g. 128,2)")
     ap.add_argument("--state-equil", type=int, default=0,
                     help="untimed Langevin steps from the placed state before timing (ecp, gb)")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000)
@@ -397,7 +399,15 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
         configure(g, w, pair_params(g, w, "newton"), langevin=True, first_step=1)
         g.step(a.state_equil)
         g.step_check()
-    tune = g.autotune(pp, reps=5)      # launch shape of the pair kernel on the live list
+    if a.launch:
+        # a fixed launch shape instead of the autotuner's pick (profiling
+        # under ncu, whose per-kernel overhead would skew the tuner's timings)
+        from sucrose_gb300 import capi as _c
+        tune = _c.TuneResult()
+        tune.block, tune.filter = [int(x) for x in a.launch.split(",")]
+        g.set_launch(pp.kind, tune.block, tune.filter)
+    else:
+        tune = g.autotune(pp, reps=5)      # launch shape of the pair kernel on the live list
     configure(g, w, pp, first_step=a.state_equil + 1)
     g.step(max(a.warmup, 3))
     g.step_check()

@@ -58,6 +58,7 @@ int sg_mc_barostat(sg_ctx* ctx, const sg_pair_params* pairs, int32_t npairs, int
                    uint64_t counter, int32_t* accept, double* volume_out) {
     if (!ctx || (npairs > 0 && !pairs) || npairs < 0 || !accept) return SG_EINVAL;
     if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "the barostat is per system: no replica contexts");
+    sg_state_touched(ctx);
     if (!ctx->periodic) return sg_fail(ctx, SG_EINVAL, "the barostat needs a periodic box");
     // the reference stops here (integrators.f90:879-882)
     if (target_pressure <= 1e-3) return sg_fail(ctx, SG_EINVAL, "Target pressure too small.");

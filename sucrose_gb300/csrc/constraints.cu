@@ -543,6 +543,7 @@ int sg_constraints_save(sg_ctx* ctx) {
 
 int sg_constraints_a(sg_ctx* ctx, double dt) {
     if (int rc = need(ctx)) return rc;
+    sg_state_touched(ctx);
     if (ctx->con_nsmall) {
         const int grid = con_grid(ctx, ctx->con_nsmall, kSmallBlock);
         if (int rc = sg_ensure_partials(ctx, grid)) return rc;
@@ -563,6 +564,7 @@ int sg_constraints_a(sg_ctx* ctx, double dt) {
 
 int sg_constraints_b(sg_ctx* ctx, double dt) {
     if (int rc = need(ctx)) return rc;
+    sg_state_touched(ctx);
     if (ctx->con_nsmall) {
         const int grid = con_grid(ctx, ctx->con_nsmall, kSmallBlock);
         if (int rc = sg_ensure_partials(ctx, grid)) return rc;

@@ -117,6 +117,7 @@ int sg_destroy(sg_ctx* ctx) {
     if (ctx->d_stage) cudaFree(ctx->d_stage);
     if (ctx->rep_alloc) cudaFree(ctx->rep_alloc);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph_exec_cont) cudaGraphExecDestroy(ctx->graph_exec_cont);
     if (ctx->step_dev) cudaFree(ctx->step_dev);
     if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -333,6 +334,7 @@ int sg_set_particles(sg_ctx* ctx, const double* mass, const double* sig_x, const
                      const double* eps_x, const double* eps_y, const double* eps_z, const double* ixx,
                      const double* iyy, const double* izz) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     const int n = ctx->n;
     std::vector<double> m(n, 1.0), sx(n, 1.0), sy(n, 1.0), sz(n, 1.0), ex(n, 1.0), ey(n, 1.0), ez(n, 1.0);
     std::vector<double> Ix(n), Iy(n), Iz(n), Ixi(n), Iyi(n), Izi(n), im(n);
@@ -393,6 +395,7 @@ int sg_upload_state(sg_ctx* ctx, const double* rx, const double* ry, const doubl
                     const double* qx, const double* qy, const double* qz, const double* vx, const double* vy,
                     const double* vz, const double* lx, const double* ly, const double* lz) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     {
         // every given column mapped page-locked memory: one kernel for the state
         const double* in[13] = {rx, ry, rz, qw, qx, qy, qz, vx, vy, vz, lx, ly, lz};

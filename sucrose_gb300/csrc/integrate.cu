@@ -290,7 +290,8 @@ __global__ void k_lgv_final(int n, float dt, float4* __restrict__ vel, const flo
 // [6..8] eta_r, [9..11] p_eta_r, [12] translational scale, [13] rotational
 // scale, [14] sum m v^2 scratch, [15] sum L_b^2/I scratch, [16] the scaled
 // sum m v^2, [17] the compat sweep's KE, [18] the two scales rounded to FP32
-// (a float pair: the particle kernels read them without an FP64 conversion).
+// (a float pair: the particle kernels read them without an FP64 conversion),
+// [22], [23] 2 KE and 2 KE_rot of the last fused final half step.
 // The standard chain's constants in double-float (hi + lo split on the host).
 struct NhDf {
     dfl t4, hdt, T, ndofT, nrotT;   // dt/4, dt/2, T, ndof T, nrot T
@@ -465,6 +466,23 @@ __global__ void k_nhc_chain(NhConst c, double* nh, int rot) {
     nhc_chain_threads(c, nh, rot, nullptr);
 }
 
+// The initial chain from the sums the previous step's final half stored in
+// nh[22], nh[23]: sum m v^2 = 2 KE and sum L_b^2/I = 2 KE_rot. Both sums run
+// the same grid partition in double-float, where halving is exact, so these
+// are the bits k_nhc_sum_chain would compute from the unchanged state.
+__global__ void k_nhc_chain_acc(NhConst c, double* nh, int rot) {
+    pdl_trigger();   // the particle pass may start loading: this kernel writes only nh
+    __shared__ double tot[2];
+    if (threadIdx.x == 0) {
+        tot[0] = nh[22];
+        tot[1] = nh[23];
+        nh[14] = tot[0];
+        nh[15] = tot[1];
+    }
+    __syncthreads();
+    nhc_chain_threads(c, nh, rot, tot);
+}
+
 // the translational and rotational scales as FP32 (nh[18])
 SG_DEV float2 nh_scale_f(const double* nh) { return *reinterpret_cast<const float2*>(nh + 18); }
 
@@ -569,7 +587,7 @@ __global__ void k_nhc_final_fused(int n, const double* nh, float dt, float4* __r
                                   const float4* __restrict__ shape, const float4* __restrict__ quat,
                                   float4* __restrict__ angm, const float4* __restrict__ torque,
                                   const float4* __restrict__ inert_inv, int rot_chain, int rotations, double* partials,
-                                  unsigned int* done, double* acc, int* step_inc) {
+                                  unsigned int* done, double* acc, int* step_inc, double* sums) {
     dfl e[2] = {{0.f, 0.f}, {0.f, 0.f}};
     const float h = 0.5f * dt;
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
@@ -607,9 +625,14 @@ __global__ void k_nhc_final_fused(int n, const double* nh, float dt, float4* __r
             }
         }
     }
-    // the sums are stored; step_inc (captured step): the step counter advances
-    if (block_reduce_finish_df<2>(e, partials, done, acc, true) && step_inc && threadIdx.x == 0)
-        *step_inc += 1;
+    // the sums are stored; step_inc (captured step): the step counter advances;
+    // sums: 2 KE and 2 KE_rot, the next initial chain's sums (k_nhc_chain_acc)
+    __shared__ double tot[2];
+    if (block_reduce_finish_df<2>(e, partials, done, acc, true, tot) && threadIdx.x == 0) {
+        if (step_inc) *step_inc += 1;
+        sums[0] = 2.0 * tot[0];
+        sums[1] = 2.0 * tot[1];
+    }
 }
 
 // scale v (and L), then optionally the VV kick + drift (initial step)
@@ -773,6 +796,7 @@ extern "C" {
 
 int sg_vv_initial(sg_ctx* ctx, double dt) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     k_vv_initial<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, (float)dt, make_geo(ctx), ctx->pos, ctx->vel,
                                                                 ctx->force);
     SG_LAUNCH_CHECK(ctx, "k_vv_initial");
@@ -781,6 +805,7 @@ int sg_vv_initial(sg_ctx* ctx, double dt) {
 
 int sg_vv_final(sg_ctx* ctx, double dt, double* kin_eng) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double), ctx->stream));
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid)) return rc;
@@ -792,6 +817,7 @@ int sg_vv_final(sg_ctx* ctx, double dt, double* kin_eng) {
 
 int sg_qq_initial(sg_ctx* ctx, double dt) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     k_qq_initial<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, (float)dt, ctx->quat, ctx->angm, ctx->torque,
                                                                 ctx->inert_inv);
     SG_LAUNCH_CHECK(ctx, "k_qq_initial");
@@ -800,6 +826,7 @@ int sg_qq_initial(sg_ctx* ctx, double dt) {
 
 int sg_qq_final(sg_ctx* ctx, double dt, double* kin_rot) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 3, 0, sizeof(double), ctx->stream));
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid)) return rc;
@@ -811,6 +838,7 @@ int sg_qq_final(sg_ctx* ctx, double dt, double* kin_rot) {
 
 int sg_lgv_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double target_temp, const uint32_t* key) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     LgvConst c;
     c.step_dev = ctx->lgv_step_dev;
     c.dt = (float)dt;
@@ -841,6 +869,7 @@ int sg_lgv_initial(sg_ctx* ctx, double dt, int32_t step, double damping, double 
 int sg_lgv_final(sg_ctx* ctx, double dt, double damping, double* kin_eng, double* kin_rot) {
     (void)damping;
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     if (!ctx->step_fused) SG_CUDA(ctx, cudaMemsetAsync(ctx->acc + 2, 0, sizeof(double) * 2, ctx->stream));
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
@@ -857,6 +886,7 @@ int sg_lgv_final(sg_ctx* ctx, double dt, double damping, double* kin_eng, double
 
 int sg_nht_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "Nose-Hoover chains are per system: not available on a replica context");
     if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
     NhConst c = nh_const(ctx, dt, target_temp, coupling);
@@ -880,6 +910,7 @@ int sg_nht_initial(sg_ctx* ctx, double dt, double target_temp, double coupling, 
 int sg_nht_final(sg_ctx* ctx, double dt, double target_temp, double coupling, int32_t mode, int32_t rot_chain,
                  double* kin_eng) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     if (ctx->nrep) return sg_fail(ctx, SG_EINVAL, "Nose-Hoover chains are per system: not available on a replica context");
     if (!(target_temp > 0.0)) return sg_fail(ctx, SG_EINVAL, "Target temperature not set.");
     NhConst c = nh_const(ctx, dt, target_temp, coupling);
@@ -917,9 +948,12 @@ int sg_nhc_step_initial(sg_ctx* ctx, double dt, double target_temp, double coupl
     NhConst c = nh_const(ctx, dt, target_temp, coupling);
     int grid = reduce_grid(ctx);
     if (int rc = sg_ensure_partials(ctx, grid * 2)) return rc;
-    k_nhc_sum_chain<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, 0, ctx->vel, ctx->force, ctx->shape, ctx->quat,
-                                                  ctx->angm, ctx->inert_inv, rot_chain, c, ctx->partials,
-                                                  ctx->done_counter, ctx->nh);
+    if (ctx->step_sums_from_acc)
+        k_nhc_chain_acc<<<1, 64, 0, ctx->stream>>>(c, ctx->nh, rot_chain);
+    else
+        k_nhc_sum_chain<<<grid, 256, 0, ctx->stream>>>(ctx->n, (float)dt, 0, ctx->vel, ctx->force, ctx->shape,
+                                                      ctx->quat, ctx->angm, ctx->inert_inv, rot_chain, c,
+                                                      ctx->partials, ctx->done_counter, ctx->nh);
     StepEpi epi;
     if (int rc = make_step_epi(ctx, epi)) return rc;
     // programmatic dependent launch: the particle loads overlap the chain
@@ -948,7 +982,7 @@ int sg_nhc_step_final(sg_ctx* ctx, double dt, double target_temp, double couplin
                             (float)dt, ctx->vel, (const float4*)ctx->shape, (const float4*)ctx->quat, ctx->angm,
                             (const float4*)ctx->torque, (const float4*)ctx->inert_inv, (int)rot_chain,
                             (int)rotations, ctx->partials, ctx->done_counter, ctx->acc + 2,
-                            ctx->step_fused ? ctx->step_dev : nullptr));
+                            ctx->step_fused ? ctx->step_dev : nullptr, ctx->nh + 22));
     return SG_OK;
 }
 

@@ -245,6 +245,7 @@ extern "C" {
 
 int sg_set_types(sg_ctx* ctx, const int32_t* type) {
     if (!ctx) return SG_EINVAL;
+    sg_state_touched(ctx);
     ctx->h_types.assign(ctx->n, 0);
     // initialize_system (fortran/system.f90:590-593): a negative type becomes 0
     for (int i = 0; type && i < ctx->n; ++i) ctx->h_types[i] = type[i] < 0 ? 0 : type[i];
@@ -466,6 +467,7 @@ int sg_save_state(sg_ctx* ctx, const char* path) {
 
 int sg_load_state(sg_ctx* ctx, const char* path) {
     if (!ctx || !path) return SG_EINVAL;
+    sg_state_touched(ctx);
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     FILE* f = std::fopen(path, "rb");
     if (!f) return sg_fail(ctx, SG_EINVAL, "cannot open %s", path);

@@ -229,6 +229,16 @@ struct sg_ctx {
 
     // captured whole-step graph (sg_step)
     cudaGraphExec_t graph_exec = nullptr;
+    // the same step for the launches after the first of an sg_step call: the
+    // Nose-Hoover initial chain takes the kinetic sums the previous step's
+    // final half stored (nothing can change the state between those launches)
+    cudaGraphExec_t graph_exec_cont = nullptr;
+    int step_sums_from_acc = 0;      // set while enqueuing that step
+    // host calls that write the particle state bump state_version; sg_step
+    // records it after its launches, so that the first launch of the next
+    // call may take the stored sums only when nothing was written in between
+    unsigned state_version = 0;
+    unsigned step_clean_version = ~0u;
     int* step_dev = nullptr;         // device step counter used by the captured Langevin kernel
     const int* lgv_step_dev = nullptr;  // set while enqueuing a step: Langevin reads the counter here
     int lgv_rotations = 1;           // Langevin also thermostats rotation
@@ -266,6 +276,9 @@ int sg_cuda_check(sg_ctx* ctx, cudaError_t e, const char* what);
     } while (0)
 #define SG_LAUNCH_CHECK(ctx, what) SG_CUDA(ctx, cudaGetLastError())
 
+// A host call wrote velocities, angular momenta, orientations or particle
+// constants: the next captured step recomputes its kinetic sums.
+inline void sg_state_touched(sg_ctx* ctx) { ctx->state_version++; }
 int sg_ensure_partials(sg_ctx* ctx, int slots);
 int sg_ensure_stage(sg_ctx* ctx, size_t bytes);
 extern "C" int sg_ensure_dstage(sg_ctx* ctx);

@@ -105,11 +105,14 @@ void record_event(cudaEvent_t e, cudaStream_t s) { cudaEventRecordWithFlags(e, s
 // ev (optional): 6 events recorded before the initial half step, the list
 // update, the force zeroing, the pair stage, the final half step and the
 // step counter (eager steps only; sg_step_stage_times).
-int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr) {
+// cont: a step that follows another step of the same sg_step call (its
+// Nose-Hoover initial chain reads the sums that step stored; cont_eligible).
+int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr, bool cont = false) {
     const double dt = c.dt;
     ctx->lgv_step_dev = ctx->step_dev;
     ctx->lgv_rotations = c.rotations;
     plan_fusion(ctx, c);
+    ctx->step_sums_from_acc = cont ? 1 : 0;
     ctx->step_events = ev != nullptr;
     const bool fused = ctx->step_fused != 0;
     int rc = SG_OK;
@@ -164,8 +167,59 @@ int enqueue_step(sg_ctx* ctx, const sg_step_config& c, cudaEvent_t* ev = nullptr
     ctx->lgv_rotations = 1;
     ctx->step_fused = 0;
     ctx->step_events = 0;
+    ctx->step_sums_from_acc = 0;
     ctx->step_prep_kind = SG_PREP_NONE;
     return rc;
+}
+
+// Whether the step's launches after the first of a call can take the stored
+// sums: the fused standard Nose-Hoover step, whose final half stores KE and,
+// when the rotational chain is on, KE_rot of the state the next step starts
+// from (it sums KE_rot only when rotations are integrated).
+bool cont_eligible(sg_ctx* ctx, const sg_step_config& c) {
+    if (c.integrator != SG_INT_NH || (c.flags & SG_STEP_CONSTRAINTS)) return false;
+    return !c.rot_chain || c.rotations;
+}
+
+// Capture one step into an executable graph; kernels: its kernel nodes.
+int capture_step(sg_ctx* ctx, const sg_step_config& c, bool cont, cudaGraphExec_t* out, int* kernels) {
+    const unsigned epoch = ctx->graph_epoch;
+    cudaGraph_t graph = nullptr;
+    SG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_step(ctx, c, nullptr, cont);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return sg_cuda_check(ctx, e, "cudaStreamEndCapture");
+    if (epoch != ctx->graph_epoch) {
+        cudaGraphDestroy(graph);
+        return sg_fail(ctx, SG_ECUDA, "a buffer was reallocated while capturing the step");
+    }
+    if (kernels) {
+        size_t nn = 0;
+        cudaGraphGetNodes(graph, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (nn) cudaGraphGetNodes(graph, nodes.data(), &nn);
+        int k = 0;   // kernels launched by a step without a rebuild
+        for (size_t m = 0; m < nn; ++m) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[m], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+        }
+        *kernels = k;
+    }
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return sg_cuda_check(ctx, e, "cudaGraphInstantiate");
+    return SG_OK;
+}
+
+void drop_graphs(sg_ctx* ctx) {
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph_exec_cont) cudaGraphExecDestroy(ctx->graph_exec_cont);
+    ctx->graph_exec = nullptr;
+    ctx->graph_exec_cont = nullptr;
 }
 
 }  // namespace
@@ -182,10 +236,7 @@ int sg_step_configure(sg_ctx* ctx, const sg_step_config* cfg) {
     if (!ctx->step_dev) SG_CUDA(ctx, cudaMalloc(&ctx->step_dev, sizeof(int)));
     SG_CUDA(ctx, cudaMemcpyAsync(ctx->step_dev, &cfg->first_step, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (ctx->graph_exec) {
-        cudaGraphExecDestroy(ctx->graph_exec);
-        ctx->graph_exec = nullptr;
-    }
+    drop_graphs(ctx);
     ctx->step_ready = 1;
     return SG_OK;
 }
@@ -203,51 +254,41 @@ int sg_step(sg_ctx* ctx, int32_t nsteps) {
     if (!ctx->step_ready) return sg_fail(ctx, SG_ENOTREADY, "sg_step_configure must precede sg_step");
     const sg_step_config& c = *reinterpret_cast<const sg_step_config*>(ctx->step_cfg);
     int done = 0;
-    if (ctx->graph_exec && ctx->graph_epoch_captured != ctx->graph_epoch) {
-        cudaGraphExecDestroy(ctx->graph_exec);
-        ctx->graph_exec = nullptr;
-    }
+    if (ctx->graph_exec && ctx->graph_epoch_captured != ctx->graph_epoch) drop_graphs(ctx);
+    // no host call wrote the state since the last step: every launch can take
+    // the sums that step stored
+    const bool clean = ctx->step_clean_version == ctx->state_version;
     if (!ctx->graph_exec && nsteps > 0) {
         // one eager step allocates every buffer the step touches
         if (int rc = enqueue_step(ctx, c)) return rc;
         done = 1;
         SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         const unsigned epoch = ctx->graph_epoch;
-        cudaGraph_t graph = nullptr;
-        SG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_step(ctx, c);
-        cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
-        if (rc) {
-            if (graph) cudaGraphDestroy(graph);
-            return rc;
-        }
-        if (e != cudaSuccess) return sg_cuda_check(ctx, e, "cudaStreamEndCapture");
-        if (epoch != ctx->graph_epoch) {
-            cudaGraphDestroy(graph);
-            return sg_fail(ctx, SG_ECUDA, "a buffer was reallocated while capturing the step");
-        }
-        size_t nn = 0;
-        cudaGraphGetNodes(graph, nullptr, &nn);
-        std::vector<cudaGraphNode_t> nodes(nn);
-        if (nn) cudaGraphGetNodes(graph, nodes.data(), &nn);
-        int kernels = 0;   // kernels launched by a step without a rebuild
-        for (size_t k = 0; k < nn; ++k) {
-            cudaGraphNodeType t;
-            if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
-        }
+        int kernels = 0;
+        if (int rc = capture_step(ctx, c, false, &ctx->graph_exec, &kernels)) return rc;
+        if (cont_eligible(ctx, c))
+            if (int rc = capture_step(ctx, c, true, &ctx->graph_exec_cont, nullptr)) {
+                drop_graphs(ctx);
+                return rc;
+            }
         ctx->graph_kernels = kernels;
-        e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return sg_cuda_check(ctx, e, "cudaGraphInstantiate");
         ctx->graph_epoch_captured = epoch;
     }
-    for (int s = done; s < nsteps; ++s) SG_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    // a launch after a step of this call, or after one of an earlier call
+    // with no state written since, takes the stored sums; otherwise the step
+    // recomputes them
+    for (int s = done; s < nsteps; ++s) {
+        cudaGraphExec_t ge = ((s > 0 || clean) && ctx->graph_exec_cont) ? ctx->graph_exec_cont : ctx->graph_exec;
+        SG_CUDA(ctx, cudaGraphLaunch(ge, ctx->stream));
+    }
+    if (nsteps > 0) ctx->step_clean_version = ctx->state_version;
     return SG_OK;
 }
 
 int sg_step_stage_times(sg_ctx* ctx, int32_t nsteps, double out_ms[7]) {
     if (!ctx || !out_ms || nsteps < 1) return SG_EINVAL;
     if (!ctx->step_ready) return sg_fail(ctx, SG_ENOTREADY, "sg_step_configure must precede sg_step_stage_times");
+    sg_state_touched(ctx);
     const sg_step_config& c = *reinterpret_cast<const sg_step_config*>(ctx->step_cfg);
     // one step captured with an event-record node between the stages, so the
     // stages are timed as the captured step runs them (no host launch gaps)

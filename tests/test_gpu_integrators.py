@@ -211,6 +211,48 @@ def test_fused_nose_hoover_step_matches_separate_calls(lib):
     a.step_check()
 
 
+def _nh_configured(p, dt, T):
+    from sucrose_gb300 import capi
+    g = _nh_system()
+    g.zero_forces()
+    g.pair_forces(p)
+    g.configure_step(p, integrator=capi.INT_NH, dt=dt, target_temp=T, rotations=1, rot_chain=1)
+    return g
+
+
+def test_nose_hoover_steps_take_the_stored_sums_bit_for_bit(lib):
+    """Launches after the first of a step call start their chain from the
+    kinetic sums the previous final half stored (no grid-wide sum): the same
+    bits as steps that recompute them, whether the steps come in one call, in
+    calls of one step, or after a state write that forces the sums again."""
+    from sucrose_gb300 import capi
+    dt, T = 0.001, 1.2
+    p = _nh_system().params(capi.ECPR, cutoff=3.0, solver=capi.SOLVER_NEWTON)
+    a, b, c = _nh_configured(p, dt, T), _nh_configured(p, dt, T), _nh_configured(p, dt, T)
+    a.step(6)                       # one call: five launches take the stored sums
+    for _ in range(6):
+        b.step(1)                   # calls of one step, nothing written between
+    for k in range(6):
+        c.configure_step(p, integrator=capi.INT_NH, dt=dt, target_temp=T, rotations=1, rot_chain=1)
+        c.step(1)                   # re-captured each time: every step sums the state itself
+    for g in (a, b, c):
+        g.step_check()
+    sa, sb, sc = a.download(), b.download(), c.download()
+    for x, y, z in zip(sa, sb, sc):
+        assert np.array_equal(x, y) and np.array_equal(x, z)
+    assert np.array_equal(a.nht_state(), b.nht_state()) and np.array_equal(a.nht_state(), c.nht_state())
+    # a host write between calls: the next step must sum the written state
+    r, q, v, l = a.download()
+    for g in (a, c):
+        g.upload(v=f32(1.05 * v))
+    c.configure_step(p, integrator=capi.INT_NH, dt=dt, target_temp=T, rotations=1, rot_chain=1)
+    a.step(2)
+    c.step(2)
+    for x, y in zip(a.download(), c.download()):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a.nht_state(), c.nht_state())
+
+
 def _gb_system(seed=6):
     sig, eps = (1.0, 1.0, 3.0), (1.0, 1.0, 0.2)
     r, q, box = ellipsoids((16, 16, 8), sig, 0.3, seed=seed, tilt=0.05)
