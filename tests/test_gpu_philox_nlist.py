@@ -66,6 +66,29 @@ def test_nlist_dense_cells_long_range(lib):
     assert _pairs_equal(P, 6.0, 0.4) > 100000
 
 
+def test_nlist_dense_cells_follow_box_changes(lib):
+    # a dense system (a warp per row over the stencil's x ranges) through a
+    # shrinking and a growing box: each rebuilt list is the oracle's pair set,
+    # so the cell grid followed the box
+    rng = np.random.default_rng(12)
+    box0 = (4096 / 0.3) ** (1 / 3)
+    r0 = rng.uniform(-box0 / 2, box0 / 2, size=(4096, 3))
+    P = Pair(r0, None, box0)
+    P.g.init_nlist(0.4, 6.0)
+    assert _pairs_equal(P, 6.0, 0.4) > 100000
+    for s in (0.97, 1.1, 1.0, 0.9):
+        r = np.asarray(r0 * s, dtype=np.float32).astype(np.float64)
+        box = box0 * s
+        P.g.set_box((box, box, box))
+        P.g.upload(r=r)
+        P.g.build_nlist()
+        pi, pj = P.g.pairs()
+        o = O.System(P.n, box)
+        o.rx[:], o.ry[:], o.rz[:] = r.T
+        oi, oj = o.pairs(6.0, 0.4)
+        assert np.array_equal(pi, oi) and np.array_equal(pj, oj), s
+
+
 def test_nlist_threshold_pairs(lib):
     # pairs placed within a few ulps of (rc+skin) on both sides, across the
     # periodic boundary: the FP64 re-test must decide them like the reference
