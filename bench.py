@@ -2,7 +2,9 @@
 
 Workload (default "ecp"): N = 65536 biaxial ellipsoids, semi-axes (1.5, 1, 0.5)
 (full axes sig = (3, 2, 1)), packing fraction 0.35 (number density 0.1114),
-repulsive ECP (ecpr) with the plain Newton contact solve, Nose-Hoover chains
+repulsive ECP (ecpr) with the Newton contact solve from the support-function
+start (the autotuner's launch: pairs beyond two upper bounds on the contact
+distance skip the solve, forces unchanged), Nose-Hoover chains
 of length 3 on translation and rotation, T* = 1.2, dt = 0.001, Verlet list
 rc 3.0 + skin 0.3. Synthetic, seeded: uniform random orientations and
 non-overlapping positions from the isotropic placement
@@ -11,8 +13,8 @@ relaxation), thermal velocities and angular momenta; the reference publishes
 no placement routine and no benchmark data set. Both arms start from the same
 bits of that state.
 
-A step is one full timestep (integrators, list check with conditional
-rebuild, forces) launched as one captured CUDA graph. value = listed pairs x
+A step is one full timestep (integrators, list check and rebuild when due,
+forces) launched as one captured CUDA graph. value = listed pairs x
 steps / device time of those steps; e2e repeats the measurement through the
 C ABI with FP64 host arrays copied in and out every step. The default line
 also carries the Gay-Berne fluid ("gb") and the 4096-replica ensemble
@@ -61,7 +63,7 @@ def parse():
     ap.add_argument("--nrep", type=int, default=4096, help="replicas (config replicas)")
     ap.add_argument("--rep-equil", type=int, default=300, help="untimed equilibration steps (config replicas)")
     ap.add_argument("--flat-graph", action="store_true",
-                    help="list build as flag-gated kernels instead of a conditional graph node (for ncu launch lists)")
+                    help="replica contexts: list build as flag-gated kernels instead of a conditional graph node (for ncu launch lists)")
     ap.add_argument("--solver", default="support", choices=["support", "newton", "brent", "mlp"],
                     help="ECP contact solve: Newton from the support-function start (default), from 1/2, "
                          "the reference's Brent, or from the learned guess")
@@ -542,8 +544,9 @@ def ellipsoid_line(a, name, rank=0, world=1, local=0, dist=None, steps=None, ext
                    "dt": w["dt"], "T": w["T"], "seed": w["seed"],
                    "integrator": "Nose-Hoover chains (3) on translation and rotation" if w["integrator"] == "NH"
                    else "Langevin on translation and rotation",
-                   "timed": "the full MD step (integrators, list check with conditional rebuild, forces), "
+                   "timed": "the full MD step (integrators, list check and rebuild when due, forces), "
                             "one captured CUDA graph per step",
+                   "pair_launch": {"block": int(tune.block), "filter": int(tune.filter)},
                    "nematic_P2_initial": p2_initial, "nematic_P2_timed_state": p2_timed, **info,
                    "untimed_equilibration_steps": a.state_equil,
                    "l2": "flushed between timed steps (256 MB write)",

@@ -234,24 +234,22 @@ __device__ __forceinline__ void row_done(int i, int cnt, int cap, int* nb_count,
     }
 }
 
-// block_order (replica contexts): the 256-row block each CTA takes, the
-// blocks with the longest rows first, so that no long block starts late and
-// leaves the other SMs idle at the end (rows and their contents unchanged)
-// pos_cell (a single system): threads take rows in cell order (thread t
-// searches for particle cell_particles[t]), so that the threads of a warp
-// scan overlapping cells and find the candidates' cell-ordered positions in
-// L1; rows and their contents are unchanged.
+// Rows of a replica context, a thread per row over the replica's 27 cells
+// (or every later particle of a replica under three cells per side).
+// block_order: the 256-row block each CTA takes, the blocks with the longest
+// rows first, so that no long block starts late and leaves the other SMs idle
+// at the end (rows and their contents unchanged)
 __global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g0, const int* __restrict__ cell_start,
                              const int* __restrict__ cell_particles, int max_nb, int* nb_pad, int* nb_count,
                              int* flags, RepDev rp, PadRep pr, const int* rep_flag,
-                             const int* __restrict__ block_order, const float4* __restrict__ pos_cell) {
+                             const int* __restrict__ block_order) {
     if (!flags[F_REBUILD]) return;
     const int bx = block_order ? block_order[blockIdx.x] : (int)blockIdx.x;
     const int t = bx * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    const int i = pos_cell ? cell_particles[t] : t;
+    const int i = t;
     if (rp.rep_of && !rep_flag[rp.rep_of[i]]) return;   // this replica keeps its rows
-    float4 pi = pos_cell ? pos_cell[t] : pos[i];
+    const float4 pi = pos[i];
     ListGeom g = g0;
     int first_cell = 0;
     int cnt = 0;
@@ -289,7 +287,7 @@ __global__ void k_rows_cells(int n, const float4* __restrict__ pos, ListGeom g0,
                 for (int k = b; k < e; ++k) {
                     int j = cell_particles[k];
                     if (j <= i) continue;
-                    if (accept_pair(pi, pos_cell ? pos_cell[k] : pos[j], g)) {
+                    if (accept_pair(pi, pos[j], g)) {
                         if (cnt < cap) nb_pad[base + (size_t)cnt * stride] = j;
                         ++cnt;
                     }
@@ -905,7 +903,7 @@ int enqueue_build(sg_ctx* ctx) {
                                                                     nullptr);
         k_rows_cells<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.cell_start, nl.cell_particles, nl.max_nb,
                                                   nl.nb_pad, nl.nb_count, nl.dev_flags, ctx->rep, pad, nl.rep_flag,
-                                                  nl.row_block_order, nullptr);
+                                                  nl.row_block_order);
     } else {
         k_begin<<<1, 32, 0, ctx->stream>>>(nl.dev_flags, nl.cell_count, nl.cell_fill, 0);
         k_rows_all<<<nb, 256, 0, ctx->stream>>>(n, ctx->pos, g, nl.max_nb, nl.nb_pad, nl.nb_count, nl.dev_flags);
