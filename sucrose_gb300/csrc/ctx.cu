@@ -202,7 +202,7 @@ __global__ void k_unpack4_host(int n, const float4* __restrict__ src, HostCols c
 
 // Device address of a host array that kernels can read and write in place:
 // page-locked memory mapped into the device's address space (under unified
-// addressing every cudaHostAlloc allocation is), as the driver reports it for
+// addressing every cudaHostAlloc allocation is), as the CUDA runtime reports it for
 // this very pointer; nullptr otherwise (pageable memory: staged by copies).
 // Queried on every call: a cached answer could outlive the allocation.
 static void* host_view(const void* p) {

@@ -1,6 +1,7 @@
-// Throughput probes for the roofline denominators that the driver does not
-// measure: dependent-chain-free FMA loops in FP32 and FP64, timed with CUDA
-// events on the context stream.
+// Throughput probes for the roofline denominators of the FP32-pipe kernels
+// (the measured peaks at hand cover only HBM and BF16 tensor throughput):
+// dependent-chain-free FMA loops in FP32 and FP64, timed with CUDA events on
+// the context stream.
 #include "sg_internal.cuh"
 
 namespace {
