@@ -323,42 +323,13 @@ __device__ __forceinline__ double exp_chain(double x) {
     return fma(f, x, 1.0);
 }
 
-// u4_propagator: G1 from the supplied sum (m v^2 or L_b^2/I), with
-// exprel(y) = (e^y - 1)/y (integrators.f90:233-301), in FP64: the
-// reference-compat chain, applied once per particle (the standard chain's
-// double-float form is u4_df).
-__device__ __forceinline__ void u4(double t, int j_start, int j_stop, int stride, double (&p)[3], const double* iHB,
-                                   double sum, double ndof, double T) {
-#pragma unroll
-    for (int j = j_start; stride > 0 ? j <= j_stop : j >= j_stop; j += stride) {
-        double gj = (j == 1) ? (sum - ndof * T) : ((p[j - 2] * p[j - 2] * iHB[j - 2]) - T);
-        if (j == 3) {
-            p[2] = p[2] + t * gj;
-        } else {
-            const double x = t * p[j] * iHB[j];
-            const double h = exp_chain(-0.5 * x);
-            const double ex = h * h;
-            double c;
-            if (fabs(x) > 0.01) {
-                c = (ex - 1.0) / (-x);
-            } else {
-                const double g[5] = {1.0 / 1, 1.0 / 6, 1.0 / 120, 1.0 / 5040, 1.0 / 362880};
-                const double y = (0.5 * x) * (0.5 * x);
-                double f = g[4];
-                for (int k = 3; k >= 0; --k) f = f * y + g[k];
-                c = h * f;
-            }
-            p[j - 1] = p[j - 1] * ex + t * gj * c;
-        }
-    }
-}
-
 // The standard chain in double-float arithmetic on the FP32 pipe (~48-bit
 // significands): one thread runs each chain, and a dependent FP64 operation
 // costs it several hundred cycles on GB300, a double-float one a few dozen.
-// u4 as above: G_j, the products and the sums in double-float, the two
-// factors e^-x and exprel(-x) in FP32 (their relative precision enters once
-// per half step, as in the FP64 form).
+// u4_propagator (integrators.f90:233-301): G_1 from the supplied sum (m v^2
+// or L_b^2/I), G_j = p_(j-1)^2 / Q_(j-1) - T, with exprel(y) = (e^y - 1)/y; G_j,
+// the products and the sums in double-float, the two factors e^-x and
+// exprel(-x) in FP32 (their relative precision enters once per half step).
 SG_DEV void u4_df(dfl t, int j_start, int j_stop, int stride, dfl (&p)[3], const dfl (&iq)[3], dfl K, dfl dofT,
                   dfl T) {
 #pragma unroll
@@ -671,67 +642,127 @@ __global__ void k_kick(int n, float dt, float4* __restrict__ vel, const float4* 
 }
 
 // The reference's per-particle chain (integrators.f90:324-352, :372-390): a
-// serial recurrence over particles in index order. The O(N) SUM that the
-// reference repeats at every particle is carried as a running FP64 sum,
-// updated by each particle's change; per-particle terms are in FP64. The
-// chain state stays in registers for the whole sweep (written back at the
-// end), the divisions by the chain masses are products with their
-// reciprocals and the exponential is exp_chain.
+// serial recurrence over particles in index order, one thread. The O(N) SUM
+// that the reference repeats at every particle is carried as a running sum,
+// updated by each particle's change. The recurrence runs in double-float on
+// the FP32 pipe (a dependent FP64 operation costs one thread several hundred
+// cycles on GB300, a double-float one a few dozen): the chain state, the
+// running sum, the per-particle terms (squares exact) and both factors of u4
+// (e^-x and exprel(-x) to ~48 bits, since N applications would accumulate an
+// FP32 factor's rounding) and the scale. The chain masses enter through their
+// reciprocals. The next particle's state is loaded while this one's chain runs.
+
+// e^-x and exprel(-x) = (1 - e^-x)/x in double-float: for |x| <= 1e-3, e^-x
+// by exp_df and 1 - x/2 + x^2/6 in double-float with -x^3/24 + x^4/120 in
+// FP32 (the rest below 1e-20 relative); larger |x| by the FP64 forms of u4.
+SG_DEV void u4_factors_df(dfl x, dfl& ex, dfl& c) {
+    if (!(fabsf(x.hi) <= 1e-3f)) {
+        const double xd = df_to_double(x);
+        const double hh = exp_chain(-0.5 * xd);
+        const double e = hh * hh;
+        double cd;
+        if (fabs(xd) > 0.01) {
+            cd = (e - 1.0) / (-xd);
+        } else {
+            const double y = (0.5 * xd) * (0.5 * xd);
+            cd = hh * (1.0 + y * (1.0 / 6 + y * (1.0 / 120 + y * (1.0 / 5040 + y / 362880))));
+        }
+        ex = df_from_double(e);
+        c = df_from_double(cd);
+        return;
+    }
+    ex = exp_df(df_neg(x));
+    constexpr float kSixthHi = 1.f / 6.f;
+    constexpr float kSixthLo = (float)(1.0 / 6.0 - (double)kSixthHi);
+    const float tail = x.hi * x.hi * x.hi * fmaf(x.hi, 1.f / 120.f, -1.f / 24.f);
+    c = df_add(df_add(df_of(1.f), dfl{-0.5f * x.hi, -0.5f * x.lo}),
+               df_add(df_mul(df_mul(x, x), dfl{kSixthHi, kSixthLo}), df_of(tail)));
+}
+
+// u4 of the reference, all in double-float (u4_factors_df for the factors).
+SG_DEV void u4_compat_df(dfl t, int j_start, int j_stop, int stride, dfl (&p)[3], const dfl (&iq)[3], dfl K,
+                         dfl dofT, dfl T) {
+#pragma unroll
+    for (int j = j_start; stride > 0 ? j <= j_stop : j >= j_stop; j += stride) {
+        const dfl gj = (j == 1) ? df_sub(K, dofT) : df_sub(df_mul(df_mul(p[j - 2], p[j - 2]), iq[j - 2]), T);
+        if (j == 3) {
+            p[2] = df_add(p[2], df_mul(t, gj));
+        } else {
+            dfl ex, c;
+            u4_factors_df(df_mul(t, df_mul(p[j], iq[j])), ex, c);
+            p[j - 1] = df_add(df_mul(p[j - 1], ex), df_mul(df_mul(t, gj), c));
+        }
+    }
+}
+
+// m (|b|^2 - |a|^2) in double-float (squares exact)
+SG_DEV dfl dmv2_df(float m, float3 b, float3 a) {
+    return df_mul_f(df_sub(df_dot3(b, b), df_dot3(a, a)), m);
+}
+
 __global__ void k_nh_compat(int n, NhConst c, int initial, Geo g, double* nh, float4* __restrict__ pos,
                             float4* __restrict__ vel, const float4* __restrict__ force,
                             const float4* __restrict__ shape) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double eta[3], p[3];
+    dfl eta[3], p[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        eta[k] = nh[k];
-        p[k] = nh[3 + k];
+        eta[k] = df_from_double(nh[k]);
+        p[k] = df_from_double(nh[3 + k]);
     }
-    const double ih[3] = {c.iHB[0], c.iHB[1], c.iHB[2]};
-    double K = nh[14];
-    double ke = 0.0;
-    const double h = 0.5 * c.dt;
+    dfl K = df_from_double(nh[14]);
+    dfl ke = df_of(0.f);
+    const float h = 0.5f * (float)c.dt, dtf = (float)c.dt;
+    float4 v_n{}, f_n{}, s_n{};
+    if (n > 0) {
+        v_n = vel[0];
+        f_n = force[0];
+        s_n = shape[0];
+    }
     for (int i = 0; i < n; ++i) {
-        float4 v = vel[i];
-        const float4 f = force[i];
-        const double m = shape[i].w, im = v.w;
-        double vx = v.x, vy = v.y, vz = v.z;
-        if (!initial) {
-            const double ox = vx, oy = vy, oz = vz;
-            vx = vx + h * (f.x * im); vy = vy + h * (f.y * im); vz = vz + h * (f.z * im);
-            vx = (float)vx; vy = (float)vy; vz = (float)vz;
-            K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
+        const float4 v = v_n, f = f_n;
+        const float m = s_n.w, im = v.w;
+        if (i + 1 < n) {   // the next particle's state, in flight during this one's chain
+            v_n = vel[i + 1];
+            f_n = force[i + 1];
+            s_n = shape[i + 1];
         }
-        u4(c.dt / 4.0, 3, 1, -1, p, ih, K, c.ndof, c.T);
-        const double sc = exp_chain(-0.5 * c.dt * p[0] * ih[0]);
+        float3 u = make_float3(v.x, v.y, v.z);
+        if (!initial) {
+            const float3 o = u;
+            u = make_float3(u.x + h * (f.x * im), u.y + h * (f.y * im), u.z + h * (f.z * im));
+            K = df_add(K, dmv2_df(m, u, o));
+        }
+        u4_compat_df(c.d.t4, 3, 1, -1, p, c.d.iHB, K, c.d.ndofT, c.d.T);
+        const dfl sc = exp_df(df_neg(df_mul(c.d.hdt, df_mul(p[0], c.d.iHB[0]))));
         {
-            const double ox = vx, oy = vy, oz = vz;
-            vx = (float)(vx * sc); vy = (float)(vy * sc); vz = (float)(vz * sc);
-            K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
+            const float3 o = u;
+            u = make_float3(fmaf(u.x, sc.hi, u.x * sc.lo), fmaf(u.y, sc.hi, u.y * sc.lo),
+                            fmaf(u.z, sc.hi, u.z * sc.lo));
+            K = df_add(K, dmv2_df(m, u, o));
         }
 #pragma unroll
-        for (int k = 0; k < 3; ++k) eta[k] = eta[k] + 0.5 * c.dt * p[k] * ih[k];
-        u4(c.dt / 4.0, 1, 3, 1, p, ih, K, c.ndof, c.T);
+        for (int k = 0; k < 3; ++k) eta[k] = df_add(eta[k], df_mul(c.d.hdt, df_mul(p[k], c.d.iHB[k])));
+        u4_compat_df(c.d.t4, 1, 3, 1, p, c.d.iHB, K, c.d.ndofT, c.d.T);
         if (initial) {
-            const double ox = vx, oy = vy, oz = vz;
-            vx = (float)(vx + h * (f.x * im)); vy = (float)(vy + h * (f.y * im)); vz = (float)(vz + h * (f.z * im));
-            K += m * ((vx * vx + vy * vy + vz * vz) - (ox * ox + oy * oy + oz * oz));
+            const float3 o = u;
+            u = make_float3(u.x + h * (f.x * im), u.y + h * (f.y * im), u.z + h * (f.z * im));
+            K = df_add(K, dmv2_df(m, u, o));
             const float4 r = pos[i];
-            float3 q = wrap_pos(make_float3(r.x + (float)c.dt * (float)vx, r.y + (float)c.dt * (float)vy,
-                                            r.z + (float)c.dt * (float)vz), g, i);
+            const float3 q = wrap_pos(make_float3(r.x + dtf * u.x, r.y + dtf * u.y, r.z + dtf * u.z), g, i);
             pos[i] = make_float4(q.x, q.y, q.z, r.w);
         } else {
-            ke += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+            ke = df_add(ke, df_half(mv2_df(m, make_float4(u.x, u.y, u.z, 0.f))));
         }
-        vel[i] = make_float4((float)vx, (float)vy, (float)vz, v.w);
+        vel[i] = make_float4(u.x, u.y, u.z, v.w);
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        nh[k] = eta[k];
-        nh[3 + k] = p[k];
+        nh[k] = df_to_double(eta[k]);
+        nh[3 + k] = df_to_double(p[k]);
     }
-    nh[14] = K;
-    nh[17] = ke;
+    nh[14] = df_to_double(K);
+    nh[17] = df_to_double(ke);
 }
 
 __global__ void k_half_into(const double* src, double* dst) { *dst = 0.5 * *src; }
