@@ -190,6 +190,54 @@ def test_ecp_force_is_minus_gradient(kind):
     assert np.allclose(F, num, rtol=2e-5, atol=1e-6 * np.abs(F).max())
 
 
+def _rotation_rows(q):
+    w, x, y, z = q
+    return np.array([[w * w + x * x - y * y - z * z, 2 * (x * y + w * z), 2 * (x * z - w * y)],
+                     [2 * (x * y - w * z), w * w - x * x + y * y - z * z, 2 * (y * z + w * x)],
+                     [2 * (x * z + w * y), 2 * (y * z - w * x), w * w - x * x - y * y + z * z]])
+
+
+@pytest.mark.parametrize("kind,kw,extra", [(O.ECPR, {}, 0.0), (O.ECP, {}, 2.0), (O.ECPW, {"wf": 0.5}, 2.5)],
+                         ids=["ecpr", "ecp", "ecpw"])
+def test_ecp_range_test_bounds_hold_at_the_converged_lambda(kind, kw, extra):
+    """The two upper bounds on the contact distance that the filtered ECP
+    launch tests before any solve: sigma = |r| / sqrt(F(lambda*)) with
+    F(l) = l(1-l) r.((1-l)A + lB)^-1 r, A = U^T S^2 U (the AR of fortran/force.f90:1294), is at
+    most h_A + h_B (the support functions along r) and at most |r| / sqrt(F(l0))
+    at l0 = h_A / (h_A + h_B), because lambda* maximises F. The converged
+    lambda here is the oracle's; a pair beyond sigma + extra (reach - sigma:
+    cutoff - 1, plus wf welded, 0 repulsive) has no energy, force or torque, so
+    turning it away before the solve changes nothing."""
+    rng = np.random.default_rng(5)
+    sig = np.array([3.0, 2.0, 1.0])
+    S2 = np.diag((sig / 2) ** 2)
+    grid = np.linspace(1e-4, 1 - 1e-4, 801)
+    beyond = 0
+    for _ in range(150):
+        q = rng.normal(size=(2, 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        d = rng.normal(size=3)
+        d *= rng.uniform(0.8, 6.0) / np.linalg.norm(d)
+        s = system_from([[0, 0, 0], d], 80.0, sig=tuple(sig), q=q)
+        out, _ = s.pair(0, 1, O.pair_params(kind, cutoff=3.0, solver=O.SOLVER_TIGHT, **kw))
+        A, B = (_rotation_rows(qq).T @ S2 @ _rotation_rows(qq) for qq in q)
+
+        def F(lam):
+            return lam * (1 - lam) * d @ np.linalg.solve((1 - lam) * A + lam * B, d)
+
+        lam = out[10]
+        assert max(F(g) for g in grid) <= F(lam) * (1 + 1e-12)     # the oracle's lambda is the maximum
+        rm = np.linalg.norm(d)
+        sigma = rm / np.sqrt(F(lam))
+        ha, hb = np.sqrt(d @ A @ d) / rm, np.sqrt(d @ B @ d) / rm
+        assert sigma <= (ha + hb) * (1 + 1e-12)
+        assert sigma <= rm / np.sqrt(F(ha / (ha + hb))) * (1 + 1e-12)
+        if rm > (sigma + extra) * (1 + 1e-9):
+            beyond += 1
+            assert np.all(out[:10] == 0.0)
+    assert beyond > 10
+
+
 def test_brent_vs_converged_gap_is_the_reference_tolerance():
     # the reference's Brent stops at atol 1e-3 / rtol 1e-2 (force.f90:1065):
     # its lambda differs from the converged one by up to ~1e-2
