@@ -253,6 +253,14 @@ module sucrose_gpu
             integer(c_int32_t), value     :: nrigid
             real(c_double), intent(out)   :: out3(3)
         end function
+        ! set_velocity_to_temperature (fortran/system.f90:361-421) on the device
+        integer(c_int) function sg_set_velocity_to_temperature(ctx, rtemp, seed, remove_com, nrigid) &
+                bind(c, name="sg_set_velocity_to_temperature")
+            import :: c_ptr, c_int, c_double, c_int32_t
+            type(c_ptr), value            :: ctx
+            real(c_double), value         :: rtemp
+            integer(c_int32_t), value     :: seed, remove_com, nrigid
+        end function
         ! ---- whole timestep as a captured CUDA graph ---------------------------
         integer(c_int) function sg_step_configure(ctx, cfg) bind(c, name="sg_step_configure")
             import :: c_ptr, c_int, sg_step_config

@@ -528,6 +528,17 @@ void sg_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]
 int sg_philox4x32_device(sg_ctx* ctx, int64_t n, const uint32_t* ctr, const uint32_t key[2], uint32_t* out);
 /* philox_normal_3seq on the device for n counters; out holds 3 doubles per counter. */
 int sg_philox_normal_3seq_device(sg_ctx* ctx, int64_t n, const int32_t* ctr, double* out);
+/* set_velocity_to_temperature (fortran/system.f90:361-421) on the device:
+ * particle I (1-based) takes the normals of counter (I, int(rtemp*1000), seed,
+ * 42) under the default key; with remove_com the mean velocity is subtracted
+ * and n_dof = 6N - NC - 3, else n_dof = 6N - NC (NC: the constraints given to
+ * sg_set_constraints, as the reference's module count); the velocities are
+ * then scaled so that sum |v|^2 = n_dof * rtemp * nrigid (mass ignored, as in
+ * the reference). Sums in FP64, the result rounded once to the FP32 state.
+ * Enqueued on the context's stream (no synchronisation). Single systems only;
+ * SG_EINVAL for a replica context, no particles, remove_com with one particle,
+ * rtemp outside (0, 2147483.647), nrigid < 1 or no degrees of freedom. */
+int sg_set_velocity_to_temperature(sg_ctx* ctx, double rtemp, int32_t seed, int32_t remove_com, int32_t nrigid);
 
 /* ---- learned contact-parameter guess (no counterpart in the reference) -------- */
 /* Weights of the 14(16)->64->64->64->1 MLP, FP32 master copy, packed

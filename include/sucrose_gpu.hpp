@@ -80,6 +80,10 @@ class Context {
     // initialize_forces (fortran/system.f90:423)
     void zero_forces() { check(ctx_, sg_zero_forces(ctx_)); }
     void synchronize() { check(ctx_, sg_synchronize(ctx_)); }
+    // set_velocity_to_temperature (fortran/system.f90:361-421), on the device
+    void set_velocity_to_temperature(double rtemp, int seed, bool remove_com_velocity = true, int nrigid = 1) {
+        check(ctx_, sg_set_velocity_to_temperature(ctx_, rtemp, seed, remove_com_velocity ? 1 : 0, nrigid));
+    }
 
     // State of a reference-shaped System (atom.rx ... atom.lz, 0-based).
     template <class SystemT>

@@ -159,6 +159,7 @@ SIGNATURES = [
     ("sg_philox4x32", None, [_U32, _U32, _U32]),
     ("sg_philox4x32_device", C.c_int, [_P, C.c_int64, _U32, _U32, _U32]),
     ("sg_philox_normal_3seq_device", C.c_int, [_P, C.c_int64, _I32, _D]),
+    ("sg_set_velocity_to_temperature", C.c_int, [_P, C.c_double, C.c_int32, C.c_int32, C.c_int32]),
     ("sg_mlp_set_weights", C.c_int, [_P, _F, C.c_int64]),
     ("sg_mlp_get_weights", C.c_int, [_P, _F, C.c_int64]),
     ("sg_mlp_weight_count", C.c_int64, []),

@@ -454,6 +454,14 @@ class GpuSystem:
         self._c(self.L.sg_thermo(self.ctx, int(dof), float(density), int(nrigid), _dp(out)))
         return out
 
+    def set_velocity_to_temperature(self, rtemp, seed, remove_com_velocity=True, nrigid=1):
+        """set_velocity_to_temperature (fortran/system.f90:361-421) on the device:
+        Philox normals of counter (I, int(rtemp*1000), seed, 42), the mean
+        removed (n_dof = 6N - NC - 3) unless remove_com_velocity is False
+        (6N - NC), scaled to sum |v|^2 = n_dof * rtemp * nrigid."""
+        self._c(self.L.sg_set_velocity_to_temperature(self.ctx, float(rtemp), int(seed),
+                                                      1 if remove_com_velocity else 0, int(nrigid)))
+
     def synchronize(self):
         self._c(self.L.sg_synchronize(self.ctx))
 

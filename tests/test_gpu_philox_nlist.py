@@ -27,6 +27,63 @@ def test_philox_normals(lib):
     np.testing.assert_allclose(dev, ref, rtol=1e-13, atol=1e-13)
 
 
+def _velocities_reference(n, temp, seed, nc=0, nrigid=1, remove_com=True):
+    """The oracle's set_velocity_to_temperature (fortran/system.f90:361-421),
+    FP64, with the module's NC and Nrigid set."""
+    o = O.System(n, 60.0)
+    o.s.nc, o.s.nrigid = nc, nrigid
+    o.set_velocity_to_temperature(temp, seed, remove_com)
+    return np.stack([o.vx, o.vy, o.vz], 1).copy()
+
+
+def test_velocity_init_matches_reference_golden(lib):
+    """The device set_velocity_to_temperature against the reference's own
+    velocities for the README system (108 particles, T = 0.722, seed 15), to
+    the FP32 rounding of the state."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "readme_velocities.npz"))["v"]
+    s = GpuSystem(108, 10.0)
+    s.set_velocity_to_temperature(0.722, 15)
+    v = s.download()[2]
+    np.testing.assert_allclose(v, g, rtol=1e-7, atol=2e-7)
+    assert abs(np.sum(v ** 2) - (6 * 108 - 3) * 0.722) < 1e-5 * (6 * 108 - 3) * 0.722
+
+
+@pytest.mark.parametrize("n,temp,seed,nc,nrigid,com", [(20000, 1.37, -3, 5000, 2, False),
+                                                        (70001, 0.8, 2024, 0, 1, True)])
+def test_velocity_init_options(lib, n, temp, seed, nc, nrigid, com):
+    """Constraints counted in n_dof, no mean removal, Nrigid, a negative seed,
+    and a grid of many blocks; the inverse mass in the velocity slot is kept
+    (a half kick afterwards moves v by dt/2 F / m)."""
+    s = GpuSystem(n, 60.0)
+    s.set_particles(mass=np.full(n, 2.5))
+    if nc:
+        s.set_constraints(2 * np.arange(nc), 2 * np.arange(nc) + 1, 1.0)
+    s.set_velocity_to_temperature(temp, seed, remove_com_velocity=com, nrigid=nrigid)
+    v = s.download()[2]
+    ref = _velocities_reference(n, temp, seed, nc, nrigid, com)
+    np.testing.assert_allclose(v, ref, rtol=1e-7, atol=1e-6)
+    f = np.tile([1.0, -2.0, 0.5], (n, 1))
+    s.set_forces(f, np.zeros((n, 3)))
+    s.vv_final(0.1)
+    v2 = s.download()[2]
+    np.testing.assert_allclose(v2 - v, 0.05 * f / 2.5, rtol=0, atol=1e-6)
+
+
+def test_velocity_init_refusals(lib):
+    s = GpuSystem(1, 10.0)
+    with pytest.raises(SgError):
+        s.set_velocity_to_temperature(1.0, 5)              # mean removal with one particle
+    s.set_velocity_to_temperature(1.0, 5, remove_com_velocity=False)
+    assert abs(np.sum(s.download()[2] ** 2) - 6.0) < 1e-5
+    s = GpuSystem(10, 10.0)
+    for t in (0.0, -1.0, float("nan")):
+        with pytest.raises(SgError):
+            s.set_velocity_to_temperature(t, 5)
+    with pytest.raises(SgError):
+        s.set_velocity_to_temperature(1.0, 5, nrigid=0)
+
+
 def _pairs_equal(P, cutoff, skin):
     opi, opj = P.o.pairs(cutoff, skin)
     gpi, gpj = P.g.pairs()

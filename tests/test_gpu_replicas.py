@@ -209,6 +209,8 @@ def test_replica_context_rejects_single_system_calls(lib, ens):
         g.init_nlist(0.3, 2.5)
     with pytest.raises(capi.SgError):
         g.nht_initial(DT, 1.0, 0.0)
+    with pytest.raises(capi.SgError):
+        g.set_velocity_to_temperature(1.0, 5)
     g.close()
 
 
