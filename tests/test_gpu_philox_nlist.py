@@ -36,10 +36,10 @@ def _velocities_reference(n, temp, seed, nc=0, nrigid=1, remove_com=True):
     return np.stack([o.vx, o.vy, o.vz], 1).copy()
 
 
-def test_velocity_init_matches_reference_golden(lib):
-    """The device set_velocity_to_temperature against the reference's own
-    velocities for the README system (108 particles, T = 0.722, seed 15), to
-    the FP32 rounding of the state."""
+def test_velocity_init_matches_readme_golden(lib):
+    """The device set_velocity_to_temperature against the committed fixture of
+    the README system (108 particles, T = 0.722, seed 15; the oracle's
+    restatement of system.f90:361-421), to the FP32 rounding of the state."""
     import os
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "readme_velocities.npz"))["v"]
     s = GpuSystem(108, 10.0)

@@ -81,6 +81,24 @@ def test_readme_velocities_golden():
     assert np.allclose(v, g["v"], rtol=0, atol=1e-13)
     # the reference's dof convention: sum v^2 = (6N - 3) T
     assert abs(np.sum(v ** 2) - (6 * 108 - 3) * 0.722) < 1e-9
+    # the fixture is the oracle's own output: a regression anchor
+    o = O.System(108, 10.0)
+    o.set_velocity_to_temperature(0.722, 15)
+    assert np.array_equal(np.stack([o.vx, o.vy, o.vz], 1), g["v"])
+
+
+@pytest.mark.parametrize("n,temp,seed,nc,nrigid,com", [(500, 1.37, -3, 120, 2, False), (777, 0.8, 2024, 0, 1, True)])
+def test_velocity_init_host_matches_oracle(n, temp, seed, nc, nrigid, com):
+    # the host routine used for replica set-up against the oracle's
+    # set_velocity_to_temperature, with NC, Nrigid, a negative seed and no
+    # mean removal
+    o = O.System(n, 10.0)
+    o.s.nc, o.s.nrigid = nc, nrigid
+    o.set_velocity_to_temperature(temp, seed, com)
+    v = configs.velocities_to_temperature(n, temp, seed, nc=nc, nrigid=nrigid, remove_com=com)
+    np.testing.assert_allclose(v, np.stack([o.vx, o.vy, o.vz], 1), rtol=1e-13, atol=1e-13)
+    dof = 6 * n - nc - (3 if com else 0)
+    assert abs(np.sum(v ** 2) - dof * temp * nrigid) < 1e-9 * dof * temp * nrigid
 
 
 # ----------------------------------------------------------- Philox structure ---
