@@ -58,12 +58,12 @@
 namespace {
 
 // ------------------------------------------------------------------ prep ---
-__global__ void k_ecp_prep(int n, const float4* __restrict__ quat, const float4* __restrict__ shape,
-                           const float4* __restrict__ eshape, float muinv, float4* __restrict__ prep,
-                           double* __restrict__ prep64) {
+__global__ void k_ecp_prep(int n, const float4* __restrict__ pos, const float4* __restrict__ quat,
+                           const float4* __restrict__ shape, const float4* __restrict__ eshape, float muinv,
+                           float4* __restrict__ prep, double* __restrict__ prep64) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    ecp_prep_one(p, quat[p], shape[p], eshape[p], muinv, prep, prep64);
+    ecp_prep_one(p, pos[p], quat[p], shape[p], eshape[p], muinv, prep, prep + 4 * (size_t)n, prep64);
 }
 
 // ------------------------------------------------------------- 3x3 SPD ----
@@ -380,17 +380,32 @@ struct PotECP {
     //      taken at the support start l0 = h_A / (h_A + h_B), one evaluation.
     // A pair with |r| >= bound + (reach - sigma) is inactive in eval and skips
     // the contact solve. The bounds are widened (2e-4 and 1e-3 relative, 1e-4)
-    // for the FP32 rounding of r, h, F and sigma; NaN keeps the pair.
+    // for the FP32 rounding of r, h, F and sigma; NaN keeps the pair. Each
+    // particle's position and A_R come from its 32-byte range record (one
+    // load), A_R as the FP16 matrix plus d I, which bounds A_R from above
+    // (ecp_range_one), so both bounds stay upper bounds.
     SG_DEV bool in_range(int i, int j) const {
         float4 a0, a1, b0, b1;
-        ld_f4x2(prep + 4 * i, a0, a1);   // A_R: the first 32 bytes of each record
-        ld_f4x2(prep + 4 * j, b0, b1);
-        return range_test(pos[i], pos[j], a0, a1, b0, b1, i);
+        ld_f4x2(range + 2 * i, a0, a1);
+        ld_f4x2(range + 2 * j, b0, b1);
+        float A[6], B[6];
+        range_matrix(a0.w, a1, A);
+        range_matrix(b0.w, b1, B);
+        return range_test(make_float3(a0.x, a0.y, a0.z), make_float3(b0.x, b0.y, b0.z), A, B, i);
     }
-    SG_DEV bool range_test(float4 pi, float4 pj, float4 a0, float4 a1, float4 b0, float4 b1, int i) const {
-        const float3 r = pair_rij_of(make_float3(pi.x, pi.y, pi.z), make_float3(pj.x, pj.y, pj.z), i, b);
-        const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
-        const float B[6] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y};
+    static SG_DEV void range_matrix(float d, float4 w, float (&A)[6]) {
+        const unsigned u[3] = {__float_as_uint(w.x), __float_as_uint(w.y), __float_as_uint(w.z)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            A[2 * k] = __half2float(__ushort_as_half((unsigned short)(u[k] & 0xffffu)));
+            A[2 * k + 1] = __half2float(__ushort_as_half((unsigned short)(u[k] >> 16)));
+        }
+        A[0] += d;
+        A[3] += d;
+        A[5] += d;
+    }
+    SG_DEV bool range_test(float3 pi, float3 pj, const float (&A)[6], const float (&B)[6], int i) const {
+        const float3 r = pair_rij_of(pi, pj, i, b);
         const float rsq = dot3(r, r), rinv = rsqrtf(rsq), rm = rsq * rinv;
         const float ha = sqrtf(dot3(r, symv(A, r))), hb = sqrtf(dot3(r, symv(B, r)));   // |r| h_A, |r| h_B
         if (rm >= ((ha + hb) * rinv + reach_extra) * 1.0002f + 1e-4f) return false;
@@ -409,6 +424,7 @@ struct PotECP {
     const float4* __restrict__ quat;
     const float4* __restrict__ shape;
     const float4* __restrict__ prep;
+    const float4* __restrict__ range;   // the range records (prep + 4n)
     const double* __restrict__ prep64;
     float* __restrict__ lam_out;
     MlpDev mlp;
@@ -796,6 +812,7 @@ int launch_ecp(sg_ctx* ctx, const sg_pair_params* p, int mu, int nu) {
     pot.quat = ctx->quat;
     pot.shape = ctx->shape;
     pot.prep = ctx->ecp_prep;
+    pot.range = ctx->ecp_prep + 4 * (size_t)ctx->n;
     pot.prep64 = ctx->ecp_prep64;
     pot.lam_out = ctx->ecp_lambda;
     if (ctx->mlp_ready) pot.mlp = *(const MlpDev*)ctx->mlp_host_desc;
@@ -831,9 +848,9 @@ int launch_ecp(sg_ctx* ctx, const sg_pair_params* p, int mu, int nu) {
 
 int sg_ecp_prepare(sg_ctx* ctx, const sg_pair_params* p, int need64) {
     int mu = p->mu > 0 ? p->mu : 2;
-    if (!ctx->ecp_prep) SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep, sizeof(float4) * 4 * (size_t)ctx->n));
+    if (!ctx->ecp_prep) SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep, sizeof(float4) * SG_PREP_F4 * (size_t)ctx->n));
     if (need64 && !ctx->ecp_prep64) SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep64, sizeof(double) * 6 * (size_t)ctx->n));
-    k_ecp_prep<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->quat, ctx->shape, ctx->eshape,
+    k_ecp_prep<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->quat, ctx->shape, ctx->eshape,
                                                              1.f / (float)mu, ctx->ecp_prep,
                                                              need64 ? ctx->ecp_prep64 : nullptr);
     SG_LAUNCH_CHECK(ctx, "k_ecp_prep");

@@ -452,7 +452,7 @@ int sg_launch_pair_gb(sg_ctx* ctx, const sg_pair_params* p) {
     if (mu == 0 && nu == 0) { mu = 1; nu = 2; }
     if (mu < 1 || nu < 1 || mu > 8 || nu > 8) return sg_fail(ctx, SG_EINVAL, "GB exponents must be in 1..8");
     // prep buffer: reuse the ECP prep allocation (large enough: 4 float4 per particle)
-    if (!ctx->ecp_prep) SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep, sizeof(float4) * 4 * (size_t)ctx->n));
+    if (!ctx->ecp_prep) SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep, sizeof(float4) * SG_PREP_F4 * (size_t)ctx->n));
     if (ctx->step_prep_kind != SG_PREP_GB) {   // else written by the step's initial half step
         k_gb_prep<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->pos, ctx->quat, ctx->shape,
                                                                 ctx->eshape, 1.f / (float)mu, ctx->ecp_prep);

@@ -113,6 +113,11 @@ struct PairTune {
     int filter = 0;    // range filter + per-warp queue of in-range pairs; ECP kinds: the split Newton path
 };
 
+// float4 per particle of the per-particle prep buffer (ecp_prep). ECP: the
+// 64-byte record of particle p at 4p and the 32-byte range record at 4n + 2p;
+// Gay-Berne: 2 at 2p, 1 at 2n + p, 1 at 3n + p.
+#define SG_PREP_F4 6
+
 struct sg_ctx {
     int n = 0;
     int device = 0;
@@ -146,8 +151,8 @@ struct sg_ctx {
     double* nh = nullptr;
 
     // ECP per-particle prep (FP32) and FP64 copies for the bit-exact Brent
-    float4* ecp_prep = nullptr;      // 6 float4 per particle
-    double* ecp_prep64 = nullptr;    // 12 doubles per particle (A_R 6, A_E 6)
+    float4* ecp_prep = nullptr;      // SG_PREP_F4 float4 per particle
+    double* ecp_prep64 = nullptr;    // A_R in FP64, 6 doubles per particle
     float* ecp_lambda = nullptr;     // per pair
     int64_t ecp_lambda_cap = 0;
 

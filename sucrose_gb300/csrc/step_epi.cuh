@@ -14,6 +14,8 @@
 
 #include <cmath>
 
+#include <cuda_fp16.h>
+
 #include "dfloat.cuh"
 #include "sg_internal.cuh"
 
@@ -92,13 +94,35 @@ SG_DEV void check_displacement(int i, float4 a, const CheckArgs& c) {
 }
 
 // ------------------------------------------------------- ECP particle prep --
+// The range record of the filtered ECP launch, 32 bytes that the range test
+// reads with one 256-bit load per particle: (x, y, z, d) and A_R rounded to
+// FP16, packed two to a word (xx|xy, xz|yy, yz|zz, 0). d >= ||A_R - A16||_F
+// >= ||A_R - A16||_2, so A16 + d I - A_R is positive semi-definite: the
+// support function sqrt(r.X r) and the contact function's 1 / F(l) taken with
+// X = A16 + d I bound those of A_R from above, and the test stays a superset.
+// An entry beyond the FP16 range gives d = inf, and the test keeps the pair.
+SG_DEV void ecp_range_one(int p, float4 a, const float (&A)[6], float4* __restrict__ range) {
+    unsigned h[6];
+    float s = 0.f;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+        const __half hv = __float2half_rn(A[m]);
+        h[m] = __half_as_ushort(hv);
+        const float e = A[m] - __half2float(hv);
+        s += (m == 1 || m == 2 || m == 4) ? 2.f * e * e : e * e;   // off-diagonal entries count twice
+    }
+    range[2 * p] = make_float4(a.x, a.y, a.z, sqrtf(s) * 1.001f);
+    reinterpret_cast<uint4*>(range)[2 * p + 1] = make_uint4(h[0] | h[1] << 16, h[2] | h[3] << 16, h[4] | h[5] << 16, 0u);
+}
+
 // A_R = U^T S^2 U and A_E = U^T E U (fortran/force.f90:1294-1297), the body z
 // axis and the sigma_t factor (:1299), as 4 float4: (A_R 0-3), (A_R 4-5,
-// A_E 0-1), (A_E 2-5), (u_z, sigma_t). prep64 (optional): A_R in FP64 in the
+// A_E 0-1), (A_E 2-5), (u_z, sigma_t); the range record of position a
+// (ecp_range_one) into range. prep64 (optional): A_R in FP64 in the
 // reference's operation order (xmath.f90:194-208, :262-279), for the Brent
 // compat solver.
-SG_DEV void ecp_prep_one(int p, float4 q, float4 s4, float4 e4, float muinv, float4* __restrict__ prep,
-                         double* __restrict__ prep64) {
+SG_DEV void ecp_prep_one(int p, float4 a, float4 q, float4 s4, float4 e4, float muinv, float4* __restrict__ prep,
+                         float4* __restrict__ range, double* __restrict__ prep64) {
     const float w = q.x, x = q.y, y = q.z, z = q.w;
     // rows of the reference's U (rotation_matrix form, :1244-1252): body axes in the lab frame
     float u[3][3];
@@ -131,6 +155,7 @@ SG_DEV void ecp_prep_one(int p, float4 q, float4 s4, float4 e4, float muinv, flo
     prep[4 * p + 1] = make_float4(A[4], A[5], B[0], B[1]);
     prep[4 * p + 2] = make_float4(B[2], B[3], B[4], B[5]);
     prep[4 * p + 3] = make_float4(u[2][0], u[2][1], u[2][2], st);
+    ecp_range_one(p, a, A, range);
     if (prep64) {
         const double W = w, X = x, Y = y, Z = z;
         double r[3][3];
@@ -219,7 +244,7 @@ inline int make_step_epi(sg_ctx* ctx, StepEpi& e) {
     e.prep_kind = ctx->step_prep_kind;
     if (e.prep_kind != SG_PREP_NONE && !ctx->ecp_prep) {
         ctx->graph_epoch++;
-        SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep, sizeof(float4) * 4 * (size_t)ctx->n));
+        SG_CUDA(ctx, cudaMalloc(&ctx->ecp_prep, sizeof(float4) * SG_PREP_F4 * (size_t)ctx->n));
     }
     e.prep = ctx->ecp_prep;
     e.shape = ctx->shape;
@@ -236,7 +261,8 @@ SG_DEV void step_epilogue(const StepEpi& e, int i, float4 a, float4 q) {
     if (e.check) check_displacement(i, a, e.chk);
     e.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     e.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (e.prep_kind == SG_PREP_ECP) ecp_prep_one(i, q, e.shape[i], e.eshape[i], e.muinv, e.prep, nullptr);
+    if (e.prep_kind == SG_PREP_ECP)
+        ecp_prep_one(i, a, q, e.shape[i], e.eshape[i], e.muinv, e.prep, e.prep + 4 * (size_t)e.n, nullptr);
     else if (e.prep_kind == SG_PREP_GB) gb_prep_one(e.n, i, a, q, e.shape[i], e.eshape[i], e.muinv, e.prep);
     if (i == 0) {
         for (int k = 0; k < 7; ++k) e.acc[k] = 0.0;
