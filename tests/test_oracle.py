@@ -256,6 +256,26 @@ def test_ecp_range_test_bounds_hold_at_the_converged_lambda(kind, kw, extra):
     assert beyond > 10
 
 
+def test_fp16_shape_matrix_widened_by_frobenius_error_bounds_it():
+    """The range record's matrix: A rounded to FP16 plus d I with d the
+    Frobenius norm of the rounding error (x 1.001, all in FP32) is >= A in
+    the positive semi-definite order, so the support functions and 1/F(l)
+    taken with it bound those of A from above (the test stays a superset)."""
+    rng = np.random.default_rng(9)
+    for _ in range(3000):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        U = _rotation_rows(q).astype(np.float32)
+        s = rng.uniform(0.05, 20.0, size=3).astype(np.float32)
+        A = (U.T @ np.diag((s / 2) ** 2) @ U).astype(np.float32)
+        A = (A + A.T) / np.float32(2)
+        Ah = A.astype(np.float16).astype(np.float32)
+        e = A - Ah
+        d = np.float32(np.sqrt(np.float32(np.sum(e * e))) * np.float32(1.001))
+        W = Ah + d * np.eye(3, dtype=np.float32)
+        assert np.linalg.eigvalsh(W.astype(np.float64) - A.astype(np.float64)).min() >= 0.0
+
+
 def test_brent_vs_converged_gap_is_the_reference_tolerance():
     # the reference's Brent stops at atol 1e-3 / rtol 1e-2 (force.f90:1065):
     # its lambda differs from the converged one by up to ~1e-2
