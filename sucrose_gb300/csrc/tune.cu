@@ -10,6 +10,7 @@
 // replica), which take the place of the unfiltered 256-thread variant. The best variant depends on the potential, the share of
 // listed pairs that are in range and the system size, so it is measured on
 // the live list and cached per (kind, particle-count bucket, density bucket).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -113,8 +114,13 @@ int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* p, int32_t reps, sg_tune
         if (gph) cudaGraphDestroy(gph);
         const float ms = tot / reps;
         res.ms[v] = ms;
-        if (!rc && ms < best) {
-            best = ms;
+        // within 1 % of the best, the same second axis with a smaller block
+        // counts as a tie and takes the pick: alone the ECP benchmark's
+        // filtered launches of 128 and 256 threads time within 0.3 %, and
+        // inside the captured step 128 is 1.3 % faster
+        const bool tie_smaller = ms <= best * 1.01f && tv.filter == pick.filter && tv.block < pick.block;
+        if (!rc && (ms < best || tie_smaller)) {
+            best = std::min(best, ms);
             pick = tv;
         }
     }
