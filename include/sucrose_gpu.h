@@ -452,7 +452,9 @@ typedef struct {
 } sg_tune_result;
 /* Time each launch variant of the params' pair kernel on the current list
  * (reps launches each), keep the fastest for this context's (kind, size,
- * density) bucket. Forces, torques and energy accumulators are restored.
+ * density) bucket; a variant with the same second axis and a smaller block
+ * within 1 % of the fastest is kept instead (a tie goes to the smaller
+ * block). Forces, torques and energy accumulators are restored.
  * Captured steps are re-captured at their next sg_step. */
 int sg_pair_autotune(sg_ctx* ctx, const sg_pair_params* params, int32_t reps, sg_tune_result* out);
 /* Set a launch variant by hand (block 64, 128 or 256; filter 0, 1, or 2 for
