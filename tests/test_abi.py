@@ -70,3 +70,31 @@ def test_create_without_gpu_fails_cleanly(built_lib):
     msg = built_lib.sg_last_error(ctx)
     assert msg
     built_lib.sg_destroy(ctx)
+
+
+def test_null_context_is_refused_by_every_entry_point(built_lib):
+    """Every entry point whose first argument is the context returns
+    SG_EINVAL for a NULL context (other arguments zero or NULL) before any
+    device work; sg_destroy and sg_reporter_close accept NULL like free."""
+    from sucrose_gb300 import capi
+    ok_null = {"sg_destroy": 0, "sg_reporter_close": 0}
+    checked = 0
+    for name, res, args in capi.SIGNATURES:
+        if not args or args[0] is not capi._P or name in ("sg_last_error", "sg_stream"):
+            continue
+        f = getattr(built_lib, name)
+        f.restype, f.argtypes = res, args
+        vals = []
+        for t in args:
+            if t in (ctypes.c_int32, ctypes.c_int, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64):
+                vals.append(0)
+            elif t in (ctypes.c_double, ctypes.c_float):
+                vals.append(0.0)
+            else:
+                vals.append(None)
+        assert f(*vals) == ok_null.get(name, capi.SG_EINVAL), name
+        checked += 1
+    assert checked > 80
+    f = built_lib.sg_last_error
+    f.restype, f.argtypes = ctypes.c_char_p, [ctypes.c_void_p]
+    assert f(None)
